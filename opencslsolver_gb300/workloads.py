@@ -1,0 +1,326 @@
+"""Seeded synthetic linear systems with the reference's CSR layout.
+
+The reference assembles its systems on a fixed CSR pattern built by
+``CFVM::define_matrix_structure`` (``cfvm.cpp:74-98``): per row the diagonal,
+one entry per neighbouring cell, and -- on every row whose cell touches a
+boundary -- one phantom column ``(size_t)-1`` holding an exact 0, all sorted
+ascending, so the phantom comes last.  Every generator here reproduces that
+layout (``row_ptr``/``column_index`` as ``uint64``), so the systems can be fed
+unchanged to the reference, to the oracle and to the GPU library.
+
+Workloads (no mesh files or datasets exist for them; everything is seeded):
+
+* ``pattern_1d``: the 1D mesh of ``generate_1d_mesh`` (cgeometry_supply.h:26-77),
+  every cell a boundary cell (empty side faces).
+* ``hex_pprime``: the p'-type system on an ``nx*ny*nz`` hex box over the unit
+  cube with interior nodes jittered uniformly by +-10% of the spacing:
+  off-diagonals ``-Gamma_f A_f / d_f`` with ``Gamma_f ~ U[0.5, 2]`` plus a
+  first-order-upwind convective part from a smooth seeded velocity field scaled
+  to a maximum cell Peclet number, diagonal ``ratio * sum |off|`` with
+  ``ratio ~ U[1.01, 1.1]`` (the compressibility term psi V / dt), RHS
+  ``U[-1, 1]``.  ``peclet=0`` gives the symmetric diffusion-only variant.
+* ``tet_pprime``: the same recipe on ``nx*ny*nz`` hexes split into 6 tetrahedra
+  each (Kuhn split along the (0,0,0)-(1,1,1) diagonal, conforming).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
+BASE_SEED = 20261203
+
+
+@dataclass
+class System:
+    """One CSR system in the reference layout."""
+
+    row_ptr: np.ndarray        # uint64[n+1]
+    column_index: np.ndarray   # uint64[nnz], phantom = 2**64-1
+    value: np.ndarray          # float64[nnz]
+    b: np.ndarray              # float64[n]
+    name: str = ""
+
+    @property
+    def n(self) -> int:
+        return self.row_ptr.size - 1
+
+    @property
+    def nnz(self) -> int:
+        return self.column_index.size
+
+    @property
+    def nnz_real(self) -> int:
+        return int(np.count_nonzero(self.column_index != PHANTOM))
+
+
+def _csr_from_slots(cols: np.ndarray, vals: np.ndarray | None, mask: np.ndarray):
+    """Compress an (n, k) slot table (already in sorted column order) to CSR."""
+    counts = mask.sum(axis=1)
+    rp = np.zeros(cols.shape[0] + 1, np.uint64)
+    np.cumsum(counts, out=rp[1:])
+    col = cols[mask].astype(np.uint64)
+    val = vals[mask] if vals is not None else None
+    return rp, col, val
+
+
+def pattern_1d(ncells: int):
+    """CSR pattern of the reference's 1D mesh: rows [i-1, i, i+1, phantom]."""
+    i = np.arange(ncells, dtype=np.int64)
+    cols = np.stack([i - 1, i, i + 1, np.full_like(i, -1)], axis=1)
+    mask = np.stack([i > 0, np.ones_like(i, bool), i < ncells - 1, np.ones_like(i, bool)], axis=1)
+    cols_u = cols.astype(np.uint64)  # -1 -> 2**64-1, the reference's phantom
+    rp, col, _ = _csr_from_slots(cols_u, None, mask)
+    return rp, col
+
+
+def hex_pattern(nx: int, ny: int, nz: int):
+    """7-point pattern in natural order (cell = i + nx*(j + ny*k)) with phantoms."""
+    rp, col, _, _ = _hex_slots(nx, ny, nz)
+    return rp, col
+
+
+def _hex_slots(nx, ny, nz):
+    n = nx * ny * nz
+    c = np.arange(n, dtype=np.int64)
+    i = c % nx
+    j = (c // nx) % ny
+    k = c // (nx * ny)
+    nxy = nx * ny
+    cols = np.stack([c - nxy, c - nx, c - 1, c, c + 1, c + nx, c + nxy,
+                     np.full_like(c, -1)], axis=1)
+    boundary = (i == 0) | (i == nx - 1) | (j == 0) | (j == ny - 1) | (k == 0) | (k == nz - 1)
+    mask = np.stack([k > 0, j > 0, i > 0, np.ones(n, bool), i < nx - 1, j < ny - 1,
+                     k < nz - 1, boundary], axis=1)
+    rp, col, _ = _csr_from_slots(cols.astype(np.uint64), None, mask)
+    return rp, col, cols, mask
+
+
+def _jittered_nodes(nx, ny, nz, rng, jitter=0.1):
+    hx, hy, hz = 1.0 / nx, 1.0 / ny, 1.0 / nz
+    X, Y, Z = np.meshgrid(np.arange(nx + 1) * hx, np.arange(ny + 1) * hy,
+                          np.arange(nz + 1) * hz, indexing="ij")
+    P = np.stack([X, Y, Z], axis=-1)  # (nx+1, ny+1, nz+1, 3)
+    J = rng.uniform(-jitter, jitter, size=P.shape) * np.array([hx, hy, hz])
+    interior = np.zeros(P.shape[:3], bool)
+    interior[1:-1, 1:-1, 1:-1] = True
+    P[interior] += J[interior]
+    return P
+
+
+def _velocity(points, rng):
+    """Smooth seeded field: a sum of three sinusoidal modes per component."""
+    u = np.zeros_like(points)
+    for _ in range(3):
+        kvec = rng.uniform(1.0, 4.0, size=3) * np.pi
+        phase = rng.uniform(0, 2 * np.pi, size=3)
+        amp = rng.uniform(-1.0, 1.0, size=3)
+        arg = points @ kvec
+        for d in range(3):
+            u[..., d] += amp[d] * np.sin(arg + phase[d])
+    return u
+
+
+def _assemble(n, L, R, D, F, ratio, slot_L, slot_R, cols, mask):
+    """Fill an (n, k) slot table from face coefficients; returns CSR values.
+
+    Face f joins cells L < R.  Upwind convection with face flux F (positive
+    from L to R):  a_LR = -D - max(-F, 0),  a_RL = -D - max(F, 0).
+    """
+    vals = np.zeros(cols.shape, np.float64)
+    aLR = -D - np.maximum(-F, 0.0)
+    aRL = -D - np.maximum(F, 0.0)
+    vals[L, slot_L] = aLR          # row L, column R
+    vals[R, slot_R] = aRL          # row R, column L
+    offsum = np.zeros(n)
+    np.add.at(offsum, L, np.abs(aLR))
+    np.add.at(offsum, R, np.abs(aRL))
+    diag_slot = np.argmax(cols == np.arange(n)[:, None], axis=1)
+    vals[np.arange(n), diag_slot] = ratio * offsum
+    return vals[mask]
+
+
+def hex_pprime(nx: int, ny: int | None = None, nz: int | None = None, *, peclet: float = 10.0,
+               seed: int = BASE_SEED, jitter: float = 0.1) -> System:
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    n = nx * ny * nz
+    rp, col, cols, mask = _hex_slots(nx, ny, nz)
+    P = _jittered_nodes(nx, ny, nz, np.random.default_rng(seed), jitter)
+    cent = 0.125 * sum(P[a:a + nx, b:b + ny, c:c + nz] for a in (0, 1) for b in (0, 1)
+                       for c in (0, 1))
+    cent = cent.transpose(2, 1, 0, 3).reshape(n, 3)  # cell = i + nx*(j + ny*k)
+
+    Ls, Rs, Av, Fc, SL, SR = [], [], [], [], [], []
+    idx = np.arange(n).reshape(nz, ny, nx)
+    # x-faces: between (i,j,k) and (i+1,j,k); face nodes at x-index i+1
+    for axis, (sl, sr) in enumerate(((4, 2), (5, 1), (6, 0))):
+        if axis == 0:
+            Lc, Rc = idx[:, :, :-1].ravel(), idx[:, :, 1:].ravel()
+            q = P[1:nx, :, :]
+            n00, n10, n01, n11 = q[:, :-1, :-1], q[:, 1:, :-1], q[:, :-1, 1:], q[:, 1:, 1:]
+            order = (2, 1, 0)
+        elif axis == 1:
+            Lc, Rc = idx[:, :-1, :].ravel(), idx[:, 1:, :].ravel()
+            q = P[:, 1:ny, :]
+            n00, n10, n01, n11 = q[:-1, :, :-1], q[:-1, :, 1:], q[1:, :, :-1], q[1:, :, 1:]
+            order = (2, 1, 0)
+        else:
+            Lc, Rc = idx[:-1, :, :].ravel(), idx[1:, :, :].ravel()
+            q = P[:, :, 1:nz]
+            n00, n10, n01, n11 = q[:-1, :-1, :], q[1:, :-1, :], q[:-1, 1:, :], q[1:, 1:, :]
+            order = (2, 1, 0)
+        area = 0.5 * np.cross(n11 - n00, n01 - n10)
+        fc = 0.25 * (n00 + n10 + n01 + n11)
+        area = area.transpose(*order, 3).reshape(-1, 3)
+        fc = fc.transpose(*order, 3).reshape(-1, 3)
+        Ls.append(Lc); Rs.append(Rc); Av.append(area); Fc.append(fc)
+        SL.append(np.full(Lc.size, sl)); SR.append(np.full(Lc.size, sr))
+    L = np.concatenate(Ls); R = np.concatenate(Rs); A = np.concatenate(Av)
+    FC = np.concatenate(Fc); slot_L = np.concatenate(SL); slot_R = np.concatenate(SR)
+    dvec = cent[R] - cent[L]
+    # orient the area vector from L to R
+    sgn = np.sign(np.einsum("ij,ij->i", A, dvec))
+    A *= sgn[:, None]
+    Amag = np.linalg.norm(A, axis=1)
+    dist = np.linalg.norm(dvec, axis=1)
+    rng1 = np.random.default_rng(seed + 1)
+    gamma = rng1.uniform(0.5, 2.0, size=L.size)
+    D = gamma * Amag / dist
+    F = np.zeros(L.size)
+    if peclet > 0:
+        u = _velocity(FC, np.random.default_rng(seed + 2))
+        F = np.einsum("ij,ij->i", u, A)
+        F *= peclet / np.max(np.abs(F) / D)
+    ratio = np.random.default_rng(seed + 3).uniform(1.01, 1.1, size=n)
+    val = _assemble(n, L, R, D, F, ratio, slot_L, slot_R, cols, mask)
+    b = np.random.default_rng(seed + 4).uniform(-1.0, 1.0, size=n)
+    name = f"hex{nx}x{ny}x{nz}_pe{peclet:g}"
+    return System(rp, col, val, b, name)
+
+
+# Kuhn split of a unit cube into 6 tetrahedra along the (0,0,0)-(1,1,1) diagonal:
+# one tet per axis permutation.  Local corner id = dx + 2*dy + 4*dz.
+def _kuhn_tets():
+    import itertools
+    tets = []
+    for perm in itertools.permutations(range(3)):
+        v = [0, 0, 0]
+        corners = [0]
+        for ax in perm:
+            v[ax] = 1
+            corners.append(v[0] + 2 * v[1] + 4 * v[2])
+        tets.append(corners)
+    return np.array(tets, np.int64)  # (6, 4)
+
+
+def tet_pprime(nx: int, ny: int | None = None, nz: int | None = None, *, peclet: float = 50.0,
+               seed: int = BASE_SEED, jitter: float = 0.1) -> System:
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    nh = nx * ny * nz
+    n = 6 * nh
+    P = _jittered_nodes(nx, ny, nz, np.random.default_rng(seed), jitter)
+    node_id = np.arange((nx + 1) * (ny + 1) * (nz + 1)).reshape(nx + 1, ny + 1, nz + 1)
+    h = np.arange(nh)
+    hi, hj, hk = h % nx, (h // nx) % ny, h // (nx * ny)
+    corner = np.empty((nh, 8), np.int64)
+    for cid in range(8):
+        dx, dy, dz = cid & 1, (cid >> 1) & 1, (cid >> 2) & 1
+        corner[:, cid] = node_id[hi + dx, hj + dy, hk + dz]
+    kt = _kuhn_tets()
+    tv = corner[:, kt].reshape(n, 4)            # cell = 6*hex + local tet
+    X = P.reshape(-1, 3)
+    cent = X[tv].mean(axis=1)
+    # faces: each tet face = the 3 vertices other than vertex m
+    faces = np.stack([np.sort(np.delete(tv, m, axis=1), axis=1) for m in range(4)], axis=1)
+    fkeys = faces.reshape(-1, 3)
+    owner = np.repeat(np.arange(n), 4)
+    order = np.lexsort((fkeys[:, 2], fkeys[:, 1], fkeys[:, 0]))
+    fs = fkeys[order]
+    same = np.all(fs[1:] == fs[:-1], axis=1)
+    a_idx = order[:-1][same]
+    b_idx = order[1:][same]
+    ca, cb = owner[a_idx], owner[b_idx]
+    L = np.minimum(ca, cb)
+    R = np.maximum(ca, cb)
+    fnodes = fkeys[a_idx]
+    p0, p1, p2 = X[fnodes[:, 0]], X[fnodes[:, 1]], X[fnodes[:, 2]]
+    A = 0.5 * np.cross(p1 - p0, p2 - p0)
+    FC = (p0 + p1 + p2) / 3.0
+    dvec = cent[R] - cent[L]
+    A *= np.sign(np.einsum("ij,ij->i", A, dvec))[:, None]
+    Amag = np.linalg.norm(A, axis=1)
+    dist = np.linalg.norm(dvec, axis=1)
+    # boundary cells: tets with fewer than 4 interior faces
+    nint = np.bincount(np.concatenate([L, R]), minlength=n)
+    boundary = nint < 4
+    # CSR slots: diag + neighbours sorted, phantom last
+    deg = nint + 1
+    rows = np.concatenate([np.arange(n), L, R])
+    cols_ = np.concatenate([np.arange(n), R, L])
+    ordr = np.lexsort((cols_, rows))
+    rows, cols_ = rows[ordr], cols_[ordr]
+    rp_real = np.zeros(n + 1, np.int64)
+    np.cumsum(deg, out=rp_real[1:])
+    # insert phantoms
+    counts = deg + boundary.astype(np.int64)
+    rp = np.zeros(n + 1, np.uint64)
+    np.cumsum(counts, out=rp[1:])
+    col = np.empty(int(rp[-1]), np.uint64)
+    pos_real = np.arange(rows.size) - rp_real[rows] + rp[rows].astype(np.int64)
+    col[pos_real] = cols_.astype(np.uint64)
+    col[(rp[1:].astype(np.int64) - 1)[boundary]] = PHANTOM
+    # values
+    rng1 = np.random.default_rng(seed + 1)
+    gamma = rng1.uniform(0.5, 2.0, size=L.size)
+    D = gamma * Amag / dist
+    F = np.zeros(L.size)
+    if peclet > 0:
+        u = _velocity(FC, np.random.default_rng(seed + 2))
+        F = np.einsum("ij,ij->i", u, A)
+        F *= peclet / np.max(np.abs(F) / D)
+    aLR = -D - np.maximum(-F, 0.0)
+    aRL = -D - np.maximum(F, 0.0)
+    val = np.zeros(col.size)
+    # position of (L, R) in row L and (R, L) in row R via searchsorted on keys
+    key_pos = pos_real
+    key = rows * np.int64(n) + cols_
+    def where(r, c):
+        return key_pos[np.searchsorted(key, r * np.int64(n) + c)]
+    val[where(L, R)] = aLR
+    val[where(R, L)] = aRL
+    offsum = np.zeros(n)
+    np.add.at(offsum, L, np.abs(aLR))
+    np.add.at(offsum, R, np.abs(aRL))
+    ratio = np.random.default_rng(seed + 3).uniform(1.01, 1.1, size=n)
+    val[where(np.arange(n), np.arange(n))] = ratio * offsum
+    b = np.random.default_rng(seed + 4).uniform(-1.0, 1.0, size=n)
+    return System(rp, col, val, b, f"tet{nx}x{ny}x{nz}_pe{peclet:g}")
+
+
+def random_rows_system(n: int, max_row: int, seed: int = 7, phantom_frac: float = 0.3) -> System:
+    """Ragged, diagonally dominant system with random sorted row patterns
+    (1..max_row entries per row, diagonal always present, some phantoms)."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for i in range(n):
+        k = int(rng.integers(0, max_row))
+        nb = rng.choice(n, size=min(k, n), replace=False) if n > 1 else np.array([], int)
+        cs = sorted(set(int(c) for c in nb) | {i})
+        rows.append(cs)
+    rp = np.zeros(n + 1, np.uint64)
+    cols, vals = [], []
+    for i, cs in enumerate(rows):
+        rowv = list(rng.uniform(-1.0, 1.0, size=len(cs)))
+        s = sum(abs(v) for c, v in zip(cs, rowv) if c != i)
+        rowv = [(s * rng.uniform(1.05, 1.5) + 0.1) if c == i else v for c, v in zip(cs, rowv)]
+        cols.extend(cs)
+        vals.extend(rowv)
+        if rng.uniform() < phantom_frac:
+            cols.append(int(PHANTOM))
+            vals.append(0.0)
+        rp[i + 1] = len(cols)
+    return System(rp, np.array(cols, np.uint64), np.array(vals), rng.uniform(-1, 1, size=n),
+                  f"random{n}_r{max_row}")

@@ -1,0 +1,275 @@
+"""TEST INFRASTRUCTURE ONLY -- Python access to the CPU oracle.
+
+Loads ``oracle/_build/libocsl_oracle.so`` (the C restatement of the reference's
+linear-solve path, see ``ocsl_oracle.h``) and, where it was built from the
+reference's own sources, ``oracle/_ref/liboracle_ref.so`` (the reference
+itself behind a small C-ABI harness).  Only tests, the smoke check and the
+CPU-baseline leg of the benchmark import this module; the product never does.
+
+All matrices use the reference's CSR layout (``cmatrix_solver.h:33-51``):
+``row_ptr`` and ``column_index`` as ``uint64`` (``size_t``) with the phantom
+column ``2**64 - 1`` on boundary rows, ``value`` as ``float64``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libocsl_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "liboracle_ref.so")
+REF_SHOCKTUBE = os.path.join(HERE, "_ref", "ref_shocktube")
+PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+_P = C.c_void_p
+_SZ = C.c_size_t
+
+
+def build(reference_dir: str | None = None) -> None:
+    """Compile the oracle (always) and the reference (when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    ref = reference_dir or "/root/reference"
+    if os.path.isfile(os.path.join(ref, "cmatrix_solver.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", f"REF={ref}"], check=True)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P) if a is not None else None
+
+
+class _Lib:
+    def __init__(self, path, protos):
+        self.lib = C.CDLL(path)
+        for name, (res, args) in protos.items():
+            f = getattr(self.lib, name)
+            f.restype = res
+            f.argtypes = args
+
+
+_CSR = [_SZ, _P, _P]
+_ORACLE_PROTOS = {
+    "orc_set_threads": (None, [C.c_int]),
+    "orc_dot": (C.c_double, [_SZ, _P, _P]),
+    "orc_dot_seq": (C.c_double, [_SZ, _P, _P]),
+    "orc_gemv": (None, _CSR + [_P, _P, C.c_int, C.c_double, _P, _P]),
+    "orc_extract_diag": (C.c_int, _CSR + [_P]),
+    "orc_ilu_fixed_point": (None, _CSR + [_P, _P, C.c_int, _P]),
+    "orc_forsub": (None, _CSR + [_P, _P, _P, _P]),
+    "orc_backsub": (None, _CSR + [_P, _P, _P, _P]),
+    "orc_cg_ref": (C.c_double, _CSR + [_P, _P, _P, _P]),
+    "orc_bicgstab_ref": (C.c_double, _CSR + [_P, _P, _P, _P]),
+    "orc_bicgstab_tol": (C.c_int, _CSR + [_P, _P, _P, C.c_double, C.c_int, C.c_int, _P, _P]),
+    "orc_pcg_tol": (C.c_int, _CSR + [_P, _P, _P, C.c_double, C.c_int, _P, _P]),
+    "orc_bicgstab_ir32": (C.c_int, _CSR + [_P, _P, _P, C.c_double, C.c_int, C.c_double,
+                                           C.c_int, C.c_int, _P, _P, _P]),
+    "orc_true_relres": (C.c_double, _CSR + [_P, _P, _P]),
+}
+_REF_CSR = [_SZ, _SZ, _P, _P]
+_REF_PROTOS = {
+    "refh_set_threads": (None, [C.c_int]),
+    "refh_cg_solve": (C.c_double, _REF_CSR + [_P, _P, _P]),
+    "refh_bicgstab_solve": (C.c_double, _REF_CSR + [_P, _P, _P]),
+    "refh_gemv": (None, _REF_CSR + [_P, C.c_double, _P, C.c_double, _P, _P]),
+    "refh_norm": (C.c_double, [_SZ, _P, _P]),
+    "refh_extract_diag": (None, _REF_CSR + [_P]),
+    "refh_ilu_decompose": (None, _REF_CSR + [_P, _P]),
+    "refh_forsub": (None, _REF_CSR + [_P, _P, _P]),
+    "refh_backsub": (None, _REF_CSR + [_P, _P, _P]),
+}
+
+
+def _c64(a, dtype=np.float64):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class Oracle:
+    """The C restatement.  Every method mirrors one reference function."""
+
+    def __init__(self, path: str = ORACLE_SO):
+        if not os.path.isfile(path):
+            raise FileNotFoundError(f"oracle library missing: {path} (run oracle.build())")
+        self._l = _Lib(path, _ORACLE_PROTOS).lib
+
+    def set_threads(self, t: int) -> None:
+        self._l.orc_set_threads(int(t))
+
+    def dot(self, x, y):
+        x, y = _c64(x), _c64(y)
+        return self._l.orc_dot(x.size, _ptr(x), _ptr(y))
+
+    def dot_seq(self, x, y):
+        x, y = _c64(x), _c64(y)
+        return self._l.orc_dot_seq(x.size, _ptr(x), _ptr(y))
+
+    @staticmethod
+    def _csr(rp, col):
+        return _c64(rp, np.uint64), _c64(col, np.uint64)
+
+    def gemv(self, rp, col, val, x, mode=0, a=0.0, z=None):
+        rp, col = self._csr(rp, col)
+        n = rp.size - 1
+        val, x = _c64(val), _c64(x)
+        z = _c64(z) if z is not None else None
+        y = np.zeros(n)
+        self._l.orc_gemv(n, _ptr(rp), _ptr(col), _ptr(val), _ptr(x), mode, a, _ptr(z), _ptr(y))
+        return y
+
+    def extract_diag(self, rp, col):
+        rp, col = self._csr(rp, col)
+        d = np.zeros(rp.size - 1, np.int32)
+        rc = self._l.orc_extract_diag(rp.size - 1, _ptr(rp), _ptr(col), _ptr(d))
+        return d, rc
+
+    def ilu(self, rp, col, A, sweeps=3):
+        rp, col = self._csr(rp, col)
+        d, _ = self.extract_diag(rp, col)
+        A = _c64(A)
+        M = np.zeros_like(A)
+        self._l.orc_ilu_fixed_point(rp.size - 1, _ptr(rp), _ptr(col), _ptr(A), _ptr(d), sweeps,
+                                    _ptr(M))
+        return M
+
+    def forsub(self, rp, col, M, b):
+        rp, col = self._csr(rp, col)
+        d, _ = self.extract_diag(rp, col)
+        M, b = _c64(M), _c64(b)
+        y = np.zeros(rp.size - 1)
+        self._l.orc_forsub(rp.size - 1, _ptr(rp), _ptr(col), _ptr(M), _ptr(d), _ptr(b), _ptr(y))
+        return y
+
+    def backsub(self, rp, col, M, y):
+        rp, col = self._csr(rp, col)
+        d, _ = self.extract_diag(rp, col)
+        M, y = _c64(M), _c64(y)
+        x = np.zeros(rp.size - 1)
+        self._l.orc_backsub(rp.size - 1, _ptr(rp), _ptr(col), _ptr(M), _ptr(d), _ptr(y), _ptr(x))
+        return x
+
+    def _solve_ref(self, fn, rp, col, val, b, x0):
+        rp, col = self._csr(rp, col)
+        val, b = _c64(val), _c64(b)
+        x = _c64(x0).copy()
+        it = C.c_int(0)
+        res = fn(rp.size - 1, _ptr(rp), _ptr(col), _ptr(val), _ptr(b), _ptr(x), C.byref(it))
+        return x, res, it.value
+
+    def cg_ref(self, rp, col, val, b, x0):
+        """cmatrix_solver.cpp:635 CG_solve -> (x, residual, iterations)."""
+        return self._solve_ref(self._l.orc_cg_ref, rp, col, val, b, x0)
+
+    def bicgstab_ref(self, rp, col, val, b, x0):
+        """cmatrix_solver.cpp:682 ILU_BICGSTAB_solve -> (x, residual, iterations)."""
+        return self._solve_ref(self._l.orc_bicgstab_ref, rp, col, val, b, x0)
+
+    def bicgstab_tol(self, rp, col, val, b, x0, tol=1e-10, maxit=2000, sweeps=3):
+        rp, col = self._csr(rp, col)
+        val, b = _c64(val), _c64(b)
+        x = _c64(x0).copy()
+        it, rr = C.c_int(0), C.c_double(0)
+        rc = self._l.orc_bicgstab_tol(rp.size - 1, _ptr(rp), _ptr(col), _ptr(val), _ptr(b),
+                                      _ptr(x), tol, maxit, sweeps, C.byref(it), C.byref(rr))
+        return x, rc, it.value, rr.value
+
+    def pcg_tol(self, rp, col, val, b, x0, tol=1e-10, maxit=5000):
+        rp, col = self._csr(rp, col)
+        val, b = _c64(val), _c64(b)
+        x = _c64(x0).copy()
+        it, rr = C.c_int(0), C.c_double(0)
+        rc = self._l.orc_pcg_tol(rp.size - 1, _ptr(rp), _ptr(col), _ptr(val), _ptr(b), _ptr(x),
+                                 tol, maxit, C.byref(it), C.byref(rr))
+        return x, rc, it.value, rr.value
+
+    def bicgstab_ir32(self, rp, col, val, b, x0, tol=1e-10, maxit=2000, inner_tol=1e-4,
+                      inner_maxit=200, sweeps=3):
+        rp, col = self._csr(rp, col)
+        val, b = _c64(val), _c64(b)
+        x = _c64(x0).copy()
+        it, out, rr = C.c_int(0), C.c_int(0), C.c_double(0)
+        rc = self._l.orc_bicgstab_ir32(rp.size - 1, _ptr(rp), _ptr(col), _ptr(val), _ptr(b),
+                                       _ptr(x), tol, maxit, inner_tol, inner_maxit, sweeps,
+                                       C.byref(it), C.byref(out), C.byref(rr))
+        return x, rc, it.value, out.value, rr.value
+
+    def true_relres(self, rp, col, val, b, x):
+        rp, col = self._csr(rp, col)
+        val, b, x = _c64(val), _c64(b), _c64(x)
+        return self._l.orc_true_relres(rp.size - 1, _ptr(rp), _ptr(col), _ptr(val), _ptr(b),
+                                       _ptr(x))
+
+
+def reference_available() -> bool:
+    return os.path.isfile(REF_SO)
+
+
+class Reference:
+    """The reference's own CMatrix_solver, built from its sources (oracle/_ref)."""
+
+    def __init__(self, path: str = REF_SO):
+        if not os.path.isfile(path):
+            raise FileNotFoundError(f"reference harness missing: {path}")
+        self._l = _Lib(path, _REF_PROTOS).lib
+        self._l.refh_set_threads(1)
+
+    def set_threads(self, t: int) -> None:
+        self._l.refh_set_threads(int(t))
+
+    @staticmethod
+    def _args(rp, col):
+        rp, col = _c64(rp, np.uint64), _c64(col, np.uint64)
+        return rp, col, rp.size - 1, col.size
+
+    def cg_solve(self, rp, col, val, b, x0):
+        rp, col, n, nnz = self._args(rp, col)
+        val, b, x = _c64(val), _c64(b), _c64(x0).copy()
+        res = self._l.refh_cg_solve(n, nnz, _ptr(rp), _ptr(col), _ptr(val), _ptr(b), _ptr(x))
+        return x, res
+
+    def bicgstab_solve(self, rp, col, val, b, x0):
+        rp, col, n, nnz = self._args(rp, col)
+        val, b, x = _c64(val), _c64(b), _c64(x0).copy()
+        res = self._l.refh_bicgstab_solve(n, nnz, _ptr(rp), _ptr(col), _ptr(val), _ptr(b),
+                                          _ptr(x))
+        return x, res
+
+    def gemv(self, rp, col, val, a, x, bcoef=0.0, z=None):
+        rp, col, n, nnz = self._args(rp, col)
+        val, x = _c64(val), _c64(x)
+        z = _c64(z) if z is not None else None
+        y = np.zeros(n)
+        self._l.refh_gemv(n, nnz, _ptr(rp), _ptr(col), _ptr(val), a, _ptr(x), bcoef, _ptr(z),
+                          _ptr(y))
+        return y
+
+    def norm(self, x, y):
+        x, y = _c64(x), _c64(y)
+        return self._l.refh_norm(x.size, _ptr(x), _ptr(y))
+
+    def extract_diag(self, rp, col):
+        rp, col, n, nnz = self._args(rp, col)
+        d = np.zeros(n, np.int32)
+        self._l.refh_extract_diag(n, nnz, _ptr(rp), _ptr(col), _ptr(d))
+        return d
+
+    def ilu_decompose(self, rp, col, A):
+        rp, col, n, nnz = self._args(rp, col)
+        A = _c64(A)
+        M = np.zeros_like(A)
+        self._l.refh_ilu_decompose(n, nnz, _ptr(rp), _ptr(col), _ptr(A), _ptr(M))
+        return M
+
+    def forsub(self, rp, col, M, b):
+        rp, col, n, nnz = self._args(rp, col)
+        M, b = _c64(M), _c64(b)
+        y = np.zeros(n)
+        self._l.refh_forsub(n, nnz, _ptr(rp), _ptr(col), _ptr(M), _ptr(b), _ptr(y))
+        return y
+
+    def backsub(self, rp, col, M, y):
+        rp, col, n, nnz = self._args(rp, col)
+        M, y = _c64(M), _c64(y)
+        x = np.zeros(n)
+        self._l.refh_backsub(n, nnz, _ptr(rp), _ptr(col), _ptr(M), _ptr(y), _ptr(x))
+        return x
