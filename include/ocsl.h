@@ -1,0 +1,141 @@
+/*
+ * ocsl.h -- C ABI of the GB300 (sm_103a) linear-solve library that replaces
+ * OpenCSLSolver's CMatrix_solver hot path (cmatrix_solver.h:27-95,
+ * cmatrix_solver.cpp:233-780).
+ *
+ * Data layout is the reference's own, so a caller hands over the members of
+ * CMatrix_solver unchanged:
+ *   row_ptr       size_t[n+1]      CCSR::row_ptr      (cmatrix_solver.h:40)
+ *   column_index  size_t[nnz]      CCSR::column_index (cmatrix_solver.h:41),
+ *                                  boundary rows carry a phantom column
+ *                                  (size_t)-1 with value 0 (cfvm.cpp:89-94);
+ *                                  it is accepted and skipped.
+ *   value         double[nnz]      CCSR::value        (cmatrix_solver.h:39)
+ *   b, x          double[n]        b_vector / x_vector (cmatrix_solver.h:88-89)
+ *
+ * Every function returns an ocsl_status.  Nothing falls back to the CPU: a
+ * process without a usable GPU gets OCSL_NO_DEVICE.  One context owns one
+ * CUDA stream on one device and is not re-entrant (like the reference's
+ * CMatrix_solver, which is driven from one thread, cflow_solver.cpp:289).
+ */
+#ifndef OCSL_H
+#define OCSL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ocsl_ctx ocsl_ctx;
+
+typedef enum {
+    OCSL_OK = 0,
+    OCSL_NOT_CONVERGED = 1, /* tolerance mode hit maxit (x holds the last iterate) */
+    OCSL_ZERO_PIVOT = 2,    /* a zero or non-finite pivot in the ILU factor       */
+    OCSL_NONFINITE = 3,     /* NaN/Inf met in the iteration                       */
+    OCSL_BAD_PATTERN = 4,   /* pattern rejected by ocsl_set_pattern               */
+    OCSL_TIMEOUT = 5,       /* a bounded device wait gave up (triangular sweep)   */
+    OCSL_CUDA_ERROR = 6,
+    OCSL_BAD_ARGUMENT = 7,
+    OCSL_NO_PATTERN = 8,    /* ocsl_set_pattern has not been called               */
+    OCSL_NO_DEVICE = 9,
+    OCSL_BREAKDOWN = 10     /* Krylov breakdown (rho, sigma or omega became 0)    */
+} ocsl_status;
+
+typedef enum {
+    /* Reference-faithful ("mode R"): the reference's own algorithms, fixed
+     * iteration counts, exits and return values.  Bit-identical to the
+     * restatement in oracle/ocsl_oracle.c.                                      */
+    OCSL_CG_REF = 0,            /* CMatrix_solver::CG_solve, cmatrix_solver.cpp:635-680          */
+    OCSL_BICGSTAB_REF = 1,      /* CMatrix_solver::ILU_BICGSTAB_solve, cmatrix_solver.cpp:682-762 */
+    /* Tolerance mode ("mode T"): run to ||b - A x||_2 / ||b||_2 <= tol.        */
+    OCSL_PCG = 2,               /* Jacobi-preconditioned CG, FP64 (symmetric systems)            */
+    OCSL_ILU_BICGSTAB = 3,      /* ILU(0)-BiCGSTAB, FP64, the reference's ILU factor             */
+    OCSL_ILU_BICGSTAB_IR32 = 4  /* FP32 ILU-BiCGSTAB inside FP64 iterative refinement            */
+} ocsl_method;
+
+typedef struct {
+    double tol;         /* relative residual target (mode T), default 1e-10            */
+    int maxit;          /* total Krylov iterations allowed (mode T), default 5000     */
+    int ilu_sweeps;     /* fixed-point ILU sweeps, default 3 (cmatrix_solver.cpp:521) */
+    double inner_tol;   /* IR32: inner relative reduction, default 1e-4               */
+    int inner_maxit;    /* IR32: iterations per inner solve, default 500              */
+} ocsl_opts;
+
+typedef struct {
+    double residual;    /* mode R: the value the reference function returns;
+                           mode T: final true relative residual (FP64)               */
+    int iterations;     /* iterations that updated x (mode T: total inner iterations) */
+    int outer_iterations; /* IR32 refinement steps                                   */
+    int status;         /* same as the return value                                 */
+    double solve_ms;    /* device time of the solve (CUDA events)                   */
+} ocsl_result;
+
+/* Fill *opts with the defaults above. */
+void ocsl_default_opts(ocsl_opts* opts);
+const char* ocsl_status_string(int status);
+/* Last error message of a context (or of creation when ctx is NULL). */
+const char* ocsl_last_error(const ocsl_ctx* ctx);
+/* Library version string. */
+const char* ocsl_version(void);
+
+/* Context.  Replaces the construction of CMatrix_solver
+ * (cmatrix_solver.cpp:30-34, called by cfvm.cpp:84). */
+int ocsl_create(ocsl_ctx** ctx, int device);
+int ocsl_destroy(ocsl_ctx* ctx);
+/* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
+int ocsl_set_stream(ocsl_ctx* ctx, void* stream);
+int ocsl_synchronize(ocsl_ctx* ctx);
+
+/* Fix the sparsity pattern once per run, as CFVM::define_matrix_structure
+ * does (cfvm.cpp:74-98) followed by extract_diag_indexes
+ * (cmatrix_solver.cpp:455-469).  Host pointers.  Builds the int32 device
+ * CSR, the diagonal map, the ILU product table and the level schedules of the
+ * triangular sweeps.  Rejects (OCSL_BAD_PATTERN) rows without a diagonal,
+ * columns >= n other than the phantom, and rows whose entries before / after
+ * the diagonal are not below / above it. */
+int ocsl_set_pattern(ocsl_ctx* ctx, size_t n, const size_t* row_ptr, const size_t* column_index);
+/* Host-only check of a pattern (no device needed): the same validation and
+ * level analysis as ocsl_set_pattern.  Writes the real nnz and the forward /
+ * backward level counts; on OCSL_BAD_PATTERN writes the reason into err. */
+int ocsl_check_pattern(size_t n, const size_t* row_ptr, const size_t* column_index,
+                       int64_t* nnz_real, int32_t* fw_levels, int32_t* bw_levels, char* err,
+                       size_t err_len);
+/* Pattern facts: n, stored nnz (with phantoms), real nnz, forward and
+ * backward level counts. */
+int ocsl_pattern_info(const ocsl_ctx* ctx, int64_t* n, int64_t* nnz, int64_t* nnz_real,
+                      int32_t* fw_levels, int32_t* bw_levels);
+
+/* One solve with HOST buffers: the drop-in for CMatrix_solver::solve()
+ * (cmatrix_solver.cpp:764-780) and, with OCSL_CG_REF / OCSL_BICGSTAB_REF, for
+ * CG_solve() / ILU_BICGSTAB_solve().  value and b are read, x is the initial
+ * guess on entry and the solution on return (x_vector is overwritten in
+ * place, as in the reference).  opts may be NULL (defaults). */
+int ocsl_solve(ocsl_ctx* ctx, int method, const double* value, const double* b, double* x,
+               const ocsl_opts* opts, ocsl_result* result);
+/* Same with DEVICE pointers (resident data, no host copies). */
+int ocsl_solve_device(ocsl_ctx* ctx, int method, const double* d_value, const double* d_b,
+                      double* d_x, const ocsl_opts* opts, ocsl_result* result);
+
+/* Kernel-level entry points on DEVICE pointers, one per reference routine. */
+/* y = A x (mode 0); y = z - A x (mode 1); y = fma(a, A x, z) (mode 2).
+ * cmatrix_solver.cpp:338-453 gemv. */
+int ocsl_gemv_device(ocsl_ctx* ctx, int mode, double a, const double* d_value, const double* d_x,
+                     const double* d_z, double* d_y);
+/* <x, y> in the library's fixed tile order; cmatrix_solver.cpp:233 norm. */
+int ocsl_dot_device(ocsl_ctx* ctx, size_t n, const double* d_x, const double* d_y,
+                    double* result);
+/* M = `sweeps` fixed-point ILU sweeps of A; cmatrix_solver.cpp:472-552. */
+int ocsl_ilu_device(ocsl_ctx* ctx, const double* d_A, double* d_M, int sweeps);
+/* y = L^-1 b, cmatrix_solver.cpp:555-572 ILU_forsub. */
+int ocsl_forsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_b, double* d_y);
+/* x = U^-1 y, cmatrix_solver.cpp:595-611 ILU_backsub. */
+int ocsl_backsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_y, double* d_x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OCSL_H */

@@ -1,0 +1,249 @@
+"""GB300-native replacement of OpenCSLSolver's linear-solve hot path.
+
+The product is the C-ABI library ``_lib/libocsl_gb300.so`` (include/ocsl.h),
+hand-written sm_103a kernels behind ``extern "C"`` entry points.  This module
+is the Python host side above that boundary:
+
+* ``Context``: one device context with a fixed CSR pattern (host arrays in the
+  reference layout, or device tensors for the resident-data entry points);
+* ``CMatrix_solver``: a mirror of the reference class (``cmatrix_solver.h:27-95``)
+  with the same members (``matrix`` with ``value``/``row_ptr``/``column_index``,
+  ``b_vector``, ``x_vector``) and entry points (``CG_solve``,
+  ``ILU_BICGSTAB_solve``, ``solve``), so code written against the reference
+  reads the same.
+
+Nothing here computes on the CPU: every numerical call goes through the CUDA
+library and fails loudly (``LibraryMissing`` / ``OcslError``) without it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import (BICGSTAB_REF, CG_REF, ILU_BICGSTAB, ILU_BICGSTAB_IR32, METHODS, PCG,
+                   LibraryMissing, OcslError, Opts, Result)
+
+PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+__all__ = ["Context", "CMatrix_solver", "check_pattern", "LibraryMissing", "OcslError",
+           "CG_REF", "BICGSTAB_REF", "PCG", "ILU_BICGSTAB", "ILU_BICGSTAB_IR32", "METHODS",
+           "PHANTOM"]
+
+
+def _method(m) -> int:
+    if isinstance(m, str):
+        return METHODS[m]
+    return int(m)
+
+
+def _u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def _dptr(t):
+    """Device pointer of a CUDA tensor (torch) or an integer address."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return C.c_void_p(t)
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("device entry points take contiguous CUDA tensors")
+    return C.c_void_p(t.data_ptr())
+
+
+def check_pattern(row_ptr, column_index):
+    """Host-only validation + level analysis (ocsl_check_pattern).
+
+    Returns ``(status, info)`` with ``info = {"nnz_real", "fw_levels",
+    "bw_levels", "error"}``.
+    """
+    rp, col = _u64(row_ptr), _u64(column_index)
+    nr, fw, bw = C.c_int64(0), C.c_int32(0), C.c_int32(0)
+    buf = C.create_string_buffer(512)
+    st = _abi.lib().ocsl_check_pattern(rp.size - 1, _ptr(rp), _ptr(col), C.byref(nr),
+                                       C.byref(fw), C.byref(bw), buf, 512)
+    return st, {"nnz_real": nr.value, "fw_levels": fw.value, "bw_levels": bw.value,
+                "error": buf.value.decode()}
+
+
+class Context:
+    """One GPU context (ocsl_create) holding one fixed CSR pattern."""
+
+    def __init__(self, device: int = 0):
+        self._L = _abi.lib()
+        h = C.c_void_p()
+        st = self._L.ocsl_create(C.byref(h), int(device))
+        if st != 0:
+            raise OcslError(st, self._L.ocsl_last_error(None).decode())
+        self._h = h
+        self.n = None
+        self.nnz = None
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ocsl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        if st not in (0,):
+            raise OcslError(st, f"{what}: {self._L.ocsl_status_string(st).decode()}: "
+                                f"{self._L.ocsl_last_error(self._h).decode()}")
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self._L.ocsl_set_stream(self._h, C.c_void_p(stream_handle or 0)),
+                    "set_stream")
+
+    def synchronize(self):
+        self._check(self._L.ocsl_synchronize(self._h), "synchronize")
+
+    # -- pattern (CFVM::define_matrix_structure, cfvm.cpp:74-98)
+    def set_pattern(self, row_ptr, column_index):
+        rp, col = _u64(row_ptr), _u64(column_index)
+        st = self._L.ocsl_set_pattern(self._h, rp.size - 1, _ptr(rp), _ptr(col))
+        self._check(st, "set_pattern")
+        self.n, self.nnz = rp.size - 1, col.size
+        return self
+
+    def pattern_info(self):
+        n, nnz, nr = C.c_int64(), C.c_int64(), C.c_int64()
+        fw, bw = C.c_int32(), C.c_int32()
+        self._check(self._L.ocsl_pattern_info(self._h, C.byref(n), C.byref(nnz), C.byref(nr),
+                                              C.byref(fw), C.byref(bw)), "pattern_info")
+        return {"n": n.value, "nnz": nnz.value, "nnz_real": nr.value, "fw_levels": fw.value,
+                "bw_levels": bw.value}
+
+    # -- solves
+    def solve(self, method, value, b, x, *, raise_on_status=False, **opts):
+        """Host-buffer solve (ocsl_solve).  ``x`` (float64 numpy) is updated in
+        place, as the reference overwrites x_vector.  Returns a result dict
+        with ``status``; ``raise_on_status`` turns non-OK statuses into errors."""
+        val, bb = _f64(value), _f64(b)
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
+            raise ValueError("x must be a C-contiguous float64 numpy array (updated in place)")
+        o = _abi.default_opts(**opts)
+        r = Result()
+        st = self._L.ocsl_solve(self._h, _method(method), _ptr(val), _ptr(bb), _ptr(x),
+                                C.byref(o), C.byref(r))
+        if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT, _abi.NO_PATTERN) or (raise_on_status and st):
+            self._check(st, "solve")
+        return r.as_dict()
+
+    def solve_device(self, method, value, b, x, *, raise_on_status=False, **opts):
+        """Resident-data solve (ocsl_solve_device) on CUDA tensors; x in/out."""
+        o = _abi.default_opts(**opts)
+        r = Result()
+        st = self._L.ocsl_solve_device(self._h, _method(method), _dptr(value), _dptr(b), _dptr(x),
+                                       C.byref(o), C.byref(r))
+        if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT, _abi.NO_PATTERN) or (raise_on_status and st):
+            self._check(st, "solve_device")
+        return r.as_dict()
+
+    # -- kernel-level entry points (device tensors)
+    def gemv_device(self, value, x, y, mode=0, a=0.0, z=None):
+        self._check(self._L.ocsl_gemv_device(self._h, mode, a, _dptr(value), _dptr(x), _dptr(z),
+                                             _dptr(y)), "gemv")
+
+    def dot_device(self, x, y):
+        out = C.c_double()
+        self._check(self._L.ocsl_dot_device(self._h, x.numel(), _dptr(x), _dptr(y),
+                                            C.byref(out)), "dot")
+        return out.value
+
+    def ilu_device(self, A, M, sweeps=3):
+        self._check(self._L.ocsl_ilu_device(self._h, _dptr(A), _dptr(M), sweeps), "ilu")
+
+    def forsub_device(self, M, b, y):
+        self._check(self._L.ocsl_forsub_device(self._h, _dptr(M), _dptr(b), _dptr(y)), "forsub")
+
+    def backsub_device(self, M, y, x):
+        self._check(self._L.ocsl_backsub_device(self._h, _dptr(M), _dptr(y), _dptr(x)),
+                    "backsub")
+
+
+class CMatrix_solver:
+    """Mirror of the reference class (cmatrix_solver.h:27-95) on the GPU library.
+
+    Members keep the reference's names and layout; ``CG_solve`` and
+    ``ILU_BICGSTAB_solve`` return what the reference returns (absolute /
+    relative squared residual) and overwrite ``x_vector.value``.  The pattern is
+    uploaded on the first solve and again only if row_ptr / column_index change.
+    """
+
+    class CCSR:
+        def __init__(self, n_rows=0, n_columns=0, n_nnz=0):
+            self.n_rows, self.n_columns, self.n_nnz = n_rows, n_columns, n_nnz
+            self.value = np.zeros(0)
+            self.row_ptr = np.zeros(n_rows + 1, np.uint64)
+            self.column_index = np.zeros(0, np.uint64)
+
+        def clear(self):  # cmatrix_solver.cpp:154-175
+            self.value[:] = 0.0
+
+    class Cvector:
+        def __init__(self, n_values=0):
+            self.n_values = n_values
+            self.value = np.zeros(n_values)
+
+        def clear(self):  # cmatrix_solver.cpp:209-230
+            self.value[:] = 0.0
+
+    def __init__(self, n_rows=0, n_columns=0, n_nnz=0, device=0, method="bicgstab_ref"):
+        self.matrix = self.CCSR(n_rows, n_columns, n_nnz)
+        self.b_vector = self.Cvector(n_rows)
+        self.x_vector = self.Cvector(n_rows)
+        self.method = method  # the reference's global MATRIX_SOLVER_TYPE
+        self.last_result = None
+        self._ctx = Context(device)
+        self._pattern_key = None
+
+    def _sync_pattern(self):
+        rp, col = _u64(self.matrix.row_ptr), _u64(self.matrix.column_index)
+        key = (rp.size, col.size, hash(rp.tobytes()), hash(col.tobytes()))
+        if key != self._pattern_key:
+            self._ctx.set_pattern(rp, col)
+            self._pattern_key = key
+
+    def _run(self, method, **opts):
+        self._sync_pattern()
+        x = np.ascontiguousarray(self.x_vector.value, dtype=np.float64).copy()
+        r = self._ctx.solve(method, self.matrix.value, self.b_vector.value, x, **opts)
+        if r["status"] not in (0, _abi.NOT_CONVERGED):
+            raise OcslError(r["status"], f"solve: {_abi.status_string(r['status'])}")
+        self.x_vector.value = x
+        self.last_result = r
+        return r
+
+    def CG_solve(self):
+        """cmatrix_solver.cpp:635-680: 4 iterations, returns ||r||^2."""
+        return self._run(CG_REF)["residual"]
+
+    def ILU_BICGSTAB_solve(self):
+        """cmatrix_solver.cpp:682-762: ILU + 3 iterations, returns ||r||^2/||b||^2."""
+        return self._run(BICGSTAB_REF)["residual"]
+
+    def solve(self, method=None, **opts):
+        """cmatrix_solver.cpp:764-780, with the method chosen per call."""
+        return self._run(_method(method if method is not None else self.method), **opts)

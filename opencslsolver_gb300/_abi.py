@@ -1,0 +1,117 @@
+"""ctypes binding of the C ABI declared in include/ocsl.h.
+
+Loads the in-tree ``_lib/libocsl_gb300.so``.  There is no fallback: if the
+library is missing, importing the package still works (so the pure-host parts
+and the docs stay usable), but every call that needs the library raises
+``LibraryMissing``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libocsl_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "ocsl.h")
+
+OK, NOT_CONVERGED, ZERO_PIVOT, NONFINITE, BAD_PATTERN, TIMEOUT = 0, 1, 2, 3, 4, 5
+CUDA_ERROR, BAD_ARGUMENT, NO_PATTERN, NO_DEVICE, BREAKDOWN = 6, 7, 8, 9, 10
+
+CG_REF, BICGSTAB_REF, PCG, ILU_BICGSTAB, ILU_BICGSTAB_IR32 = 0, 1, 2, 3, 4
+METHODS = {
+    "cg_ref": CG_REF,
+    "bicgstab_ref": BICGSTAB_REF,
+    "pcg": PCG,
+    "ilu_bicgstab": ILU_BICGSTAB,
+    "ilu_bicgstab_ir32": ILU_BICGSTAB_IR32,
+}
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+class OcslError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("ilu_sweeps", C.c_int),
+                ("inner_tol", C.c_double), ("inner_maxit", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("residual", C.c_double), ("iterations", C.c_int),
+                ("outer_iterations", C.c_int), ("status", C.c_int), ("solve_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_P = C.c_void_p
+_SZ = C.c_size_t
+_CTX = C.c_void_p
+_PROTOS = {
+    "ocsl_default_opts": (None, [C.POINTER(Opts)]),
+    "ocsl_status_string": (C.c_char_p, [C.c_int]),
+    "ocsl_last_error": (C.c_char_p, [_CTX]),
+    "ocsl_version": (C.c_char_p, []),
+    "ocsl_create": (C.c_int, [C.POINTER(_CTX), C.c_int]),
+    "ocsl_destroy": (C.c_int, [_CTX]),
+    "ocsl_set_stream": (C.c_int, [_CTX, _P]),
+    "ocsl_synchronize": (C.c_int, [_CTX]),
+    "ocsl_set_pattern": (C.c_int, [_CTX, _SZ, _P, _P]),
+    "ocsl_check_pattern": (C.c_int, [_SZ, _P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32), C.c_char_p, _SZ]),
+    "ocsl_pattern_info": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32)]),
+    "ocsl_solve": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts), C.POINTER(Result)]),
+    "ocsl_solve_device": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts),
+                                    C.POINTER(Result)]),
+    "ocsl_gemv_device": (C.c_int, [_CTX, C.c_int, C.c_double, _P, _P, _P, _P]),
+    "ocsl_dot_device": (C.c_int, [_CTX, _SZ, _P, _P, C.POINTER(C.c_double)]),
+    "ocsl_ilu_device": (C.c_int, [_CTX, _P, _P, C.c_int]),
+    "ocsl_forsub_device": (C.c_int, [_CTX, _P, _P, _P]),
+    "ocsl_backsub_device": (C.c_int, [_CTX, _P, _P, _P]),
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Names of every function include/ocsl.h declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ocsl_[a-z_0-9]+)\s*\(", text)))
+
+
+def lib():
+    """The loaded C library (raises LibraryMissing when it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            raise LibraryMissing(f"{LIB_PATH} is missing: run opencslsolver_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _PROTOS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(s: int) -> str:
+    return lib().ocsl_status_string(int(s)).decode()
+
+
+def default_opts(**kw) -> Opts:
+    o = Opts()
+    lib().ocsl_default_opts(C.byref(o))
+    for k, v in kw.items():
+        if v is not None:
+            setattr(o, k, v)
+    return o

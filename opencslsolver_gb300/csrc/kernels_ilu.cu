@@ -1,0 +1,342 @@
+// ILU factor (fixed-point sweeps) and the sync-free, level-ordered triangular
+// sweeps.
+//
+// Triangular sweeps (cmatrix_solver.cpp:555-572 forward, :595-611 backward)
+// keep the reference's natural ordering.  The host builds a level schedule
+// (level of a row = 1 + the deepest level it depends on) and cuts every level
+// into chunks of <= 256 rows; one CTA solves one chunk, one thread one row.
+// CTAs take chunks from an atomic dispenser in level order, so a CTA only
+// ever waits on rows of chunks that resident CTAs already hold: the sweep
+// cannot deadlock whatever the residency.
+//
+// The output vector is pre-filled with an all-ones bit pattern (a NaN no
+// arithmetic produces; a result that happens to carry it is stored as the
+// canonical NaN instead).  A row's thread reads each dependency with a relaxed
+// gpu-scope load until it differs from that pattern -- the value is its own
+// ready flag, so one L2 round trip serves both.  Every wait is bounded: after
+// the limit the thread records OCSL_TIMEOUT, stores a NaN (so nobody waits on
+// it in turn) and the host turns the flag into the solve's status.
+//
+// Each row's sum runs over its CSR entries in storage order with fma from 0,
+// exactly as the reference's sequential loop, so the schedule does not
+// change a single bit of the result.
+#include <cfloat>
+
+#include "ocsl_internal.cuh"
+
+namespace ocsl {
+
+namespace {
+
+constexpr long kSpinLimit = 1L << 21;  // polls per dependency: ~1 s with back-off
+
+template <typename T>
+struct Bits;
+template <>
+struct Bits<double> {
+    using U = unsigned long long;
+    static constexpr U kSentinel = ~0ull;
+    static constexpr U kCanonicalNaN = 0x7FF8000000000000ull;
+    static __device__ __forceinline__ U load(const double* p)
+    {
+        U v;
+        asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+        return v;
+    }
+    static __device__ __forceinline__ void store(double* p, U v)
+    {
+        asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    }
+    static __device__ __forceinline__ U to(double x) { return (U)__double_as_longlong(x); }
+    static __device__ __forceinline__ double from(U u) { return __longlong_as_double((long long)u); }
+};
+template <>
+struct Bits<float> {
+    using U = unsigned int;
+    static constexpr U kSentinel = ~0u;
+    static constexpr U kCanonicalNaN = 0x7FC00000u;
+    static __device__ __forceinline__ U load(const float* p)
+    {
+        U v;
+        asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        return v;
+    }
+    static __device__ __forceinline__ void store(float* p, U v)
+    {
+        asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    }
+    static __device__ __forceinline__ U to(float x) { return __float_as_uint(x); }
+    static __device__ __forceinline__ float from(U u) { return __uint_as_float(u); }
+};
+
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Wait (bounded) until out[j] holds a value, then return it.
+template <typename T>
+__device__ __forceinline__ T wait_value(const T* p, int* err)
+{
+    using B = Bits<T>;
+    typename B::U u = B::load(p);
+    if (u != B::kSentinel) return B::from(u);
+    unsigned ns = 0;
+    for (long it = 0; it < kSpinLimit; ++it) {
+        if (ns) __nanosleep(ns);
+        ns = ns == 0 ? (it > 32 ? 32u : 0u) : (ns < 256u ? ns * 2u : 256u);
+        u = B::load(p);
+        if (u != B::kSentinel) return B::from(u);
+        if ((it & 255) == 255 && *((volatile int*)err) != 0) break;  // another wait gave up
+    }
+    atomicCAS(err, 0, (int)OCSL_TIMEOUT);
+    return B::from(B::kCanonicalNaN);
+}
+
+template <typename T>
+__device__ __forceinline__ void publish(T* p, T v)
+{
+    using B = Bits<T>;
+    typename B::U u = B::to(v);
+    if (u == B::kSentinel) u = B::kCanonicalNaN;
+    B::store(p, u);
+}
+
+template <typename T>
+struct SweepParams {
+    int n;
+    const int* rp;
+    const int* col;
+    const int* diag;
+    const int* order;
+    const int* chunk;
+    int nchunks;
+    const T* M;
+    const T* dinv;
+    const T* rhs;
+    T* out;
+    SweepSync S;
+    const int* done;
+};
+
+__device__ __forceinline__ void sweep_epilogue(const SweepSync& S)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(S.finished, 1u) == gridDim.x - 1) {
+            *S.ticket = 0u;
+            *S.finished = 0u;
+        }
+    }
+}
+
+// y = L^-1 b with unit L (cmatrix_solver.cpp:558-571).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) fw_sweep_kernel(SweepParams<T> p)
+{
+    if (p.done && *p.done) return;
+    __shared__ int s_chunk;
+    if (threadIdx.x == 0) s_chunk = (int)atomicAdd(p.S.ticket, 1u);
+    __syncthreads();
+    const int c = s_chunk;
+    const int t = __ldg(p.chunk + c) + (int)threadIdx.x;
+    if (t < __ldg(p.chunk + c + 1)) {
+        const int i = __ldg(p.order + t);
+        const int b = __ldg(p.rp + i), d = __ldg(p.diag + i);
+        T sum = T(0);
+        for (int q = b; q < d; ++q) {
+            const int j = __ldg(p.col + q);
+            sum = fma_t(__ldg(p.M + q), wait_value(p.out + j, p.S.err), sum);
+        }
+        publish(p.out + i, p.rhs[i] - sum);
+    }
+    sweep_epilogue(p.S);
+}
+
+// x = U^-1 y (cmatrix_solver.cpp:598-610).  DIV: divide by the stored
+// diagonal as the reference does; otherwise multiply by a precomputed
+// reciprocal (tolerance mode).
+template <typename T, bool DIV>
+__global__ void __launch_bounds__(kThreads) bw_sweep_kernel(SweepParams<T> p)
+{
+    if (p.done && *p.done) return;
+    __shared__ int s_chunk;
+    if (threadIdx.x == 0) s_chunk = (int)atomicAdd(p.S.ticket, 1u);
+    __syncthreads();
+    const int c = s_chunk;
+    const int t = __ldg(p.chunk + c) + (int)threadIdx.x;
+    if (t < __ldg(p.chunk + c + 1)) {
+        const int i = __ldg(p.order + t);
+        const int d = __ldg(p.diag + i), e = __ldg(p.rp + i + 1);
+        T sum = T(0);
+        for (int q = d + 1; q < e; ++q) {
+            const int j = __ldg(p.col + q);
+            if (j < 0) continue;  // phantom: the reference adds 0 * x[-1]
+            sum = fma_t(__ldg(p.M + q), wait_value(p.out + j, p.S.err), sum);
+        }
+        const T num = p.rhs[i] - sum;
+        const T xi = DIV ? num / __ldg(p.M + d) : num * __ldg(p.dinv + i);
+        publish(p.out + i, xi);
+    }
+    sweep_epilogue(p.S);
+}
+
+struct IluParams {
+    int n;
+    const int* rp;
+    const int* col;
+    const int* diag;
+    const int* pair_ptr;
+    const int* pair_k;
+    const int* pair_slot;
+    const double* A;
+    const double* Mold;
+    double* Mnew;
+    double* dinv;
+    float* M32;
+    float* dinv32;
+    float* A32;
+    const int* done;
+};
+
+// One Jacobi sweep of the reference's fixed-point ILU (cmatrix_solver.cpp:525-549):
+//   lower  (col < i):  Mnew_ij = (A_ij - sum_k M_ik M_kj) / M_jj
+//   other           :  Mnew_ij =  A_ij - sum_k M_ik M_kj
+// with the products listed by the host in the reference's k order (the
+// table omits products whose CCSR::get_element would return 0).  Optional
+// outputs of the last sweep: reciprocal diagonal and FP32 copies.
+__global__ void __launch_bounds__(kThreads) ilu_sweep_kernel(IluParams p)
+{
+    if (p.done && *p.done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const int b = __ldg(p.rp + i), e = __ldg(p.rp + i + 1), di = __ldg(p.diag + i);
+    for (int j = b; j < e; ++j) {
+        const int c = __ldg(p.col + j);
+        double dum = 0.0;
+        const int q1 = __ldg(p.pair_ptr + j + 1);
+        for (int q = __ldg(p.pair_ptr + j); q < q1; ++q)
+            dum = fma(p.Mold[__ldg(p.pair_k + q)], p.Mold[__ldg(p.pair_slot + q)], dum);
+        const double a = p.A[j];
+        const double m = (c >= 0 && c < i) ? (a - dum) / p.Mold[__ldg(p.diag + c)] : a - dum;
+        p.Mnew[j] = m;
+        if (p.M32) p.M32[j] = (float)m;
+        if (p.A32) p.A32[j] = (float)a;
+        if (j == di) {
+            if (p.dinv) {
+                const double r = 1.0 / m;
+                p.dinv[i] = r;
+                if (p.dinv32) p.dinv32[i] = (float)r;
+            }
+        }
+    }
+}
+
+__global__ void factor_outputs_kernel(int n, const int* rp, const int* diag, const double* M,
+                                      const double* A, double* dinv, float* M32, float* dinv32,
+                                      float* A32)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = rp[i], e = rp[i + 1];
+    for (int j = b; j < e; ++j) {
+        if (M32) M32[j] = (float)M[j];
+        if (A32) A32[j] = (float)A[j];
+    }
+    const double r = 1.0 / M[diag[i]];
+    if (dinv) dinv[i] = r;
+    if (dinv32) dinv32[i] = (float)r;
+}
+
+template <typename T>
+SweepParams<T> make_sweep(const DevPattern& P, bool forward, const T* M, const T* dinv,
+                          const T* rhs, T* out, const SweepSync& S, const int* done)
+{
+    SweepParams<T> p;
+    p.n = P.n;
+    p.rp = P.rp;
+    p.col = P.col;
+    p.diag = P.diag;
+    p.order = forward ? P.fw_order : P.bw_order;
+    p.chunk = forward ? P.fw_chunk : P.bw_chunk;
+    p.nchunks = forward ? P.fw_nchunks : P.bw_nchunks;
+    p.M = M;
+    p.dinv = dinv;
+    p.rhs = rhs;
+    p.out = out;
+    p.S = S;
+    p.done = done;
+    return p;
+}
+
+}  // namespace
+
+template <typename T>
+void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* rhs, T* out,
+                     const SweepSync& S, const int* done)
+{
+    if (P.n == 0) return;
+    cudaMemsetAsync(out, 0xFF, sizeof(T) * (size_t)P.n, st);
+    auto p = make_sweep<T>(P, true, M, nullptr, rhs, out, S, done);
+    fw_sweep_kernel<T><<<p.nchunks, kThreads, 0, st>>>(p);
+}
+
+template <typename T>
+void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
+                     const T* rhs, T* out, int divmode, const SweepSync& S, const int* done)
+{
+    if (P.n == 0) return;
+    cudaMemsetAsync(out, 0xFF, sizeof(T) * (size_t)P.n, st);
+    auto p = make_sweep<T>(P, false, M, dinv, rhs, out, S, done);
+    if (divmode == 0)
+        bw_sweep_kernel<T, true><<<p.nchunks, kThreads, 0, st>>>(p);
+    else
+        bw_sweep_kernel<T, false><<<p.nchunks, kThreads, 0, st>>>(p);
+}
+
+template <typename T>
+void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
+                      double* dinv, float* M32, float* dinv32, float* A32, const int* done)
+{
+    static_assert(sizeof(T) == 8, "the ILU factor is computed in FP64");
+    if (P.n == 0) return;
+    IluParams p;
+    p.n = P.n;
+    p.rp = P.rp;
+    p.col = P.col;
+    p.diag = P.diag;
+    p.pair_ptr = P.pair_ptr;
+    p.pair_k = P.pair_k;
+    p.pair_slot = P.pair_slot;
+    p.A = A;
+    p.Mold = Mold;
+    p.Mnew = Mnew;
+    p.dinv = dinv;
+    p.M32 = M32;
+    p.dinv32 = dinv32;
+    p.A32 = A32;
+    p.done = done;
+    ilu_sweep_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(p);
+}
+
+void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
+                           double* dinv, float* M32, float* dinv32, float* A32)
+{
+    if (P.n == 0) return;
+    factor_outputs_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+        P.n, P.rp, P.diag, M, A, dinv, M32, dinv32, A32);
+}
+
+template void launch_fw_sweep<double>(cudaStream_t, const DevPattern&, const double*,
+                                      const double*, double*, const SweepSync&, const int*);
+template void launch_fw_sweep<float>(cudaStream_t, const DevPattern&, const float*, const float*,
+                                     float*, const SweepSync&, const int*);
+template void launch_bw_sweep<double>(cudaStream_t, const DevPattern&, const double*,
+                                      const double*, const double*, double*, int,
+                                      const SweepSync&, const int*);
+template void launch_bw_sweep<float>(cudaStream_t, const DevPattern&, const float*, const float*,
+                                     const float*, float*, int, const SweepSync&, const int*);
+template void launch_ilu_sweep<double>(cudaStream_t, const DevPattern&, const double*,
+                                       const double*, double*, double*, float*, float*, float*,
+                                       const int*);
+
+}  // namespace ocsl

@@ -1,0 +1,605 @@
+// SpMV, fused vector updates and tile-order reductions for the Krylov solvers.
+//
+// Every kernel here is a "tile kernel": CTA b owns rows / elements
+// [2048 b, 2048 b + 2048); thread t handles 2048 b + 256 j + t for j = 0..7,
+// so all global traffic is coalesced and every fused dot product is
+// accumulated in the tile order the CPU oracle restates (ocsl_oracle.h).
+// The last CTA to finish (atomic ticket) reduces the per-tile partial sums and
+// applies a small scalar epilogue (alpha, omega, convergence tests), so the
+// Krylov scalars never leave the device.
+//
+// Rounding follows the reference's expressions (cmatrix_solver.cpp): fma where
+// the reference computes a*x + y, separately rounded operations elsewhere;
+// the library is compiled with --fmad=false so that only explicit fma fuses.
+#include <cfloat>
+#include <cstdio>
+
+#include "ocsl_internal.cuh"
+
+namespace ocsl {
+
+namespace {
+
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <int MASK>
+struct DotCount {
+    static constexpr int value = ((MASK & 1) ? 1 : 0) + ((MASK & 2) ? 1 : 0) + ((MASK & 4) ? 1 : 0);
+};
+
+// Per-thread dot accumulator.  FP64 vectors: fma chain from 0.0 (tile order).
+// FP32 vectors: compensated FP32 (exact product split + TwoSum, Ogita, Rump &
+// Oishi 2005), folded into FP64 before the warp butterfly.
+template <typename T>
+struct DotAcc;
+
+template <>
+struct DotAcc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct DotAcc<float> {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float a, float b)
+    {
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);
+        const float t = s + p;
+        const float bp = t - s;
+        const float err = (s - (t - bp)) + (p - bp);
+        s = t;
+        c = c + (err + e);
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+__device__ __forceinline__ double warp_butterfly(double v)
+{
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Reduce ND lane values of a CTA to ND sums (valid in thread 0):
+// butterfly per warp, then the 8 warp sums in order.
+template <int ND>
+__device__ __forceinline__ void cta_sum(double (&v)[ND], double* s_red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        const double w = warp_butterfly(v[k]);
+        if (lane == 0) s_red[k * 8 + warp] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+            double s = s_red[k * 8];
+            for (int w = 1; w < kThreads / 32; ++w) s = s + s_red[k * 8 + w];
+            v[k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+__device__ void apply_epilogue(int epi, const double* s, int nd, Scalars* sc, int it, int maxit)
+{
+    for (int k = 0; k < nd && k < 4; ++k) sc->sum[k] = s[k];
+    switch (epi) {
+    // ---- CG_solve, cmatrix_solver.cpp:635-680
+    case EP_RC_INIT:
+        sc->rr = s[0];
+        sc->iters = 0;
+        break;
+    case EP_RC_ALPHA:  // a = norm(r,r) / (norm(p,dum) + 1e-40), :660
+        sc->alpha = sc->rr / (s[0] + 1.0e-40);
+        break;
+    case EP_RC_RES:  // res = norm(r_next, r_next); exit if < 1e-6, :667-672
+        sc->res = s[0];
+        sc->iters = it + 1;
+        if (s[0] < 1.0e-6) {
+            sc->done = 1;
+        } else {
+            sc->beta = s[0] / (sc->rr + 1.0e-40);
+            sc->rr = s[0];
+        }
+        break;
+    // ---- ILU_BICGSTAB_solve, cmatrix_solver.cpp:682-762
+    case EP_RB_INIT: {  // r = b - A x; r0 = r; iteration 0's rhon and res
+        sc->rr = s[0];
+        sc->bb = s[1];
+        sc->rhon = s[0];
+        const double res = s[0] / s[1] + DBL_MIN;  // :733
+        sc->res = res;
+        sc->iters = 0;
+        if (res < 1.0e-20) sc->done = 1;           // :734-735
+        break;
+    }
+    case EP_RB_ALPHA:  // alpha = rhon / (norm(r0, v) + DBL_MIN), :727-728
+        sc->alpha = sc->rhon / (s[0] + DBL_MIN);
+        break;
+    case EP_RB_OMEGA:  // omega = norm(dum, dum2) / (norm(dum, dum) + 1e-40), :750
+        sc->omega = s[0] / (s[1] + 1.0e-40);
+        break;
+    case EP_RB_RUPD:  // end of iteration `it`: next iteration's rhon and res
+        sc->iters = it + 1;
+        if (it + 1 < maxit) {
+            sc->rhon = s[0];
+            sc->rr = s[1];
+            const double res = s[1] / sc->bb + DBL_MIN;
+            sc->res = res;
+            if (res < 1.0e-20) sc->done = 1;
+        }
+        break;
+    // ---- tolerance-mode BiCGSTAB (van der Vorst 1992)
+    case EP_TB_INIT:  // s0 = <r,r>, s1 = <b,b>
+        sc->rr = s[0];
+        sc->bb = s[1];
+        sc->rnorm = sqrt(s[0]);
+        sc->res = s[1] > 0.0 ? sqrt(s[0] / s[1]) : 0.0;
+        sc->rho = s[0];
+        sc->sum[3] = sc->rnorm > 0.0 ? 1.0 / sc->rnorm : 0.0;
+        if (!isfinite(s[0]) || !isfinite(s[1])) {
+            sc->status = OCSL_NONFINITE;
+            sc->done = 1;
+        } else if (s[1] == 0.0 || s[0] <= sc->tol2 * s[1]) {
+            sc->done = 1;
+        }
+        break;
+    case EP_TB_SIGMA:  // sigma = <r^, v>
+        sc->sigma = s[0];
+        if (s[0] == 0.0 || !isfinite(s[0])) {
+            sc->breakdown = 1;
+            sc->done = 1;
+        } else {
+            sc->alpha = sc->rho / s[0];
+        }
+        break;
+    case EP_TB_S:  // <s,s>: half-step convergence test
+        sc->ss = s[0];
+        sc->iters += 1;
+        if (!isfinite(s[0])) {
+            sc->status = OCSL_NONFINITE;
+            sc->done = 1;
+        } else if (s[0] <= sc->tol2 * sc->bb) {
+            sc->half = 1;
+            sc->done = 1;
+        }
+        break;
+    case EP_TB_OMEGA:  // s0 = <t,t>, s1 = <s,t>
+        sc->omega = s[0] != 0.0 ? s[1] / s[0] : 0.0;
+        break;
+    case EP_TB_RUPD: {  // s0 = <r,r>, s1 = <r^,r>
+        sc->rr = s[0];
+        if (!isfinite(s[0])) {
+            sc->status = OCSL_NONFINITE;
+            sc->done = 1;
+        } else if (s[0] <= sc->tol2 * sc->bb) {
+            sc->done = 1;
+        } else if (sc->omega == 0.0 || sc->rho == 0.0) {
+            sc->breakdown = 1;
+            sc->done = 1;
+        } else {
+            sc->beta = (s[1] / sc->rho) * (sc->alpha / sc->omega);
+            sc->rho = s[1];
+        }
+        break;
+    }
+    case EP_TRUE_RES:
+        sc->rr = s[0];
+        sc->res = s[1] > 0.0 ? sqrt(s[0] / s[1]) : 0.0;
+        break;
+    // ---- tolerance-mode Jacobi PCG
+    case EP_PC_INIT:  // rho = <r,z>
+        sc->rho = s[0];
+        break;
+    case EP_PC_ALPHA:  // <p, q>
+        if (s[0] == 0.0 || !isfinite(s[0])) {
+            sc->breakdown = 1;
+            sc->done = 1;
+        } else {
+            sc->alpha = sc->rho / s[0];
+        }
+        break;
+    case EP_PC_RUPD:  // s0 = <r,r>, s1 = <r,z>
+        sc->rr = s[0];
+        sc->iters += 1;
+        if (!isfinite(s[0])) {
+            sc->status = OCSL_NONFINITE;
+            sc->done = 1;
+        } else if (s[0] <= sc->tol2 * sc->bb) {
+            sc->done = 1;
+        } else if (sc->rho == 0.0) {
+            sc->breakdown = 1;
+            sc->done = 1;
+        } else {
+            sc->beta = s[1] / sc->rho;
+            sc->rho = s[1];
+        }
+        break;
+    case EP_IR_INNER_INIT:  // inner residual target relative to ||r32||^2
+        sc->rr = s[0];
+        sc->bb = s[0];
+        sc->rho = s[0];
+        if (!(s[0] > 0.0) || !isfinite(s[0])) sc->done = 1;
+        break;
+    default:
+        break;
+    }
+}
+
+// Store this CTA's tile partials; if it is the last CTA, reduce all tiles and
+// apply the epilogue.  Must be reached by every thread of every CTA.
+template <int ND>
+__device__ __forceinline__ void finish_reduction(double (&v)[ND], int tile, int ntiles,
+                                                 const ReduceState& R, Scalars* sc, int epi,
+                                                 int it, int maxit, double* s_red, int* s_last)
+{
+    cta_sum<ND>(v, s_red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < ND; ++k) R.partials[k * R.max_tiles + tile] = v[k];
+        __threadfence();
+        const unsigned prev = atomicAdd(R.counter, 1u);
+        *s_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!*s_last) return;
+    __threadfence();
+    double acc[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        double a = 0.0;
+        for (int t = threadIdx.x; t < ntiles; t += kThreads) a = a + __ldcg(R.partials + k * R.max_tiles + t);
+        acc[k] = a;
+    }
+    cta_sum<ND>(acc, s_red);
+    if (threadIdx.x == 0) {
+        if (sc) apply_epilogue(epi, acc, ND, sc, it, maxit);
+        *R.counter = 0u;
+    }
+}
+
+template <typename T>
+struct SpmvParams {
+    int n;
+    const int* rp;
+    const int* col;
+    const T* val;
+    const T* x;
+    T* y;
+    const T* z;
+    T* y_copy;
+    const T* w;
+    T a;
+    ReduceState R;
+    Scalars* sc;
+    int epi, it, maxit;
+};
+
+// y = A x (MODE 0), y = z - A x (MODE 1), y = fma(a, A x, z) (MODE 2);
+// cmatrix_solver.cpp:338-453.  Each 256-row slab of the tile is staged
+// into shared memory with coalesced loads; each thread then sums its row in
+// CSR storage order with fma from 0.0 (:346-350), skipping phantom columns.
+template <typename T, int MODE, int DOTS>
+__global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
+{
+    if (p.sc && p.sc->done) return;
+    constexpr int ND = DotCount<DOTS>::value;
+    __shared__ T s_val[kSpmvCap];
+    __shared__ int s_col[kSpmvCap];
+    __shared__ double s_red[kMaxDots * 8];
+    __shared__ int s_last;
+    const int tile = blockIdx.x;
+    const int n = p.n;
+    DotAcc<T> acc[ND > 0 ? ND : 1];
+
+#pragma unroll 1
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int r0 = tile * kTile + j * kThreads;
+        if (r0 >= n) break;  // uniform over the CTA
+        const int r1 = min(r0 + kThreads, n);
+        const int q0 = __ldg(p.rp + r0), q1 = __ldg(p.rp + r1);
+        const bool staged = (q1 - q0) <= kSpmvCap;
+        if (staged) {
+            for (int q = q0 + (int)threadIdx.x; q < q1; q += kThreads) {
+                s_val[q - q0] = __ldg(p.val + q);
+                s_col[q - q0] = __ldg(p.col + q);
+            }
+        }
+        __syncthreads();
+        const int row = r0 + (int)threadIdx.x;
+        if (row < n) {
+            const int b = __ldg(p.rp + row), e = __ldg(p.rp + row + 1);
+            T dum = T(0);
+            if (staged) {
+                for (int q = b - q0; q < e - q0; ++q) {
+                    const int c = s_col[q];
+                    if (c >= 0) dum = fma_t(s_val[q], __ldg(p.x + c), dum);
+                }
+            } else {
+                for (int q = b; q < e; ++q) {
+                    const int c = __ldg(p.col + q);
+                    if (c >= 0) dum = fma_t(__ldg(p.val + q), __ldg(p.x + c), dum);
+                }
+            }
+            T y, zv = T(0);
+            if constexpr (MODE == 0) {
+                y = dum;
+            } else if constexpr (MODE == 1) {
+                zv = p.z[row];
+                y = zv - dum;
+            } else {
+                zv = p.z[row];
+                y = fma_t(p.a, dum, zv);
+            }
+            p.y[row] = y;
+            if (MODE == 1 && p.y_copy) p.y_copy[row] = y;
+            int k = 0;
+            if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
+            if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
+            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(p.w[row], y);
+            (void)k;
+        }
+        __syncthreads();
+    }
+    if constexpr (ND > 0) {
+        double v[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) v[k] = acc[k].value();
+        finish_reduction<ND>(v, tile, gridDim.x, p.R, p.sc, p.epi, p.it, p.maxit, s_red, &s_last);
+    }
+}
+
+template <int OP>
+struct OpDots {
+    static constexpr int value =
+        (OP == V_RB_XR || OP == V_DOT2 || OP == V_TB_XR || OP == V_PC_XRZ) ? 2
+        : (OP == V_DOT1 || OP == V_RC_XR || OP == V_TB_S || OP == V_PC_INIT || OP == V_IR_SCALE) ? 1
+                                                                                                  : 0;
+};
+
+struct VecParams {
+    int n;
+    VecPtrs p;
+    ReduceState R;
+    Scalars* sc;
+    const Scalars* outer;
+    int epi, it, maxit;
+};
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
+{
+    if constexpr (OP == V_TB_HALF) {
+        if (!P.sc->half) return;
+    } else if constexpr (OP == V_IR_SCALE || OP == V_IR_UPDATE) {
+        if (P.outer->done) return;
+    } else if (P.sc && P.sc->done) {
+        return;
+    }
+    constexpr int ND = OpDots<OP>::value;
+    __shared__ double s_red[kMaxDots * 8];
+    __shared__ int s_last;
+    const int tile = blockIdx.x;
+    const int n = P.n;
+    T* const* v = reinterpret_cast<T* const*>(P.p.v);
+
+    // Scalars of this step, read once per thread (written by earlier kernels).
+    const double alpha = P.sc ? P.sc->alpha : 0.0;
+    const double omega = P.sc ? P.sc->omega : 0.0;
+    const double beta = P.sc ? P.sc->beta : 0.0;
+    const T a = (T)alpha, w = (T)omega, be = (T)beta;
+    DotAcc<T> acc[ND > 0 ? ND : 1];
+
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int e = tile * kTile + j * kThreads + (int)threadIdx.x;
+        if (e >= n) continue;
+        if constexpr (OP == V_RB_P) {  // :718-720
+            const T dum = fma_t(-w, v[1][e], v[0][e]);
+            v[0][e] = fma_t(w, dum, v[2][e]);
+        } else if constexpr (OP == V_RB_HS) {  // :731, :738
+            v[0][e] = fma_t(a, v[2][e], v[1][e]);
+            v[3][e] = fma_t(-a, v[4][e], v[5][e]);
+        } else if constexpr (OP == V_RB_XR) {  // :753, :756, next :714 and :733
+            v[0][e] = fma_t(w, v[1][e], v[2][e]);
+            const T r = fma_t(-w, v[4][e], v[5][e]);
+            v[3][e] = r;
+            acc[0].add(v[6][e], r);
+            acc[1].add(r, r);
+        } else if constexpr (OP == V_DOT2) {
+            const T x = v[0][e];
+            acc[0].add(x, v[1][e]);
+            acc[1].add(x, x);
+        } else if constexpr (OP == V_DOT1) {
+            acc[0].add(v[0][e], v[1][e]);
+        } else if constexpr (OP == V_RC_XR) {  // :662-667
+            v[0][e] = fma_t(a, v[1][e], v[0][e]);
+            const T rn = fma_t(-a, v[3][e], v[4][e]);
+            v[2][e] = rn;
+            acc[0].add(rn, rn);
+        } else if constexpr (OP == V_RC_P) {  // :674
+            v[0][e] = fma_t(be, v[0][e], v[1][e]);
+        } else if constexpr (OP == V_TB_S) {
+            const T s = fma_t(-a, v[1][e], v[2][e]);
+            v[0][e] = s;
+            acc[0].add(s, s);
+        } else if constexpr (OP == V_TB_XR) {
+            v[0][e] = fma_t(w, v[2][e], fma_t(a, v[1][e], v[0][e]));
+            const T r = fma_t(-w, v[4][e], v[5][e]);
+            v[3][e] = r;
+            acc[0].add(r, r);
+            acc[1].add(v[6][e], r);
+        } else if constexpr (OP == V_TB_P) {
+            v[0][e] = fma_t(be, fma_t(-w, v[1][e], v[0][e]), v[2][e]);
+        } else if constexpr (OP == V_TB_HALF) {
+            v[0][e] = fma_t(a, v[1][e], v[0][e]);
+        } else if constexpr (OP == V_COPY2) {
+            const T r = v[2][e];
+            v[0][e] = r;
+            v[1][e] = r;
+        } else if constexpr (OP == V_PC_INIT) {
+            const T r = v[2][e];
+            const T z = r * v[3][e];
+            v[0][e] = z;
+            v[1][e] = z;
+            acc[0].add(r, z);
+        } else if constexpr (OP == V_PC_XRZ) {
+            v[0][e] = fma_t(a, v[1][e], v[0][e]);
+            const T r = fma_t(-a, v[3][e], v[2][e]);
+            v[2][e] = r;
+            const T z = r * v[5][e];
+            v[4][e] = z;
+            acc[0].add(r, r);
+            acc[1].add(r, z);
+        } else if constexpr (OP == V_PC_P) {
+            v[0][e] = fma_t(be, v[0][e], v[1][e]);
+        } else if constexpr (OP == V_IR_SCALE) {
+            const double* r = reinterpret_cast<const double*>(P.p.v[0]);
+            const float f = (float)(r[e] * P.outer->sum[3]);
+            reinterpret_cast<float*>(P.p.v[1])[e] = f;
+            reinterpret_cast<float*>(P.p.v[2])[e] = f;
+            reinterpret_cast<float*>(P.p.v[3])[e] = f;
+            reinterpret_cast<float*>(P.p.v[4])[e] = 0.0f;
+            acc[0].add(f, f);
+        } else if constexpr (OP == V_IR_UPDATE) {
+            double* x = reinterpret_cast<double*>(P.p.v[0]);
+            const float d = reinterpret_cast<const float*>(P.p.v[1])[e];
+            x[e] = fma((double)d, P.outer->rnorm, x[e]);
+        }
+    }
+    if constexpr (ND > 0) {
+        double vals[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) vals[k] = acc[k].value();
+        finish_reduction<ND>(vals, tile, gridDim.x, P.R, P.sc, P.epi, P.it, P.maxit, s_red,
+                             &s_last);
+    }
+}
+
+__global__ void convert_kernel(int n, const double* in, float* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
+inline int ntiles_of(int n) { return (n + kTile - 1) / kTile; }
+
+template <typename T, int MODE, int DOTS>
+void spmv_dispatch(cudaStream_t st, const SpmvParams<T>& p)
+{
+    const int nt = ntiles_of(p.n);
+    if (nt == 0) return;
+    spmv_kernel<T, MODE, DOTS><<<nt, kThreads, 0, st>>>(p);
+}
+
+template <typename T, int MODE>
+void spmv_dots(cudaStream_t st, const SpmvParams<T>& p, int dots)
+{
+    switch (dots) {
+    case 0: spmv_dispatch<T, MODE, 0>(st, p); break;
+    case DOT_YY: spmv_dispatch<T, MODE, DOT_YY>(st, p); break;
+    case DOT_YY | DOT_ZZ: spmv_dispatch<T, MODE, DOT_YY | DOT_ZZ>(st, p); break;
+    case DOT_WY: spmv_dispatch<T, MODE, DOT_WY>(st, p); break;
+    case DOT_YY | DOT_WY: spmv_dispatch<T, MODE, DOT_YY | DOT_WY>(st, p); break;
+    default: break;
+    }
+}
+
+template <typename T, int OP>
+void vec_dispatch(cudaStream_t st, const VecParams& P)
+{
+    const int nt = ntiles_of(P.n);
+    if (nt == 0) return;
+    vec_kernel<T, OP><<<nt, kThreads, 0, st>>>(P);
+}
+
+}  // namespace
+
+template <typename T>
+void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x, T* y, int mode,
+                 const double* /*scal_a*/, double a_const, const T* z, T* y_copy, const T* w,
+                 int dots, const ReduceState& R, Scalars* sc, int epi, int it, int maxit)
+{
+    SpmvParams<T> p;
+    p.n = P.n;
+    p.rp = P.rp;
+    p.col = P.col;
+    p.val = val;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.y_copy = y_copy;
+    p.w = w;
+    p.a = (T)a_const;
+    p.R = R;
+    p.sc = sc;
+    p.epi = epi;
+    p.it = it;
+    p.maxit = maxit;
+    switch (mode) {
+    case 0: spmv_dots<T, 0>(st, p, dots); break;
+    case 1: spmv_dots<T, 1>(st, p, dots); break;
+    default: spmv_dots<T, 2>(st, p, dots); break;
+    }
+}
+
+template <typename T>
+void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& ptrs, const ReduceState& R,
+                Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit)
+{
+    VecParams P;
+    P.n = n;
+    P.p = ptrs;
+    P.R = R;
+    P.sc = sc;
+    P.outer = sc_outer;
+    P.epi = epi;
+    P.it = it;
+    P.maxit = maxit;
+    switch (op) {
+    case V_RB_P: vec_dispatch<T, V_RB_P>(st, P); break;
+    case V_RB_HS: vec_dispatch<T, V_RB_HS>(st, P); break;
+    case V_RB_XR: vec_dispatch<T, V_RB_XR>(st, P); break;
+    case V_DOT2: vec_dispatch<T, V_DOT2>(st, P); break;
+    case V_DOT1: vec_dispatch<T, V_DOT1>(st, P); break;
+    case V_RC_XR: vec_dispatch<T, V_RC_XR>(st, P); break;
+    case V_RC_P: vec_dispatch<T, V_RC_P>(st, P); break;
+    case V_TB_S: vec_dispatch<T, V_TB_S>(st, P); break;
+    case V_TB_XR: vec_dispatch<T, V_TB_XR>(st, P); break;
+    case V_TB_P: vec_dispatch<T, V_TB_P>(st, P); break;
+    case V_TB_HALF: vec_dispatch<T, V_TB_HALF>(st, P); break;
+    case V_COPY2: vec_dispatch<T, V_COPY2>(st, P); break;
+    case V_PC_INIT: vec_dispatch<T, V_PC_INIT>(st, P); break;
+    case V_PC_XRZ: vec_dispatch<T, V_PC_XRZ>(st, P); break;
+    case V_PC_P: vec_dispatch<T, V_PC_P>(st, P); break;
+    case V_IR_SCALE: vec_dispatch<float, V_IR_SCALE>(st, P); break;
+    case V_IR_UPDATE: vec_dispatch<float, V_IR_UPDATE>(st, P); break;
+    default: break;
+    }
+}
+
+void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out)
+{
+    if (n <= 0) return;
+    convert_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, in, out);
+}
+
+template void launch_spmv<double>(cudaStream_t, const DevPattern&, const double*, const double*,
+                                  double*, int, const double*, double, const double*, double*,
+                                  const double*, int, const ReduceState&, Scalars*, int, int, int);
+template void launch_spmv<float>(cudaStream_t, const DevPattern&, const float*, const float*,
+                                 float*, int, const double*, double, const float*, float*,
+                                 const float*, int, const ReduceState&, Scalars*, int, int, int);
+template void launch_vec<double>(cudaStream_t, int, int, const VecPtrs&, const ReduceState&,
+                                 Scalars*, const Scalars*, int, int, int);
+template void launch_vec<float>(cudaStream_t, int, int, const VecPtrs&, const ReduceState&,
+                                Scalars*, const Scalars*, int, int, int);
+
+}  // namespace ocsl

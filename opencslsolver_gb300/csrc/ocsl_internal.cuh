@@ -1,0 +1,149 @@
+// Internal declarations shared by the library's translation units.
+//
+// Device layout (one context, one pattern, sizes for the 128^3 hex case in
+// brackets):
+//   rp    int32[n+1]  row pointers            [8.4 MB]
+//   col   int32[nnz]  columns, phantom -> -1  [58.7 MB]
+//   diag  int32[n]    position of (i, i)      [8.4 MB]
+//   pair_ptr/k/slot   ILU product table: for stored entry j of row i, the
+//                     positions (k, slot) of the products M_ik * M_(col k, col j)
+//                     the reference's fixed-point sweep adds, in its order
+//   fw_order/fw_chunk, bw_order/bw_chunk: level schedules of the sweeps
+//   values double[nnz] (and float[nnz] copies for the FP32 inner solver)
+//   vectors double[n] / float[n]
+//
+// Reductions follow the "tile order" (see tile_reduce below), which the CPU
+// oracle restates exactly, so reduced scalars are bit-identical to it.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ocsl.h"
+
+namespace ocsl {
+
+constexpr int kThreads = 256;          // threads per CTA of every tile kernel
+constexpr int kRowsPerThread = 8;      // rows / elements per thread per tile
+constexpr int kTile = kThreads * kRowsPerThread;  // 2048 rows per tile
+constexpr int kSpmvCap = 2560;         // staged nnz per 256-row slab
+constexpr int kMaxDots = 3;
+
+// Scalars of one Krylov iteration, resident on the device.  Reduction
+// epilogues write them, vector kernels read them; the host reads the block
+// only to decide whether to stop.
+struct Scalars {
+    double rr, bb, rho, rhon, alpha, omega, beta, ss, res, rnorm, tol2, sigma;
+    double sum[4];   // raw results of the last reduction
+    int done;        // set -> every later kernel of the solve returns at once
+    int half;        // tolerance mode: converged at the half step, x += alpha p^ pending
+    int iters;       // iterations that updated x
+    int breakdown;   // Krylov breakdown seen
+    int status;      // ocsl_status of the device side
+    int pad[3];
+};
+
+// Epilogue applied by the last CTA of a reduction to the reduced sums.
+enum EpiOp : int {
+    EP_STORE = 0,
+    // reference CG (cmatrix_solver.cpp:635-680)
+    EP_RC_INIT, EP_RC_ALPHA, EP_RC_RES,
+    // reference ILU-BiCGSTAB (cmatrix_solver.cpp:682-762)
+    EP_RB_INIT, EP_RB_ALPHA, EP_RB_OMEGA, EP_RB_RUPD,
+    // tolerance-mode BiCGSTAB
+    EP_TB_INIT, EP_TB_SIGMA, EP_TB_S, EP_TB_OMEGA, EP_TB_RUPD, EP_TRUE_RES,
+    // tolerance-mode PCG
+    EP_PC_INIT, EP_PC_ALPHA, EP_PC_RUPD,
+    // FP32 inner solve of the refinement loop: s0 = <r32, r32>
+    EP_IR_INNER_INIT,
+};
+
+// Dot-product selection of a fused kernel (bit mask, slots in this order).
+enum DotSel : int { DOT_YY = 1, DOT_ZZ = 2, DOT_WY = 4 };
+
+struct ReduceState {
+    double* partials;    // [kMaxDots][max_tiles]
+    unsigned* counter;   // CTAs finished (reset by the last one)
+    int max_tiles;
+};
+
+struct DevPattern {
+    int n;
+    int nnz;
+    const int* rp;
+    const int* col;
+    const int* diag;
+    const int* pair_ptr;
+    const int* pair_k;
+    const int* pair_slot;
+    const int* fw_order;
+    const int* fw_chunk;
+    int fw_nchunks;
+    const int* bw_order;
+    const int* bw_chunk;
+    int bw_nchunks;
+};
+
+struct SweepSync {
+    unsigned* ticket;    // chunk dispenser (reset by the last CTA)
+    unsigned* finished;
+    int* err;            // ocsl_status of a bounded wait that gave up
+};
+
+// ------------------------------------------------------------------ host-side launchers
+// All launchers enqueue on `st` and never synchronise.
+
+template <typename T>
+void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x, T* y,
+                 int mode, const double* scal_a, double a_const, const T* z, T* y_copy,
+                 const T* w, int dots, const ReduceState& R, Scalars* sc, int epi, int it,
+                 int maxit);
+
+// Vector kernels: the op decides which pointers it uses.
+enum VecOp : int {
+    V_RB_P = 0,   // dum = fma(-w, v, p); p = fma(w, dum, r)
+    V_RB_HS,      // h = fma(a, y, x); s = fma(-a, v, r)
+    V_RB_XR,      // x = fma(w, z, h); r = fma(-w, t, s); dots <r0,r>, <r,r>
+    V_DOT2,       // dots <a,b>, <a,a>
+    V_DOT1,       // dot <a,b>
+    V_RC_XR,      // x = fma(a, p, x); rn = fma(-a, q, r); dot <rn,rn>
+    V_RC_P,       // p = fma(beta, p, rn)
+    V_TB_S,       // s = fma(-a, v, r); dot <s,s>
+    V_TB_XR,      // x = fma(w, sh, fma(a, ph, x)); r = fma(-w, t, s); dots <r,r>, <rh,r>
+    V_TB_P,       // p = fma(beta, fma(-w, v, p), r)
+    V_TB_HALF,    // if half: x = fma(a, ph, x)
+    V_COPY2,      // u = r; v = r
+    V_PC_INIT,    // z = r * dinv; p = z; dot <r,z>
+    V_PC_XRZ,     // x = fma(a,p,x); r = fma(-a,q,r); z = r*dinv; dots <r,r>, <r,z>
+    V_PC_P,       // p = fma(beta, p, z)
+    V_IR_SCALE,   // f0 = float(r * (1/rnorm)); f1 = f0; f2 = f0; f3 = 0; dot <f0,f0>
+    V_IR_UPDATE,  // x = fma(double(f0), rnorm, x)
+};
+
+struct VecPtrs {
+    void* v[8];
+};
+
+template <typename T>
+void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& p, const ReduceState& R,
+                Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit);
+
+template <typename T>
+void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
+                      double* dinv, float* M32, float* dinv32, float* A32, const int* done);
+
+template <typename T>
+void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* rhs, T* out,
+                     const SweepSync& S, const int* done);
+// divmode 0: divide by M_ii (reference); 1: multiply by dinv
+template <typename T>
+void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
+                     const T* rhs, T* out, int divmode, const SweepSync& S, const int* done);
+
+void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out);
+
+// Factor side outputs without a sweep: dinv = 1 / M_ii and FP32 copies.
+void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
+                           double* dinv, float* M32, float* dinv32, float* A32);
+
+}  // namespace ocsl

@@ -1,0 +1,150 @@
+// Host-side analysis of the fixed CSR pattern (done once per run, like the
+// reference's CFVM::define_matrix_structure, cfvm.cpp:74-98).
+//
+// Produces everything the device needs besides values:
+//   * int32 CSR with the phantom column (size_t)-1 mapped to -1;
+//   * the diagonal positions (extract_diag_indexes, cmatrix_solver.cpp:455-469);
+//   * the ILU product table: for stored entry j of row i, the pairs (k, slot)
+//     such that the reference's sweep (cmatrix_solver.cpp:527-547) adds
+//     M[k] * M.get_element(col[k], col[j]) with a match at `slot`, in the
+//     reference's k order; products whose get_element finds nothing add an
+//     exact 0 and are left out;
+//   * level schedules of the forward (strict lower part) and backward
+//     (strict upper part) sweeps, each level cut into chunks of <= 256 rows.
+#include "pattern.h"
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+
+namespace ocsl {
+
+namespace {
+
+constexpr uint64_t kPhantom = ~uint64_t(0);
+
+bool fail(std::string& err, const char* fmt, long long a, long long b = 0)
+{
+    char buf[256];
+    std::snprintf(buf, sizeof buf, fmt, a, b);
+    err = buf;
+    return false;
+}
+
+void schedule(int n, const std::vector<int>& level, int nlevels, std::vector<int>& order,
+              std::vector<int>& chunk, int chunk_rows)
+{
+    std::vector<int> count(nlevels + 1, 0);
+    for (int i = 0; i < n; ++i) ++count[level[i] + 1];
+    for (int l = 0; l < nlevels; ++l) count[l + 1] += count[l];
+    std::vector<int> start(count.begin(), count.end() - 1);
+    order.assign(n, 0);
+    for (int i = 0; i < n; ++i) order[start[level[i]]++] = i;  // ascending rows per level
+    chunk.clear();
+    for (int l = 0; l < nlevels; ++l) {
+        for (int b = count[l]; b < count[l + 1]; b += chunk_rows) chunk.push_back(b);
+    }
+    chunk.push_back(n);
+}
+
+}  // namespace
+
+bool analyse_pattern(size_t n_in, const size_t* rp, const size_t* col, HostPattern& hp,
+                     std::string& err)
+{
+    if (n_in >= (size_t)INT_MAX) return fail(err, "n = %lld exceeds the int32 limit", (long long)n_in);
+    const int n = (int)n_in;
+    hp = HostPattern();
+    hp.n = n;
+    if (n == 0) {
+        hp.rp.assign(1, 0);
+        hp.fw_chunk.assign(1, 0);
+        hp.bw_chunk.assign(1, 0);
+        hp.pair_ptr.assign(1, 0);
+        return true;
+    }
+    if (!rp || !col) return fail(err, "null row_ptr or column_index (n = %lld)", n);
+    if (rp[0] != 0) return fail(err, "row_ptr[0] = %lld, expected 0", (long long)rp[0]);
+    for (int i = 0; i < n; ++i)
+        if (rp[i + 1] < rp[i]) return fail(err, "row_ptr decreases at row %lld", i);
+    if (rp[n] >= (size_t)INT_MAX) return fail(err, "nnz = %lld exceeds the int32 limit", (long long)rp[n]);
+    const int nnz = (int)rp[n];
+    hp.nnz = nnz;
+    hp.rp.resize(n + 1);
+    hp.col.resize(nnz);
+    hp.diag.resize(n);
+    for (int i = 0; i <= n; ++i) hp.rp[i] = (int)rp[i];
+
+    for (int i = 0; i < n; ++i) {
+        int d = -1;
+        for (int q = hp.rp[i]; q < hp.rp[i + 1]; ++q) {
+            const uint64_t c = col[q];
+            if (c >= (uint64_t)n && c != kPhantom)
+                return fail(err, "row %lld: column %lld out of range", i, (long long)c);
+            hp.col[q] = c == kPhantom ? -1 : (int)c;
+            if (c != kPhantom) ++hp.nnz_real;
+            if (d < 0 && c == (uint64_t)i) d = q;
+        }
+        if (d < 0) return fail(err, "row %lld has no diagonal entry", i);
+        hp.diag[i] = d;
+        for (int q = hp.rp[i]; q < d; ++q)
+            if (!(col[q] < (uint64_t)i))
+                return fail(err, "row %lld: entry before the diagonal is not below it (col %lld)", i,
+                            (long long)col[q]);
+        for (int q = d + 1; q < hp.rp[i + 1]; ++q)
+            if (!(col[q] > (uint64_t)i))
+                return fail(err, "row %lld: entry after the diagonal is not above it (col %lld)", i,
+                            (long long)col[q]);
+    }
+
+    // ILU product table.
+    hp.pair_ptr.assign(nnz + 1, 0);
+    hp.pair_k.clear();
+    hp.pair_slot.clear();
+    for (int i = 0; i < n; ++i) {
+        const int b = hp.rp[i], e = hp.rp[i + 1], d = hp.diag[i];
+        for (int j = b; j < e; ++j) {
+            const uint64_t cj = col[j];
+            const bool lower = cj != kPhantom && (uint64_t)i > cj;
+            const int kend = lower ? j : d;
+            for (int k = b; k < kend; ++k) {
+                const uint64_t r = col[k];  // a row index: entries before the diagonal are < i
+                int slot = -1;
+                for (size_t q = rp[r]; q < rp[r + 1]; ++q)
+                    if (col[q] == cj) { slot = (int)q; break; }
+                if (slot >= 0) {
+                    if (hp.pair_k.size() >= (size_t)INT_MAX)
+                        return fail(err, "ILU product table exceeds the int32 limit at row %lld", i);
+                    hp.pair_k.push_back(k);
+                    hp.pair_slot.push_back(slot);
+                }
+            }
+            hp.pair_ptr[j + 1] = (int)hp.pair_k.size();
+        }
+    }
+
+    // Level schedules.
+    std::vector<int> level(n, 0);
+    int nl = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int q = hp.rp[i]; q < hp.diag[i]; ++q) l = std::max(l, level[hp.col[q]] + 1);
+        level[i] = l;
+        nl = std::max(nl, l + 1);
+    }
+    hp.fw_levels = nl;
+    schedule(n, level, nl, hp.fw_order, hp.fw_chunk, kChunkRows);
+    nl = 0;
+    for (int i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int q = hp.diag[i] + 1; q < hp.rp[i + 1]; ++q)
+            if (hp.col[q] >= 0) l = std::max(l, level[hp.col[q]] + 1);
+        level[i] = l;
+        nl = std::max(nl, l + 1);
+    }
+    hp.bw_levels = nl;
+    schedule(n, level, nl, hp.bw_order, hp.bw_chunk, kChunkRows);
+    return true;
+}
+
+}  // namespace ocsl

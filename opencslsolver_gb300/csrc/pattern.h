@@ -1,0 +1,29 @@
+// Host-side pattern analysis (see pattern.cpp).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ocsl {
+
+constexpr int kChunkRows = 256;  // rows per chunk of a sweep level (one CTA)
+
+struct HostPattern {
+    int n = 0;
+    int nnz = 0;
+    long long nnz_real = 0;
+    int fw_levels = 0;
+    int bw_levels = 0;
+    std::vector<int> rp, col, diag;
+    std::vector<int> pair_ptr, pair_k, pair_slot;
+    std::vector<int> fw_order, fw_chunk, bw_order, bw_chunk;
+};
+
+// Validate the reference-layout pattern and build the device tables.
+// Returns false with a message on a rejected pattern.
+bool analyse_pattern(size_t n, const size_t* row_ptr, const size_t* column_index, HostPattern& hp,
+                     std::string& err);
+
+}  // namespace ocsl

@@ -1,0 +1,899 @@
+// Context, pattern upload, Krylov drivers and the extern "C" boundary
+// (include/ocsl.h).
+//
+// Drivers enqueue every kernel of a solve on the context's stream; the Krylov
+// scalars live on the device (Scalars) and every kernel returns at once when
+// `done` is set, so the reference-faithful solvers (at most 4 / 3 iterations)
+// run without a single host round trip, and the tolerance-mode solvers look at
+// the scalars only between batches of iterations, one batch ahead.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ocsl_internal.cuh"
+#include "pattern.h"
+
+using namespace ocsl;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+const char* kVersion = "ocsl-gb300 0.1 (sm_103a)";
+
+struct CudaError {
+    cudaError_t code;
+    const char* what;
+};
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) throw CudaError{e_, #call};    \
+    } while (0)
+
+template <typename T>
+T* dalloc(size_t count)
+{
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc(&p, count * sizeof(T)));
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+T* upload(const std::vector<T>& v)
+{
+    T* d = dalloc<T>(v.size());
+    if (!v.empty()) CK(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return d;
+}
+
+// Fixed-iteration counts and exits of the reference (cmatrix_solver.cpp:637,684).
+constexpr int kRefCgIters = 4;
+constexpr int kRefBicgIters = 3;
+
+enum Vec64 { R, P, Q, RN, V, R0, S, DUM, H, T, Y, Z, DUM2, PH, SH, RH, TMP, NVEC64 };
+enum Vec32 { F_RI, F_RH, F_P, F_PH, F_V, F_S, F_SH, F_T, F_TMP, F_D, NVEC32 };
+
+}  // namespace
+
+struct ocsl_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+
+    bool has_pattern = false;
+    HostPattern hp;  // kept for ocsl_pattern_info
+    DevPattern P{};
+    int* d_pat[10] = {};
+
+    double* d_A = nullptr;  // values of host-buffer solves
+    double* d_b = nullptr;
+    double* d_x = nullptr;
+    double* d_Ma = nullptr;
+    double* d_Mb = nullptr;
+    double* d_dinv = nullptr;
+    double* v64[NVEC64] = {};
+    float* d_A32 = nullptr;
+    float* d_M32 = nullptr;
+    float* d_dinv32 = nullptr;
+    float* v32[NVEC32] = {};
+
+    ReduceState R{};
+    Scalars* d_sc = nullptr;  // [0] main / outer, [1] inner, [2] utility
+    Scalars* h_sc = nullptr;  // pinned mirrors, 2 slots x 3 blocks
+    SweepSync S{};
+    unsigned* d_sync = nullptr;
+    int* d_err = nullptr;
+    int* h_err = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    cudaEvent_t ev_batch[2] = {nullptr, nullptr};
+
+    void free_pattern();
+    void free_all();
+    void ensure_reduce(int ntiles);
+    void ensure_fp32();
+};
+
+void ocsl_ctx::free_pattern()
+{
+    for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
+    double** d64[] = {&d_A, &d_b, &d_x, &d_Ma, &d_Mb, &d_dinv};
+    for (auto pp : d64) { if (*pp) cudaFree(*pp); *pp = nullptr; }
+    for (auto& v : v64) { if (v) cudaFree(v); v = nullptr; }
+    float** d32[] = {&d_A32, &d_M32, &d_dinv32};
+    for (auto pp : d32) { if (*pp) cudaFree(*pp); *pp = nullptr; }
+    for (auto& v : v32) { if (v) cudaFree(v); v = nullptr; }
+    has_pattern = false;
+    P = DevPattern{};
+}
+
+void ocsl_ctx::free_all()
+{
+    free_pattern();
+    if (R.partials) cudaFree(R.partials);
+    if (R.counter) cudaFree(R.counter);
+    R = ReduceState{};
+    if (d_sc) cudaFree(d_sc);
+    if (h_sc) cudaFreeHost(h_sc);
+    if (d_sync) cudaFree(d_sync);
+    if (d_err) cudaFree(d_err);
+    if (h_err) cudaFreeHost(h_err);
+    d_sc = nullptr; h_sc = nullptr; d_sync = nullptr; d_err = nullptr; h_err = nullptr;
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+    for (auto& e : ev_batch) { if (e) cudaEventDestroy(e); e = nullptr; }
+    if (own_stream) cudaStreamDestroy(own_stream);
+    own_stream = stream = nullptr;
+}
+
+void ocsl_ctx::ensure_reduce(int ntiles)
+{
+    ntiles = std::max(ntiles, 1);
+    if (R.partials && R.max_tiles >= ntiles) return;
+    if (R.partials) CK(cudaFree(R.partials));
+    R.partials = dalloc<double>((size_t)kMaxDots * ntiles);
+    R.max_tiles = ntiles;
+    if (!R.counter) {
+        R.counter = dalloc<unsigned>(1);
+        CK(cudaMemset(R.counter, 0, sizeof(unsigned)));
+    }
+}
+
+void ocsl_ctx::ensure_fp32()
+{
+    if (d_A32) return;
+    const size_t n = (size_t)P.n, nnz = (size_t)P.nnz;
+    d_A32 = dalloc<float>(nnz);
+    d_M32 = dalloc<float>(nnz);
+    d_dinv32 = dalloc<float>(n);
+    for (auto& v : v32) v = dalloc<float>(n);
+}
+
+namespace {
+
+int fail(ocsl_ctx* c, int status, const std::string& msg)
+{
+    if (c) c->last_error = msg;
+    return status;
+}
+
+int from_cuda(ocsl_ctx* c, const CudaError& e)
+{
+    std::string msg = std::string(e.what) + ": " + cudaGetErrorString(e.code);
+    return fail(c, OCSL_CUDA_ERROR, msg);
+}
+
+ocsl_opts resolve(const ocsl_opts* o)
+{
+    ocsl_opts d;
+    ocsl_default_opts(&d);
+    if (!o) return d;
+    ocsl_opts r = *o;
+    if (!(r.tol > 0.0)) r.tol = d.tol;
+    if (r.maxit <= 0) r.maxit = d.maxit;
+    if (r.ilu_sweeps < 0) r.ilu_sweeps = d.ilu_sweeps;
+    if (!(r.inner_tol > 0.0)) r.inner_tol = d.inner_tol;
+    if (r.inner_maxit <= 0) r.inner_maxit = d.inner_maxit;
+    return r;
+}
+
+// ------------------------------------------------------------------ helpers
+
+struct Solve {
+    ocsl_ctx* c;
+    cudaStream_t st;
+    const DevPattern& P;
+    int n;
+
+    Scalars* sc(int k) const { return c->d_sc + k; }
+
+    void reset_scalars(int k, double tol2, double omega0 = 1.0)
+    {
+        Scalars s;
+        std::memset(&s, 0, sizeof s);
+        s.tol2 = tol2;
+        s.alpha = 1.0;
+        s.omega = omega0;
+        s.rhon = 1.0;
+        s.rho = 1.0;
+        // pinned staging slots 3..5 are private to these uploads
+        Scalars* stage = c->h_sc + 3 + k;
+        CK(cudaStreamSynchronize(st));  // the staging slot may still be in flight
+        *stage = s;
+        CK(cudaMemcpyAsync(c->d_sc + k, stage, sizeof(Scalars), cudaMemcpyHostToDevice, st));
+    }
+    Scalars read_scalars(int k)
+    {
+        CK(cudaMemcpyAsync(c->h_sc + k, c->d_sc + k, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return c->h_sc[k];
+    }
+    const int* done(int k) const { return &c->d_sc[k].done; }
+
+    template <typename TT>
+    void spmv(const TT* val, const TT* x, TT* y, int mode, const TT* z, TT* ycopy, const TT* w,
+              int dots, int k, int epi, int it = 0, int maxit = 0)
+    {
+        launch_spmv<TT>(st, P, val, x, y, mode, nullptr, 0.0, z, ycopy, w, dots, c->R,
+                        k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+    }
+    template <typename TT>
+    void vec(int op, std::initializer_list<const void*> ptrs, int k, int epi, int it = 0,
+             int maxit = 0)
+    {
+        VecPtrs vp{};
+        int i = 0;
+        for (const void* p : ptrs) vp.v[i++] = const_cast<void*>(p);
+        launch_vec<TT>(st, op, n, vp, c->R, k >= 0 ? sc(k) : nullptr, sc(0), epi, it, maxit);
+    }
+    // Fixed-point ILU factor (cmatrix_solver.cpp:702-704): M starts as A,
+    // `sweeps` Jacobi sweeps; returns the buffer holding the factor.  The
+    // last sweep also writes the reciprocal diagonal and the FP32 copies
+    // when asked; with zero sweeps the factor is A itself.
+    const double* factor(const double* A, int sweeps, bool want_dinv, bool want_fp32, int k)
+    {
+        const int* dn = k >= 0 ? done(k) : nullptr;
+        double* dinv = want_dinv ? c->d_dinv : nullptr;
+        float* M32 = want_fp32 ? c->d_M32 : nullptr;
+        float* dinv32 = want_fp32 ? c->d_dinv32 : nullptr;
+        float* A32 = want_fp32 ? c->d_A32 : nullptr;
+        if (sweeps == 0) {
+            if (want_dinv || want_fp32) launch_factor_outputs(st, P, A, A, dinv, M32, dinv32, A32);
+            return A;
+        }
+        const double* src = A;
+        double* bufs[2] = {c->d_Ma, c->d_Mb};
+        for (int s = 0; s < sweeps; ++s) {
+            double* dst = bufs[s & 1];
+            const bool last = s == sweeps - 1;
+            launch_ilu_sweep<double>(st, P, A, src, dst, last ? dinv : nullptr,
+                                     last ? M32 : nullptr, last ? dinv32 : nullptr,
+                                     last ? A32 : nullptr, dn);
+            src = dst;
+        }
+        return src;
+    }
+    template <typename TT>
+    void fw(const TT* M, const TT* rhs, TT* out, int k)
+    {
+        launch_fw_sweep<TT>(st, P, M, rhs, out, c->S, k >= 0 ? done(k) : nullptr);
+    }
+    template <typename TT>
+    void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k)
+    {
+        launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S, k >= 0 ? done(k) : nullptr);
+    }
+    int device_error()
+    {
+        CK(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return *c->h_err;
+    }
+};
+
+// ------------------------------------------------------------------ reference-faithful
+
+// CMatrix_solver::CG_solve (cmatrix_solver.cpp:635-680).
+void run_cg_ref(Solve& s, const double* A, const double* b, double* x)
+{
+    double** v = s.c->v64;
+    s.reset_scalars(0, 0.0);
+    // r = b - A x (:652), p = r (:655), rr = <r,r>
+    s.spmv<double>(A, x, v[R], 1, b, v[P], nullptr, DOT_YY, 0, EP_RC_INIT);
+    double* r = v[R];
+    double* rn = v[RN];
+    for (int it = 0; it < kRefCgIters; ++it) {
+        // q = A p (:659), a = rr / (<p,q> + 1e-40) (:660)
+        s.spmv<double>(A, v[P], v[Q], 0, nullptr, nullptr, v[P], DOT_WY, 0, EP_RC_ALPHA);
+        // x += a p (:662-663); r_next = r - a A p (:665); res = <r_next, r_next> (:667)
+        s.vec<double>(V_RC_XR, {x, v[P], rn, v[Q], r}, 0, EP_RC_RES, it, kRefCgIters);
+        // p = r_next + beta p (:674)
+        s.vec<double>(V_RC_P, {v[P], rn}, 0, EP_STORE);
+        std::swap(r, rn);  // :676
+    }
+}
+
+// CMatrix_solver::ILU_BICGSTAB_solve (cmatrix_solver.cpp:682-762), quirks kept:
+// omega in the direction update, rho never updated, the residual test on the
+// r from the start of the iteration, x not updated on that exit.
+void run_bicgstab_ref(Solve& s, const double* A, const double* b, double* x, int sweeps)
+{
+    double** v = s.c->v64;
+    const size_t bytes = sizeof(double) * (size_t)s.n;
+    s.reset_scalars(0, 0.0);
+    CK(cudaMemsetAsync(v[P], 0, bytes, s.st));  // Cvector(n) starts at 0 (:690-700)
+    CK(cudaMemsetAsync(v[V], 0, bytes, s.st));
+    const double* M = s.factor(A, sweeps, false, false, 0);  // :702-704
+    // r = b - A x (:708), r0 = r (:710), iteration 0's rhon and res
+    s.spmv<double>(A, x, v[R], 1, b, v[R0], nullptr, DOT_YY | DOT_ZZ, 0, EP_RB_INIT);
+    for (int it = 0; it < kRefBicgIters; ++it) {
+        s.vec<double>(V_RB_P, {v[P], v[V], v[R]}, 0, EP_STORE);                 // :718-720
+        s.fw<double>(M, v[P], v[DUM], 0);                                       // :722
+        s.bw<double>(M, nullptr, v[DUM], v[Y], 0, 0);                           // :723
+        s.spmv<double>(A, v[Y], v[V], 0, nullptr, nullptr, v[R0], DOT_WY, 0, EP_RB_ALPHA);  // :725-728
+        s.vec<double>(V_RB_HS, {v[H], x, v[Y], v[S], v[V], v[R]}, 0, EP_STORE);  // :731, :738
+        s.fw<double>(M, v[S], v[DUM2], 0);                                      // :741 (= :747)
+        s.bw<double>(M, nullptr, v[DUM2], v[Z], 0, 0);                          // :742
+        s.spmv<double>(A, v[Z], v[T], 0, nullptr, nullptr, nullptr, 0, 0, EP_STORE);  // :744
+        s.fw<double>(M, v[T], v[DUM], 0);                                       // :746
+        s.vec<double>(V_DOT2, {v[DUM], v[DUM2]}, 0, EP_RB_OMEGA);              // :750
+        s.vec<double>(V_RB_XR, {x, v[Z], v[H], v[R], v[T], v[S], v[R0]}, 0, EP_RB_RUPD, it,
+                      kRefBicgIters);                                            // :753, :756
+    }
+}
+
+// ------------------------------------------------------------------ tolerance mode
+
+struct TolResult {
+    int iters = 0;
+    int outer = 0;
+    double relres = 0.0;
+    int status = OCSL_OK;
+};
+
+constexpr int kBatch = 2;  // iterations enqueued between looks at the scalars
+
+// Run enqueue(it) for at most `budget` iterations, in batches of kBatch, until
+// scalars block k reports done.  Two batches are kept in flight: while the GPU
+// runs one, the host inspects the scalars copied after the previous one.
+// Batches enqueued after convergence cost only no-op launches.
+template <typename F>
+Scalars run_batches(Solve& s, int k, int budget, F&& enqueue)
+{
+    Scalars* slot = s.c->h_sc + 6;  // two pinned inspection slots
+    int it = 0, issued = 0, inspected = 0;
+    while (true) {
+        while (issued - inspected < 2 && it < budget) {
+            const int m = std::min(kBatch, budget - it);
+            for (int j = 0; j < m; ++j) enqueue(it + j);
+            it += m;
+            CK(cudaMemcpyAsync(slot + (issued & 1), s.c->d_sc + k, sizeof(Scalars),
+                               cudaMemcpyDeviceToHost, s.st));
+            CK(cudaEventRecord(s.c->ev_batch[issued & 1], s.st));
+            ++issued;
+        }
+        if (inspected == issued) break;
+        CK(cudaEventSynchronize(s.c->ev_batch[inspected & 1]));
+        const bool done = slot[inspected & 1].done != 0;
+        ++inspected;
+        if (done) break;
+    }
+    return s.read_scalars(k);
+}
+
+// Preconditioned BiCGSTAB (van der Vorst 1992) on the reference's ILU factor.
+template <typename TT>
+void bicgstab_iteration(Solve& s, const TT* A, const TT* M, const TT* dinv, TT* x, TT* r, TT* rh,
+                        TT* p, TT* ph, TT* vv, TT* ss, TT* sh, TT* t, TT* tmp, int k)
+{
+    s.fw<TT>(M, p, tmp, k);
+    s.bw<TT>(M, dinv, tmp, ph, 1, k);
+    s.spmv<TT>(A, ph, vv, 0, nullptr, nullptr, rh, DOT_WY, k, EP_TB_SIGMA);
+    s.vec<TT>(V_TB_S, {ss, vv, r}, k, EP_TB_S);
+    s.fw<TT>(M, ss, tmp, k);
+    s.bw<TT>(M, dinv, tmp, sh, 1, k);
+    s.spmv<TT>(A, sh, t, 0, nullptr, nullptr, ss, DOT_YY | DOT_WY, k, EP_TB_OMEGA);
+    s.vec<TT>(V_TB_XR, {x, ph, sh, r, t, ss, rh}, k, EP_TB_RUPD);
+    s.vec<TT>(V_TB_P, {p, vv, r}, k, EP_STORE);
+}
+
+// Restarted driver shared by BiCGSTAB and PCG: start from x, iterate until
+// the recursive residual meets tol, confirm with a true FP64 residual, restart
+// from the current x when they disagree or on breakdown.
+template <typename Init, typename Iter, typename Half>
+TolResult run_restarted(Solve& s, const double* A, const double* b, double* x, const ocsl_opts& o,
+                        Init&& init, Iter&& iteration, Half&& half)
+{
+    double** v = s.c->v64;
+    TolResult res;
+    const double tol2 = o.tol * o.tol;
+    int total = 0;
+    bool converged = false;
+    bool broke = false;
+    for (int restart = 0; restart < 64 && !converged; ++restart) {
+        s.reset_scalars(0, tol2);
+        s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 0, EP_TB_INIT);
+        init();
+        Scalars st = s.read_scalars(0);
+        res.relres = st.res;
+        if (st.status) { res.status = st.status; break; }
+        if (st.bb == 0.0) {  // b = 0: x = 0 is exact
+            CK(cudaMemsetAsync(x, 0, sizeof(double) * (size_t)s.n, s.st));
+            res.relres = 0.0;
+            converged = true;
+            break;
+        }
+        if (st.done) { converged = true; break; }
+        if (total >= o.maxit) break;
+        st = run_batches(s, 0, o.maxit - total, iteration);
+        total += st.iters;
+        broke = st.breakdown != 0;
+        if (st.status) { res.status = st.status; break; }
+        half();
+        s.reset_scalars(2, tol2);
+        s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 2, EP_TRUE_RES);
+        const Scalars tr = s.read_scalars(2);
+        res.relres = tr.res;
+        if (!std::isfinite(tr.res)) { res.status = OCSL_NONFINITE; break; }
+        converged = tr.rr <= tol2 * tr.bb;
+        if (broke && st.iters == 0) break;  // breakdown before any progress
+    }
+    if (!converged && res.status == OCSL_OK) res.status = broke ? OCSL_BREAKDOWN : OCSL_NOT_CONVERGED;
+    res.iters = total;
+    return res;
+}
+
+TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x,
+                           const ocsl_opts& o)
+{
+    double** v = s.c->v64;
+    const double* M = s.factor(A, o.ilu_sweeps, true, false, -1);
+    return run_restarted(
+        s, A, b, x, o, [&] { s.vec<double>(V_COPY2, {v[RH], v[P], v[R]}, 0, EP_STORE); },
+        [&](int) {
+            bicgstab_iteration<double>(s, A, M, s.c->d_dinv, x, v[R], v[RH], v[P], v[PH], v[V],
+                                       v[S], v[SH], v[T], v[TMP], 0);
+        },
+        [&] { s.vec<double>(V_TB_HALF, {x, v[PH]}, 0, EP_STORE); });
+}
+
+TolResult run_pcg_tol(Solve& s, const double* A, const double* b, double* x, const ocsl_opts& o)
+{
+    double** v = s.c->v64;
+    s.factor(A, 0, true, false, -1);  // Jacobi: dinv = 1 / A_ii
+    return run_restarted(
+        s, A, b, x, o,
+        [&] { s.vec<double>(V_PC_INIT, {v[Z], v[P], v[R], s.c->d_dinv}, 0, EP_PC_INIT); },
+        [&](int) {
+            s.spmv<double>(A, v[P], v[Q], 0, nullptr, nullptr, v[P], DOT_WY, 0, EP_PC_ALPHA);
+            s.vec<double>(V_PC_XRZ, {x, v[P], v[R], v[Q], v[Z], s.c->d_dinv}, 0, EP_PC_RUPD);
+            s.vec<double>(V_PC_P, {v[P], v[Z]}, 0, EP_STORE);
+        },
+        [] {});
+}
+
+// FP32 inner ILU-BiCGSTAB (FP32 matrix, factor and vectors; compensated-FP32
+// reductions folded to FP64; FP64 alpha / beta / omega) inside FP64
+// iterative refinement: r = b - A x, x += ||r|| d in FP64.
+TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* x,
+                            const ocsl_opts& o)
+{
+    ocsl_ctx* c = s.c;
+    c->ensure_fp32();
+    double** v = c->v64;
+    float** f = c->v32;
+    TolResult res;
+    const double tol2 = o.tol * o.tol;
+    s.factor(A, o.ilu_sweeps, true, true, -1);
+    int total = 0;
+    s.reset_scalars(0, tol2);
+    for (int outer = 0;; ++outer) {
+        // FP64 residual; EP_TB_INIT also stores ||r|| and 1/||r||
+        s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 0, EP_TB_INIT);
+        const Scalars so = s.read_scalars(0);
+        res.relres = so.res;
+        res.outer = outer;
+        if (so.status) { res.status = so.status; break; }
+        if (so.bb == 0.0) {
+            CK(cudaMemsetAsync(x, 0, sizeof(double) * (size_t)s.n, s.st));
+            res.relres = 0.0;
+            break;
+        }
+        if (so.done) break;
+        if (total >= o.maxit || outer >= 1000) { res.status = OCSL_NOT_CONVERGED; break; }
+        // inner solve of A d = r / ||r|| in FP32 from d = 0
+        s.reset_scalars(1, o.inner_tol * o.inner_tol);
+        s.vec<float>(V_IR_SCALE, {v[R], f[F_RI], f[F_RH], f[F_P], f[F_D]}, 1, EP_IR_INNER_INIT);
+        const int budget = std::min(o.inner_maxit, o.maxit - total);
+        const Scalars si = run_batches(s, 1, budget, [&](int) {
+            bicgstab_iteration<float>(s, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI], f[F_RH],
+                                      f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH], f[F_T], f[F_TMP], 1);
+        });
+        total += si.iters;
+        s.vec<float>(V_TB_HALF, {f[F_D], f[F_PH]}, 1, EP_STORE);
+        s.vec<float>(V_IR_UPDATE, {x, f[F_D]}, -1, EP_STORE);
+        if (si.status == OCSL_NONFINITE) { res.status = OCSL_NONFINITE; break; }
+        if (si.iters == 0 && !si.done) { res.status = OCSL_BREAKDOWN; break; }
+        // the next residual reuses block 0: clear its done flag, keep tol2
+        s.reset_scalars(0, tol2);
+    }
+    res.iters = total;
+    return res;
+}
+
+int check_ready(ocsl_ctx* c)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (!c->has_pattern) return fail(c, OCSL_NO_PATTERN, "ocsl_set_pattern has not been called");
+    return OCSL_OK;
+}
+
+int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b, double* x,
+                      const ocsl_opts* opts, ocsl_result* out)
+{
+    const ocsl_opts o = resolve(opts);
+    ocsl_result r;
+    std::memset(&r, 0, sizeof r);
+    if (method < OCSL_CG_REF || method > OCSL_ILU_BICGSTAB_IR32)
+        return fail(c, OCSL_BAD_ARGUMENT, "unknown method");
+    if (c->P.n == 0) {
+        if (out) *out = r;
+        return OCSL_OK;
+    }
+    if (!A || !b || !x) return fail(c, OCSL_BAD_ARGUMENT, "null value, b or x pointer");
+    Solve s{c, c->stream, c->P, c->P.n};
+    int status = OCSL_OK;
+    try {
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+        CK(cudaEventRecord(c->ev_start, c->stream));
+        if (method == OCSL_CG_REF || method == OCSL_BICGSTAB_REF) {
+            if (method == OCSL_CG_REF)
+                run_cg_ref(s, A, b, x);
+            else
+                run_bicgstab_ref(s, A, b, x, o.ilu_sweeps);
+            CK(cudaEventRecord(c->ev_stop, c->stream));
+            const Scalars sc = s.read_scalars(0);
+            r.residual = sc.res;
+            r.iterations = sc.iters;
+        } else {
+            TolResult t;
+            if (method == OCSL_PCG)
+                t = run_pcg_tol(s, A, b, x, o);
+            else if (method == OCSL_ILU_BICGSTAB)
+                t = run_bicgstab_tol(s, A, b, x, o);
+            else
+                t = run_bicgstab_ir32(s, A, b, x, o);
+            CK(cudaEventRecord(c->ev_stop, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            r.residual = t.relres;
+            r.iterations = t.iters;
+            r.outer_iterations = t.outer;
+            status = t.status;
+        }
+        CK(cudaEventSynchronize(c->ev_stop));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev_start, c->ev_stop));
+        r.solve_ms = ms;
+        const int derr = s.device_error();
+        if (derr) status = derr;
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        status = from_cuda(c, e);
+    }
+    r.status = status;
+    if (out) *out = r;
+    if (status == OCSL_TIMEOUT) c->last_error = "a triangular-sweep wait hit its bound";
+    return status;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+
+extern "C" {
+
+void ocsl_default_opts(ocsl_opts* o)
+{
+    if (!o) return;
+    o->tol = 1e-10;
+    o->maxit = 5000;
+    o->ilu_sweeps = 3;
+    o->inner_tol = 1e-4;
+    o->inner_maxit = 500;
+}
+
+const char* ocsl_version(void) { return kVersion; }
+
+const char* ocsl_status_string(int s)
+{
+    switch (s) {
+    case OCSL_OK: return "OCSL_OK";
+    case OCSL_NOT_CONVERGED: return "OCSL_NOT_CONVERGED";
+    case OCSL_ZERO_PIVOT: return "OCSL_ZERO_PIVOT";
+    case OCSL_NONFINITE: return "OCSL_NONFINITE";
+    case OCSL_BAD_PATTERN: return "OCSL_BAD_PATTERN";
+    case OCSL_TIMEOUT: return "OCSL_TIMEOUT";
+    case OCSL_CUDA_ERROR: return "OCSL_CUDA_ERROR";
+    case OCSL_BAD_ARGUMENT: return "OCSL_BAD_ARGUMENT";
+    case OCSL_NO_PATTERN: return "OCSL_NO_PATTERN";
+    case OCSL_NO_DEVICE: return "OCSL_NO_DEVICE";
+    case OCSL_BREAKDOWN: return "OCSL_BREAKDOWN";
+    default: return "OCSL_UNKNOWN";
+    }
+}
+
+const char* ocsl_last_error(const ocsl_ctx* c)
+{
+    return c ? c->last_error.c_str() : g_create_error.c_str();
+}
+
+int ocsl_create(ocsl_ctx** out, int device)
+{
+    if (!out) return OCSL_BAD_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        g_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return OCSL_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) {
+        g_create_error = "device index out of range";
+        return OCSL_BAD_ARGUMENT;
+    }
+    auto* c = new ocsl_ctx();
+    c->device = device;
+    try {
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+        c->stream = c->own_stream;
+        c->d_sc = dalloc<Scalars>(3);
+        CK(cudaMemset(c->d_sc, 0, 3 * sizeof(Scalars)));
+        CK(cudaMallocHost(&c->h_sc, 8 * sizeof(Scalars)));
+        c->d_sync = dalloc<unsigned>(2);
+        CK(cudaMemset(c->d_sync, 0, 2 * sizeof(unsigned)));
+        c->S.ticket = c->d_sync;
+        c->S.finished = c->d_sync + 1;
+        c->d_err = dalloc<int>(1);
+        CK(cudaMemset(c->d_err, 0, sizeof(int)));
+        c->S.err = c->d_err;
+        CK(cudaMallocHost(&c->h_err, sizeof(int)));
+        CK(cudaEventCreate(&c->ev_start));
+        CK(cudaEventCreate(&c->ev_stop));
+        CK(cudaEventCreateWithFlags(&c->ev_batch[0], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->ev_batch[1], cudaEventDisableTiming));
+        c->ensure_reduce(1);
+    } catch (const CudaError& err) {
+        g_create_error = std::string(err.what) + ": " + cudaGetErrorString(err.code);
+        c->free_all();
+        delete c;
+        return OCSL_CUDA_ERROR;
+    }
+    *out = c;
+    return OCSL_OK;
+}
+
+int ocsl_destroy(ocsl_ctx* c)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->free_all();
+    delete c;
+    return OCSL_OK;
+}
+
+int ocsl_set_stream(ocsl_ctx* c, void* stream)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    return OCSL_OK;
+}
+
+int ocsl_synchronize(ocsl_ctx* c)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail(c, OCSL_CUDA_ERROR, cudaGetErrorString(e));
+    return OCSL_OK;
+}
+
+int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    HostPattern hp;
+    std::string err;
+    if (!analyse_pattern(n, rp, col, hp, err)) return fail(c, OCSL_BAD_PATTERN, err);
+    try {
+        CK(cudaSetDevice(c->device));
+        CK(cudaStreamSynchronize(c->stream));
+        c->free_pattern();
+        const std::vector<int>* tabs[10] = {&hp.rp, &hp.col, &hp.diag, &hp.pair_ptr, &hp.pair_k,
+                                            &hp.pair_slot, &hp.fw_order, &hp.fw_chunk,
+                                            &hp.bw_order, &hp.bw_chunk};
+        for (int i = 0; i < 10; ++i) c->d_pat[i] = upload(*tabs[i]);
+        DevPattern& P = c->P;
+        P.n = hp.n;
+        P.nnz = hp.nnz;
+        P.rp = c->d_pat[0];
+        P.col = c->d_pat[1];
+        P.diag = c->d_pat[2];
+        P.pair_ptr = c->d_pat[3];
+        P.pair_k = c->d_pat[4];
+        P.pair_slot = c->d_pat[5];
+        P.fw_order = c->d_pat[6];
+        P.fw_chunk = c->d_pat[7];
+        P.fw_nchunks = (int)hp.fw_chunk.size() - 1;
+        P.bw_order = c->d_pat[8];
+        P.bw_chunk = c->d_pat[9];
+        P.bw_nchunks = (int)hp.bw_chunk.size() - 1;
+        const size_t nn = (size_t)hp.n, nz = (size_t)hp.nnz;
+        c->d_A = dalloc<double>(nz);
+        c->d_b = dalloc<double>(nn);
+        c->d_x = dalloc<double>(nn);
+        c->d_Ma = dalloc<double>(nz);
+        c->d_Mb = dalloc<double>(nz);
+        c->d_dinv = dalloc<double>(nn);
+        for (auto& v : c->v64) v = dalloc<double>(nn);
+        c->ensure_reduce((hp.n + kTile - 1) / kTile);
+        // drop the large host tables, keep the facts
+        c->hp.n = hp.n;
+        c->hp.nnz = hp.nnz;
+        c->hp.nnz_real = hp.nnz_real;
+        c->hp.fw_levels = hp.fw_levels;
+        c->hp.bw_levels = hp.bw_levels;
+        c->has_pattern = true;
+    } catch (const CudaError& e) {
+        c->free_pattern();
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_check_pattern(size_t n, const size_t* rp, const size_t* col, int64_t* nnz_real,
+                       int32_t* fw_levels, int32_t* bw_levels, char* err, size_t err_len)
+{
+    HostPattern hp;
+    std::string msg;
+    const bool ok = analyse_pattern(n, rp, col, hp, msg);
+    if (err && err_len) {
+        std::snprintf(err, err_len, "%s", ok ? "" : msg.c_str());
+    }
+    if (!ok) return OCSL_BAD_PATTERN;
+    if (nnz_real) *nnz_real = hp.nnz_real;
+    if (fw_levels) *fw_levels = hp.fw_levels;
+    if (bw_levels) *bw_levels = hp.bw_levels;
+    return OCSL_OK;
+}
+
+int ocsl_pattern_info(const ocsl_ctx* c, int64_t* n, int64_t* nnz, int64_t* nnz_real,
+                      int32_t* fw_levels, int32_t* bw_levels)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (!c->has_pattern) return OCSL_NO_PATTERN;
+    if (n) *n = c->hp.n;
+    if (nnz) *nnz = c->hp.nnz;
+    if (nnz_real) *nnz_real = c->hp.nnz_real;
+    if (fw_levels) *fw_levels = c->hp.fw_levels;
+    if (bw_levels) *bw_levels = c->hp.bw_levels;
+    return OCSL_OK;
+}
+
+int ocsl_solve_device(ocsl_ctx* c, int method, const double* A, const double* b, double* x,
+                      const ocsl_opts* opts, ocsl_result* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, OCSL_CUDA_ERROR, "cudaSetDevice");
+    return solve_device_impl(c, method, A, b, x, opts, out);
+}
+
+int ocsl_solve(ocsl_ctx* c, int method, const double* value, const double* b, double* x,
+               const ocsl_opts* opts, ocsl_result* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (c->P.n == 0) {
+        if (out) std::memset(out, 0, sizeof *out);
+        return OCSL_OK;
+    }
+    if (!value || !b || !x) return fail(c, OCSL_BAD_ARGUMENT, "null value, b or x pointer");
+    const size_t n = (size_t)c->P.n, nnz = (size_t)c->P.nnz;
+    try {
+        CK(cudaSetDevice(c->device));
+        CK(cudaMemcpyAsync(c->d_A, value, nnz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->d_b, b, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    rc = solve_device_impl(c, method, c->d_A, c->d_b, c->d_x, opts, out);
+    if (rc == OCSL_CUDA_ERROR) return rc;
+    try {
+        CK(cudaMemcpyAsync(x, c->d_x, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return rc;
+}
+
+int ocsl_gemv_device(ocsl_ctx* c, int mode, double a, const double* val, const double* x,
+                     const double* z, double* y)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (mode < 0 || mode > 2 || !val || !x || !y || (mode > 0 && !z))
+        return fail(c, OCSL_BAD_ARGUMENT, "bad gemv arguments");
+    try {
+        CK(cudaSetDevice(c->device));
+        launch_spmv<double>(c->stream, c->P, val, x, y, mode, nullptr, a, z, nullptr, nullptr, 0,
+                            c->R, nullptr, EP_STORE, 0, 0);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_dot_device(ocsl_ctx* c, size_t n, const double* x, const double* y, double* result)
+{
+    if (!c || !result) return OCSL_BAD_ARGUMENT;
+    if (n >= (size_t)INT32_MAX) return fail(c, OCSL_BAD_ARGUMENT, "n exceeds the int32 limit");
+    if (n == 0) { *result = 0.0; return OCSL_OK; }
+    if (!x || !y) return fail(c, OCSL_BAD_ARGUMENT, "null vector");
+    try {
+        CK(cudaSetDevice(c->device));
+        c->ensure_reduce((int)((n + kTile - 1) / kTile));
+        Solve s{c, c->stream, c->P, (int)n};
+        s.reset_scalars(2, 0.0);
+        s.vec<double>(V_DOT1, {x, y}, 2, EP_STORE);
+        CK(cudaGetLastError());
+        *result = s.read_scalars(2).sum[0];
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_ilu_device(ocsl_ctx* c, const double* A, double* M, int sweeps)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!A || !M || sweeps < 0) return fail(c, OCSL_BAD_ARGUMENT, "bad ilu arguments");
+    try {
+        CK(cudaSetDevice(c->device));
+        Solve s{c, c->stream, c->P, c->P.n};
+        const double* F = s.factor(A, sweeps, false, false, -1);
+        CK(cudaMemcpyAsync(M, F, sizeof(double) * (size_t)c->P.nnz, cudaMemcpyDeviceToDevice,
+                           c->stream));
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double* in, double* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!M || !in || !out || in == out) return fail(c, OCSL_BAD_ARGUMENT, "bad sweep arguments");
+    try {
+        CK(cudaSetDevice(c->device));
+        Solve s{c, c->stream, c->P, c->P.n};
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+        if (forward)
+            s.fw<double>(M, in, out, -1);
+        else
+            s.bw<double>(M, nullptr, in, out, 0, -1);
+        CK(cudaGetLastError());
+        if (s.device_error()) return fail(c, OCSL_TIMEOUT, "a triangular-sweep wait hit its bound");
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_forsub_device(ocsl_ctx* c, const double* M, const double* b, double* y)
+{
+    return sweep_entry(c, true, M, b, y);
+}
+
+int ocsl_backsub_device(ocsl_ctx* c, const double* M, const double* y, double* x)
+{
+    return sweep_entry(c, false, M, y, x);
+}
+
+}  // extern "C"

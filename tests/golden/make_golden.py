@@ -1,0 +1,153 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a container where the reference's sources are present:
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+It builds the reference from its own sources (oracle/Makefile, target `ref`),
+then writes:
+
+* kat_tridiag10.npz -- the reference's own solver unit-test system
+  (cmatrix_solver_supply.h:29-114: 10x10 tridiagonal [1, 5, 1], b = 2,
+  x0 = 1), with the residual and x returned by the reference's CG_solve and
+  ILU_BICGSTAB_solve (the latter with M prepared as cfvm.cpp:96-97 does; the
+  unit test as written never prepares it and crashes);
+* shocktube_calls.npz -- linear systems captured from the reference's SIMPLE
+  loop on the 1000-cell shock tube (momentum solves with CG, p' and enthalpy
+  with ILU-BiCGSTAB): values, b, x0, the reference's x and residual, and the
+  final fields (p, u, T, rho) at full precision;
+* small_systems.npz -- seeded small systems in the reference layout with the
+  reference's gemv, ILU_decompose, ILU_forsub/backsub, CG_solve and
+  ILU_BICGSTAB_solve outputs.
+
+All reference calls use one OpenMP thread (deterministic reduction order).
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from opencslsolver_gb300 import workloads as W  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+# Recorded solve calls: (step, inner iteration) of the 200-step, 5-inner run.
+SHOCKTUBE_RECORD = ["0:0", "0:4", "100:2", "199:4"]
+
+
+def tridiag10():
+    n = 10
+    rp, col, val = [0], [], []
+    for i in range(n):
+        for j in (i - 1, i, i + 1):
+            if 0 <= j < n:
+                col.append(j)
+                val.append(5.0 if j == i else 1.0)
+        rp.append(len(col))
+    return (np.array(rp, np.uint64), np.array(col, np.uint64), np.array(val), np.full(n, 2.0),
+            np.ones(n))
+
+
+def make_kat(ref, out):
+    rp, col, val, b, x0 = tridiag10()
+    xc, rc = ref.cg_solve(rp, col, val, b, x0)
+    xb, rb = ref.bicgstab_solve(rp, col, val, b, x0)
+    np.savez_compressed(out, row_ptr=rp, column_index=col, value=val, b=b, x0=x0, cg_x=xc,
+                        cg_res=rc, bicg_x=xb, bicg_res=rb)
+
+
+def make_shocktube(out):
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([orc.REF_SHOCKTUBE, d, "1", "200", "5", *SHOCKTUBE_RECORD], cwd=d,
+                       check=True, stdout=subprocess.DEVNULL)
+        raw = open(os.path.join(d, "pattern.bin"), "rb").read()
+        n, nnz = np.frombuffer(raw[:16], np.uint64).astype(int)
+        rp = np.frombuffer(raw[16:16 + 8 * (n + 1)], np.uint64)
+        col = np.frombuffer(raw[16 + 8 * (n + 1):], np.uint64)
+        calls = sorted(f for f in os.listdir(d) if f.startswith("call_"))
+        meta, res, vals, bs, x0s, xs = [], [], [], [], [], []
+        for f in calls:
+            buf = open(os.path.join(d, f), "rb").read()
+            hdr = np.frombuffer(buf[:16], np.int32)
+            nn, nz = np.frombuffer(buf[16:32], np.uint64).astype(int)
+            r = np.frombuffer(buf[32:40], np.float64)[0]
+            off = 40
+            v = np.frombuffer(buf[off:off + 8 * nz], np.float64); off += 8 * nz
+            b = np.frombuffer(buf[off:off + 8 * nn], np.float64); off += 8 * nn
+            x0 = np.frombuffer(buf[off:off + 8 * nn], np.float64); off += 8 * nn
+            x = np.frombuffer(buf[off:off + 8 * nn], np.float64); off += 8 * nn
+            xcopy = np.frombuffer(buf[off:off + 8 * nn], np.float64)
+            assert np.array_equal(x, xcopy), f"{f}: reference not deterministic"
+            meta.append(np.concatenate([hdr, [int(f[5:10])]]))
+            res.append(r); vals.append(v); bs.append(b); x0s.append(x0); xs.append(x)
+        fields = np.loadtxt(os.path.join(d, "fields.txt"))
+    np.savez_compressed(out, row_ptr=rp, column_index=col, meta=np.array(meta, np.int32),
+                        residual=np.array(res), value=np.array(vals), b=np.array(bs),
+                        x0=np.array(x0s), x=np.array(xs), fields=fields)
+
+
+def small_cases():
+    return [W.hex_pprime(6, peclet=10.0), W.hex_pprime(6, 5, 4, peclet=0.0),
+            W.tet_pprime(3, peclet=50.0), W.random_rows_system(200, 9, seed=11),
+            W.System(*W.pattern_1d(50), np.zeros(0), np.zeros(0), "oned50")]
+
+
+def make_small(ref, out):
+    arrays = {}
+    rng = np.random.default_rng(5)
+    for k, s in enumerate(small_cases()):
+        if s.name == "oned50":  # 1D pattern with diagonally dominant values
+            rp, col = s.row_ptr, s.column_index
+            val = np.where(col == W.PHANTOM, 0.0, -1.0)
+            rows = np.repeat(np.arange(s.n), np.diff(rp.astype(np.int64)))
+            val[(col == rows.astype(np.uint64))] = 2.5
+            s = W.System(rp, col, val, rng.uniform(-1, 1, s.n), "oned50")
+        rp, col, val, b = s.row_ptr, s.column_index, s.value, s.b
+        x0 = rng.uniform(-1, 1, s.n) * 0.1
+        z = rng.uniform(-1, 1, s.n)
+        xin = rng.uniform(-1, 1, s.n)
+        p = f"c{k}_"
+        arrays[p + "name"] = np.array(s.name)
+        arrays[p + "row_ptr"], arrays[p + "column_index"] = rp, col
+        arrays[p + "value"], arrays[p + "b"], arrays[p + "x0"] = val, b, x0
+        arrays[p + "z"], arrays[p + "xin"] = z, xin
+        arrays[p + "gemv0"] = ref.gemv(rp, col, val, 1.0, xin)
+        arrays[p + "gemv1"] = ref.gemv(rp, col, val, -1.0, xin, 1.0, z)
+        arrays[p + "gemv2"] = ref.gemv(rp, col, val, -0.37, xin, 1.0, z)
+        M = ref.ilu_decompose(rp, col, val)
+        arrays[p + "ilu"] = M
+        arrays[p + "forsub"] = ref.forsub(rp, col, M, z)
+        arrays[p + "backsub"] = ref.backsub(rp, col, M, z)
+        xc, rc = ref.cg_solve(rp, col, val, b, x0)
+        xb, rb = ref.bicgstab_solve(rp, col, val, b, x0)
+        arrays[p + "cg_x"], arrays[p + "cg_res"] = xc, rc
+        arrays[p + "bicg_x"], arrays[p + "bicg_res"] = xb, rb
+    arrays["count"] = np.array(len(small_cases()))
+    np.savez_compressed(out, **arrays)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    a = ap.parse_args()
+    orc.build(a.reference)
+    ref = orc.Reference()
+    ref.set_threads(1)
+    make_kat(ref, os.path.join(HERE, "kat_tridiag10.npz"))
+    make_shocktube(os.path.join(HERE, "shocktube_calls.npz"))
+    make_small(ref, os.path.join(HERE, "small_systems.npz"))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
