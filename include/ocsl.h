@@ -134,6 +134,17 @@ int ocsl_forsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_b, doub
 /* x = U^-1 y, cmatrix_solver.cpp:595-611 ILU_backsub. */
 int ocsl_backsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_y, double* d_x);
 
+/* Kernel timing.  While enabled, every kernel the context launches is
+ * bracketed by CUDA events on its stream and accounted to a category:
+ *   0 spmv_f64  1 spmv_f32  2 fw_sweep_f64  3 bw_sweep_f64  4 fw_sweep_f32
+ *   5 bw_sweep_f32  6 ilu_factor  7 vector_f64  8 vector_f32  9 sweep_fill
+ * ocsl_profile_read synchronises, writes per-category milliseconds and launch
+ * counts (arrays of OCSL_PROFILE_CATEGORIES) and clears the record. */
+#define OCSL_PROFILE_CATEGORIES 10
+int ocsl_profile_enable(ocsl_ctx* ctx, int enable);
+int ocsl_profile_read(ocsl_ctx* ctx, double* ms, int64_t* launches);
+const char* ocsl_profile_category_name(int category);
+
 #ifdef __cplusplus
 }
 #endif

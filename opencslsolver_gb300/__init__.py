@@ -161,6 +161,19 @@ class Context:
             self._check(st, "solve_device")
         return r.as_dict()
 
+    # -- kernel timing (ocsl_profile_*)
+    def profile(self, enable: bool = True):
+        self._check(self._L.ocsl_profile_enable(self._h, int(bool(enable))), "profile_enable")
+
+    def profile_read(self):
+        """Per-category device milliseconds and launch counts since the last read."""
+        K = _abi.PROFILE_CATEGORIES
+        ms = (C.c_double * K)()
+        cnt = (C.c_int64 * K)()
+        self._check(self._L.ocsl_profile_read(self._h, ms, cnt), "profile_read")
+        return {self._L.ocsl_profile_category_name(k).decode(): (ms[k], cnt[k])
+                for k in range(K)}
+
     # -- kernel-level entry points (device tensors)
     def gemv_device(self, value, x, y, mode=0, a=0.0, z=None):
         self._check(self._L.ocsl_gemv_device(self._h, mode, a, _dptr(value), _dptr(x), _dptr(z),

@@ -77,7 +77,11 @@ _PROTOS = {
     "ocsl_ilu_device": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "ocsl_forsub_device": (C.c_int, [_CTX, _P, _P, _P]),
     "ocsl_backsub_device": (C.c_int, [_CTX, _P, _P, _P]),
+    "ocsl_profile_enable": (C.c_int, [_CTX, C.c_int]),
+    "ocsl_profile_read": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "ocsl_profile_category_name": (C.c_char_p, [C.c_int]),
 }
+PROFILE_CATEGORIES = 10
 
 _lib = None
 

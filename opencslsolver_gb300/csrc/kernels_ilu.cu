@@ -138,6 +138,11 @@ __global__ void __launch_bounds__(kThreads) fw_sweep_kernel(SweepParams<T> p)
     if (threadIdx.x == 0) s_chunk = (int)atomicAdd(p.S.ticket, 1u);
     __syncthreads();
     const int c = s_chunk;
+    if (c >= p.nchunks) {  // never happens with a fresh dispenser; keeps every read in bounds
+        atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
+        sweep_epilogue(p.S);
+        return;
+    }
     const int t = __ldg(p.chunk + c) + (int)threadIdx.x;
     if (t < __ldg(p.chunk + c + 1)) {
         const int i = __ldg(p.order + t);
@@ -163,6 +168,11 @@ __global__ void __launch_bounds__(kThreads) bw_sweep_kernel(SweepParams<T> p)
     if (threadIdx.x == 0) s_chunk = (int)atomicAdd(p.S.ticket, 1u);
     __syncthreads();
     const int c = s_chunk;
+    if (c >= p.nchunks) {  // never happens with a fresh dispenser; keeps every read in bounds
+        atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
+        sweep_epilogue(p.S);
+        return;
+    }
     const int t = __ldg(p.chunk + c) + (int)threadIdx.x;
     if (t < __ldg(p.chunk + c + 1)) {
         const int i = __ldg(p.order + t);
@@ -274,8 +284,7 @@ template <typename T>
 void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* rhs, T* out,
                      const SweepSync& S, const int* done)
 {
-    if (P.n == 0) return;
-    cudaMemsetAsync(out, 0xFF, sizeof(T) * (size_t)P.n, st);
+    if (P.n == 0) return;  // `out` holds the all-ones pattern (filled by the caller)
     auto p = make_sweep<T>(P, true, M, nullptr, rhs, out, S, done);
     fw_sweep_kernel<T><<<p.nchunks, kThreads, 0, st>>>(p);
 }
@@ -284,8 +293,7 @@ template <typename T>
 void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
                      const T* rhs, T* out, int divmode, const SweepSync& S, const int* done)
 {
-    if (P.n == 0) return;
-    cudaMemsetAsync(out, 0xFF, sizeof(T) * (size_t)P.n, st);
+    if (P.n == 0) return;  // `out` holds the all-ones pattern (filled by the caller)
     auto p = make_sweep<T>(P, false, M, dinv, rhs, out, S, done);
     if (divmode == 0)
         bw_sweep_kernel<T, true><<<p.nchunks, kThreads, 0, st>>>(p);

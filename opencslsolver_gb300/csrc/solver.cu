@@ -96,6 +96,12 @@ struct ocsl_ctx {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaEvent_t ev_batch[2] = {nullptr, nullptr};
 
+    // kernel timing (ocsl_profile_*)
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_ev;  // pairs
+    std::vector<int> prof_cat;
+    size_t prof_used = 0;
+
     void free_pattern();
     void free_all();
     void ensure_reduce(int ntiles);
@@ -130,6 +136,8 @@ void ocsl_ctx::free_all()
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
     for (auto& e : ev_batch) { if (e) cudaEventDestroy(e); e = nullptr; }
+    for (auto& e : prof_ev) cudaEventDestroy(e);
+    prof_ev.clear();
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = stream = nullptr;
 }
@@ -187,6 +195,41 @@ ocsl_opts resolve(const ocsl_opts* o)
 
 // ------------------------------------------------------------------ helpers
 
+enum ProfCat { PC_SPMV64, PC_SPMV32, PC_FW64, PC_BW64, PC_FW32, PC_BW32, PC_ILU, PC_VEC64, PC_VEC32,
+               PC_FILL, PC_COUNT };
+const char* kProfNames[PC_COUNT] = {"spmv_f64", "spmv_f32", "fw_sweep_f64", "bw_sweep_f64",
+                                    "fw_sweep_f32", "bw_sweep_f32", "ilu_factor", "vector_f64",
+                                    "vector_f32", "sweep_fill"};
+constexpr size_t kProfMaxPairs = 1 << 18;
+
+// Brackets one launch with events when profiling is on.
+struct ProfScope {
+    ocsl_ctx* c;
+    cudaStream_t st;
+    size_t slot = ~size_t(0);
+    ProfScope(ocsl_ctx* c_, cudaStream_t st_, int cat) : c(c_), st(st_)
+    {
+        if (!c->prof_on || c->prof_used >= kProfMaxPairs) return;
+        if (2 * c->prof_used + 2 > c->prof_ev.size()) {
+            for (int k = 0; k < 2; ++k) {
+                cudaEvent_t e;
+                CK(cudaEventCreate(&e));
+                c->prof_ev.push_back(e);
+            }
+        }
+        slot = c->prof_used++;
+        c->prof_cat.push_back(cat);
+        CK(cudaEventRecord(c->prof_ev[2 * slot], st));
+    }
+    ~ProfScope()
+    {
+        if (slot != ~size_t(0)) cudaEventRecord(c->prof_ev[2 * slot + 1], st);
+    }
+};
+
+template <typename TT>
+constexpr bool is_f64() { return sizeof(TT) == 8; }
+
 struct Solve {
     ocsl_ctx* c;
     cudaStream_t st;
@@ -222,6 +265,7 @@ struct Solve {
     void spmv(const TT* val, const TT* x, TT* y, int mode, const TT* z, TT* ycopy, const TT* w,
               int dots, int k, int epi, int it = 0, int maxit = 0)
     {
+        ProfScope ps(c, st, is_f64<TT>() ? PC_SPMV64 : PC_SPMV32);
         launch_spmv<TT>(st, P, val, x, y, mode, nullptr, 0.0, z, ycopy, w, dots, c->R,
                         k >= 0 ? sc(k) : nullptr, epi, it, maxit);
     }
@@ -232,6 +276,7 @@ struct Solve {
         VecPtrs vp{};
         int i = 0;
         for (const void* p : ptrs) vp.v[i++] = const_cast<void*>(p);
+        ProfScope ps(c, st, is_f64<TT>() ? PC_VEC64 : PC_VEC32);
         launch_vec<TT>(st, op, n, vp, c->R, k >= 0 ? sc(k) : nullptr, sc(0), epi, it, maxit);
     }
     // Fixed-point ILU factor (cmatrix_solver.cpp:702-704): M starts as A,
@@ -246,7 +291,10 @@ struct Solve {
         float* dinv32 = want_fp32 ? c->d_dinv32 : nullptr;
         float* A32 = want_fp32 ? c->d_A32 : nullptr;
         if (sweeps == 0) {
-            if (want_dinv || want_fp32) launch_factor_outputs(st, P, A, A, dinv, M32, dinv32, A32);
+            if (want_dinv || want_fp32) {
+                ProfScope ps(c, st, PC_ILU);
+                launch_factor_outputs(st, P, A, A, dinv, M32, dinv32, A32);
+            }
             return A;
         }
         const double* src = A;
@@ -254,6 +302,7 @@ struct Solve {
         for (int s = 0; s < sweeps; ++s) {
             double* dst = bufs[s & 1];
             const bool last = s == sweeps - 1;
+            ProfScope ps(c, st, PC_ILU);
             launch_ilu_sweep<double>(st, P, A, src, dst, last ? dinv : nullptr,
                                      last ? M32 : nullptr, last ? dinv32 : nullptr,
                                      last ? A32 : nullptr, dn);
@@ -264,11 +313,26 @@ struct Solve {
     template <typename TT>
     void fw(const TT* M, const TT* rhs, TT* out, int k)
     {
+        {
+            ProfScope ps(c, st, PC_FILL);
+            fill_sentinel(out);
+        }
+        ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
         launch_fw_sweep<TT>(st, P, M, rhs, out, c->S, k >= 0 ? done(k) : nullptr);
+    }
+    template <typename TT>
+    void fill_sentinel(TT* out)
+    {
+        if (P.n) CK(cudaMemsetAsync(out, 0xFF, sizeof(TT) * (size_t)P.n, st));
     }
     template <typename TT>
     void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k)
     {
+        {
+            ProfScope ps(c, st, PC_FILL);
+            fill_sentinel(out);
+        }
+        ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
         launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S, k >= 0 ? done(k) : nullptr);
     }
     int device_error()
@@ -884,6 +948,44 @@ static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double*
         return from_cuda(c, e);
     }
     return OCSL_OK;
+}
+
+int ocsl_profile_enable(ocsl_ctx* c, int enable)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    c->prof_on = enable != 0;
+    return OCSL_OK;
+}
+
+int ocsl_profile_read(ocsl_ctx* c, double* ms, int64_t* launches)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    for (int k = 0; k < PC_COUNT; ++k) {
+        if (ms) ms[k] = 0.0;
+        if (launches) launches[k] = 0;
+    }
+    try {
+        CK(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < c->prof_used; ++i) {
+            float t = 0.f;
+            CK(cudaEventElapsedTime(&t, c->prof_ev[2 * i], c->prof_ev[2 * i + 1]));
+            const int k = c->prof_cat[i];
+            if (ms) ms[k] += t;
+            if (launches) launches[k] += 1;
+        }
+    } catch (const CudaError& e) {
+        c->prof_used = 0;
+        c->prof_cat.clear();
+        return from_cuda(c, e);
+    }
+    c->prof_used = 0;
+    c->prof_cat.clear();
+    return OCSL_OK;
+}
+
+const char* ocsl_profile_category_name(int k)
+{
+    return (k >= 0 && k < PC_COUNT) ? kProfNames[k] : "unknown";
 }
 
 int ocsl_forsub_device(ocsl_ctx* c, const double* M, const double* b, double* y)

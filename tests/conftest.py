@@ -85,3 +85,11 @@ def ctx(lib_built, torch_cuda):
     c = ocsl.Context(0)
     yield c
     c.close()
+
+
+@pytest.fixture(scope="session")
+def hex128():
+    """The 128^3 jittered hex p' system (2,097,152 cells), generated once."""
+    from opencslsolver_gb300 import workloads as W
+
+    return W.hex_pprime(128, peclet=10.0)

@@ -1,0 +1,134 @@
+"""GPU parity of the kernel-level entry points (gemv, dot, ILU factor,
+triangular sweeps) against the CPU oracle -- bit for bit -- and against the
+reference's own outputs recorded in tests/golden (tight relative tolerance).
+
+Device buffers come from torch; every call goes through the C ABI."""
+import numpy as np
+import pytest
+
+from opencslsolver_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def rel(a, b):
+    den = max(float(np.max(np.abs(b))), 1e-300) if np.size(b) else 1.0
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)))) / den if np.size(b) else 0.0
+
+
+def systems():
+    return [W.hex_pprime(20, peclet=10.0), W.hex_pprime(9, 13, 7, peclet=0.0),
+            W.tet_pprime(6, peclet=50.0), W.random_rows_system(3000, 14, seed=4),
+            W.random_rows_system(700, 40, seed=9)]
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_gemv_bit_exact(ctx, torch_cuda, oracle, k):
+    s = systems()[k]
+    rng = np.random.default_rng(k)
+    x, z = rng.standard_normal(s.n), rng.standard_normal(s.n)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A, X, Z = dev(torch_cuda, s.value), dev(torch_cuda, x), dev(torch_cuda, z)
+    Y = torch_cuda.empty_like(X)
+    for mode, a in ((0, 0.0), (1, 0.0), (2, -0.731)):
+        ctx.gemv_device(A, X, Y, mode=mode, a=a, z=Z if mode else None)
+        want = oracle.gemv(s.row_ptr, s.column_index, s.value, x, mode, a, z)
+        assert np.array_equal(host(Y), want), (s.name, mode)
+
+
+def test_gemv_matches_reference_golden(ctx, torch_cuda, golden_small):
+    for c in golden_small:
+        ctx.set_pattern(c["row_ptr"], c["column_index"])
+        A, X, Z = dev(torch_cuda, c["value"]), dev(torch_cuda, c["xin"]), dev(torch_cuda, c["z"])
+        Y = torch_cuda.empty_like(X)
+        ctx.gemv_device(A, X, Y, mode=0)
+        assert rel(host(Y), c["gemv0"]) <= 1e-15
+        ctx.gemv_device(A, X, Y, mode=1, z=Z)
+        assert rel(host(Y), c["gemv1"]) <= 1e-15
+        ctx.gemv_device(A, X, Y, mode=2, a=-0.37, z=Z)
+        assert rel(host(Y), c["gemv2"]) <= 1e-15
+
+
+@pytest.mark.parametrize("n", [1, 255, 2047, 2048, 2049, 100_003, 3_000_001])
+def test_dot_bit_exact(ctx, torch_cuda, oracle, n):
+    rng = np.random.default_rng(n)
+    x, y = rng.standard_normal(n), rng.standard_normal(n)
+    got = ctx.dot_device(dev(torch_cuda, x), dev(torch_cuda, y))
+    assert got == oracle.dot(x, y)
+
+
+@pytest.mark.parametrize("k", range(5))
+@pytest.mark.parametrize("sweeps", [0, 1, 3, 5])
+def test_ilu_bit_exact(ctx, torch_cuda, oracle, k, sweeps):
+    s = systems()[k]
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = dev(torch_cuda, s.value)
+    M = torch_cuda.empty_like(A)
+    ctx.ilu_device(A, M, sweeps)
+    assert np.array_equal(host(M), oracle.ilu(s.row_ptr, s.column_index, s.value, sweeps))
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_sweeps_bit_exact(ctx, torch_cuda, oracle, k):
+    s = systems()[k]
+    rng = np.random.default_rng(10 + k)
+    b = rng.standard_normal(s.n)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    Mh = oracle.ilu(s.row_ptr, s.column_index, s.value)
+    M, B = dev(torch_cuda, Mh), dev(torch_cuda, b)
+    Y = torch_cuda.empty_like(B)
+    X = torch_cuda.empty_like(B)
+    ctx.forsub_device(M, B, Y)
+    y = oracle.forsub(s.row_ptr, s.column_index, Mh, b)
+    assert np.array_equal(host(Y), y)
+    ctx.backsub_device(M, Y, X)
+    assert np.array_equal(host(X), oracle.backsub(s.row_ptr, s.column_index, Mh, y))
+
+
+def test_factor_and_sweeps_match_reference_golden(ctx, torch_cuda, golden_small):
+    for c in golden_small:
+        ctx.set_pattern(c["row_ptr"], c["column_index"])
+        A = dev(torch_cuda, c["value"])
+        M = torch_cuda.empty_like(A)
+        ctx.ilu_device(A, M, 3)
+        assert rel(host(M), c["ilu"]) <= 1e-15, str(c["name"])
+        Mref, Z = dev(torch_cuda, c["ilu"]), dev(torch_cuda, c["z"])
+        Y = torch_cuda.empty_like(Z)
+        ctx.forsub_device(Mref, Z, Y)
+        assert rel(host(Y), c["forsub"]) <= 1e-14
+        ctx.backsub_device(Mref, Z, Y)
+        assert rel(host(Y), c["backsub"]) <= 1e-14
+
+
+def test_full_size_spmv_and_sweeps(ctx, torch_cuda, oracle, hex128):
+    """128^3 jittered hex p' system (n = 2,097,152): SpMV and both sweeps are
+    bit-identical to the oracle at full size."""
+    s = hex128
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    info = ctx.pattern_info()
+    assert info["n"] == 2_097_152 and info["nnz_real"] == 14_581_760
+    assert info["fw_levels"] == 382 and info["bw_levels"] == 382
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(s.n)
+    A, X = dev(torch_cuda, s.value), dev(torch_cuda, x)
+    Y = torch_cuda.empty_like(X)
+    ctx.gemv_device(A, X, Y)
+    assert np.array_equal(host(Y), oracle.gemv(s.row_ptr, s.column_index, s.value, x))
+    Mh = oracle.ilu(s.row_ptr, s.column_index, s.value)
+    M = torch_cuda.empty_like(A)
+    ctx.ilu_device(A, M, 3)
+    assert np.array_equal(host(M), Mh)
+    ctx.forsub_device(M, X, Y)
+    y = oracle.forsub(s.row_ptr, s.column_index, Mh, x)
+    assert np.array_equal(host(Y), y)
+    Z = torch_cuda.empty_like(X)
+    ctx.backsub_device(M, Y, Z)
+    assert np.array_equal(host(Z), oracle.backsub(s.row_ptr, s.column_index, Mh, y))
