@@ -257,6 +257,23 @@ __global__ void factor_outputs_kernel(int n, const int* rp, const int* diag, con
     if (dinv32) dinv32[i] = (float)r;
 }
 
+// Fill a sweep's output with the all-ones pattern, unless the solve is done:
+// a batch queued after convergence must not clobber vectors still in use.
+// `head` 32-bit words bring the pointer to a 16-byte boundary, then 16-byte
+// stores, then `tail` words.
+__global__ void __launch_bounds__(kThreads) fill_ones_kernel(unsigned* out, int head,
+                                                            long long n16, int tail,
+                                                            const int* done)
+{
+    if (done && *done) return;
+    const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (gid < head) out[gid] = ~0u;
+    uint4* body = reinterpret_cast<uint4*>(out + head);
+    const uint4 ones = make_uint4(~0u, ~0u, ~0u, ~0u);
+    for (long long i = gid; i < n16; i += (long long)gridDim.x * blockDim.x) body[i] = ones;
+    if (gid < tail) out[head + 4 * n16 + gid] = ~0u;
+}
+
 template <typename T>
 SweepParams<T> make_sweep(const DevPattern& P, bool forward, const T* M, const T* dinv,
                           const T* rhs, T* out, const SweepSync& S, const int* done)
@@ -324,6 +341,23 @@ void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T*
     p.A32 = A32;
     p.done = done;
     ilu_sweep_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(p);
+}
+
+void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done)
+{
+    // `out` is element-aligned (4 or 8 bytes); the entry points check that.
+    const size_t words = bytes / 4;
+    if (words == 0) return;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(out);
+    size_t head = ((16 - (a & 15)) & 15) / 4;
+    if (head > words) head = words;
+    const long long n16 = (long long)((words - head) / 4);
+    const int tail = (int)(words - head - 4 * (size_t)n16);
+    long long blocks = (n16 + kThreads - 1) / kThreads;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 4096) blocks = 4096;
+    fill_ones_kernel<<<(int)blocks, kThreads, 0, st>>>(static_cast<unsigned*>(out), (int)head,
+                                                       n16, tail, done);
 }
 
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,

@@ -142,6 +142,9 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 
 void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out);
 
+// All-ones fill of a sweep output (skipped once the solve is done).
+void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done);
+
 // Factor side outputs without a sweep: dinv = 1 / M_ii and FP32 copies.
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
                            double* dinv, float* M32, float* dinv32, float* A32);

@@ -315,22 +315,22 @@ struct Solve {
     {
         {
             ProfScope ps(c, st, PC_FILL);
-            fill_sentinel(out);
+            fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
         launch_fw_sweep<TT>(st, P, M, rhs, out, c->S, k >= 0 ? done(k) : nullptr);
     }
     template <typename TT>
-    void fill_sentinel(TT* out)
+    void fill_sentinel(TT* out, int k)
     {
-        if (P.n) CK(cudaMemsetAsync(out, 0xFF, sizeof(TT) * (size_t)P.n, st));
+        launch_fill_ones(st, out, sizeof(TT) * (size_t)P.n, k >= 0 ? done(k) : nullptr);
     }
     template <typename TT>
     void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k)
     {
         {
             ProfScope ps(c, st, PC_FILL);
-            fill_sentinel(out);
+            fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
         launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S, k >= 0 ? done(k) : nullptr);
@@ -573,6 +573,8 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
     return res;
 }
 
+bool aligned8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
+
 int check_ready(ocsl_ctx* c)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
@@ -593,6 +595,8 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
         return OCSL_OK;
     }
     if (!A || !b || !x) return fail(c, OCSL_BAD_ARGUMENT, "null value, b or x pointer");
+    if (!aligned8(A) || !aligned8(b) || !aligned8(x))
+        return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
     Solve s{c, c->stream, c->P, c->P.n};
     int status = OCSL_OK;
     try {
@@ -878,6 +882,8 @@ int ocsl_gemv_device(ocsl_ctx* c, int mode, double a, const double* val, const d
     if (rc) return rc;
     if (mode < 0 || mode > 2 || !val || !x || !y || (mode > 0 && !z))
         return fail(c, OCSL_BAD_ARGUMENT, "bad gemv arguments");
+    if (!aligned8(val) || !aligned8(x) || !aligned8(y) || (z && !aligned8(z)))
+        return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
     try {
         CK(cudaSetDevice(c->device));
         launch_spmv<double>(c->stream, c->P, val, x, y, mode, nullptr, a, z, nullptr, nullptr, 0,
@@ -896,6 +902,8 @@ int ocsl_dot_device(ocsl_ctx* c, size_t n, const double* x, const double* y, dou
     if (n >= (size_t)INT32_MAX) return fail(c, OCSL_BAD_ARGUMENT, "n exceeds the int32 limit");
     if (n == 0) { *result = 0.0; return OCSL_OK; }
     if (!x || !y) return fail(c, OCSL_BAD_ARGUMENT, "null vector");
+    if (!aligned8(x) || !aligned8(y))
+        return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
     try {
         CK(cudaSetDevice(c->device));
         c->ensure_reduce((int)((n + kTile - 1) / kTile));
@@ -914,7 +922,8 @@ int ocsl_ilu_device(ocsl_ctx* c, const double* A, double* M, int sweeps)
 {
     int rc = check_ready(c);
     if (rc) return rc;
-    if (!A || !M || sweeps < 0) return fail(c, OCSL_BAD_ARGUMENT, "bad ilu arguments");
+    if (!A || !M || sweeps < 0 || !aligned8(A) || !aligned8(M))
+        return fail(c, OCSL_BAD_ARGUMENT, "bad ilu arguments");
     try {
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
@@ -933,7 +942,8 @@ static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double*
 {
     int rc = check_ready(c);
     if (rc) return rc;
-    if (!M || !in || !out || in == out) return fail(c, OCSL_BAD_ARGUMENT, "bad sweep arguments");
+    if (!M || !in || !out || in == out || !aligned8(M) || !aligned8(in) || !aligned8(out))
+        return fail(c, OCSL_BAD_ARGUMENT, "bad sweep arguments");
     try {
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};

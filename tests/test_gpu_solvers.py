@@ -229,3 +229,17 @@ def test_full_size_solves(ctx, oracle, hex128):
     xr, rr = run(ctx, ocsl.BICGSTAB_REF, s, x0)
     xo, res, it = oracle.bicgstab_ref(s.row_ptr, s.column_index, s.value, s.b, x0)
     assert np.array_equal(xr, xo) and rr["residual"] == res
+
+
+def test_misaligned_device_pointer_rejected(ctx, torch_cuda):
+    """A device pointer that is not 8-byte aligned is refused on the host,
+    before any kernel runs."""
+    s = W.hex_pprime(4)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = torch_cuda.from_numpy(s.value).cuda()
+    X = torch_cuda.zeros(s.n + 1, dtype=torch_cuda.float64, device="cuda")
+    Y = torch_cuda.zeros(s.n, dtype=torch_cuda.float64, device="cuda")
+    with pytest.raises(ocsl.OcslError) as e:
+        ctx.gemv_device(A, X.data_ptr() + 4, Y)
+    assert e.value.status == _abi.BAD_ARGUMENT
+    ctx.gemv_device(A, X[1:], Y)  # element-aligned offsets are fine
