@@ -98,11 +98,13 @@ int ocsl_synchronize(ocsl_ctx* ctx);
  * the diagonal are not below / above it. */
 int ocsl_set_pattern(ocsl_ctx* ctx, size_t n, const size_t* row_ptr, const size_t* column_index);
 /* Host-only check of a pattern (no device needed): the same validation and
- * level analysis as ocsl_set_pattern.  Writes the real nnz and the forward /
- * backward level counts; on OCSL_BAD_PATTERN writes the reason into err. */
+ * level analysis as ocsl_set_pattern.  Writes the real nnz, the forward /
+ * backward level counts and the detected 7-point box dims (nx, ny, nz; zeros
+ * when the pattern is not a box); on OCSL_BAD_PATTERN writes the reason into
+ * err.  Any output pointer may be NULL. */
 int ocsl_check_pattern(size_t n, const size_t* row_ptr, const size_t* column_index,
-                       int64_t* nnz_real, int32_t* fw_levels, int32_t* bw_levels, char* err,
-                       size_t err_len);
+                       int64_t* nnz_real, int32_t* fw_levels, int32_t* bw_levels,
+                       int32_t* box_dims, char* err, size_t err_len);
 /* Pattern facts: n, stored nnz (with phantoms), real nnz, forward and
  * backward level counts. */
 int ocsl_pattern_info(const ocsl_ctx* ctx, int64_t* n, int64_t* nnz, int64_t* nnz_real,
@@ -133,6 +135,16 @@ int ocsl_ilu_device(ocsl_ctx* ctx, const double* d_A, double* d_M, int sweeps);
 int ocsl_forsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_b, double* d_y);
 /* x = U^-1 y, cmatrix_solver.cpp:595-611 ILU_backsub. */
 int ocsl_backsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_y, double* d_x);
+
+/* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
+ * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
+ * level-scheduled kernel, 2 the structured kernel (OCSL_BAD_ARGUMENT if the
+ * pattern is not a box).  tile_a / tile_b set the structured kernel's column
+ * tile (0 = default 16 x 16).  Both kernels give bit-identical results. */
+int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
+/* The sweep kernel in use (1 level-scheduled, 2 structured), the detected box
+ * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB). */
+int ocsl_sweep_info(const ocsl_ctx* ctx, int* kind, int* dims, int* tiles);
 
 /* Kernel timing.  While enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream and accounted to a category:

@@ -65,15 +65,17 @@ def check_pattern(row_ptr, column_index):
     """Host-only validation + level analysis (ocsl_check_pattern).
 
     Returns ``(status, info)`` with ``info = {"nnz_real", "fw_levels",
-    "bw_levels", "error"}``.
+    "bw_levels", "box", "error"}``; ``box`` is the detected 7-point box
+    ``(nx, ny, nz)`` or zeros.
     """
     rp, col = _u64(row_ptr), _u64(column_index)
     nr, fw, bw = C.c_int64(0), C.c_int32(0), C.c_int32(0)
+    box = (C.c_int32 * 3)()
     buf = C.create_string_buffer(512)
     st = _abi.lib().ocsl_check_pattern(rp.size - 1, _ptr(rp), _ptr(col), C.byref(nr),
-                                       C.byref(fw), C.byref(bw), buf, 512)
+                                       C.byref(fw), C.byref(bw), box, buf, 512)
     return st, {"nnz_real": nr.value, "fw_levels": fw.value, "bw_levels": bw.value,
-                "error": buf.value.decode()}
+                "box": tuple(box), "error": buf.value.decode()}
 
 
 class Context:
@@ -160,6 +162,18 @@ class Context:
         if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT, _abi.NO_PATTERN) or (raise_on_status and st):
             self._check(st, "solve_device")
         return r.as_dict()
+
+    # -- triangular-sweep kernel choice
+    def set_sweep_kernel(self, kind: int = 0, tile_a: int = 0, tile_b: int = 0):
+        """0 automatic, 1 level-scheduled, 2 structured (7-point box patterns)."""
+        self._check(self._L.ocsl_set_sweep_kernel(self._h, kind, tile_a, tile_b), "sweep kernel")
+
+    def sweep_info(self):
+        kind = C.c_int()
+        dims = (C.c_int * 3)()
+        tiles = (C.c_int * 2)()
+        self._check(self._L.ocsl_sweep_info(self._h, C.byref(kind), dims, tiles), "sweep_info")
+        return {"kind": kind.value, "dims": tuple(dims), "tiles": tuple(tiles)}
 
     # -- kernel timing (ocsl_profile_*)
     def profile(self, enable: bool = True):

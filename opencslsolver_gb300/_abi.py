@@ -65,7 +65,8 @@ _PROTOS = {
     "ocsl_synchronize": (C.c_int, [_CTX]),
     "ocsl_set_pattern": (C.c_int, [_CTX, _SZ, _P, _P]),
     "ocsl_check_pattern": (C.c_int, [_SZ, _P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
-                                     C.POINTER(C.c_int32), C.c_char_p, _SZ]),
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_char_p,
+                                     _SZ]),
     "ocsl_pattern_info": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_int32)]),
@@ -77,6 +78,9 @@ _PROTOS = {
     "ocsl_ilu_device": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "ocsl_forsub_device": (C.c_int, [_CTX, _P, _P, _P]),
     "ocsl_backsub_device": (C.c_int, [_CTX, _P, _P, _P]),
+    "ocsl_set_sweep_kernel": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_int]),
+    "ocsl_sweep_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)]),
     "ocsl_profile_enable": (C.c_int, [_CTX, C.c_int]),
     "ocsl_profile_read": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "ocsl_profile_category_name": (C.c_char_p, [C.c_int]),

@@ -67,7 +67,19 @@ struct ReduceState {
     int max_tiles;
 };
 
+// Geometry of the structured sweep (7-point box patterns): canonical dims
+// (a, b, s) with s the dimension a CTA spans, (a, b) cut into TA x TB tiles.
+struct BoxGeom {
+    int D[3];      // extents of a, b, s
+    int S[3];      // row strides of a, b, s
+    int order[3];  // dims by descending stride = CSR order of the lower entries
+    int span;      // which of x (0), y (1), z (2) is the spanned dimension s
+    int TA, TB, nta, ntb;
+};
+
 struct DevPattern {
+    bool box_ok;
+    BoxGeom box;
     int n;
     int nnz;
     const int* rp;
@@ -141,6 +153,16 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
                      const T* rhs, T* out, int divmode, const SweepSync& S, const int* done);
 
 void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out);
+
+// Structured sweep on the stencil-SoA factor ([7][n]: z-, y-, x-, diag or
+// 1/diag, x+, y+, z+); divmode 0 divides by slot 3, 1 multiplies by it.
+template <typename T>
+void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, const T* rhs, T* out,
+                      bool forward, int divmode, const SweepSync& S, const int* done);
+// CSR factor (FP64) -> stencil SoA in TO; slot 3 = diagonal or (recip) 1/diagonal.
+template <typename TO>
+void launch_box_to_soa(cudaStream_t st, const int* dims, int n, const int* rp, const double* M,
+                       TO* soa, int recip);
 
 // All-ones fill of a sweep output (skipped once the solve is done).
 void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done);

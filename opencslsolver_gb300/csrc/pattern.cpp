@@ -49,6 +49,52 @@ void schedule(int n, const std::vector<int>& level, int nlevels, std::vector<int
 
 }  // namespace
 
+BoxShape detect_box(int n, const std::vector<int>& rp, const std::vector<int>& col)
+{
+    BoxShape none;
+    if (n < 2) return none;
+    // Row 0's real upper columns give the strides: [1], [1, nx] or [1, nx, nx*ny].
+    std::vector<long long> up;
+    for (int q = rp[0]; q < rp[1]; ++q)
+        if (col[q] > 0) up.push_back(col[q]);
+    long long nx, ny, nz;
+    if (up.size() == 1 && up[0] == 1) {
+        nx = n; ny = 1; nz = 1;
+    } else if (up.size() == 2 && up[0] == 1 && up[1] > 1 && n % up[1] == 0) {
+        nx = up[1]; ny = n / up[1]; nz = 1;
+    } else if (up.size() == 3 && up[0] == 1 && up[1] > 1 && up[2] % up[1] == 0 && up[2] > up[1] &&
+               n % up[2] == 0) {
+        nx = up[1]; ny = up[2] / up[1]; nz = n / up[2];
+    } else {
+        return none;
+    }
+    const long long nxy = nx * ny;
+    for (int r = 0; r < n; ++r) {
+        const long long i = r % nx, j = (r / nx) % ny, k = r / nxy;
+        long long want[7];
+        int m = 0;
+        if (k > 0) want[m++] = r - nxy;
+        if (j > 0) want[m++] = r - nx;
+        if (i > 0) want[m++] = r - 1;
+        want[m++] = r;
+        if (i < nx - 1) want[m++] = r + 1;
+        if (j < ny - 1) want[m++] = r + nx;
+        if (k < nz - 1) want[m++] = r + nxy;
+        int q = rp[r], t = 0;
+        for (; q < rp[r + 1] && col[q] >= 0; ++q, ++t)
+            if (t >= m || col[q] != want[t]) return none;
+        if (t != m) return none;
+        for (; q < rp[r + 1]; ++q)
+            if (col[q] >= 0) return none;  // only phantoms may follow
+    }
+    BoxShape b;
+    b.ok = true;
+    b.dim[0] = (int)nx;
+    b.dim[1] = (int)ny;
+    b.dim[2] = (int)nz;
+    return b;
+}
+
 bool analyse_pattern(size_t n_in, const size_t* rp, const size_t* col, HostPattern& hp,
                      std::string& err)
 {
@@ -144,6 +190,7 @@ bool analyse_pattern(size_t n_in, const size_t* rp, const size_t* col, HostPatte
     }
     hp.bw_levels = nl;
     schedule(n, level, nl, hp.bw_order, hp.bw_chunk, kChunkRows);
+    hp.box = detect_box(n, hp.rp, hp.col);
     return true;
 }
 

@@ -10,7 +10,16 @@ namespace ocsl {
 
 constexpr int kChunkRows = 256;  // rows per chunk of a sweep level (one CTA)
 
+// A pattern that is exactly the 7-point stencil of an nx * ny * nz box in
+// natural order (row = i + nx * (j + ny * k)), with optional phantom columns
+// after the real ones.  Such rows can be swept by the structured kernel.
+struct BoxShape {
+    bool ok = false;
+    int dim[3] = {0, 0, 0};     // nx, ny, nz
+};
+
 struct HostPattern {
+    BoxShape box;
     int n = 0;
     int nnz = 0;
     long long nnz_real = 0;
@@ -20,6 +29,9 @@ struct HostPattern {
     std::vector<int> pair_ptr, pair_k, pair_slot;
     std::vector<int> fw_order, fw_chunk, bw_order, bw_chunk;
 };
+
+// Recognise the 7-point box stencil (see BoxShape); O(nnz).
+BoxShape detect_box(int n, const std::vector<int>& rp, const std::vector<int>& col);
 
 // Validate the reference-layout pattern and build the device tables.
 // Returns false with a message on a rejected pattern.

@@ -85,6 +85,8 @@ struct ocsl_ctx {
     float* d_M32 = nullptr;
     float* d_dinv32 = nullptr;
     float* v32[NVEC32] = {};
+    double* d_soa64 = nullptr;  // stencil-SoA factor copies (7-point box patterns)
+    float* d_soa32 = nullptr;
 
     ReduceState R{};
     Scalars* d_sc = nullptr;  // [0] main / outer, [1] inner, [2] utility
@@ -95,6 +97,10 @@ struct ocsl_ctx {
     int* h_err = nullptr;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaEvent_t ev_batch[2] = {nullptr, nullptr};
+
+    // sweep kernel choice (ocsl_set_sweep_kernel): 0 auto, 1 level-scheduled, 2 structured
+    int sweep_kernel = 0;
+    int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
 
     // kernel timing (ocsl_profile_*)
     bool prof_on = false;
@@ -114,7 +120,9 @@ void ocsl_ctx::free_pattern()
     double** d64[] = {&d_A, &d_b, &d_x, &d_Ma, &d_Mb, &d_dinv};
     for (auto pp : d64) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     for (auto& v : v64) { if (v) cudaFree(v); v = nullptr; }
-    float** d32[] = {&d_A32, &d_M32, &d_dinv32};
+    float** d32[] = {&d_A32, &d_M32, &d_dinv32, &d_soa32};
+    if (d_soa64) cudaFree(d_soa64);
+    d_soa64 = nullptr;
     for (auto pp : d32) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     for (auto& v : v32) { if (v) cudaFree(v); v = nullptr; }
     has_pattern = false;
@@ -163,6 +171,7 @@ void ocsl_ctx::ensure_fp32()
     d_M32 = dalloc<float>(nnz);
     d_dinv32 = dalloc<float>(n);
     for (auto& v : v32) v = dalloc<float>(n);
+    if (hp.box.ok) d_soa32 = dalloc<float>(7 * n);
 }
 
 namespace {
@@ -230,11 +239,47 @@ struct ProfScope {
 template <typename TT>
 constexpr bool is_f64() { return sizeof(TT) == 8; }
 
+// Canonical geometry of the structured sweep: the longest dimension is spanned
+// by each CTA (ties to the larger stride), the other two are tiled.
+BoxGeom make_box_geom(const BoxShape& bs, int TA_req, int TB_req)
+{
+    const int E[3] = {bs.dim[0], bs.dim[1], bs.dim[2]};
+    const int St[3] = {1, bs.dim[0], bs.dim[0] * bs.dim[1]};
+    int span = 2;
+    for (int d = 1; d >= 0; --d)
+        if (E[d] > E[span]) span = d;
+    int rest[2], m = 0;
+    for (int d = 0; d < 3; ++d)
+        if (d != span) rest[m++] = d;  // ascending stride
+    BoxGeom g{};
+    g.span = span;
+    const int dims[3] = {rest[0], rest[1], span};
+    for (int k = 0; k < 3; ++k) {
+        g.D[k] = E[dims[k]];
+        g.S[k] = St[dims[k]];
+    }
+    int ord[3] = {0, 1, 2};
+    std::sort(ord, ord + 3, [&](int x, int y) { return g.S[x] > g.S[y]; });
+    for (int k = 0; k < 3; ++k) g.order[k] = ord[k];
+    // one warp per tile: WA x WB <= 32 lanes (8 x 4 by default; 32 x 1 when b is flat)
+    int wa = TA_req > 0 ? TA_req : (g.D[1] == 1 ? 32 : 8);
+    int wb = TB_req > 0 ? TB_req : (g.D[1] == 1 ? 1 : 4);
+    wa = std::max(1, std::min(wa, 32));
+    wb = std::max(1, std::min(wb, 32 / wa));
+    g.TA = std::min(wa, std::max(1, g.D[0]));
+    g.TB = std::min(wb, std::max(1, g.D[1]));
+    g.nta = (g.D[0] + g.TA - 1) / g.TA;
+    g.ntb = (g.D[1] + g.TB - 1) / g.TB;
+    return g;
+}
+
 struct Solve {
     ocsl_ctx* c;
     cudaStream_t st;
     const DevPattern& P;
     int n;
+    const double* soa64 = nullptr;  // stencil-SoA copy of the current factor
+    const float* soa32 = nullptr;
 
     Scalars* sc(int k) const { return c->d_sc + k; }
 
@@ -318,7 +363,36 @@ struct Solve {
             fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
-        launch_fw_sweep<TT>(st, P, M, rhs, out, c->S, k >= 0 ? done(k) : nullptr);
+        if (use_box() && soa<TT>())
+            launch_box_sweep<TT>(st, P.box, P.n, soa<TT>(), rhs, out, true, 0, c->S,
+                                 k >= 0 ? done(k) : nullptr);
+        else
+            launch_fw_sweep<TT>(st, P, M, rhs, out, c->S, k >= 0 ? done(k) : nullptr);
+    }
+    bool use_box() const { return P.box_ok && c->sweep_kernel != 1; }
+    // After a factorisation: the structured sweeps read the factor in the
+    // stencil-SoA layout (slot 3: diagonal for the reference's division, or
+    // its reciprocal for the tolerance-mode multiply).
+    void prepare_box(const double* M, bool want64, bool recip64, bool want32)
+    {
+        soa64 = nullptr;
+        soa32 = nullptr;
+        if (!use_box()) return;
+        ProfScope ps(c, st, PC_ILU);
+        if (want64) {
+            launch_box_to_soa<double>(st, c->hp.box.dim, P.n, P.rp, M, c->d_soa64, recip64 ? 1 : 0);
+            soa64 = c->d_soa64;
+        }
+        if (want32) {
+            launch_box_to_soa<float>(st, c->hp.box.dim, P.n, P.rp, M, c->d_soa32, 1);
+            soa32 = c->d_soa32;
+        }
+    }
+    template <typename TT>
+    const TT* soa() const
+    {
+        if constexpr (sizeof(TT) == 8) return soa64;
+        else return soa32;
     }
     template <typename TT>
     void fill_sentinel(TT* out, int k)
@@ -333,7 +407,12 @@ struct Solve {
             fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
-        launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S, k >= 0 ? done(k) : nullptr);
+        if (use_box() && soa<TT>())
+            launch_box_sweep<TT>(st, P.box, P.n, soa<TT>(), rhs, out, false, divmode, c->S,
+                                 k >= 0 ? done(k) : nullptr);
+        else
+            launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S,
+                                k >= 0 ? done(k) : nullptr);
     }
     int device_error()
     {
@@ -376,6 +455,7 @@ void run_bicgstab_ref(Solve& s, const double* A, const double* b, double* x, int
     CK(cudaMemsetAsync(v[P], 0, bytes, s.st));  // Cvector(n) starts at 0 (:690-700)
     CK(cudaMemsetAsync(v[V], 0, bytes, s.st));
     const double* M = s.factor(A, sweeps, false, false, 0);  // :702-704
+    s.prepare_box(M, true, false, false);
     // r = b - A x (:708), r0 = r (:710), iteration 0's rhon and res
     s.spmv<double>(A, x, v[R], 1, b, v[R0], nullptr, DOT_YY | DOT_ZZ, 0, EP_RB_INIT);
     for (int it = 0; it < kRefBicgIters; ++it) {
@@ -500,6 +580,7 @@ TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x
 {
     double** v = s.c->v64;
     const double* M = s.factor(A, o.ilu_sweeps, true, false, -1);
+    s.prepare_box(M, true, true, false);
     return run_restarted(
         s, A, b, x, o, [&] { s.vec<double>(V_COPY2, {v[RH], v[P], v[R]}, 0, EP_STORE); },
         [&](int) {
@@ -536,7 +617,8 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
     float** f = c->v32;
     TolResult res;
     const double tol2 = o.tol * o.tol;
-    s.factor(A, o.ilu_sweeps, true, true, -1);
+    const double* M = s.factor(A, o.ilu_sweeps, true, true, -1);
+    s.prepare_box(M, false, true, true);
     int total = 0;
     s.reset_scalars(0, tol2);
     for (int outer = 0;; ++outer) {
@@ -784,6 +866,9 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         P.bw_order = c->d_pat[8];
         P.bw_chunk = c->d_pat[9];
         P.bw_nchunks = (int)hp.bw_chunk.size() - 1;
+        P.box_ok = hp.box.ok && c->sweep_kernel != 1;
+        if (hp.box.ok) P.box = make_box_geom(hp.box, c->box_tile[0], c->box_tile[1]);
+        c->hp.box = hp.box;
         const size_t nn = (size_t)hp.n, nz = (size_t)hp.nnz;
         c->d_A = dalloc<double>(nz);
         c->d_b = dalloc<double>(nn);
@@ -792,6 +877,7 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         c->d_Mb = dalloc<double>(nz);
         c->d_dinv = dalloc<double>(nn);
         for (auto& v : c->v64) v = dalloc<double>(nn);
+        if (hp.box.ok) c->d_soa64 = dalloc<double>(7 * nn);
         c->ensure_reduce((hp.n + kTile - 1) / kTile);
         // drop the large host tables, keep the facts
         c->hp.n = hp.n;
@@ -808,7 +894,8 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
 }
 
 int ocsl_check_pattern(size_t n, const size_t* rp, const size_t* col, int64_t* nnz_real,
-                       int32_t* fw_levels, int32_t* bw_levels, char* err, size_t err_len)
+                       int32_t* fw_levels, int32_t* bw_levels, int32_t* box_dims, char* err,
+                       size_t err_len)
 {
     HostPattern hp;
     std::string msg;
@@ -820,6 +907,8 @@ int ocsl_check_pattern(size_t n, const size_t* rp, const size_t* col, int64_t* n
     if (nnz_real) *nnz_real = hp.nnz_real;
     if (fw_levels) *fw_levels = hp.fw_levels;
     if (bw_levels) *bw_levels = hp.bw_levels;
+    if (box_dims)
+        for (int k = 0; k < 3; ++k) box_dims[k] = hp.box.ok ? hp.box.dim[k] : 0;
     return OCSL_OK;
 }
 
@@ -948,6 +1037,7 @@ static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double*
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
         CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+        s.prepare_box(M, true, false, false);  // the reference's backsub divides
         if (forward)
             s.fw<double>(M, in, out, -1);
         else
@@ -956,6 +1046,34 @@ static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double*
         if (s.device_error()) return fail(c, OCSL_TIMEOUT, "a triangular-sweep wait hit its bound");
     } catch (const CudaError& e) {
         return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
+{
+    if (!c || kind < 0 || kind > 2 || tile_a < 0 || tile_b < 0) return OCSL_BAD_ARGUMENT;
+    if (kind == 2 && c->has_pattern && !c->hp.box.ok)
+        return fail(c, OCSL_BAD_ARGUMENT, "the pattern is not a 7-point box stencil");
+    c->sweep_kernel = kind;
+    c->box_tile[0] = tile_a;
+    c->box_tile[1] = tile_b;
+    if (c->has_pattern) {
+        c->P.box_ok = c->hp.box.ok && kind != 1;
+        if (c->hp.box.ok) c->P.box = make_box_geom(c->hp.box, tile_a, tile_b);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (!c->has_pattern) return OCSL_NO_PATTERN;
+    if (kind) *kind = c->P.box_ok ? 2 : 1;
+    if (dims) for (int k = 0; k < 3; ++k) dims[k] = c->hp.box.ok ? c->hp.box.dim[k] : 0;
+    if (tiles) {
+        tiles[0] = c->P.box_ok ? c->P.box.TA : 0;
+        tiles[1] = c->P.box_ok ? c->P.box.TB : 0;
     }
     return OCSL_OK;
 }

@@ -132,3 +132,51 @@ def test_full_size_spmv_and_sweeps(ctx, torch_cuda, oracle, hex128):
     Z = torch_cuda.empty_like(X)
     ctx.backsub_device(M, Y, Z)
     assert np.array_equal(host(Z), oracle.backsub(s.row_ptr, s.column_index, Mh, y))
+
+
+BOXES = [(20, 20, 20), (13, 7, 9), (5, 17, 3), (33, 1, 1), (9, 12, 1), (1000, 1, 1)]
+
+
+@pytest.mark.parametrize("dims", BOXES)
+@pytest.mark.parametrize("tiles", [(0, 0), (4, 8), (3, 5), (32, 8)])
+def test_structured_sweeps_bit_exact(ctx, torch_cuda, oracle, dims, tiles):
+    """The structured (box) sweep kernel against the oracle and against the
+    level-scheduled kernel, for several box shapes and column tiles."""
+    if dims[1] == 1:
+        rp, col = W.pattern_1d(dims[0])
+        rng = np.random.default_rng(2)
+        val = np.where(col == W.PHANTOM, 0.0, rng.uniform(-1, 0, col.size))
+        rows = np.repeat(np.arange(dims[0]), np.diff(rp.astype(np.int64)))
+        val[col == rows.astype(np.uint64)] = 3.0
+        s = W.System(rp, col, val, rng.uniform(-1, 1, dims[0]))
+    else:
+        s = W.hex_pprime(*dims)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    ctx.set_sweep_kernel(2, *tiles)
+    info = ctx.sweep_info()
+    assert info["kind"] == 2
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal(s.n)
+    Mh = oracle.ilu(s.row_ptr, s.column_index, s.value)
+    M, B = dev(torch_cuda, Mh), dev(torch_cuda, b)
+    Y, X = torch_cuda.empty_like(B), torch_cuda.empty_like(B)
+    ctx.forsub_device(M, B, Y)
+    y = oracle.forsub(s.row_ptr, s.column_index, Mh, b)
+    assert np.array_equal(host(Y), y)
+    ctx.backsub_device(M, Y, X)
+    assert np.array_equal(host(X), oracle.backsub(s.row_ptr, s.column_index, Mh, y))
+    ctx.set_sweep_kernel(1)
+    assert ctx.sweep_info()["kind"] == 1
+    X2 = torch_cuda.empty_like(B)
+    ctx.backsub_device(M, Y, X2)
+    assert torch_cuda.equal(X, X2)
+
+
+def test_structured_kernel_refused_for_unstructured(ctx):
+    s = W.tet_pprime(3)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    assert ctx.sweep_info()["kind"] == 1
+    import opencslsolver_gb300 as ocsl
+
+    with pytest.raises(ocsl.OcslError):
+        ctx.set_sweep_kernel(2)

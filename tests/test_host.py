@@ -153,3 +153,30 @@ def test_workload_properties():
     A = sp.csr_matrix((sym.value[real], (rows[real], sym.column_index[real].astype(np.int64))),
                       shape=(n, n))
     assert abs(A - A.T).max() == 0
+
+
+def test_box_detection():
+    for dims in ((4, 4, 4), (7, 5, 3), (16, 1, 1), (9, 6, 1), (2, 2, 2)):
+        rp, col = W.hex_pattern(*dims)
+        st, info = ocsl.check_pattern(rp, col)
+        assert st == 0
+        nx, ny, nz = dims
+        want = (nx, ny, nz) if ny > 1 else (nx, 1, 1)
+        if ny > 1 and nz == 1:
+            want = (nx, ny, 1)
+        assert info["box"] == want, (dims, info["box"])
+    # the reference's 1D shock-tube pattern is a 1000 x 1 x 1 box
+    rp, col = W.pattern_1d(1000)
+    assert ocsl.check_pattern(rp, col)[1]["box"] == (1000, 1, 1)
+    # unstructured patterns are not
+    s = W.tet_pprime(3)
+    assert ocsl.check_pattern(s.row_ptr, s.column_index)[1]["box"] == (0, 0, 0)
+    s = W.random_rows_system(200, 8)
+    assert ocsl.check_pattern(s.row_ptr, s.column_index)[1]["box"] == (0, 0, 0)
+    # a box pattern with one stencil entry dropped is not a box
+    rp, col = W.hex_pattern(5, 5, 5)
+    rp2 = rp.copy()
+    col2 = np.delete(col, int(rp[62]) + 1)  # row 62 loses an entry (sorted order kept)
+    rp2[63:] -= 1
+    st, info = ocsl.check_pattern(rp2, col2)
+    assert st == 0 and info["box"] == (0, 0, 0)
