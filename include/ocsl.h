@@ -140,7 +140,8 @@ int ocsl_backsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_y, dou
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured kernel (OCSL_BAD_ARGUMENT if the
  * pattern is not a box).  tile_a / tile_b set the structured kernel's column
- * tile (0 = default 16 x 16).  Both kernels give bit-identical results. */
+ * tile, one thread per column, at most 256 (0 = default 16 x 8).  All
+ * kernels give bit-identical results. */
 int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
 /* The sweep kernel in use (1 level-scheduled, 2 structured), the detected box
  * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB). */

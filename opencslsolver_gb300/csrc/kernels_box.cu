@@ -4,29 +4,23 @@
 // nx * ny * nz box (recognised on the host), a row's dependencies are its
 // -1 neighbours in each dimension (+1 for the backward sweep).
 //
-// Factor layout.  box_to_soa_kernel copies the CSR factor into seven arrays
-// indexed by row ("stencil SoA"): coefficient of the z-, y-, x- neighbour,
-// the diagonal (or its reciprocal), x+, y+, z+.  An absent neighbour is
-// stored as an exact 0 and its dependency value is taken as 0, so its fma
-// adds exactly nothing to a sum that starts at +0: the straight-line fma
-// chain below equals the reference's loop over the row's CSR entries in
-// storage order (cmatrix_solver.cpp:562-570 forward, :602-610 backward), bit
-// for bit.  Every load is affine in the row index.
+// Factor layout.  box_to_soa_kernel copies the CSR factor into two arrays of
+// packed 4-element row records: (z-, y-, x-, 0) for the forward sweep and
+// (x+, y+, z+, diagonal or its reciprocal) for the backward sweep.  An absent
+// neighbour is stored as an exact 0 and its dependency value is taken as 0,
+// so its fma adds exactly nothing to a sum that starts at +0: the
+// straight-line fma chain below equals the reference's loop over the row's
+// CSR entries in storage order (cmatrix_solver.cpp:562-570 forward,
+// :602-610 backward), bit for bit.  A row's record is one aligned 16-byte
+// (FP32) or 32-byte (FP64) copy.
 //
 // Schedule.  The box is viewed in canonical coordinates (a, b, s): s spans
-// the longest dimension, (a, b) are cut into WA x WB tiles (8 x 4 by
-// default); one warp owns one tile of columns and all of s, one lane one
-// column, and the lanes run skewed in time (see box_sweep_kernel):
-//   * the dependency along s is the lane's own previous row (a register);
-//   * dependencies inside the tile come from the neighbouring lanes by
-//     __shfl_up -- no barrier, no shared memory;
-//   * the tile faces read the neighbouring tiles' rows from global memory;
-//     the output was filled with an all-ones pattern, so a value is its own
-//     ready flag (bounded wait, OCSL_TIMEOUT on expiry).
-// Tiles are handed out by an atomic ticket in an order where a tile's two
-// predecessors always come first, so waits cannot deadlock.  Row data and
-// face values are prefetched kPF steps ahead with cp.async into a shared-memory
-// ring whose slot is t mod kPF.
+// the longest dimension, (a, b) are cut into TA x TB tiles; one CTA owns one
+// tile of columns and all of s (see box_cta_kernel).  Tiles are handed out by
+// an atomic ticket in an order where a tile's two predecessors always come
+// first, so waits cannot deadlock.  The output was filled with an all-ones
+// pattern, so a face value is its own ready flag (bounded wait, OCSL_TIMEOUT
+// on expiry).
 #include "ocsl_internal.cuh"
 
 namespace ocsl {
@@ -34,7 +28,6 @@ namespace ocsl {
 namespace {
 
 constexpr long kSpinLimit = 1L << 21;
-constexpr int kPF = 8;  // wavefronts of prefetch per thread
 
 // Relaxed gpu-scope accesses of the value-as-flag protocol.  `volatile` keeps
 // every poll a fresh load; no "memory" clobber, since nothing else is ordered
@@ -122,6 +115,16 @@ __device__ __forceinline__ void cp_async(T* smem_dst, const T* gsrc)
     else
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gsrc) : "memory");
 }
+// One packed 4-element record (16 bytes for FP32, 32 bytes for FP64).
+template <typename T>
+__device__ __forceinline__ void cp_async_vec(void* smem_dst, const void* gsrc)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    const char* s = static_cast<const char*>(gsrc);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(s) : "memory");
+    if constexpr (sizeof(T) == 8)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16), "l"(s + 16) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
@@ -130,7 +133,7 @@ template <typename T>
 struct BoxParams {
     BoxGeom g;
     int n;
-    const T* soa;  // [7][n]: z-, y-, x-, diag or 1/diag, x+, y+, z+
+    const T* soa;  // packed records [2][n][4]: (z-, y-, x-, 0), (x+, y+, z+, diagonal term)
     const T* rhs;
     T* out;
     SweepSync S;
@@ -142,128 +145,136 @@ struct BoxParams {
 // SPAN: which of x (0), y (1), z (2) the canonical s dimension is; a and b
 // are the other two in ascending stride.
 //
-// One warp sweeps one WA x WB tile of columns.  Lane (la, lb) handles column
-// (ca, cb) and sweeps its row cs = t - la - lb at warp step t, so at step t
-// the a-neighbour (lane - 1) and the b-neighbour (lane - WA) hold, from step
-// t - 1, exactly the values this row needs: they arrive by __shfl_up, with
-// no barrier and no shared memory.  The s-neighbour is the lane's own value
-// from step t - 1.  Lanes on the tile's a / b faces read the neighbouring
-// tiles' rows from global memory instead.
+// One CTA (TA x TB threads, 16 x 8 by default) sweeps one tile of columns,
+// walking the wavefronts W = a + b + s of its tile with one __syncthreads per
+// wavefront.  The s-neighbour is the thread's own previous row, in-tile a / b
+// neighbours come from a 2-slot shared-memory ring, tile faces from the
+// neighbouring CTAs' rows in global memory.  Row data (one 16- or 32-byte
+// packed coefficient record, rhs, face values) are staged kPFc wavefronts
+// ahead with cp.async into shared memory, slot W mod kPFc (uniform over the
+// CTA); a face word still all-ones at use is polled again from L2.
+constexpr int kPFc = 6;
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    float v[4];
+};
+template <>
+struct Vec4<double> {
+    double v[4];
+};
+
 template <typename T, bool FWD, bool DIV, int SPAN>
-__global__ void __launch_bounds__(32) box_sweep_kernel(BoxParams<T> p)
+__global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
 {
     if (p.done && *p.done) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const BoxGeom& g = p.g;
-    const int lane = threadIdx.x;
-    int tile = 0;
-    if (lane == 0) tile = (int)atomicAdd(p.S.ticket, 1u);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
+    const int TA = g.TA, TB = g.TB, NT = g.TA * g.TB;
+    using V4 = Vec4<T>;
+    V4* coef = reinterpret_cast<V4*>(smem_raw);  // [kPFc][NT] packed row records
+    T* ring = reinterpret_cast<T*>(coef + kPFc * NT);  // [2][NT]
+    T* sc = ring + 2 * NT;                      // [kPFc][3][NT]: rhs, face a, face b
+    __shared__ int s_tile;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
+    __syncthreads();
+    const int tile = s_tile;
     if (tile >= g.nta * g.ntb) {
-        if (lane == 0) atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
+        if (threadIdx.x == 0) atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
     } else {
         using B = Bits<T>;
         using U = typename B::U;
-        const int WA = g.TA, WB = g.TB;
+        const int tid = threadIdx.x;
         const int ta = tile % g.nta, tb = tile / g.nta;
-        const int la = lane % WA, lb = lane / WA;
-        const int ca = ta * WA + la, cb = tb * WB + lb;
+        const int la = tid % TA, lb = tid / TA;
+        const int ca = ta * TA + la, cb = tb * TB + lb;
         const int Da = g.D[0], Db = g.D[1], Ds = g.D[2];
-        const bool col_ok = lb < WB && ca < Da && cb < Db;
+        const bool col_ok = ca < Da && cb < Db;
         const int a = FWD ? ca : Da - 1 - ca;
         const int b = FWD ? cb : Db - 1 - cb;
         const int base = a * g.S[0] + b * g.S[1];
-        const int sstep = FWD ? g.S[2] : -g.S[2];  // row step along the column
+        const int sstep = FWD ? g.S[2] : -g.S[2];
         const int row0 = FWD ? base : base + (Ds - 1) * g.S[2];
-        const int dstep = FWD ? -1 : 1;             // offset sign of a dependency
+        const int dstep = FWD ? -1 : 1;
+        const int ta_end = min(ta * TA + TA, Da), tb_end = min(tb * TB + TB, Db);
+        const int W0 = ta * TA + tb * TB;
+        const int W1 = (ta_end - 1) + (tb_end - 1) + Ds - 1;
         const bool has_a = ca > 0, has_b = cb > 0;
         const bool face_a = col_ok && has_a && la == 0;
         const bool face_b = col_ok && has_b && lb == 0;
         const int off_a = dstep * g.S[0], off_b = dstep * g.S[1];
-        const int c0 = la + lb;                     // skew: row cs = t - c0 at step t
-        const int Tmax = (WA - 1) + (WB - 1) + Ds - 1;
-        const int n = p.n;
-        // coefficient arrays in the order of the row's CSR entries
-        const T* C0 = p.soa + (size_t)(FWD ? 0 : 4) * n;  // z- | x+
-        const T* C1 = p.soa + (size_t)(FWD ? 1 : 5) * n;  // y- | y+
-        const T* C2 = p.soa + (size_t)(FWD ? 2 : 6) * n;  // x- | z+
-        const T* CD = p.soa + (size_t)3 * n;
+        const int c0 = ca + cb;  // the thread sweeps row cs = W - c0 at wavefront W
+        const V4* pack = reinterpret_cast<const V4*>(p.soa) + (FWD ? 0 : p.n);
         auto in_range = [&](int cs) { return col_ok && cs >= 0 && cs < Ds; };
-
-        // Prefetch ring in shared memory, slot j = t mod kPF: stage[j][f][lane]
-        // holds the row's three coefficients (f 0-2), diagonal term (3), rhs
-        // (4) and face values (5, 6), copied with cp.async kPF steps ahead;
-        // one commit group per step, so wait_group(kPF - 1) before use leaves
-        // exactly the slot of this step complete.  A face word still holding
-        // the all-ones pattern is polled from L2.
-        __shared__ T stage[kPF][7][32];
         auto refill = [&](int cs, int j) {
             if (in_range(cs)) {
                 const int r = row0 + cs * sstep;
-                cp_async(&stage[j][0][lane], C0 + r);
-                cp_async(&stage[j][1][lane], C1 + r);
-                cp_async(&stage[j][2][lane], C2 + r);
-                if (!FWD) cp_async(&stage[j][3][lane], CD + r);
-                cp_async(&stage[j][4][lane], p.rhs + r);
-                if (face_a) cp_async(&stage[j][5][lane], (const T*)p.out + r + off_a);
-                if (face_b) cp_async(&stage[j][6][lane], (const T*)p.out + r + off_b);
+                cp_async_vec<T>(&coef[j * NT + tid], pack + r);
+                cp_async(&sc[(j * 3 + 0) * NT + tid], p.rhs + r);
+                if (face_a) cp_async(&sc[(j * 3 + 1) * NT + tid], (const T*)p.out + r + off_a);
+                if (face_b) cp_async(&sc[(j * 3 + 2) * NT + tid], (const T*)p.out + r + off_b);
             }
             cp_async_commit();
         };
+        const int Wbase = W0 - (W0 % kPFc);
 #pragma unroll
-        for (int j = 0; j < kPF; ++j) refill(j - c0, j);
+        for (int j = 0; j < kPFc; ++j) refill(Wbase + j - c0, j);
 
-        T ylast = T(0);  // this lane's value from the previous step
-        for (int t0 = 0; t0 <= Tmax; t0 += kPF) {
+        T prev = T(0);
+        for (int Wb = Wbase; Wb <= W1; Wb += kPFc) {
 #pragma unroll
-            for (int j = 0; j < kPF; ++j) {
-                const int t = t0 + j;
-                if (t > Tmax) break;  // warp-uniform
-                const int cs = t - c0;
-                const T ya = __shfl_up_sync(0xffffffffu, ylast, 1);
-                const T yb = __shfl_up_sync(0xffffffffu, ylast, WA);
-                cp_async_wait<kPF - 1>();
-                if (in_range(cs)) {
-                    const int r = row0 + cs * sstep;
+            for (int j = 0; j < kPFc; ++j) {
+                const int W = Wb + j;
+                if (W > W1) break;  // uniform over the CTA
+                const int cs = W - c0;
+                cp_async_wait<kPFc - 1>();
+                if (W >= W0 && in_range(cs)) {
+                    const V4 c = coef[j * NT + tid];
+                    const T* rd = ring + ((W - 1) & 1) * NT;
                     T va = T(0), vb = T(0);
                     if (has_a) {
                         if (la > 0) {
-                            va = ya;
+                            va = rd[tid - 1];
                         } else {
-                            const U u = B::to(stage[j][5][lane]);
-                            va = u != B::kSentinel ? B::from(u) : wait_value(p.out + r + off_a, p.S.err);
+                            const U u = B::to(sc[(j * 3 + 1) * NT + tid]);
+                            va = u != B::kSentinel ? B::from(u)
+                                                   : wait_value(p.out + row0 + cs * sstep + off_a, p.S.err);
                         }
                     }
                     if (has_b) {
                         if (lb > 0) {
-                            vb = yb;
+                            vb = rd[tid - TA];
                         } else {
-                            const U u = B::to(stage[j][6][lane]);
-                            vb = u != B::kSentinel ? B::from(u) : wait_value(p.out + r + off_b, p.S.err);
+                            const U u = B::to(sc[(j * 3 + 2) * NT + tid]);
+                            vb = u != B::kSentinel ? B::from(u)
+                                                   : wait_value(p.out + row0 + cs * sstep + off_b, p.S.err);
                         }
                     }
-                    const T vs = cs > 0 ? ylast : T(0);
-                    // dependency values of the x, y, z neighbours
+                    const T vs = cs > 0 ? prev : T(0);
                     const T vx = SPAN == 0 ? vs : va;
                     const T vy = SPAN == 0 ? va : (SPAN == 1 ? vs : vb);
                     const T vz = SPAN == 2 ? vs : vb;
-                    // CSR order: z-, y-, x- (forward); x+, y+, z+ (backward)
-                    T sum = fma_t(stage[j][0][lane], FWD ? vz : vx, T(0));
-                    sum = fma_t(stage[j][1][lane], vy, sum);
-                    sum = fma_t(stage[j][2][lane], FWD ? vx : vz, sum);
-                    const T num = stage[j][4][lane] - sum;
-                    const T y = FWD ? num : (DIV ? num / stage[j][3][lane] : num * stage[j][3][lane]);
-                    publish(p.out + r, y);
-                    ylast = y;
+                    // packed record: z-, y-, x-, (unused) | x+, y+, z+, diagonal term;
+                    // the fma order is the row's CSR order
+                    T sum = fma_t(c.v[0], FWD ? vz : vx, T(0));
+                    sum = fma_t(c.v[1], vy, sum);
+                    sum = fma_t(c.v[2], FWD ? vx : vz, sum);
+                    const T num = sc[(j * 3 + 0) * NT + tid] - sum;
+                    const T y = FWD ? num : (DIV ? num / c.v[3] : num * c.v[3]);
+                    ring[(W & 1) * NT + tid] = y;
+                    publish(p.out + row0 + cs * sstep, y);
+                    prev = y;
                 }
-                __syncwarp();  // the slot's reads are done before it is refilled
-                refill(cs + kPF, j);
+                refill(cs + kPFc, j);
+                if (W >= W0) __syncthreads();  // uniform over the CTA
             }
         }
         cp_async_wait<0>();
     }
-    // reset the dispenser after the last tile
-    __syncwarp();
-    if (lane == 0) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(p.S.finished, 1u) == gridDim.x - 1) {
             *p.S.ticket = 0u;
@@ -272,36 +283,59 @@ __global__ void __launch_bounds__(32) box_sweep_kernel(BoxParams<T> p)
     }
 }
 
-// CSR factor -> stencil SoA.  Row r's real entries are, in storage order,
-// z-, y-, x-, diagonal, x+, y+, z+ (absent ones skipped), then phantoms; the
-// host verified exactly this pattern.  Slot 3 gets the diagonal (RECIP == 0)
-// or 1 / diagonal computed in FP64.
+// CSR factor -> packed stencil records.  Row r's real entries are, in
+// storage order, z-, y-, x-, diagonal, x+, y+, z+ (absent ones skipped), then
+// phantoms; the host verified exactly this pattern.  pack[0][r] = (z-, y-,
+// x-, 0), pack[1][r] = (x+, y+, z+, diagonal) with the diagonal replaced by
+// 1 / diagonal (computed in FP64) when RECIP.  Absent entries are exact 0.
 template <typename TO, int RECIP>
 __global__ void box_to_soa_kernel(int n, int nx, int ny, int nz, const int* rp, const double* M,
-                                  TO* soa)
+                                  TO* pack)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const int i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
     const bool present[7] = {k > 0, j > 0, i > 0, true, i < nx - 1, j < ny - 1, k < nz - 1};
+    double v[7];
     int q = rp[r];
 #pragma unroll
-    for (int d = 0; d < 7; ++d) {
-        double v = 0.0;
-        if (present[d]) v = M[q++];
-        if (d == 3 && RECIP) v = 1.0 / v;
-        soa[(size_t)d * n + r] = (TO)v;
+    for (int d = 0; d < 7; ++d) v[d] = present[d] ? M[q++] : 0.0;
+    if (RECIP) v[3] = 1.0 / v[3];
+    TO* lo = pack + (size_t)4 * r;
+    TO* hi = pack + (size_t)4 * n + (size_t)4 * r;
+    lo[0] = (TO)v[0];
+    lo[1] = (TO)v[1];
+    lo[2] = (TO)v[2];
+    lo[3] = (TO)0;
+    hi[0] = (TO)v[4];
+    hi[1] = (TO)v[5];
+    hi[2] = (TO)v[6];
+    hi[3] = (TO)v[3];
+}
+
+template <typename T, bool FWD, bool DIV, int SPAN>
+void launch_one(cudaStream_t st, const BoxParams<T>& p)
+{
+    const int grid = p.g.nta * p.g.ntb;
+    const int threads = p.g.TA * p.g.TB;
+    const size_t per = sizeof(Vec4<T>) * kPFc + sizeof(T) * (2 + 3 * kPFc);
+    const size_t smem = per * threads;
+    static bool attr_set = false;  // one opt-in per instantiation
+    if (!attr_set) {
+        cudaFuncSetAttribute(box_cta_kernel<T, FWD, DIV, SPAN>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(per * 256));
+        attr_set = true;
     }
+    box_cta_kernel<T, FWD, DIV, SPAN><<<grid, threads, smem, st>>>(p);
 }
 
 template <typename T, bool FWD, bool DIV>
-void launch_span(cudaStream_t st, int span, const BoxParams<T>& p, int threads, size_t smem,
-                 int grid)
+void launch_span(cudaStream_t st, int span, const BoxParams<T>& p)
 {
     switch (span) {
-    case 0: box_sweep_kernel<T, FWD, DIV, 0><<<grid, threads, smem, st>>>(p); break;
-    case 1: box_sweep_kernel<T, FWD, DIV, 1><<<grid, threads, smem, st>>>(p); break;
-    default: box_sweep_kernel<T, FWD, DIV, 2><<<grid, threads, smem, st>>>(p); break;
+    case 0: launch_one<T, FWD, DIV, 0>(st, p); break;
+    case 1: launch_one<T, FWD, DIV, 1>(st, p); break;
+    default: launch_one<T, FWD, DIV, 2>(st, p); break;
     }
 }
 
@@ -319,15 +353,12 @@ void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, co
     p.out = out;
     p.S = S;
     p.done = done;
-    const int threads = 32;  // one warp per tile
-    const size_t smem = 0;
-    const int grid = g.nta * g.ntb;
     if (forward)
-        launch_span<T, true, false>(st, g.span, p, threads, smem, grid);
+        launch_span<T, true, false>(st, g.span, p);
     else if (divmode == 0)
-        launch_span<T, false, true>(st, g.span, p, threads, smem, grid);
+        launch_span<T, false, true>(st, g.span, p);
     else
-        launch_span<T, false, false>(st, g.span, p, threads, smem, grid);
+        launch_span<T, false, false>(st, g.span, p);
 }
 
 template <typename TO>

@@ -154,12 +154,14 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 
 void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out);
 
-// Structured sweep on the stencil-SoA factor ([7][n]: z-, y-, x-, diag or
-// 1/diag, x+, y+, z+); divmode 0 divides by slot 3, 1 multiplies by it.
+// Structured sweep on the packed stencil factor ([2][n][4]: (z-, y-, x-, 0),
+// (x+, y+, z+, diagonal term)); divmode 0 divides by the diagonal term, 1
+// multiplies by it.
 template <typename T>
 void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, const T* rhs, T* out,
                       bool forward, int divmode, const SweepSync& S, const int* done);
-// CSR factor (FP64) -> stencil SoA in TO; slot 3 = diagonal or (recip) 1/diagonal.
+// CSR factor (FP64) -> packed stencil records in TO; diagonal term =
+// diagonal, or 1/diagonal with recip.
 template <typename TO>
 void launch_box_to_soa(cudaStream_t st, const int* dims, int n, const int* rp, const double* M,
                        TO* soa, int recip);

@@ -171,7 +171,7 @@ void ocsl_ctx::ensure_fp32()
     d_M32 = dalloc<float>(nnz);
     d_dinv32 = dalloc<float>(n);
     for (auto& v : v32) v = dalloc<float>(n);
-    if (hp.box.ok) d_soa32 = dalloc<float>(7 * n);
+    if (hp.box.ok) d_soa32 = dalloc<float>(8 * n);
 }
 
 namespace {
@@ -261,13 +261,13 @@ BoxGeom make_box_geom(const BoxShape& bs, int TA_req, int TB_req)
     int ord[3] = {0, 1, 2};
     std::sort(ord, ord + 3, [&](int x, int y) { return g.S[x] > g.S[y]; });
     for (int k = 0; k < 3; ++k) g.order[k] = ord[k];
-    // one warp per tile: WA x WB <= 32 lanes (8 x 4 by default; 32 x 1 when b is flat)
-    int wa = TA_req > 0 ? TA_req : (g.D[1] == 1 ? 32 : 8);
-    int wb = TB_req > 0 ? TB_req : (g.D[1] == 1 ? 1 : 4);
-    wa = std::max(1, std::min(wa, 32));
-    wb = std::max(1, std::min(wb, 32 / wa));
-    g.TA = std::min(wa, std::max(1, g.D[0]));
-    g.TB = std::min(wb, std::max(1, g.D[1]));
+    // one CTA per tile, TA x TB <= 256 threads (16 x 8 by default)
+    int ta_ = TA_req > 0 ? TA_req : (g.D[1] == 1 ? 128 : 16);
+    int tb_ = TB_req > 0 ? TB_req : (g.D[1] == 1 ? 1 : 8);
+    ta_ = std::max(1, std::min(ta_, 256));
+    tb_ = std::max(1, std::min(tb_, 256 / ta_));
+    g.TA = std::min(ta_, std::max(1, g.D[0]));
+    g.TB = std::min(tb_, std::max(1, g.D[1]));
     g.nta = (g.D[0] + g.TA - 1) / g.TA;
     g.ntb = (g.D[1] + g.TB - 1) / g.TB;
     return g;
@@ -877,7 +877,7 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         c->d_Mb = dalloc<double>(nz);
         c->d_dinv = dalloc<double>(nn);
         for (auto& v : c->v64) v = dalloc<double>(nn);
-        if (hp.box.ok) c->d_soa64 = dalloc<double>(7 * nn);
+        if (hp.box.ok) c->d_soa64 = dalloc<double>(8 * nn);
         c->ensure_reduce((hp.n + kTile - 1) / kTile);
         // drop the large host tables, keep the facts
         c->hp.n = hp.n;

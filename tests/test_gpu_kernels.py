@@ -140,6 +140,7 @@ BOXES = [(20, 20, 20), (13, 7, 9), (5, 17, 3), (33, 1, 1), (9, 12, 1), (1000, 1,
 @pytest.mark.parametrize("dims", BOXES)
 @pytest.mark.parametrize("tiles", [(0, 0), (4, 8), (3, 5), (32, 8)])
 def test_structured_sweeps_bit_exact(ctx, torch_cuda, oracle, dims, tiles):
+    kind = 2
     """The structured (box) sweep kernel against the oracle and against the
     level-scheduled kernel, for several box shapes and column tiles."""
     if dims[1] == 1:
@@ -152,9 +153,9 @@ def test_structured_sweeps_bit_exact(ctx, torch_cuda, oracle, dims, tiles):
     else:
         s = W.hex_pprime(*dims)
     ctx.set_pattern(s.row_ptr, s.column_index)
-    ctx.set_sweep_kernel(2, *tiles)
+    ctx.set_sweep_kernel(kind, *tiles)
     info = ctx.sweep_info()
-    assert info["kind"] == 2
+    assert info["kind"] == kind
     rng = np.random.default_rng(7)
     b = rng.standard_normal(s.n)
     Mh = oracle.ilu(s.row_ptr, s.column_index, s.value)
