@@ -147,6 +147,25 @@ int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
  * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB). */
 int ocsl_sweep_info(const ocsl_ctx* ctx, int* kind, int* dims, int* tiles);
 
+/* Allocation-free dot product.  This entry point has no counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc -- code that
+ * runs while a CUDA stream is being captured in global mode (where
+ * cudaMalloc is a prohibited call) and programs whose device memory is
+ * reserved up front by another allocator, so that a cudaMalloc would fail.
+ * It needs no context and allocates nothing: its scratch is a fixed
+ * 32,832-byte device array that every GPU loading this library keeps until
+ * exit.  Computes <x, y> over n <= 8,388,608 elements (larger n:
+ * OCSL_BAD_ARGUMENT) in the same fixed tile order as ocsl_dot_device, writing
+ * the result to the device double *d_result, asynchronously on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream).  The first call on a
+ * device resolves the scratch address with cudaGetSymbolAddress, so make it
+ * before any stream capture.  All calls share the scratch: calls that overlap
+ * on the GPU (concurrent streams) race and must be serialised by the caller. */
+int ocsl_dot_noalloc(size_t n, const double* d_x, const double* d_y, double* d_result,
+                     void* stream);
+/* Message of the last failed ocsl_dot_noalloc on this thread. */
+const char* ocsl_noalloc_last_error(void);
+
 /* Kernel timing.  While enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream and accounted to a category:
  *   0 spmv_f64  1 spmv_f32  2 fw_sweep_f64  3 bw_sweep_f64  4 fw_sweep_f32
