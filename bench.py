@@ -132,19 +132,29 @@ def lu_counts(rp, col):
     return lower, upper
 
 
-def algorithmic_bytes(n, nnz_real, nnz_l, nnz_u):
-    """Bytes each kernel must move per launch (int32 indices), by category."""
-    return {
-        # values + columns once, row pointers, x once, y, one fused-dot vector
+def algorithmic_bytes(n, nnz_real, nnz_l, nnz_u, structured):
+    """Bytes each kernel must move per launch, by category.
+
+    SpMV (int32 CSR): values and columns once, row pointers, x once, y, and
+    the one vector its fused dot reads.  Level-scheduled sweeps (CSR): strict
+    lower / upper values and columns, row pointers, diagonal positions (and
+    the reciprocal diagonal backward), rhs, result.  Structured sweeps read
+    no indices: the strict lower / upper values, rhs, result (and the
+    reciprocal diagonal backward).
+    """
+    out = {
         "spmv_f32": 8 * nnz_real + 4 * (n + 1) + 12 * n,
         "spmv_f64": 12 * nnz_real + 4 * (n + 1) + 24 * n,
-        # strict lower part, row pointers, diagonal positions, rhs, y
-        "fw_sweep_f32": 8 * nnz_l + 4 * (n + 1) + 12 * n,
-        "fw_sweep_f64": 12 * nnz_l + 4 * (n + 1) + 20 * n,
-        # strict upper part, row pointers, diagonal positions, 1/diag, rhs, x
-        "bw_sweep_f32": 8 * nnz_u + 4 * (n + 1) + 16 * n,
-        "bw_sweep_f64": 12 * nnz_u + 4 * (n + 1) + 28 * n,
     }
+    if structured:
+        out.update({"fw_sweep_f32": 4 * nnz_l + 8 * n, "bw_sweep_f32": 4 * nnz_u + 12 * n,
+                    "fw_sweep_f64": 8 * nnz_l + 16 * n, "bw_sweep_f64": 8 * nnz_u + 24 * n})
+    else:
+        out.update({"fw_sweep_f32": 8 * nnz_l + 4 * (n + 1) + 12 * n,
+                    "fw_sweep_f64": 12 * nnz_l + 4 * (n + 1) + 20 * n,
+                    "bw_sweep_f32": 8 * nnz_u + 4 * (n + 1) + 16 * n,
+                    "bw_sweep_f64": 12 * nnz_u + 4 * (n + 1) + 28 * n})
+    return out
 
 
 def cpu_reference_rate(sysm, seconds, threads, max_calls=None):
@@ -311,14 +321,15 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel in the headline timed region
     peak, peak_kind = load_peaks()
-    algo = algorithmic_bytes(s.n, s.nnz_real, nnz_l, nnz_u)
+    structured = ctx.sweep_info()["kind"] == 2
+    algo = algorithmic_bytes(s.n, s.nnz_real, nnz_l, nnz_u, structured)
     per_cat = {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof_ir.items() if v[1]}
     total_ms = sum(v["ms_total"] for k, v in per_cat.items())
     dom = max((k for k in per_cat if k in algo), key=lambda k: per_cat[k]["ms_total"])
     launches = per_cat[dom]["launches"]
     avg_ms = per_cat[dom]["ms_total"] / launches
     achieved = algo[dom] / (avg_ms * 1e-3) / 1e9
-    traffic = load_traffic().get(dom)
+    traffic = load_traffic().get(dom) if structured else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -366,6 +377,7 @@ def run_ours(args):
             "kernel_gbs": kernel_gbs,
             "kernel_ms": {k: round(v["ms_total"] / args.steps, 4) for k, v in per_cat.items()},
             "setup_s": {"generate": round(t_gen, 2), "set_pattern": round(t_pat, 3)},
+            "sweep_kernel": ctx.sweep_info(),
         }
         print(json.dumps(line))
     ctx.close()

@@ -22,18 +22,32 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libocsl_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liboracle_ref.so")
 REF_SHOCKTUBE = os.path.join(HERE, "_ref", "ref_shocktube")
+REF_DIR = os.environ.get("OCSL_REFERENCE_DIR", "/root/reference")
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 _P = C.c_void_p
 _SZ = C.c_size_t
 
 
+def reference_sources_present(reference_dir: str | None = None) -> bool:
+    return os.path.isfile(os.path.join(reference_dir or REF_DIR, "cmatrix_solver.cpp"))
+
+
 def build(reference_dir: str | None = None) -> None:
     """Compile the oracle (always) and the reference (when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    ref = reference_dir or "/root/reference"
-    if os.path.isfile(os.path.join(ref, "cmatrix_solver.cpp")):
+    ref = reference_dir or REF_DIR
+    if reference_sources_present(ref):
         subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", f"REF={ref}"], check=True)
+
+
+def build_shim_drivers(reference_dir: str | None = None) -> dict:
+    """Link the reference's own program with the C++ drop-in (oracle/Makefile
+    ``shim``); returns the paths of the three drivers.  Needs the reference's
+    sources and the built GPU library."""
+    ref = reference_dir or REF_DIR
+    subprocess.run(["make", "-s", "-C", HERE, "-j8", "shim", f"REF={ref}"], check=True)
+    return {k: os.path.join(HERE, "_ref", f"ref_driver_{k}") for k in ("cpu", "fake", "gpu")}
 
 
 def _ptr(a):
