@@ -136,6 +136,24 @@ int ocsl_forsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_b, doub
 /* x = U^-1 y, cmatrix_solver.cpp:595-611 ILU_backsub. */
 int ocsl_backsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_y, double* d_x);
 
+/* Adjoint solve.  No counterpart in the reference (it has no adjoint); it
+ * serves gradients of a loss L(x) of the solution x = A^-1 b:
+ *   A^T lambda = g (g = dL/dx)  gives  dL/db = lambda,  dL/dA_ij = -lambda_i x_j.
+ * Solves A^T lambda = g for the context's pattern and the values of A in A's
+ * own CSR order (the transpose is formed on the device through a slot map
+ * built once per pattern, on the first call).  Any method of ocsl_solve;
+ * lambda is in/out (initial guess, then the solution). */
+int ocsl_solve_transpose(ocsl_ctx* ctx, int method, const double* value, const double* g,
+                         double* lambda, const ocsl_opts* opts, ocsl_result* result);
+int ocsl_solve_transpose_device(ocsl_ctx* ctx, int method, const double* d_value,
+                                const double* d_g, double* d_lambda, const ocsl_opts* opts,
+                                ocsl_result* result);
+/* d_out[k] = (alpha * u_i) * v_j for every stored entry k = (i, j) of the
+ * pattern, 0 on phantom entries: with alpha = -1, u = lambda, v = x this is
+ * dL/dA on A's sparsity pattern.  No reference counterpart. */
+int ocsl_pattern_outer_device(ocsl_ctx* ctx, double alpha, const double* d_u, const double* d_v,
+                              double* d_out);
+
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured kernel (OCSL_BAD_ARGUMENT if the

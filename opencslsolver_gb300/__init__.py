@@ -163,6 +163,38 @@ class Context:
             self._check(st, "solve_device")
         return r.as_dict()
 
+    # -- adjoint (no reference counterpart)
+    def solve_transpose(self, method, value, g, lam, *, raise_on_status=False, **opts):
+        """Host-buffer adjoint solve A^T lam = g (ocsl_solve_transpose); ``value``
+        holds A in A's own CSR order, ``lam`` (float64 numpy) is in/out."""
+        val, gg = _f64(value), _f64(g)
+        if not (isinstance(lam, np.ndarray) and lam.dtype == np.float64 and lam.flags.c_contiguous):
+            raise ValueError("lam must be a C-contiguous float64 numpy array (updated in place)")
+        o = _abi.default_opts(**opts)
+        r = Result()
+        st = self._L.ocsl_solve_transpose(self._h, _method(method), _ptr(val), _ptr(gg), _ptr(lam),
+                                          C.byref(o), C.byref(r))
+        if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT, _abi.NO_PATTERN, _abi.BAD_PATTERN) or (
+                raise_on_status and st):
+            self._check(st, "solve_transpose")
+        return r.as_dict()
+
+    def solve_transpose_device(self, method, value, g, lam, *, raise_on_status=False, **opts):
+        """Resident-data adjoint solve A^T lam = g on CUDA tensors; lam in/out."""
+        o = _abi.default_opts(**opts)
+        r = Result()
+        st = self._L.ocsl_solve_transpose_device(self._h, _method(method), _dptr(value), _dptr(g),
+                                                 _dptr(lam), C.byref(o), C.byref(r))
+        if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT, _abi.NO_PATTERN, _abi.BAD_PATTERN) or (
+                raise_on_status and st):
+            self._check(st, "solve_transpose_device")
+        return r.as_dict()
+
+    def pattern_outer_device(self, u, v, out, alpha=-1.0):
+        """out[k] = alpha * u[i] * v[j] on the pattern (dL/dA = -lam_i x_j)."""
+        self._check(self._L.ocsl_pattern_outer_device(self._h, float(alpha), _dptr(u), _dptr(v),
+                                                      _dptr(out)), "pattern_outer")
+
     # -- triangular-sweep kernel choice
     def set_sweep_kernel(self, kind: int = 0, tile_a: int = 0, tile_b: int = 0):
         """0 automatic, 1 level-scheduled, 2 structured (7-point box patterns)."""

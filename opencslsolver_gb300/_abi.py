@@ -78,6 +78,11 @@ _PROTOS = {
     "ocsl_ilu_device": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "ocsl_forsub_device": (C.c_int, [_CTX, _P, _P, _P]),
     "ocsl_backsub_device": (C.c_int, [_CTX, _P, _P, _P]),
+    "ocsl_solve_transpose": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts),
+                                       C.POINTER(Result)]),
+    "ocsl_solve_transpose_device": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts),
+                                              C.POINTER(Result)]),
+    "ocsl_pattern_outer_device": (C.c_int, [_CTX, C.c_double, _P, _P, _P]),
     "ocsl_set_sweep_kernel": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_int]),
     "ocsl_sweep_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),

@@ -173,4 +173,10 @@ void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done)
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
                            double* dinv, float* M32, float* dinv32, float* A32);
 
+// adjoint.cu
+void launch_gather_values(cudaStream_t st, long long nnz, const int* perm, const double* val,
+                          double* out);
+void launch_pattern_outer(cudaStream_t st, const DevPattern& P, double alpha, const double* u,
+                          const double* v, double* out);
+
 }  // namespace ocsl

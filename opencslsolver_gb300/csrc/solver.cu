@@ -102,6 +102,12 @@ struct ocsl_ctx {
     int sweep_kernel = 0;
     int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
 
+    // adjoint: a child context holding the transposed pattern, and the map
+    // from its CSR slots to this pattern's slots (built on first use)
+    ocsl_ctx* tctx = nullptr;
+    int* d_tperm = nullptr;
+    long long nnzT = 0;
+
     // kernel timing (ocsl_profile_*)
     bool prof_on = false;
     std::vector<cudaEvent_t> prof_ev;  // pairs
@@ -116,6 +122,11 @@ struct ocsl_ctx {
 
 void ocsl_ctx::free_pattern()
 {
+    if (tctx) ocsl_destroy(tctx);
+    tctx = nullptr;
+    if (d_tperm) cudaFree(d_tperm);
+    d_tperm = nullptr;
+    nnzT = 0;
     for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
     double** d64[] = {&d_A, &d_b, &d_x, &d_Ma, &d_Mb, &d_dinv};
     for (auto pp : d64) { if (*pp) cudaFree(*pp); *pp = nullptr; }
@@ -724,6 +735,50 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
     return status;
 }
 
+// Builds the transposed pattern (real entries only; rows of A ascending give
+// ascending columns in every row of A^T) and its child context.
+int ensure_transpose(ocsl_ctx* c)
+{
+    if (c->tctx) return OCSL_OK;
+    const int n = c->P.n, nnz = c->P.nnz;
+    std::vector<int> rp(n + 1), col(nnz);
+    CK(cudaMemcpy(rp.data(), c->P.rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    if (nnz) CK(cudaMemcpy(col.data(), c->P.col, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    std::vector<size_t> trp(n + 1, 0);
+    for (int k = 0; k < nnz; ++k)
+        if (col[k] >= 0) ++trp[col[k] + 1];
+    for (int i = 0; i < n; ++i) trp[i + 1] += trp[i];
+    std::vector<size_t> tcol(trp[n]), next(trp.begin(), trp.end() - 1);
+    std::vector<int> perm(trp[n]);
+    for (int i = 0; i < n; ++i)
+        for (int k = rp[i]; k < rp[i + 1]; ++k) {
+            const int j = col[k];
+            if (j < 0) continue;
+            const size_t q = next[j]++;
+            tcol[q] = (size_t)i;
+            perm[q] = k;
+        }
+    ocsl_ctx* t = nullptr;
+    int rc = ocsl_create(&t, c->device);
+    if (rc != OCSL_OK) return fail(c, rc, "adjoint context: " + g_create_error);
+    ocsl_set_sweep_kernel(t, c->sweep_kernel, c->box_tile[0], c->box_tile[1]);
+    rc = ocsl_set_pattern(t, (size_t)n, trp.data(), tcol.data());
+    if (rc != OCSL_OK) {
+        const std::string msg = t->last_error;
+        ocsl_destroy(t);
+        return fail(c, rc, "transposed pattern: " + msg);
+    }
+    try {
+        c->d_tperm = upload(perm);
+    } catch (...) {
+        ocsl_destroy(t);
+        throw;
+    }
+    c->nnzT = (long long)perm.size();
+    c->tctx = t;
+    return OCSL_OK;
+}
+
 }  // namespace
 
 // =================================================================== C ABI
@@ -1114,6 +1169,83 @@ int ocsl_profile_read(ocsl_ctx* c, double* ms, int64_t* launches)
 const char* ocsl_profile_category_name(int k)
 {
     return (k >= 0 && k < PC_COUNT) ? kProfNames[k] : "unknown";
+}
+
+int ocsl_solve_transpose_device(ocsl_ctx* c, int method, const double* val, const double* g,
+                                double* lambda, const ocsl_opts* opts, ocsl_result* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (c->P.n == 0) {
+        if (out) std::memset(out, 0, sizeof *out);
+        return OCSL_OK;
+    }
+    if (!val || !g || !lambda) return fail(c, OCSL_BAD_ARGUMENT, "null value, g or lambda pointer");
+    if (!aligned8(val) || !aligned8(g) || !aligned8(lambda))
+        return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
+    try {
+        CK(cudaSetDevice(c->device));
+        rc = ensure_transpose(c);
+        if (rc) return rc;
+        c->tctx->stream = c->stream;
+        launch_gather_values(c->stream, c->nnzT, c->d_tperm, val, c->tctx->d_A);
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    rc = solve_device_impl(c->tctx, method, c->tctx->d_A, g, lambda, opts, out);
+    if (rc != OCSL_OK) c->last_error = c->tctx->last_error;
+    return rc;
+}
+
+int ocsl_solve_transpose(ocsl_ctx* c, int method, const double* value, const double* g,
+                         double* lambda, const ocsl_opts* opts, ocsl_result* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (c->P.n == 0) {
+        if (out) std::memset(out, 0, sizeof *out);
+        return OCSL_OK;
+    }
+    if (!value || !g || !lambda) return fail(c, OCSL_BAD_ARGUMENT, "null value, g or lambda pointer");
+    const size_t n = (size_t)c->P.n, nnz = (size_t)c->P.nnz;
+    try {
+        CK(cudaSetDevice(c->device));
+        CK(cudaMemcpyAsync(c->d_A, value, nnz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->d_b, g, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(c->d_x, lambda, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    rc = ocsl_solve_transpose_device(c, method, c->d_A, c->d_b, c->d_x, opts, out);
+    if (rc == OCSL_CUDA_ERROR || rc == OCSL_BAD_PATTERN) return rc;
+    try {
+        CK(cudaMemcpyAsync(lambda, c->d_x, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return rc;
+}
+
+int ocsl_pattern_outer_device(ocsl_ctx* c, double alpha, const double* u, const double* v,
+                              double* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (c->P.n == 0) return OCSL_OK;
+    if (!u || !v || !out) return fail(c, OCSL_BAD_ARGUMENT, "null u, v or out pointer");
+    if (!aligned8(u) || !aligned8(v) || !aligned8(out))
+        return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
+    try {
+        CK(cudaSetDevice(c->device));
+        launch_pattern_outer(c->stream, c->P, alpha, u, v, out);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
 }
 
 int ocsl_forsub_device(ocsl_ctx* c, const double* M, const double* b, double* y)

@@ -61,7 +61,7 @@ GpuSolver& gpu_for(CMatrix_solver* s)
         const int rc = ocsl_create(&g.ctx, dev ? std::atoi(dev) : 0);
         if (rc != OCSL_OK) die("ocsl_create", rc, nullptr);
     }
-    // The pattern is fixed once per run (cfvm.cpp:87-95); upload it again only
+    // The pattern is fixed once per run (cfvm.cpp:84-97); upload it again only
     // if the vectors were replaced or resized.
     const size_t n = s->matrix.row_ptr.size() - 1, nnz = s->matrix.column_index.size();
     if (g.n != n || g.nnz != nnz || g.rp != s->matrix.row_ptr.data() ||
