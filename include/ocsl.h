@@ -154,6 +154,104 @@ int ocsl_solve_transpose_device(ocsl_ctx* ctx, int method, const double* d_value
 int ocsl_pattern_outer_device(ocsl_ctx* ctx, double alpha, const double* d_u, const double* d_v,
                               double* d_out);
 
+/* ------------------------------------------------------------------------
+ * Face-loop coefficient assembly of the flow solver
+ * (cflow_solver_cell_face_loops.cpp:37-446 with solvers_common.h:32-151):
+ * fills the context's CSR values, b and x0 of one momentum component, the
+ * pressure correction or the enthalpy equation from the cell / face state,
+ * as the reference's face loop, boundary-face loop and cell loop do between
+ * `clear()` and `solve()` (cflow_solver.cpp:258-290, 319-349, 431-460).
+ * One GPU thread per cell gathers its faces in face order, so there are no
+ * atomics and every entry is summed in the order of the reference's
+ * single-thread loops.  Viscosity is Sutherland's law written
+ * C1 * T * sqrt(T) / (T + C2) (the reference's pow(T, 1.5) differs by at most
+ * an ulp).  The viscous stress part of the momentum faces,
+ * CFlow_face::stress_explicit_part (cflow_solver_cell_face_loops.cpp:25-35),
+ * is an input.
+ * ---------------------------------------------------------------------- */
+typedef enum { OCSL_EQ_MOMENTUM = 0, OCSL_EQ_PRESSURE = 1, OCSL_EQ_ENTHALPY = 2 } ocsl_equation;
+/* Boundary kinds: the values of enums::Eflow_BC_type and Ewall_BC_type (enums.h:39-41). */
+typedef enum {
+    OCSL_BC_EMPTY = 0, OCSL_BC_SYMMETRY = 1, OCSL_BC_WALL = 2, OCSL_BC_VELOCITY_INLET = 3,
+    OCSL_BC_SUPERSONIC_INLET = 4, OCSL_BC_PRESSURE_OUTLET = 5
+} ocsl_bc_type;
+typedef enum { OCSL_WALL_NO_SLIP = 0, OCSL_WALL_SLIP = 1 } ocsl_wall_type;
+
+typedef struct {
+    int equation;       /* ocsl_equation                                          */
+    int dimension;      /* momentum component 0, 1, 2                             */
+    int viscous;        /* Eflow_type_visc::Viscous (else inviscid)               */
+    int blended;        /* Econv_flux_type::Blended_central (else first-order upwind) */
+    int transient;      /* Etimestepping_type::Transient (else steady)            */
+    double implicit_underrelaxation;  /* CFlow_solver::implicit_underrelaxation  */
+    double R_specific, gamma, sutherland[2], prandtl;  /* Cfluid_properties      */
+} ocsl_assembly;
+
+/* Per-assembly state, DEVICE pointers.  Face arrays follow the order given to
+ * ocsl_set_faces; vector quantities are [3][count] (component-major). */
+typedef struct {
+    /* interior faces (CFVM_face, CFlow_face) */
+    const double* geo_aver;
+    const double* ksi_A;          /* diffusion_ksi_A                              */
+    const double* mdot;
+    const double* density;        /* face density                                 */
+    const double* qy;
+    const double* stress;         /* [3][n_faces]; viscous momentum only          */
+    /* boundary faces (CFVM_BC_face, CFlow_BC_face) */
+    const int32_t* bc_type;       /* ocsl_bc_type                                 */
+    const int32_t* bc_wall;       /* ocsl_wall_type                               */
+    const int32_t* bc_supersonic; /* supersonic_flag                              */
+    const double* bc_area;
+    const double* bc_area_vector; /* [3][n_bc]                                    */
+    const double* bc_perp_dist;
+    const double* bc_ksi_A;
+    const double* bc_mdot;
+    const double* bc_density;
+    const double* bc_qy;
+    const double* bc_temperature;
+    const double* bc_enthalpy;
+    const double* bc_velocity;    /* [3][n_bc]                                    */
+    const double* bc_value;       /* Dirichlet value of the pressure-correction
+                                     boundary terms; NULL = 0, as the reference  */
+    /* cells (CFVM_cell, CFlow_cell) */
+    const double* volume;
+    const double* delta_t;
+    const double* velocity;       /* [3][n]                                       */
+    const double* velocity_last;  /* [3][n]                                       */
+    const double* pressure_grad;  /* [3][n]                                       */
+    const double* density_c;
+    const double* density_last;
+    const double* pressure;
+    const double* pressure_last;
+    const double* pressure_corr;
+    const double* temperature;
+    const double* enthalpy;
+    const double* enthalpy_last;
+} ocsl_flow_state;
+
+/* The mesh's face-to-cell connectivity (host arrays, once per mesh, after
+ * ocsl_set_pattern): interior face f joins cells left[f] and right[f],
+ * boundary face g belongs to cell bc_left[g].  Every (left, right) and
+ * (right, left) pair must be stored in the pattern (OCSL_BAD_ARGUMENT
+ * otherwise).  No reference counterpart (the reference walks pointers). */
+int ocsl_set_faces(ocsl_ctx* ctx, int64_t n_faces, const int32_t* left, const int32_t* right,
+                   int64_t n_bc, const int32_t* bc_left);
+/* Assemble one equation into d_value (nnz, phantoms 0), d_b and d_x0 (n);
+ * optional outputs (NULL to skip): d_ap (n) the final diagonal (ap_vec of a
+ * momentum component, cflow_solver_cell_face_loops.cpp:168-169) and
+ * d_total_mdot (n) the cell mass balance of the pressure equation (:180-183). */
+int ocsl_assemble_device(ocsl_ctx* ctx, const ocsl_assembly* eq, const ocsl_flow_state* state,
+                         double* d_value, double* d_b, double* d_x0, double* d_ap,
+                         double* d_total_mdot);
+/* Adjoint of the pressure-correction boundary values: for a loss with
+ * dL/db = lambda, d_grad[g] = lambda[bc_left[g]] * D_g where D_g multiplies
+ * bc_value[g] in b (the Dirichlet terms of supersonic inlets and subsonic
+ * outlets, solvers_common.h:56-67), 0 for other faces.  No reference
+ * counterpart. */
+int ocsl_bc_value_grad_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
+                              const ocsl_flow_state* state, const double* d_lambda,
+                              double* d_grad);
+
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured kernel (OCSL_BAD_ARGUMENT if the

@@ -163,6 +163,43 @@ class Context:
             self._check(st, "solve_device")
         return r.as_dict()
 
+    # -- face-loop assembly (cflow_solver_cell_face_loops.cpp)
+    def set_faces(self, left, right, bc_left):
+        """Mesh face connectivity (interior faces: left/right cells; boundary
+        faces: their cell), once per mesh after set_pattern."""
+        l = np.ascontiguousarray(left, dtype=np.int32)
+        r = np.ascontiguousarray(right, dtype=np.int32)
+        bl = np.ascontiguousarray(bc_left, dtype=np.int32)
+        self._check(self._L.ocsl_set_faces(self._h, l.size, _ptr(l), _ptr(r), bl.size, _ptr(bl)),
+                    "set_faces")
+
+    @staticmethod
+    def _assembly(eq: dict):
+        q = _abi.Assembly()
+        for k in ("equation", "dimension", "viscous", "blended", "transient"):
+            setattr(q, k, int(eq.get(k, 0)))
+        for k in ("implicit_underrelaxation", "R_specific", "gamma", "prandtl"):
+            setattr(q, k, float(eq[k]))
+        q.sutherland[0], q.sutherland[1] = (float(v) for v in eq["sutherland"])
+        return q
+
+    def assemble_device(self, eq: dict, state: dict, value, b, x0, ap=None, total_mdot=None):
+        """Assemble one equation on the device.  ``state`` maps the fields of
+        ocsl_flow_state to CUDA tensors (float64; bc_type, bc_wall,
+        bc_supersonic int32); outputs are CUDA float64 tensors."""
+        q = self._assembly(eq)
+        st = _abi.flow_state(state, lambda t: _dptr(t).value)
+        self._check(self._L.ocsl_assemble_device(self._h, C.byref(q), C.byref(st), _dptr(value),
+                                                 _dptr(b), _dptr(x0), _dptr(ap),
+                                                 _dptr(total_mdot)), "assemble")
+
+    def bc_value_grad_device(self, eq: dict, state: dict, lam, grad):
+        """grad[g] = lam[cell of g] * D_g for the Dirichlet p' boundary faces."""
+        q = self._assembly(eq)
+        st = _abi.flow_state(state, lambda t: _dptr(t).value)
+        self._check(self._L.ocsl_bc_value_grad_device(self._h, C.byref(q), C.byref(st),
+                                                      _dptr(lam), _dptr(grad)), "bc_value_grad")
+
     # -- adjoint (no reference counterpart)
     def solve_transpose(self, method, value, g, lam, *, raise_on_status=False, **opts):
         """Host-buffer adjoint solve A^T lam = g (ocsl_solve_transpose); ``value``

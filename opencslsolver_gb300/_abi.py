@@ -53,6 +53,44 @@ class Result(C.Structure):
 
 _P = C.c_void_p
 _SZ = C.c_size_t
+
+# ocsl_assembly / ocsl_flow_state (include/ocsl.h), in declaration order.
+EQ_MOMENTUM, EQ_PRESSURE, EQ_ENTHALPY = 0, 1, 2
+BC_EMPTY, BC_SYMMETRY, BC_WALL, BC_VELOCITY_INLET, BC_SUPERSONIC_INLET, BC_PRESSURE_OUTLET = range(6)
+WALL_NO_SLIP, WALL_SLIP = 0, 1
+
+
+class Assembly(C.Structure):
+    _fields_ = [("equation", C.c_int), ("dimension", C.c_int), ("viscous", C.c_int),
+                ("blended", C.c_int), ("transient", C.c_int),
+                ("implicit_underrelaxation", C.c_double), ("R_specific", C.c_double),
+                ("gamma", C.c_double), ("sutherland", C.c_double * 2), ("prandtl", C.c_double)]
+
+
+FLOW_STATE_FIELDS = (
+    "geo_aver", "ksi_A", "mdot", "density", "qy", "stress",
+    "bc_type", "bc_wall", "bc_supersonic", "bc_area", "bc_area_vector", "bc_perp_dist",
+    "bc_ksi_A", "bc_mdot", "bc_density", "bc_qy", "bc_temperature", "bc_enthalpy",
+    "bc_velocity", "bc_value",
+    "volume", "delta_t", "velocity", "velocity_last", "pressure_grad", "density_c",
+    "density_last", "pressure", "pressure_last", "pressure_corr", "temperature", "enthalpy",
+    "enthalpy_last")
+INT_FIELDS = ("bc_type", "bc_wall", "bc_supersonic")
+
+
+class FlowState(C.Structure):
+    _fields_ = [(f, C.c_void_p) for f in FLOW_STATE_FIELDS]
+
+
+def flow_state(arrays: dict, ptr) -> FlowState:
+    """FlowState from named arrays; ``ptr(a)`` gives each array's address
+    (host numpy or device tensor); missing names are NULL."""
+    st = FlowState()
+    for f in FLOW_STATE_FIELDS:
+        a = arrays.get(f)
+        setattr(st, f, None if a is None else ptr(a))
+    return st
+
 _CTX = C.c_void_p
 _PROTOS = {
     "ocsl_default_opts": (None, [C.POINTER(Opts)]),
@@ -83,6 +121,11 @@ _PROTOS = {
     "ocsl_solve_transpose_device": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts),
                                               C.POINTER(Result)]),
     "ocsl_pattern_outer_device": (C.c_int, [_CTX, C.c_double, _P, _P, _P]),
+    "ocsl_set_faces": (C.c_int, [_CTX, C.c_int64, _P, _P, C.c_int64, _P]),
+    "ocsl_assemble_device": (C.c_int, [_CTX, C.POINTER(Assembly), C.POINTER(FlowState), _P, _P,
+                                       _P, _P, _P]),
+    "ocsl_bc_value_grad_device": (C.c_int, [_CTX, C.POINTER(Assembly), C.POINTER(FlowState), _P,
+                                            _P]),
     "ocsl_set_sweep_kernel": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_int]),
     "ocsl_sweep_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),

@@ -21,7 +21,7 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libocsl_gb300.so")
 
 SOURCES = ["kernels_krylov.cu", "kernels_ilu.cu", "kernels_box.cu", "solver.cu", "pattern.cpp",
-           "noalloc.cu", "adjoint.cu"]
+           "noalloc.cu", "adjoint.cu", "assembly.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -149,11 +149,30 @@ struct BoxParams {
 // walking the wavefronts W = a + b + s of its tile with one __syncthreads per
 // wavefront.  The s-neighbour is the thread's own previous row, in-tile a / b
 // neighbours come from a 2-slot shared-memory ring, tile faces from the
-// neighbouring CTAs' rows in global memory.  Row data (one 16- or 32-byte
-// packed coefficient record, rhs, face values) are staged kPFc wavefronts
-// ahead with cp.async into shared memory, slot W mod kPFc (uniform over the
-// CTA); a face word still all-ones at use is polled again from L2.
-constexpr int kPFc = 6;
+// neighbouring CTAs' rows in global memory.
+//
+// Latency hiding.  A wavefront's own work is a few dependent operations, so
+// every memory latency left on the per-wavefront path sets the sweep's speed:
+//   * the row's packed coefficient record and rhs come from DRAM and are
+//     staged kPF wavefronts ahead with cp.async into shared memory, slot
+//     W mod kPF (uniform over the CTA);
+//   * a tile-face value is loaded kDF wavefronts before its use into a
+//     register ring (slot W mod kDF, a compile-time index after unrolling).
+//     The CTA first waits until both upstream tiles have published their first
+//     face row, so it runs behind them by about one L2 round trip, which is
+//     more than kDF wavefronts: a prefetched face word is then normally final;
+//     one still all-ones is polled again from L2 (bounded wait).
+#ifndef OCSL_BOX_PF
+#define OCSL_BOX_PF 16
+#endif
+#ifndef OCSL_BOX_DF
+#define OCSL_BOX_DF 4
+#endif
+constexpr int kPF = OCSL_BOX_PF;
+constexpr int kDF = OCSL_BOX_DF;
+static_assert(kPF % kDF == 0, "the face ring must tile the record ring");
+// shared memory of a 256-thread CTA in FP64 must fit the 227 KB opt-in limit
+static_assert((32 * kPF + 8 * (2 + kPF)) * 256 <= 227 * 1024, "staging too deep for FP64");
 
 template <typename T>
 struct Vec4;
@@ -174,9 +193,9 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
     const BoxGeom& g = p.g;
     const int TA = g.TA, TB = g.TB, NT = g.TA * g.TB;
     using V4 = Vec4<T>;
-    V4* coef = reinterpret_cast<V4*>(smem_raw);  // [kPFc][NT] packed row records
-    T* ring = reinterpret_cast<T*>(coef + kPFc * NT);  // [2][NT]
-    T* sc = ring + 2 * NT;                      // [kPFc][3][NT]: rhs, face a, face b
+    V4* coef = reinterpret_cast<V4*>(smem_raw);         // [kPF][NT] packed row records
+    T* ring = reinterpret_cast<T*>(coef + kPF * NT);    // [2][NT]
+    T* srhs = ring + 2 * NT;                            // [kPF][NT] rhs
     __shared__ int s_tile;
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
     __syncthreads();
@@ -207,50 +226,65 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
         const int off_a = dstep * g.S[0], off_b = dstep * g.S[1];
         const int c0 = ca + cb;  // the thread sweeps row cs = W - c0 at wavefront W
         const V4* pack = reinterpret_cast<const V4*>(p.soa) + (FWD ? 0 : p.n);
+        const T* out_c = p.out;
         auto in_range = [&](int cs) { return col_ok && cs >= 0 && cs < Ds; };
         auto refill = [&](int cs, int j) {
             if (in_range(cs)) {
                 const int r = row0 + cs * sstep;
                 cp_async_vec<T>(&coef[j * NT + tid], pack + r);
-                cp_async(&sc[(j * 3 + 0) * NT + tid], p.rhs + r);
-                if (face_a) cp_async(&sc[(j * 3 + 1) * NT + tid], (const T*)p.out + r + off_a);
-                if (face_b) cp_async(&sc[(j * 3 + 2) * NT + tid], (const T*)p.out + r + off_b);
+                cp_async(&srhs[j * NT + tid], p.rhs + r);
             }
             cp_async_commit();
         };
-        const int Wbase = W0 - (W0 % kPFc);
+        const int Wbase = W0 - (W0 % kPF);
 #pragma unroll
-        for (int j = 0; j < kPFc; ++j) refill(Wbase + j - c0, j);
+        for (int j = 0; j < kPF; ++j) refill(Wbase + j - c0, j);
+
+        // Start behind the upstream tiles: thread (0, 0) waits for the first
+        // face row of each (their row at s = 0 next to this tile's corner).
+        if (tid == 0) {
+            if (face_a) (void)wait_value(out_c + row0 + off_a, p.S.err);
+            if (face_b) (void)wait_value(out_c + row0 + off_b, p.S.err);
+        }
+        __syncthreads();
+
+        U fa[kDF], fb[kDF];
+#pragma unroll
+        for (int j = 0; j < kDF; ++j) {
+            const int cs = Wbase + j - c0;
+            fa[j] = B::kSentinel;
+            fb[j] = B::kSentinel;
+            if (face_a && in_range(cs)) fa[j] = B::load(out_c + row0 + cs * sstep + off_a);
+            if (face_b && in_range(cs)) fb[j] = B::load(out_c + row0 + cs * sstep + off_b);
+        }
 
         T prev = T(0);
-        for (int Wb = Wbase; Wb <= W1; Wb += kPFc) {
+        for (int Wb = Wbase; Wb <= W1; Wb += kPF) {
 #pragma unroll
-            for (int j = 0; j < kPFc; ++j) {
+            for (int j = 0; j < kPF; ++j) {
                 const int W = Wb + j;
                 if (W > W1) break;  // uniform over the CTA
+                const int jf = j % kDF;
                 const int cs = W - c0;
-                cp_async_wait<kPFc - 1>();
+                cp_async_wait<kPF - 1>();
                 if (W >= W0 && in_range(cs)) {
                     const V4 c = coef[j * NT + tid];
                     const T* rd = ring + ((W - 1) & 1) * NT;
+                    const int r = row0 + cs * sstep;
                     T va = T(0), vb = T(0);
                     if (has_a) {
-                        if (la > 0) {
+                        if (la > 0)
                             va = rd[tid - 1];
-                        } else {
-                            const U u = B::to(sc[(j * 3 + 1) * NT + tid]);
-                            va = u != B::kSentinel ? B::from(u)
-                                                   : wait_value(p.out + row0 + cs * sstep + off_a, p.S.err);
-                        }
+                        else
+                            va = fa[jf] != B::kSentinel ? B::from(fa[jf])
+                                                        : wait_value(out_c + r + off_a, p.S.err);
                     }
                     if (has_b) {
-                        if (lb > 0) {
+                        if (lb > 0)
                             vb = rd[tid - TA];
-                        } else {
-                            const U u = B::to(sc[(j * 3 + 2) * NT + tid]);
-                            vb = u != B::kSentinel ? B::from(u)
-                                                   : wait_value(p.out + row0 + cs * sstep + off_b, p.S.err);
-                        }
+                        else
+                            vb = fb[jf] != B::kSentinel ? B::from(fb[jf])
+                                                        : wait_value(out_c + r + off_b, p.S.err);
                     }
                     const T vs = cs > 0 ? prev : T(0);
                     const T vx = SPAN == 0 ? vs : va;
@@ -261,13 +295,19 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
                     T sum = fma_t(c.v[0], FWD ? vz : vx, T(0));
                     sum = fma_t(c.v[1], vy, sum);
                     sum = fma_t(c.v[2], FWD ? vx : vz, sum);
-                    const T num = sc[(j * 3 + 0) * NT + tid] - sum;
+                    const T num = srhs[j * NT + tid] - sum;
                     const T y = FWD ? num : (DIV ? num / c.v[3] : num * c.v[3]);
                     ring[(W & 1) * NT + tid] = y;
-                    publish(p.out + row0 + cs * sstep, y);
+                    publish(p.out + r, y);
                     prev = y;
                 }
-                refill(cs + kPFc, j);
+                // next face words of this ring slot: wavefront W + kDF
+                {
+                    const int csn = cs + kDF;
+                    if (face_a && in_range(csn)) fa[jf] = B::load(out_c + row0 + csn * sstep + off_a);
+                    if (face_b && in_range(csn)) fb[jf] = B::load(out_c + row0 + csn * sstep + off_b);
+                }
+                refill(cs + kPF, j);
                 if (W >= W0) __syncthreads();  // uniform over the CTA
             }
         }
@@ -318,7 +358,7 @@ void launch_one(cudaStream_t st, const BoxParams<T>& p)
 {
     const int grid = p.g.nta * p.g.ntb;
     const int threads = p.g.TA * p.g.TB;
-    const size_t per = sizeof(Vec4<T>) * kPFc + sizeof(T) * (2 + 3 * kPFc);
+    const size_t per = sizeof(Vec4<T>) * kPF + sizeof(T) * (2 + kPF);
     const size_t smem = per * threads;
     static bool attr_set = false;  // one opt-in per instantiation
     if (!attr_set) {

@@ -96,6 +96,19 @@ struct DevPattern {
     int bw_nchunks;
 };
 
+// Face-to-cell incidence of the mesh (ocsl_set_faces), for the assembly.
+struct DevFaces {
+    int nf = 0, nb = 0;
+    const int* left = nullptr;      // [nf]
+    const int* right = nullptr;     // [nf]
+    const int* bc_left = nullptr;   // [nb]
+    const int* cell_ptr = nullptr;  // [n+1] interior-face entries of each cell
+    const int* cell_ent = nullptr;  // face << 1 | (1 if the cell is the face's right cell)
+    const int* cell_slot = nullptr; // CSR slot of the entry (cell, other cell) in the cell's row
+    const int* bc_ptr = nullptr;    // [n+1] boundary-face entries of each cell
+    const int* bc_ent = nullptr;    // boundary face index
+};
+
 struct SweepSync {
     unsigned* ticket;    // chunk dispenser (reset by the last CTA)
     unsigned* finished;
@@ -172,6 +185,13 @@ void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done)
 // Factor side outputs without a sweep: dinv = 1 / M_ii and FP32 copies.
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
                            double* dinv, float* M32, float* dinv32, float* A32);
+
+// assembly.cu
+void launch_assemble(cudaStream_t st, const DevPattern& P, const DevFaces& F,
+                     const ocsl_assembly& q, const ocsl_flow_state& s, double* value, double* b,
+                     double* x0, double* ap, double* total_mdot);
+void launch_bc_value_grad(cudaStream_t st, const DevFaces& F, const ocsl_assembly& q,
+                          const ocsl_flow_state& s, const double* lambda, double* grad);
 
 // adjoint.cu
 void launch_gather_values(cudaStream_t st, long long nnz, const int* perm, const double* val,

@@ -194,4 +194,55 @@ bool analyse_pattern(size_t n_in, const size_t* rp, const size_t* col, HostPatte
     return true;
 }
 
+bool build_face_tables(int n, const std::vector<int>& rp, const std::vector<int>& col,
+                       long long nf, const int32_t* left, const int32_t* right, long long nb,
+                       const int32_t* bc_left, FaceTables& ft, std::string& err)
+{
+    if (nf < 0 || nb < 0 || nf >= (1LL << 30) || nb >= INT_MAX)
+        return fail(err, "face counts out of range (%lld, %lld)", nf, nb);
+    auto find = [&](int i, int j) {
+        for (int q = rp[i]; q < rp[i + 1]; ++q)
+            if (col[q] == j) return q;
+        return -1;
+    };
+    ft = FaceTables();
+    std::vector<int> cnt(n + 1, 0), bcnt(n + 1, 0);
+    for (long long f = 0; f < nf; ++f) {
+        const int L = left[f], R = right[f];
+        if (L < 0 || L >= n || R < 0 || R >= n || L == R)
+            return fail(err, "interior face %lld joins cells out of range or itself (%lld)", f, L);
+        ++cnt[L + 1];
+        ++cnt[R + 1];
+    }
+    for (long long g = 0; g < nb; ++g) {
+        if (bc_left[g] < 0 || bc_left[g] >= n)
+            return fail(err, "boundary face %lld names cell %lld", g, bc_left[g]);
+        ++bcnt[bc_left[g] + 1];
+    }
+    for (int i = 0; i < n; ++i) {
+        cnt[i + 1] += cnt[i];
+        bcnt[i + 1] += bcnt[i];
+    }
+    ft.cell_ptr = cnt;
+    ft.bc_ptr = bcnt;
+    ft.cell_ent.assign(cnt[n], 0);
+    ft.cell_slot.assign(cnt[n], 0);
+    ft.bc_ent.assign(bcnt[n], 0);
+    std::vector<int> next(cnt.begin(), cnt.end() - 1), bnext(bcnt.begin(), bcnt.end() - 1);
+    for (long long f = 0; f < nf; ++f) {  // ascending f keeps every list in face order
+        const int L = left[f], R = right[f];
+        const int kLR = find(L, R), kRL = find(R, L);
+        if (kLR < 0 || kRL < 0)
+            return fail(err, "face %lld: pair (%lld, right) is not in the pattern", f, L);
+        int e = next[L]++;
+        ft.cell_ent[e] = (int)(f << 1);
+        ft.cell_slot[e] = kLR;
+        e = next[R]++;
+        ft.cell_ent[e] = (int)(f << 1) | 1;
+        ft.cell_slot[e] = kRL;
+    }
+    for (long long g = 0; g < nb; ++g) ft.bc_ent[bnext[bc_left[g]]++] = (int)g;
+    return true;
+}
+
 }  // namespace ocsl

@@ -38,4 +38,17 @@ BoxShape detect_box(int n, const std::vector<int>& rp, const std::vector<int>& c
 bool analyse_pattern(size_t n, const size_t* row_ptr, const size_t* column_index, HostPattern& hp,
                      std::string& err);
 
+// Per-cell incidence lists of the mesh's faces for the gather assembly: the
+// interior faces of each cell in ascending face order, each with its side
+// (bit 0: 1 when the cell is the face's right cell) and the CSR slot of the
+// off-diagonal entry (cell, other cell); the boundary faces of each cell in
+// ascending order.  Returns false with a message if a face names a cell out
+// of range or its pair is not stored in the pattern.
+struct FaceTables {
+    std::vector<int> cell_ptr, cell_ent, cell_slot, bc_ptr, bc_ent;
+};
+bool build_face_tables(int n, const std::vector<int>& rp, const std::vector<int>& col,
+                       long long nf, const int32_t* left, const int32_t* right, long long nb,
+                       const int32_t* bc_left, FaceTables& ft, std::string& err);
+
 }  // namespace ocsl

@@ -102,6 +102,11 @@ struct ocsl_ctx {
     int sweep_kernel = 0;
     int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
 
+    // face-loop assembly: the mesh's face incidence (ocsl_set_faces)
+    DevFaces F{};
+    int* d_faces[8] = {};
+    bool has_faces = false;
+
     // adjoint: a child context holding the transposed pattern, and the map
     // from its CSR slots to this pattern's slots (built on first use)
     ocsl_ctx* tctx = nullptr;
@@ -127,6 +132,9 @@ void ocsl_ctx::free_pattern()
     if (d_tperm) cudaFree(d_tperm);
     d_tperm = nullptr;
     nnzT = 0;
+    for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
+    F = DevFaces{};
+    has_faces = false;
     for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
     double** d64[] = {&d_A, &d_b, &d_x, &d_Ma, &d_Mb, &d_dinv};
     for (auto pp : d64) { if (*pp) cudaFree(*pp); *pp = nullptr; }
@@ -779,6 +787,57 @@ int ensure_transpose(ocsl_ctx* c)
     return OCSL_OK;
 }
 
+// Names the first state field an equation needs that is NULL, else nullptr.
+const char* missing_state_field(const ocsl_assembly& q, const ocsl_flow_state& s, bool has_nf,
+                                bool has_nb)
+{
+    struct Need {
+        const void* p;
+        const char* name;
+        bool want;
+    };
+    const bool mom = q.equation == OCSL_EQ_MOMENTUM, pre = q.equation == OCSL_EQ_PRESSURE,
+               ent = q.equation == OCSL_EQ_ENTHALPY, tr = q.transient != 0, vis = q.viscous != 0;
+    const Need need[] = {
+        {s.geo_aver, "geo_aver", has_nf},
+        {s.mdot, "mdot", has_nf},
+        {s.ksi_A, "ksi_A", has_nf && ((mom && vis) || ent)},
+        {s.stress, "stress", has_nf && mom && vis},
+        {s.density, "density", has_nf && pre},
+        {s.qy, "qy", has_nf && pre},
+        {s.bc_type, "bc_type", has_nb},
+        {s.bc_mdot, "bc_mdot", has_nb},
+        {s.bc_wall, "bc_wall", has_nb && mom && vis},
+        {s.bc_area, "bc_area", has_nb && mom && vis},
+        {s.bc_area_vector, "bc_area_vector", has_nb && mom && vis},
+        {s.bc_perp_dist, "bc_perp_dist", has_nb && mom && vis},
+        {s.bc_velocity, "bc_velocity", has_nb && mom},
+        {s.bc_supersonic, "bc_supersonic", has_nb && pre},
+        {s.bc_qy, "bc_qy", has_nb && pre},
+        {s.bc_density, "bc_density", has_nb && pre},
+        {s.bc_temperature, "bc_temperature", has_nb && (pre || ent)},
+        {s.bc_enthalpy, "bc_enthalpy", has_nb && ent},
+        {s.bc_ksi_A, "bc_ksi_A", has_nb && ent},
+        {s.volume, "volume", true},
+        {s.delta_t, "delta_t", tr},
+        {s.velocity, "velocity", mom},
+        {s.velocity_last, "velocity_last", mom},
+        {s.pressure_grad, "pressure_grad", mom},
+        {s.density_c, "density_c", (mom && tr) || pre || ent || (has_nb && pre)},
+        {s.density_last, "density_last", tr && (mom || pre || ent)},
+        {s.temperature, "temperature", (mom && vis) || pre},
+        {s.temperature, "temperature", ent},
+        {s.pressure_corr, "pressure_corr", pre},
+        {s.enthalpy, "enthalpy", ent},
+        {s.enthalpy_last, "enthalpy_last", ent},
+        {s.pressure, "pressure", ent && tr},
+        {s.pressure_last, "pressure_last", ent && tr},
+    };
+    for (const Need& x : need)
+        if (x.want && !x.p) return x.name;
+    return nullptr;
+}
+
 }  // namespace
 
 // =================================================================== C ABI
@@ -1169,6 +1228,100 @@ int ocsl_profile_read(ocsl_ctx* c, double* ms, int64_t* launches)
 const char* ocsl_profile_category_name(int k)
 {
     return (k >= 0 && k < PC_COUNT) ? kProfNames[k] : "unknown";
+}
+
+int ocsl_set_faces(ocsl_ctx* c, int64_t n_faces, const int32_t* left, const int32_t* right,
+                   int64_t n_bc, const int32_t* bc_left)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if ((n_faces > 0 && (!left || !right)) || (n_bc > 0 && !bc_left))
+        return fail(c, OCSL_BAD_ARGUMENT, "null face array");
+    try {
+        CK(cudaSetDevice(c->device));
+        const int n = c->P.n, nnz = c->P.nnz;
+        std::vector<int> rp(n + 1), col(nnz);
+        CK(cudaMemcpy(rp.data(), c->P.rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+        if (nnz) CK(cudaMemcpy(col.data(), c->P.col, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+        FaceTables ft;
+        std::string err;
+        if (!build_face_tables(n, rp, col, n_faces, left, right, n_bc, bc_left, ft, err))
+            return fail(c, OCSL_BAD_ARGUMENT, err);
+        CK(cudaStreamSynchronize(c->stream));
+        for (auto& p : c->d_faces) { if (p) cudaFree(p); p = nullptr; }
+        c->has_faces = false;
+        const std::vector<int> l(left, left + n_faces), r(right, right + n_faces),
+            bl(bc_left, bc_left + n_bc);
+        const std::vector<int>* tabs[8] = {&l, &r, &bl, &ft.cell_ptr, &ft.cell_ent, &ft.cell_slot,
+                                           &ft.bc_ptr, &ft.bc_ent};
+        for (int i = 0; i < 8; ++i) c->d_faces[i] = upload(*tabs[i]);
+        DevFaces& F = c->F;
+        F.nf = (int)n_faces;
+        F.nb = (int)n_bc;
+        F.left = c->d_faces[0];
+        F.right = c->d_faces[1];
+        F.bc_left = c->d_faces[2];
+        F.cell_ptr = c->d_faces[3];
+        F.cell_ent = c->d_faces[4];
+        F.cell_slot = c->d_faces[5];
+        F.bc_ptr = c->d_faces[6];
+        F.bc_ent = c->d_faces[7];
+        c->has_faces = true;
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+static int check_assembly(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!c->has_faces) return fail(c, OCSL_BAD_ARGUMENT, "ocsl_set_faces has not been called");
+    if (!q || !s) return fail(c, OCSL_BAD_ARGUMENT, "null assembly or state");
+    if (q->equation < OCSL_EQ_MOMENTUM || q->equation > OCSL_EQ_ENTHALPY)
+        return fail(c, OCSL_BAD_ARGUMENT, "unknown equation");
+    if (q->equation == OCSL_EQ_MOMENTUM && (q->dimension < 0 || q->dimension > 2))
+        return fail(c, OCSL_BAD_ARGUMENT, "momentum dimension must be 0, 1 or 2");
+    if (const char* m = missing_state_field(*q, *s, c->F.nf > 0, c->F.nb > 0))
+        return fail(c, OCSL_BAD_ARGUMENT, std::string("state field needed but NULL: ") + m);
+    return OCSL_OK;
+}
+
+int ocsl_assemble_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s,
+                         double* value, double* b, double* x0, double* ap, double* total_mdot)
+{
+    int rc = check_assembly(c, q, s);
+    if (rc) return rc;
+    if (c->P.n == 0) return OCSL_OK;
+    if (!value || !b || !x0) return fail(c, OCSL_BAD_ARGUMENT, "null value, b or x0");
+    try {
+        CK(cudaSetDevice(c->device));
+        launch_assemble(c->stream, c->P, c->F, *q, *s, value, b, x0, ap, total_mdot);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_bc_value_grad_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s,
+                              const double* lambda, double* grad)
+{
+    int rc = check_assembly(c, q, s);
+    if (rc) return rc;
+    if (c->F.nb == 0) return OCSL_OK;
+    if (!lambda || !grad) return fail(c, OCSL_BAD_ARGUMENT, "null lambda or grad");
+    try {
+        CK(cudaSetDevice(c->device));
+        launch_bc_value_grad(c->stream, c->F, *q, *s, lambda, grad);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
 }
 
 int ocsl_solve_transpose_device(ocsl_ctx* c, int method, const double* val, const double* g,

@@ -324,3 +324,128 @@ def random_rows_system(n: int, max_row: int, seed: int = 7, phantom_frac: float 
         rp[i + 1] = len(cols)
     return System(rp, np.array(cols, np.uint64), np.array(vals), rng.uniform(-1, 1, size=n),
                   f"random{n}_r{max_row}")
+
+
+@dataclass
+class FlowCase:
+    """A finite-volume mesh with a flow state in the argument form of the
+    face-loop assembly (ocsl_set_faces / ocsl_assemble_device): the
+    reference-layout pattern, face connectivity, the per-field state arrays
+    and the equation settings."""
+    name: str
+    row_ptr: np.ndarray
+    column_index: np.ndarray
+    left: np.ndarray
+    right: np.ndarray
+    bc_left: np.ndarray
+    state: dict
+    eq: dict
+    inlet: np.ndarray  # boundary faces on x = 0 (the inlet set)
+
+    @property
+    def n(self) -> int:
+        return self.row_ptr.size - 1
+
+
+AIR = {"R_specific": 8.31446261815324 / (28.9651159 / 1000.0), "gamma": 1.4,
+       "sutherland": (1.458e-6, 110.4), "prandtl": 0.713}
+
+
+def hex_flow_state(nx: int, ny: int | None = None, nz: int | None = None, *, seed: int = 20261203,
+                   equation: int = 1, transient: bool = True, blended: bool = True,
+                   inlet_value: float = 0.0) -> FlowCase:
+    """Seeded flow state on an nx*ny*nz unit-box hex mesh for the assembly.
+
+    Interior faces in x-, then y-, then z-direction order; boundary faces:
+    x = 0 a supersonic inlet (its pressure-correction term is the Dirichlet
+    term a_PP += D, b_P += D * p_in of solvers_common.h:56-67 with
+    p_in = ``inlet_value``), x = 1 a subsonic pressure outlet, the other four
+    sides slip walls.  Fields: T = 300 K +- 20 K and a smooth seeded velocity
+    (3 sinusoidal modes, ~100 m/s); density from the ideal gas at p = 1e5 Pa;
+    face mass flow rho_f (u_f . A); Qy ~ U[0.5, 2] x scale (seed + 1), so the
+    pressure-correction system is diffusion-dominated with a convective part
+    (cell Peclet ~ 0.4 at 128^3) and a transient diagonal (dt = 1e-4 s)."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    rp, col = hex_pattern(nx, ny, nz)
+    h = np.array([1.0 / nx, 1.0 / ny, 1.0 / nz])
+    c = np.arange(n, dtype=np.int64)
+    ijk = np.stack([c % nx, (c // nx) % ny, c // (nx * ny)], axis=1)
+    centers = (ijk + 0.5) * h
+    vel = 100.0 * (1.0 + 0.2 * _velocity(centers, rng))  # (n, 3), mostly +x
+    T = 300.0 + 20.0 * np.sin(2 * np.pi * centers[:, 0]) * np.cos(np.pi * centers[:, 1])
+    p = np.full(n, 1.0e5)
+    rho = p / AIR["R_specific"] / T
+    strides = (1, nx, nx * ny)
+    dims = (nx, ny, nz)
+    left, right, axis = [], [], []
+    for a in range(3):
+        m = ijk[:, a] < dims[a] - 1
+        left.append(c[m])
+        right.append(c[m] + strides[a])
+        axis.append(np.full(int(m.sum()), a))
+    left, right, axis = np.concatenate(left), np.concatenate(right), np.concatenate(axis)
+    area = np.where(axis == 0, h[1] * h[2], np.where(axis == 1, h[0] * h[2], h[0] * h[1]))
+    dist = h[axis]
+    rho_f = 0.5 * (rho[left] + rho[right])
+    un = 0.5 * (vel[left, axis] + vel[right, axis])
+    mdot = rho_f * un * area
+    # Qy sized so that the six faces' D = Qy rho_f sum to ~20x the transient
+    # diagonal vol / (dt R T gamma): diagonal dominance ~1.05, as a p' system
+    dt = 1e-4
+    qy_scale = 20.0 / 6.0 * h.prod() / (dt * AIR["R_specific"] * 300.0 * AIR["gamma"] * rho_f)
+    qy = np.random.default_rng(seed + 1).uniform(0.5, 2.0, left.size) * qy_scale
+    # boundary faces: (cell, outward axis, sign)
+    bl, bt, ba, bs = [], [], [], []
+    for a in range(3):
+        for side, sign in ((0, -1.0), (dims[a] - 1, 1.0)):
+            cells = c[ijk[:, a] == side]
+            bl.append(cells)
+            ba.append(np.full(cells.size, a))
+            bs.append(np.full(cells.size, sign))
+            if a == 0:
+                kind = _abi_bc("SUPERSONIC_INLET") if sign < 0 else _abi_bc("PRESSURE_OUTLET")
+            else:
+                kind = _abi_bc("WALL")
+            bt.append(np.full(cells.size, kind))
+    bc_left, bc_type = np.concatenate(bl), np.concatenate(bt).astype(np.int32)
+    bc_axis, bc_sign = np.concatenate(ba), np.concatenate(bs)
+    nb = bc_left.size
+    bc_area = np.where(bc_axis == 0, h[1] * h[2], np.where(bc_axis == 1, h[0] * h[2], h[0] * h[1]))
+    bc_av = np.zeros((3, nb))
+    bc_av[bc_axis, np.arange(nb)] = bc_sign * bc_area
+    bc_vel = vel[bc_left].T.copy()
+    bc_rho = rho[bc_left]
+    bc_mdot = bc_rho * (bc_vel[bc_axis, np.arange(nb)] * bc_sign) * bc_area
+    bc_mdot[bc_type == _abi_bc("WALL")] = 0.0
+    inlet = np.nonzero(bc_type == _abi_bc("SUPERSONIC_INLET"))[0]
+    bc_value = np.zeros(nb)
+    bc_value[inlet] = inlet_value
+    vol = np.full(n, h[0] * h[1] * h[2])
+    state = {
+        "geo_aver": np.full(left.size, 0.5), "ksi_A": area / dist, "mdot": mdot,
+        "density": rho_f, "qy": qy, "stress": np.zeros((3, left.size)),
+        "bc_type": bc_type, "bc_wall": np.full(nb, 1, np.int32),
+        "bc_supersonic": np.zeros(nb, np.int32), "bc_area": bc_area, "bc_area_vector": bc_av,
+        "bc_perp_dist": 0.5 * h[bc_axis], "bc_ksi_A": bc_area / (0.5 * h[bc_axis]),
+        "bc_mdot": bc_mdot, "bc_density": bc_rho, "bc_qy": np.full(nb, float(np.mean(qy))),
+        "bc_temperature": T[bc_left], "bc_enthalpy": 1005.0 * T[bc_left],
+        "bc_velocity": bc_vel, "bc_value": bc_value,
+        "volume": vol, "delta_t": np.full(n, dt), "velocity": vel.T.copy(),
+        "velocity_last": vel.T.copy(), "pressure_grad": np.zeros((3, n)), "density_c": rho,
+        "density_last": rho * (1.0 + 1e-4 * np.sin(7.0 * centers[:, 2])), "pressure": p,
+        "pressure_last": p.copy(), "pressure_corr": np.zeros(n), "temperature": T,
+        "enthalpy": 1005.0 * T, "enthalpy_last": 1005.0 * T,
+    }
+    eq = dict(AIR, equation=equation, dimension=0, viscous=0, blended=int(blended),
+              transient=int(transient), implicit_underrelaxation=0.7)
+    return FlowCase(f"hexflow{nx}x{ny}x{nz}", rp, col, left.astype(np.int32),
+                    right.astype(np.int32), bc_left.astype(np.int32), state, eq, inlet)
+
+
+def _abi_bc(name: str) -> int:
+    from . import _abi
+
+    return getattr(_abi, "BC_" + name)

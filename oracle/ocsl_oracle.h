@@ -34,6 +34,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "ocsl.h" /* data layout of the assembly inputs (ocsl_assembly, ocsl_flow_state) */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -87,6 +89,17 @@ int orc_pcg_tol(size_t n, const uint64_t* rp, const uint64_t* col, const double*
 int orc_bicgstab_ir32(size_t n, const uint64_t* rp, const uint64_t* col, const double* val,
                       const double* b, double* x, double tol, int maxit, double inner_tol,
                       int inner_maxit, int ilu_sweeps, int* iters, int* outer, double* relres);
+
+/* Face-loop coefficient assembly (ocsl_oracle_assembly.c): the reference's
+ * single-thread loop order; `st` holds HOST pointers.  ap / total_mdot may be
+ * NULL. */
+void orc_assemble(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
+                  const int32_t* left, const int32_t* right, int64_t nb, const int32_t* bc_left,
+                  const ocsl_assembly* q, const ocsl_flow_state* st, double* value, double* b,
+                  double* x0, double* ap, double* total_mdot);
+void orc_bc_value_grad(size_t n, const uint64_t* rp, int64_t nb, const int32_t* bc_left,
+                       const ocsl_assembly* q, const ocsl_flow_state* st, const double* lambda,
+                       double* grad);
 
 /* Exact relative residual ||b - A x||_2 / ||b||_2 in long double. */
 double orc_true_relres(size_t n, const uint64_t* rp, const uint64_t* col, const double* val,

@@ -80,6 +80,9 @@ _ORACLE_PROTOS = {
     "orc_bicgstab_ir32": (C.c_int, _CSR + [_P, _P, _P, C.c_double, C.c_int, C.c_double,
                                            C.c_int, C.c_int, _P, _P, _P]),
     "orc_true_relres": (C.c_double, _CSR + [_P, _P, _P]),
+    "orc_assemble": (None, _CSR + [C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, _P, _P, _P,
+                                   _P]),
+    "orc_bc_value_grad": (None, [_SZ, _P, C.c_int64, _P, _P, _P, _P, _P]),
 }
 _REF_CSR = [_SZ, _SZ, _P, _P]
 _REF_PROTOS = {
@@ -212,6 +215,62 @@ class Oracle:
         val, b, x = _c64(val), _c64(b), _c64(x)
         return self._l.orc_true_relres(rp.size - 1, _ptr(rp), _ptr(col), _ptr(val), _ptr(b),
                                        _ptr(x))
+
+
+def _assembly_struct(eq: dict):
+    from opencslsolver_gb300 import _abi
+
+    q = _abi.Assembly()
+    for k in ("equation", "dimension", "viscous", "blended", "transient"):
+        setattr(q, k, int(eq.get(k, 0)))
+    for k in ("implicit_underrelaxation", "R_specific", "gamma", "prandtl"):
+        setattr(q, k, float(eq[k]))
+    q.sutherland[0], q.sutherland[1] = float(eq["sutherland"][0]), float(eq["sutherland"][1])
+    return q
+
+
+def _host_state(state: dict):
+    from opencslsolver_gb300 import _abi
+
+    keep = {}
+    for k, v in state.items():
+        if v is None:
+            continue
+        dt = np.int32 if k in _abi.INT_FIELDS else np.float64
+        keep[k] = np.ascontiguousarray(v, dtype=dt)
+    return _abi.flow_state(keep, lambda a: a.ctypes.data), keep
+
+
+def assemble(rp, col, left, right, bc_left, eq: dict, state: dict):
+    """Oracle face-loop assembly (ocsl_oracle_assembly.c) -> value, b, x0, ap, total_mdot."""
+    lib = Oracle()._l
+    rp, col = np.ascontiguousarray(rp, np.uint64), np.ascontiguousarray(col, np.uint64)
+    left, right = np.ascontiguousarray(left, np.int32), np.ascontiguousarray(right, np.int32)
+    bc_left = np.ascontiguousarray(bc_left, np.int32)
+    n = rp.size - 1
+    q = _assembly_struct(eq)
+    st, keep = _host_state(state)
+    value, b, x0, ap, tm = (np.zeros(col.size), np.zeros(n), np.zeros(n), np.zeros(n),
+                            np.zeros(n))
+    lib.orc_assemble(n, _ptr(rp), _ptr(col), left.size, _ptr(left), _ptr(right), bc_left.size,
+                     _ptr(bc_left), C.addressof(q), C.addressof(st), _ptr(value), _ptr(b),
+                     _ptr(x0), _ptr(ap), _ptr(tm))
+    del keep
+    return value, b, x0, ap, tm
+
+
+def bc_value_grad(rp, bc_left, eq: dict, state: dict, lam):
+    lib = Oracle()._l
+    rp = np.ascontiguousarray(rp, np.uint64)
+    bc_left = np.ascontiguousarray(bc_left, np.int32)
+    q = _assembly_struct(eq)
+    st, keep = _host_state(state)
+    lam = np.ascontiguousarray(lam, np.float64)
+    g = np.zeros(bc_left.size)
+    lib.orc_bc_value_grad(rp.size - 1, _ptr(rp), bc_left.size, _ptr(bc_left), C.addressof(q),
+                          C.addressof(st), _ptr(lam), _ptr(g))
+    del keep
+    return g
 
 
 def reference_available() -> bool:

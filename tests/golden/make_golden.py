@@ -18,7 +18,16 @@ then writes:
   final fields (p, u, T, rho) at full precision;
 * small_systems.npz -- seeded small systems in the reference layout with the
   reference's gemv, ILU_decompose, ILU_forsub/backsub, CG_solve and
-  ILU_BICGSTAB_solve outputs.
+  ILU_BICGSTAB_solve outputs;
+* assembly_<case>.npz -- the inputs (cell / face state) and outputs (matrix
+  values, b, x0, ap_vec, total_mdot) of the reference's face-loop assembly,
+  recorded by oracle/ref_assembly.cpp right before the 5 solve calls of one
+  SIMPLE inner iteration, for three cases: the 1000-cell shock tube
+  (inviscid, blended, transient, slip walls), a 200-cell viscous channel
+  (upwind, transient, velocity inlet, no-slip walls, pressure outlet) and a
+  200-cell steady case (viscous, blended, implicit under-relaxation,
+  supersonic inlet, slip walls, outlet).  Mesh arrays are stored once per
+  case, state and outputs per call with the prefix c<k>_.
 
 All reference calls use one OpenMP thread (deterministic reduction order).
 """
@@ -134,6 +143,49 @@ def make_small(ref, out):
     np.savez_compressed(out, **arrays)
 
 
+# (case, first recorded solve call): the last inner iteration of each run.
+ASSEMBLY_CASES = [("shocktube", 25), ("channel", 25), ("steady", 15)]
+MESH_KEYS = ("face_left", "face_right", "face_geo_aver", "face_ksi_A", "bc_left", "bc_area",
+             "bc_area_vector", "bc_perp_dist", "bc_ksi_A", "cell_volume", "row_ptr",
+             "column_index", "bc_type", "bc_wall", "bc_thermal")
+
+
+def read_named_arrays(path):
+    """The dump format of oracle/ref_assembly.cpp."""
+    kinds = {"d": "<f8", "i": "<i4", "u": "<u8"}
+    data = open(path, "rb").read()
+    out, o = {}, 0
+    while o < len(data):
+        ln = int(np.frombuffer(data, "<u4", 1, o)[0]); o += 4
+        name = data[o:o + ln].decode(); o += ln
+        dt = np.dtype(kinds[chr(data[o])]); o += 1
+        cnt = int(np.frombuffer(data, "<u8", 1, o)[0]); o += 8
+        out[name] = np.frombuffer(data, dt, cnt, o).copy(); o += dt.itemsize * cnt
+    return out
+
+
+def make_assembly(out_dir):
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_assembly")
+    for case, first in ASSEMBLY_CASES:
+        arrays = {}
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.run([exe, d, case, str(first), "5"], cwd=d, check=True,
+                           stdout=subprocess.DEVNULL)
+            calls = sorted(f for f in os.listdir(d) if f.startswith("call_"))
+            assert len(calls) == 5, calls
+            for k, f in enumerate(calls):
+                z = read_named_arrays(os.path.join(d, f))
+                for key, v in z.items():
+                    if key in MESH_KEYS:
+                        if key in arrays:
+                            assert np.array_equal(arrays[key], v), key
+                        arrays[key] = v
+                    else:
+                        arrays[f"c{k}_{key}"] = v
+        arrays["count"] = np.array(5)
+        np.savez_compressed(os.path.join(out_dir, f"assembly_{case}.npz"), **arrays)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -144,6 +196,7 @@ def main():
     make_kat(ref, os.path.join(HERE, "kat_tridiag10.npz"))
     make_shocktube(os.path.join(HERE, "shocktube_calls.npz"))
     make_small(ref, os.path.join(HERE, "small_systems.npz"))
+    make_assembly(HERE)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
