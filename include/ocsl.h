@@ -121,6 +121,39 @@ int ocsl_solve(ocsl_ctx* ctx, int method, const double* value, const double* b, 
 int ocsl_solve_device(ocsl_ctx* ctx, int method, const double* d_value, const double* d_b,
                       double* d_x, const ocsl_opts* opts, ocsl_result* result);
 
+/* Several right-hand sides that share one matrix (the three momentum
+ * components of an inviscid or slip case, cflow_solver.cpp:258-290):
+ * d_b and d_x are [nrhs][n]; the factor is built once and reused by every
+ * right-hand side.  result[nrhs].  No reference counterpart (the reference
+ * assembles and solves each component separately). */
+int ocsl_solve_multi_device(ocsl_ctx* ctx, int method, const double* d_value, int nrhs,
+                            const double* d_b, double* d_x, const ocsl_opts* opts,
+                            ocsl_result* result);
+
+/* Batched solves of many independent systems (no reference counterpart).
+ * A batch owns one context per system (pattern analysed once, device memory
+ * reused) and `workers` host threads, each driving its own CUDA stream, which
+ * take systems largest first; the systems' solves overlap on the GPU.
+ * Systems are given in the reference's CSR layout, each with nrhs >= 1
+ * right-hand sides sharing its matrix. */
+typedef struct ocsl_batch ocsl_batch;
+typedef struct {
+    size_t n;
+    const size_t* row_ptr;
+    const size_t* column_index;
+    int nrhs;
+} ocsl_batch_system;
+int ocsl_batch_create(ocsl_batch** batch, int device, int count, const ocsl_batch_system* systems,
+                      int workers);
+int ocsl_batch_destroy(ocsl_batch* batch);
+/* d_value[i] (nnz_i), d_b[i] and d_x[i] ([nrhs_i][n_i]) are DEVICE pointers;
+ * result holds sum(nrhs_i) entries, system by system.  Returns the first
+ * non-OK status of any solve (every solve still runs). */
+int ocsl_batch_solve_device(ocsl_batch* batch, int method, const double* const* d_value,
+                            const double* const* d_b, double* const* d_x, const ocsl_opts* opts,
+                            ocsl_result* result);
+const char* ocsl_batch_last_error(const ocsl_batch* batch);
+
 /* Kernel-level entry points on DEVICE pointers, one per reference routine. */
 /* y = A x (mode 0); y = z - A x (mode 1); y = fma(a, A x, z) (mode 2).
  * cmatrix_solver.cpp:338-453 gemv. */

@@ -27,7 +27,7 @@ from ._abi import (BICGSTAB_REF, CG_REF, ILU_BICGSTAB, ILU_BICGSTAB_IR32, METHOD
 
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
-__all__ = ["Context", "CMatrix_solver", "check_pattern", "LibraryMissing", "OcslError",
+__all__ = ["Context", "Batch", "CMatrix_solver", "check_pattern", "LibraryMissing", "OcslError",
            "CG_REF", "BICGSTAB_REF", "PCG", "ILU_BICGSTAB", "ILU_BICGSTAB_IR32", "METHODS",
            "PHANTOM"]
 
@@ -232,6 +232,18 @@ class Context:
         self._check(self._L.ocsl_pattern_outer_device(self._h, float(alpha), _dptr(u), _dptr(v),
                                                       _dptr(out)), "pattern_outer")
 
+    def solve_multi_device(self, method, value, B, X, **opts):
+        """Several right-hand sides sharing the matrix: B, X are [nrhs, n] CUDA
+        tensors; the factor is built once.  Returns a list of result dicts."""
+        nrhs = int(B.shape[0])
+        o = _abi.default_opts(**opts)
+        res = (Result * nrhs)()
+        st = self._L.ocsl_solve_multi_device(self._h, _method(method), _dptr(value), nrhs,
+                                             _dptr(B), _dptr(X), C.byref(o), res)
+        if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT, _abi.NO_PATTERN):
+            self._check(st, "solve_multi_device")
+        return [r.as_dict() for r in res]
+
     # -- triangular-sweep kernel choice
     def set_sweep_kernel(self, kind: int = 0, tile_a: int = 0, tile_b: int = 0):
         """0 automatic, 1 level-scheduled, 2 structured (7-point box patterns)."""
@@ -277,6 +289,59 @@ class Context:
     def backsub_device(self, M, y, x):
         self._check(self._L.ocsl_backsub_device(self._h, _dptr(M), _dptr(y), _dptr(x)),
                     "backsub")
+
+
+class Batch:
+    """Many independent systems solved concurrently (ocsl_batch_*): one
+    context per system, ``workers`` host threads each driving its own stream.
+    ``systems`` is a list of (row_ptr, column_index, nrhs)."""
+
+    def __init__(self, systems, device: int = 0, workers: int = 8):
+        self._L = _abi.lib()
+        self._keep = []
+        arr = (_abi.BatchSystem * len(systems))()
+        self.nrhs = []
+        self.n = []
+        for i, (rp, col, nrhs) in enumerate(systems):
+            rp, col = _u64(rp), _u64(col)
+            self._keep += [rp, col]
+            arr[i].n, arr[i].nrhs = rp.size - 1, int(nrhs)
+            arr[i].row_ptr, arr[i].column_index = rp.ctypes.data, col.ctypes.data
+            self.nrhs.append(int(nrhs))
+            self.n.append(rp.size - 1)
+        h = C.c_void_p()
+        st = self._L.ocsl_batch_create(C.byref(h), int(device), len(systems), arr, int(workers))
+        if st != 0:
+            raise OcslError(st, f"batch_create: {self._L.ocsl_status_string(st).decode()}: "
+                                f"{self._L.ocsl_last_error(None).decode()}")
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ocsl_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve_device(self, method, values, Bs, Xs, **opts):
+        """values[i], Bs[i] ([nrhs_i, n_i]) and Xs[i] are CUDA tensors; returns
+        (status, list of per-right-hand-side result dicts)."""
+        k = len(values)
+        P = C.c_void_p * k
+        pv = P(*[_dptr(t).value for t in values])
+        pb = P(*[_dptr(t).value for t in Bs])
+        px = P(*[_dptr(t).value for t in Xs])
+        o = _abi.default_opts(**opts)
+        res = (Result * sum(self.nrhs))()
+        st = self._L.ocsl_batch_solve_device(self._h, _method(method), pv, pb, px, C.byref(o), res)
+        if st in (_abi.CUDA_ERROR, _abi.BAD_ARGUMENT):
+            raise OcslError(st, self._L.ocsl_batch_last_error(self._h).decode())
+        return st, [r.as_dict() for r in res]
 
 
 class CMatrix_solver:

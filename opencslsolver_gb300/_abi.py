@@ -78,6 +78,11 @@ FLOW_STATE_FIELDS = (
 INT_FIELDS = ("bc_type", "bc_wall", "bc_supersonic")
 
 
+class BatchSystem(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("row_ptr", C.c_void_p), ("column_index", C.c_void_p),
+                ("nrhs", C.c_int)]
+
+
 class FlowState(C.Structure):
     _fields_ = [(f, C.c_void_p) for f in FLOW_STATE_FIELDS]
 
@@ -111,6 +116,14 @@ _PROTOS = {
     "ocsl_solve": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts), C.POINTER(Result)]),
     "ocsl_solve_device": (C.c_int, [_CTX, C.c_int, _P, _P, _P, C.POINTER(Opts),
                                     C.POINTER(Result)]),
+    "ocsl_solve_multi_device": (C.c_int, [_CTX, C.c_int, _P, C.c_int, _P, _P, C.POINTER(Opts),
+                                          C.POINTER(Result)]),
+    "ocsl_batch_create": (C.c_int, [C.POINTER(_P), C.c_int, C.c_int, C.POINTER(BatchSystem),
+                                    C.c_int]),
+    "ocsl_batch_destroy": (C.c_int, [_P]),
+    "ocsl_batch_solve_device": (C.c_int, [_P, C.c_int, C.POINTER(_P), C.POINTER(_P),
+                                          C.POINTER(_P), C.POINTER(Opts), C.POINTER(Result)]),
+    "ocsl_batch_last_error": (C.c_char_p, [_P]),
     "ocsl_gemv_device": (C.c_int, [_CTX, C.c_int, C.c_double, _P, _P, _P, _P]),
     "ocsl_dot_device": (C.c_int, [_CTX, _SZ, _P, _P, C.POINTER(C.c_double)]),
     "ocsl_ilu_device": (C.c_int, [_CTX, _P, _P, C.c_int]),

@@ -21,7 +21,7 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libocsl_gb300.so")
 
 SOURCES = ["kernels_krylov.cu", "kernels_ilu.cu", "kernels_box.cu", "solver.cu", "pattern.cpp",
-           "noalloc.cu", "adjoint.cu", "assembly.cu"]
+           "noalloc.cu", "adjoint.cu", "assembly.cu", "batch.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -34,6 +34,8 @@ def nvcc() -> str:
 
 def _flags(src: str) -> list[str]:
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+    # tuning overrides, e.g. OCSL_NVCC_DEFINES="-DOCSL_BOX_PF=16 -DOCSL_BOX_DF=2" (rebuild with -f)
+    common += os.environ.get("OCSL_NVCC_DEFINES", "").split()
     if src.endswith(".cu"):
         return common + ARCH + ["-lineinfo", "--fmad=false", "-Xptxas", "-v"]
     return common

@@ -166,7 +166,7 @@ struct BoxParams {
 #define OCSL_BOX_PF 16
 #endif
 #ifndef OCSL_BOX_DF
-#define OCSL_BOX_DF 4
+#define OCSL_BOX_DF 2
 #endif
 constexpr int kPF = OCSL_BOX_PF;
 constexpr int kDF = OCSL_BOX_DF;

@@ -102,6 +102,11 @@ struct ocsl_ctx {
     int sweep_kernel = 0;
     int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
 
+    // factor of the last solve (buffer and SoA copies), for solves that reuse it
+    const double* fac_M = nullptr;
+    const double* fac_soa64 = nullptr;
+    const float* fac_soa32 = nullptr;
+
     // face-loop assembly: the mesh's face incidence (ocsl_set_faces)
     DevFaces F{};
     int* d_faces[8] = {};
@@ -127,6 +132,9 @@ struct ocsl_ctx {
 
 void ocsl_ctx::free_pattern()
 {
+    fac_M = nullptr;
+    fac_soa64 = nullptr;
+    fac_soa32 = nullptr;
     if (tctx) ocsl_destroy(tctx);
     tctx = nullptr;
     if (d_tperm) cudaFree(d_tperm);
@@ -299,6 +307,7 @@ struct Solve {
     int n;
     const double* soa64 = nullptr;  // stencil-SoA copy of the current factor
     const float* soa32 = nullptr;
+    bool reuse = false;  // the factor of the previous solve on the same values is still valid
 
     Scalars* sc(int k) const { return c->d_sc + k; }
 
@@ -407,6 +416,22 @@ struct Solve {
             soa32 = c->d_soa32;
         }
     }
+    // factor() + prepare_box(), or the previous solve's factor when reusing
+    const double* factored(const double* A, int sweeps, bool want_dinv, bool want_fp32, int k,
+                           bool want64, bool recip64, bool want32)
+    {
+        if (reuse && c->fac_M) {
+            soa64 = c->fac_soa64;
+            soa32 = c->fac_soa32;
+            return c->fac_M;
+        }
+        const double* M = factor(A, sweeps, want_dinv, want_fp32, k);
+        prepare_box(M, want64, recip64, want32);
+        c->fac_M = M;
+        c->fac_soa64 = soa64;
+        c->fac_soa32 = soa32;
+        return M;
+    }
     template <typename TT>
     const TT* soa() const
     {
@@ -473,8 +498,7 @@ void run_bicgstab_ref(Solve& s, const double* A, const double* b, double* x, int
     s.reset_scalars(0, 0.0);
     CK(cudaMemsetAsync(v[P], 0, bytes, s.st));  // Cvector(n) starts at 0 (:690-700)
     CK(cudaMemsetAsync(v[V], 0, bytes, s.st));
-    const double* M = s.factor(A, sweeps, false, false, 0);  // :702-704
-    s.prepare_box(M, true, false, false);
+    const double* M = s.factored(A, sweeps, false, false, 0, true, false, false);  // :702-704
     // r = b - A x (:708), r0 = r (:710), iteration 0's rhon and res
     s.spmv<double>(A, x, v[R], 1, b, v[R0], nullptr, DOT_YY | DOT_ZZ, 0, EP_RB_INIT);
     for (int it = 0; it < kRefBicgIters; ++it) {
@@ -598,8 +622,7 @@ TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x
                            const ocsl_opts& o)
 {
     double** v = s.c->v64;
-    const double* M = s.factor(A, o.ilu_sweeps, true, false, -1);
-    s.prepare_box(M, true, true, false);
+    const double* M = s.factored(A, o.ilu_sweeps, true, false, -1, true, true, false);
     return run_restarted(
         s, A, b, x, o, [&] { s.vec<double>(V_COPY2, {v[RH], v[P], v[R]}, 0, EP_STORE); },
         [&](int) {
@@ -612,7 +635,7 @@ TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x
 TolResult run_pcg_tol(Solve& s, const double* A, const double* b, double* x, const ocsl_opts& o)
 {
     double** v = s.c->v64;
-    s.factor(A, 0, true, false, -1);  // Jacobi: dinv = 1 / A_ii
+    s.factored(A, 0, true, false, -1, false, false, false);  // Jacobi: dinv = 1 / A_ii
     return run_restarted(
         s, A, b, x, o,
         [&] { s.vec<double>(V_PC_INIT, {v[Z], v[P], v[R], s.c->d_dinv}, 0, EP_PC_INIT); },
@@ -636,8 +659,7 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
     float** f = c->v32;
     TolResult res;
     const double tol2 = o.tol * o.tol;
-    const double* M = s.factor(A, o.ilu_sweeps, true, true, -1);
-    s.prepare_box(M, false, true, true);
+    const double* M = s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
     int total = 0;
     s.reset_scalars(0, tol2);
     for (int outer = 0;; ++outer) {
@@ -684,7 +706,7 @@ int check_ready(ocsl_ctx* c)
 }
 
 int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b, double* x,
-                      const ocsl_opts* opts, ocsl_result* out)
+                      const ocsl_opts* opts, ocsl_result* out, bool reuse_factor = false)
 {
     const ocsl_opts o = resolve(opts);
     ocsl_result r;
@@ -699,6 +721,8 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
     if (!aligned8(A) || !aligned8(b) || !aligned8(x))
         return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
     Solve s{c, c->stream, c->P, c->P.n};
+    s.reuse = reuse_factor;
+    if (!reuse_factor) c->fac_M = nullptr;
     int status = OCSL_OK;
     try {
         CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
@@ -1048,6 +1072,26 @@ int ocsl_solve_device(ocsl_ctx* c, int method, const double* A, const double* b,
     return solve_device_impl(c, method, A, b, x, opts, out);
 }
 
+int ocsl_solve_multi_device(ocsl_ctx* c, int method, const double* A, int nrhs, const double* b,
+                            double* x, const ocsl_opts* opts, ocsl_result* out)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (nrhs < 1) return fail(c, OCSL_BAD_ARGUMENT, "nrhs must be >= 1");
+    if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, OCSL_CUDA_ERROR, "cudaSetDevice");
+    const size_t n = (size_t)c->P.n;
+    int first = OCSL_OK;
+    for (int r = 0; r < nrhs; ++r) {
+        ocsl_result one;
+        const int st = solve_device_impl(c, method, A, b ? b + r * n : nullptr,
+                                         x ? x + r * n : nullptr, opts, &one, r > 0);
+        if (out) out[r] = one;
+        if (st == OCSL_CUDA_ERROR || st == OCSL_BAD_ARGUMENT) return st;
+        if (first == OCSL_OK) first = st;
+    }
+    return first;
+}
+
 int ocsl_solve(ocsl_ctx* c, int method, const double* value, const double* b, double* x,
                const ocsl_opts* opts, ocsl_result* out)
 {
@@ -1130,6 +1174,7 @@ int ocsl_ilu_device(ocsl_ctx* c, const double* A, double* M, int sweeps)
     try {
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
+        c->fac_M = nullptr;
         const double* F = s.factor(A, sweeps, false, false, -1);
         CK(cudaMemcpyAsync(M, F, sizeof(double) * (size_t)c->P.nnz, cudaMemcpyDeviceToDevice,
                            c->stream));
@@ -1150,6 +1195,7 @@ static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double*
     try {
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
+        c->fac_M = nullptr;
         CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
         s.prepare_box(M, true, false, false);  // the reference's backsub divides
         if (forward)

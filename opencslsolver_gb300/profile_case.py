@@ -22,6 +22,9 @@ def main(argv=None):
     ap.add_argument("--sweep-kernel", type=int, default=0)
     ap.add_argument("--tet", action="store_true", help="tetrahedral (6 per hex) system")
     ap.add_argument("--dims", type=int, nargs=3, default=None, help="hex box nx ny nz")
+    ap.add_argument("--tiles", type=int, nargs=2, default=(0, 0), help="structured sweep tile")
+    ap.add_argument("--profile", action="store_true",
+                    help="print CUDA-event time per launch by kernel category (last solve)")
     a = ap.parse_args(argv)
 
     import torch
@@ -37,17 +40,24 @@ def main(argv=None):
         s = W.hex_pprime(a.size, peclet=10.0)
     ctx = ocsl.Context(0)
     ctx.set_pattern(s.row_ptr, s.column_index)
-    ctx.set_sweep_kernel(a.sweep_kernel)
+    ctx.set_sweep_kernel(a.sweep_kernel, *a.tiles)
     A = torch.from_numpy(s.value).cuda()
     B = torch.from_numpy(s.b).cuda()
     X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
-    for _ in range(a.solves):
+    for k in range(a.solves):
+        if a.profile and k == a.solves - 1:
+            ctx.profile(True)
+            ctx.profile_read()
         X.zero_()
         r = ctx.solve_device(a.method, A, B, X)
         if r["status"] != 0:
             print("solve failed", r, file=sys.stderr)
             return 1
     torch.cuda.synchronize()
+    if a.profile:
+        for name, (ms, count) in ctx.profile_read().items():
+            if count:
+                print(f"{name:14s} {count:5d} launches  {1000.0 * ms / count:9.1f} us/launch")
     print(f"{s.name}: {a.solves} x {a.method}: {r}")
     ctx.close()
     return 0

@@ -449,3 +449,42 @@ def _abi_bc(name: str) -> int:
     from . import _abi
 
     return getattr(_abi, "BC_" + name)
+
+
+@dataclass
+class BatchSystem:
+    system: System       # matrix (reference layout) and its first right-hand side
+    rhs: np.ndarray      # [nrhs][n] right-hand sides sharing the matrix
+    kind: str            # "pprime" or "momentum"
+
+
+def batch_boxes(count: int = 64, *, seed: int = BASE_SEED + 40, min_cells: int = 10_000,
+                max_cells: int = 500_000) -> list[tuple[int, int, int]]:
+    """Box dimensions of the batching workload: cell counts log-uniform in
+    [min_cells, max_cells], aspect ratios U[1, 4] per axis (seeded)."""
+    rng = np.random.default_rng(seed)
+    dims = []
+    for _ in range(count):
+        cells = float(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells))))
+        aspect = rng.uniform(1.0, 4.0, size=3)
+        base = (cells / aspect.prod()) ** (1.0 / 3.0)
+        d = np.maximum(2, np.rint(base * aspect)).astype(int)
+        dims.append((int(d[0]), int(d[1]), int(d[2])))
+    return dims
+
+
+def batch_systems(count: int = 64, *, seed: int = BASE_SEED + 40, min_cells: int = 10_000,
+                  max_cells: int = 500_000) -> list[BatchSystem]:
+    """The batching workload: for each box one pressure-correction system
+    (the hex p' recipe, Peclet <= 10, one right-hand side) and one momentum
+    system (the same recipe at Peclet <= 50 with a stronger transient
+    diagonal, three right-hand sides sharing the matrix)."""
+    out = []
+    for k, (nx, ny, nz) in enumerate(batch_boxes(count, seed=seed, min_cells=min_cells,
+                                                 max_cells=max_cells)):
+        s = hex_pprime(nx, ny, nz, peclet=10.0, seed=seed + 100 * k)
+        out.append(BatchSystem(s, s.b[None, :].copy(), "pprime"))
+        m = hex_pprime(nx, ny, nz, peclet=50.0, seed=seed + 100 * k + 50)
+        rhs = np.random.default_rng(seed + 100 * k + 60).uniform(-1.0, 1.0, size=(3, m.n))
+        out.append(BatchSystem(m, rhs, "momentum"))
+    return out
