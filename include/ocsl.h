@@ -60,7 +60,8 @@ typedef struct {
     double tol;         /* relative residual target (mode T), default 1e-10            */
     int maxit;          /* total Krylov iterations allowed (mode T), default 5000     */
     int ilu_sweeps;     /* fixed-point ILU sweeps, default 3 (cmatrix_solver.cpp:521) */
-    double inner_tol;   /* IR32: inner relative reduction, default 1e-4               */
+    double inner_tol;   /* IR32: inner relative reduction per refinement step, default
+                           1e-5; the last step asks only for what is still missing    */
     int inner_maxit;    /* IR32: iterations per inner solve, default 500              */
 } ocsl_opts;
 
@@ -162,6 +163,16 @@ int ocsl_gemv_device(ocsl_ctx* ctx, int mode, double a, const double* d_value, c
 /* <x, y> in the library's fixed tile order; cmatrix_solver.cpp:233 norm. */
 int ocsl_dot_device(ocsl_ctx* ctx, size_t n, const double* d_x, const double* d_y,
                     double* result);
+/* sum (absolute = 0, cmatrix_solver.cpp:244-252 sum) or sum of |x|
+ * (absolute = 1, :255-263 ABSsum) of n elements, in the tile order. */
+int ocsl_sum_device(ocsl_ctx* ctx, size_t n, const double* d_x, int absolute, double* result);
+/* out = x * y element by element; :266-272 product. */
+int ocsl_product_device(ocsl_ctx* ctx, size_t n, const double* d_x, const double* d_y,
+                        double* d_out);
+/* out = a x + b y with the reference's special cases for b = +-1 and a = +-1
+ * (:284-335); d_y = NULL gives out = a x (:275-281). */
+int ocsl_axpy_device(ocsl_ctx* ctx, size_t n, double a, const double* d_x, double b,
+                     const double* d_y, double* d_out);
 /* M = `sweeps` fixed-point ILU sweeps of A; cmatrix_solver.cpp:472-552. */
 int ocsl_ilu_device(ocsl_ctx* ctx, const double* d_A, double* d_M, int sweeps);
 /* y = L^-1 b, cmatrix_solver.cpp:555-572 ILU_forsub. */

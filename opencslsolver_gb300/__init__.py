@@ -280,6 +280,22 @@ class Context:
                                             C.byref(out)), "dot")
         return out.value
 
+    def sum_device(self, x, absolute=False):
+        """cmatrix_solver.cpp:244-263 sum / ABSsum (tile order)."""
+        out = C.c_double()
+        self._check(self._L.ocsl_sum_device(self._h, x.numel(), _dptr(x), int(bool(absolute)),
+                                            C.byref(out)), "sum")
+        return out.value
+
+    def product_device(self, x, y, out):
+        self._check(self._L.ocsl_product_device(self._h, x.numel(), _dptr(x), _dptr(y),
+                                                _dptr(out)), "product")
+
+    def axpy_device(self, a, x, out, b=0.0, y=None):
+        """out = a x + b y (the reference's axpy, :275-335); y None: out = a x."""
+        self._check(self._L.ocsl_axpy_device(self._h, x.numel(), float(a), _dptr(x), float(b),
+                                             _dptr(y), _dptr(out)), "axpy")
+
     def ilu_device(self, A, M, sweeps=3):
         self._check(self._L.ocsl_ilu_device(self._h, _dptr(A), _dptr(M), sweeps), "ilu")
 

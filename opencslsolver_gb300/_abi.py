@@ -126,6 +126,9 @@ _PROTOS = {
     "ocsl_batch_last_error": (C.c_char_p, [_P]),
     "ocsl_gemv_device": (C.c_int, [_CTX, C.c_int, C.c_double, _P, _P, _P, _P]),
     "ocsl_dot_device": (C.c_int, [_CTX, _SZ, _P, _P, C.POINTER(C.c_double)]),
+    "ocsl_sum_device": (C.c_int, [_CTX, _SZ, _P, C.c_int, C.POINTER(C.c_double)]),
+    "ocsl_product_device": (C.c_int, [_CTX, _SZ, _P, _P, _P]),
+    "ocsl_axpy_device": (C.c_int, [_CTX, _SZ, C.c_double, _P, C.c_double, _P, _P]),
     "ocsl_ilu_device": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "ocsl_forsub_device": (C.c_int, [_CTX, _P, _P, _P]),
     "ocsl_backsub_device": (C.c_int, [_CTX, _P, _P, _P]),

@@ -360,8 +360,9 @@ template <int OP>
 struct OpDots {
     static constexpr int value =
         (OP == V_RB_XR || OP == V_DOT2 || OP == V_TB_XR || OP == V_PC_XRZ) ? 2
-        : (OP == V_DOT1 || OP == V_RC_XR || OP == V_TB_S || OP == V_PC_INIT || OP == V_IR_SCALE) ? 1
-                                                                                                  : 0;
+        : (OP == V_DOT1 || OP == V_RC_XR || OP == V_TB_S || OP == V_PC_INIT || OP == V_IR_SCALE ||
+           OP == V_SUM || OP == V_ABSSUM) ? 1
+                                          : 0;
 };
 
 struct VecParams {
@@ -472,6 +473,26 @@ __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
             double* x = reinterpret_cast<double*>(P.p.v[0]);
             const float d = reinterpret_cast<const float*>(P.p.v[1])[e];
             x[e] = fma((double)d, P.outer->rnorm, x[e]);
+        } else if constexpr (OP == V_SUM) {  // fma(x, 1, s) == s + x exactly
+            acc[0].add(v[0][e], T(1));
+        } else if constexpr (OP == V_ABSSUM) {
+            acc[0].add(fabs(v[0][e]), T(1));
+        } else if constexpr (OP == V_PRODUCT) {
+            v[2][e] = v[0][e] * v[1][e];
+        } else if constexpr (OP == V_SCALE) {
+            v[2][e] = a * v[0][e];
+        } else if constexpr (OP == V_AXPY) {
+            // a = alpha, b = beta of the scalars block; the reference's branches
+            const T x = v[0][e], y = v[1][e];
+            T o;
+            if (be == T(1)) {
+                o = a == T(1) ? x + y : (a == T(-1) ? y - x : fma_t(a, x, y));
+            } else if (be == T(-1)) {
+                o = a == T(1) ? x - y : (a == T(-1) ? -y - x : fma_t(a, x, -y));
+            } else {
+                o = fma_t(a, x, be * y);
+            }
+            v[2][e] = o;
         }
     }
     if constexpr (ND > 0) {
@@ -581,6 +602,11 @@ void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& ptrs, const Reduc
     case V_PC_P: vec_dispatch<T, V_PC_P>(st, P); break;
     case V_IR_SCALE: vec_dispatch<float, V_IR_SCALE>(st, P); break;
     case V_IR_UPDATE: vec_dispatch<float, V_IR_UPDATE>(st, P); break;
+    case V_SUM: vec_dispatch<T, V_SUM>(st, P); break;
+    case V_ABSSUM: vec_dispatch<T, V_ABSSUM>(st, P); break;
+    case V_PRODUCT: vec_dispatch<T, V_PRODUCT>(st, P); break;
+    case V_AXPY: vec_dispatch<T, V_AXPY>(st, P); break;
+    case V_SCALE: vec_dispatch<T, V_SCALE>(st, P); break;
     default: break;
     }
 }

@@ -143,6 +143,11 @@ enum VecOp : int {
     V_PC_P,       // p = fma(beta, p, z)
     V_IR_SCALE,   // f0 = float(r * (1/rnorm)); f1 = f0; f2 = f0; f3 = 0; dot <f0,f0>
     V_IR_UPDATE,  // x = fma(double(f0), rnorm, x)
+    V_SUM,        // dot-free sum: s = s + x (cmatrix_solver.cpp:244-252)
+    V_ABSSUM,     // s = s + |x| (:255-263)
+    V_PRODUCT,    // out = x * y (:266-272)
+    V_AXPY,       // out = a x + b y with the reference's special cases (:275-335)
+    V_SCALE,      // out = a x (:275-281)
 };
 
 struct VecPtrs {

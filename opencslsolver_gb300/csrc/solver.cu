@@ -676,8 +676,10 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
         }
         if (so.done) break;
         if (total >= o.maxit || outer >= 1000) { res.status = OCSL_NOT_CONVERGED; break; }
-        // inner solve of A d = r / ||r|| in FP32 from d = 0
-        s.reset_scalars(1, o.inner_tol * o.inner_tol);
+        // inner solve of A d = r / ||r|| in FP32 from d = 0, to the reduction
+        // still missing (with a margin of 2), at most inner_tol
+        const double itol = std::max(o.inner_tol, 0.5 * o.tol / so.res);
+        s.reset_scalars(1, itol * itol);
         s.vec<float>(V_IR_SCALE, {v[R], f[F_RI], f[F_RH], f[F_P], f[F_D]}, 1, EP_IR_INNER_INIT);
         const int budget = std::min(o.inner_maxit, o.maxit - total);
         const Scalars si = run_batches(s, 1, budget, [&](int) {
@@ -874,7 +876,7 @@ void ocsl_default_opts(ocsl_opts* o)
     o->tol = 1e-10;
     o->maxit = 5000;
     o->ilu_sweeps = 3;
-    o->inner_tol = 1e-4;
+    o->inner_tol = 1e-5;
     o->inner_maxit = 500;
 }
 
@@ -1163,6 +1165,64 @@ int ocsl_dot_device(ocsl_ctx* c, size_t n, const double* x, const double* y, dou
         return from_cuda(c, e);
     }
     return OCSL_OK;
+}
+
+static int vector_entry(ocsl_ctx* c, size_t n, std::initializer_list<const void*> ptrs, int op,
+                        double a, double b, double* result)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (n >= (size_t)INT32_MAX) return fail(c, OCSL_BAD_ARGUMENT, "n exceeds the int32 limit");
+    for (const void* p : ptrs)
+        if (n > 0 && (!p || !aligned8(p)))
+            return fail(c, OCSL_BAD_ARGUMENT, "null or misaligned device pointer");
+    if (n == 0) {
+        if (result) *result = 0.0;
+        return OCSL_OK;
+    }
+    try {
+        CK(cudaSetDevice(c->device));
+        c->ensure_reduce((int)((n + kTile - 1) / kTile));
+        Solve s{c, c->stream, c->P, (int)n};
+        s.reset_scalars(2, 0.0);
+        if (!result) {  // elementwise: a and b ride in the scalars block
+            Scalars* stage = c->h_sc + 5;
+            CK(cudaStreamSynchronize(c->stream));
+            stage->alpha = a;
+            stage->beta = b;
+            stage->done = 0;
+            CK(cudaMemcpyAsync(&c->d_sc[2].alpha, &stage->alpha, sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(&c->d_sc[2].beta, &stage->beta, sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+        }
+        s.vec<double>(op, ptrs, 2, EP_STORE);
+        CK(cudaGetLastError());
+        if (result)
+            *result = s.read_scalars(2).sum[0];
+        else
+            CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_sum_device(ocsl_ctx* c, size_t n, const double* x, int absolute, double* result)
+{
+    if (!c || !result) return OCSL_BAD_ARGUMENT;
+    return vector_entry(c, n, {x}, absolute ? V_ABSSUM : V_SUM, 0.0, 0.0, result);
+}
+
+int ocsl_product_device(ocsl_ctx* c, size_t n, const double* x, const double* y, double* out)
+{
+    return vector_entry(c, n, {x, y, out}, V_PRODUCT, 0.0, 0.0, nullptr);
+}
+
+int ocsl_axpy_device(ocsl_ctx* c, size_t n, double a, const double* x, double b, const double* y,
+                     double* out)
+{
+    if (!y) return vector_entry(c, n, {x, x, out}, V_SCALE, a, 0.0, nullptr);
+    return vector_entry(c, n, {x, y, out}, V_AXPY, a, b, nullptr);
 }
 
 int ocsl_ilu_device(ocsl_ctx* c, const double* A, double* M, int sweeps)

@@ -23,6 +23,7 @@ def main(argv=None):
     ap.add_argument("--tet", action="store_true", help="tetrahedral (6 per hex) system")
     ap.add_argument("--dims", type=int, nargs=3, default=None, help="hex box nx ny nz")
     ap.add_argument("--tiles", type=int, nargs=2, default=(0, 0), help="structured sweep tile")
+    ap.add_argument("--inner-tol", type=float, default=None, help="IR32 inner tolerance")
     ap.add_argument("--profile", action="store_true",
                     help="print CUDA-event time per launch by kernel category (last solve)")
     a = ap.parse_args(argv)
@@ -49,7 +50,8 @@ def main(argv=None):
             ctx.profile(True)
             ctx.profile_read()
         X.zero_()
-        r = ctx.solve_device(a.method, A, B, X)
+        opts = {} if a.inner_tol is None else {"inner_tol": a.inner_tol}
+        r = ctx.solve_device(a.method, A, B, X, **opts)
         if r["status"] != 0:
             print("solve failed", r, file=sys.stderr)
             return 1

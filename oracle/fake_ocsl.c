@@ -28,7 +28,7 @@ void ocsl_default_opts(ocsl_opts* o)
     o->tol = 1e-10;
     o->maxit = 5000;
     o->ilu_sweeps = 3;
-    o->inner_tol = 1e-4;
+    o->inner_tol = 1e-5;
     o->inner_maxit = 500;
 }
 

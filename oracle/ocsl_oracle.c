@@ -83,6 +83,56 @@ double orc_dot(size_t n, const double* x, const double* y)
     return s;
 }
 
+static double tile_sum(size_t n, size_t tile, const double* x, int absolute)
+{
+    double lanes[ORC_LANES];
+    const size_t base = tile * ORC_TILE;
+    for (int t = 0; t < ORC_LANES; ++t) {
+        double acc = 0.0;
+        for (int j = 0; j < ORC_TILE / ORC_LANES; ++j) {
+            size_t e = base + (size_t)j * ORC_LANES + (size_t)t;
+            if (e < n) acc = acc + (absolute ? fabs(x[e]) : x[e]);
+        }
+        lanes[t] = acc;
+    }
+    return lanes_to_sum(lanes);
+}
+
+/* cmatrix_solver.cpp:244-252 sum and :255-263 ABSsum, in the tile order. */
+double orc_sum(size_t n, const double* x, int absolute)
+{
+    if (n == 0) return 0.0;
+    const size_t P = (n + ORC_TILE - 1) / ORC_TILE;
+    double* part = (double*)malloc(P * sizeof(double));
+    for (size_t p = 0; p < P; ++p) part[p] = tile_sum(n, p, x, absolute);
+    double s = reduce_partials(P, part);
+    free(part);
+    return s;
+}
+
+/* :266-272 product */
+void orc_product(size_t n, const double* x, const double* y, double* out)
+{
+    for (size_t i = 0; i < n; ++i) out[i] = x[i] * y[i];
+}
+
+/* :275-335 axpy; y == NULL is the one-vector overload out = a x.  The
+ * reference's a*x + y forms are contracted under -ffast-math: fma here. */
+void orc_axpy(size_t n, double a, const double* x, double b, const double* y, double* out)
+{
+    for (size_t i = 0; i < n; ++i) {
+        if (!y) {
+            out[i] = a * x[i];
+        } else if (b == 1.0) {
+            out[i] = a == 1.0 ? x[i] + y[i] : (a == -1.0 ? y[i] - x[i] : fma(a, x[i], y[i]));
+        } else if (b == -1.0) {
+            out[i] = a == 1.0 ? x[i] - y[i] : (a == -1.0 ? -y[i] - x[i] : fma(a, x[i], -y[i]));
+        } else {
+            out[i] = fma(a, x[i], b * y[i]);
+        }
+    }
+}
+
 double orc_dot_seq(size_t n, const double* x, const double* y)
 {
     double s = 0.0;
@@ -570,7 +620,9 @@ int orc_bicgstab_ir32(size_t n, const uint64_t* rp, const uint64_t* col, const d
             d[k] = 0.0f;
         }
         double rho = dot32(n, rh, ri);
-        const double r0 = dot32(n, ri, ri), itol2 = inner_tol * inner_tol * r0;
+        /* inner target: the reduction still missing (margin 2), at most inner_tol */
+        const double itol = fmax(inner_tol, 0.5 * tol / sqrt(rr / bb));
+        const double r0 = dot32(n, ri, ri), itol2 = itol * itol * r0;
         for (int k = 0; k < inner_maxit && it < maxit; ++k) {
             ++it;
             precond32(n, rp, col, M32, diag, dinv32, p, tmp, ph);

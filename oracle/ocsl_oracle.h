@@ -50,6 +50,12 @@ void orc_set_threads(int threads);
 double orc_dot(size_t n, const double* x, const double* y);      /* tile order */
 double orc_dot_seq(size_t n, const double* x, const double* y);  /* sequential */
 
+/* cmatrix_solver.cpp:244-263 sum / ABSsum (tile order), :266-272 product,
+ * :275-335 axpy (y == NULL: out = a x). */
+double orc_sum(size_t n, const double* x, int absolute);
+void orc_product(size_t n, const double* x, const double* y, double* out);
+void orc_axpy(size_t n, double a, const double* x, double b, const double* y, double* out);
+
 /* y = A x (mode 0), y = z - A x (mode 1), y = fma(a, A x, z) (mode 2);
  * cmatrix_solver.cpp:338-453 gemv.  Phantom columns (>= n) are skipped. */
 void orc_gemv(size_t n, const uint64_t* rp, const uint64_t* col, const double* val,

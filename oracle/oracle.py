@@ -80,6 +80,9 @@ _ORACLE_PROTOS = {
     "orc_bicgstab_ir32": (C.c_int, _CSR + [_P, _P, _P, C.c_double, C.c_int, C.c_double,
                                            C.c_int, C.c_int, _P, _P, _P]),
     "orc_true_relres": (C.c_double, _CSR + [_P, _P, _P]),
+    "orc_sum": (C.c_double, [_SZ, _P, C.c_int]),
+    "orc_product": (None, [_SZ, _P, _P, _P]),
+    "orc_axpy": (None, [_SZ, C.c_double, _P, C.c_double, _P, _P]),
     "orc_assemble": (None, _CSR + [C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, _P, _P, _P,
                                    _P]),
     "orc_bc_value_grad": (None, [_SZ, _P, C.c_int64, _P, _P, _P, _P, _P]),
@@ -91,6 +94,9 @@ _REF_PROTOS = {
     "refh_bicgstab_solve": (C.c_double, _REF_CSR + [_P, _P, _P]),
     "refh_gemv": (None, _REF_CSR + [_P, C.c_double, _P, C.c_double, _P, _P]),
     "refh_norm": (C.c_double, [_SZ, _P, _P]),
+    "refh_sum": (C.c_double, [_SZ, _P, C.c_int]),
+    "refh_product": (None, [_SZ, _P, _P, _P]),
+    "refh_axpy": (None, [_SZ, C.c_double, _P, C.c_double, _P, _P]),
     "refh_extract_diag": (None, _REF_CSR + [_P]),
     "refh_ilu_decompose": (None, _REF_CSR + [_P, _P]),
     "refh_forsub": (None, _REF_CSR + [_P, _P, _P]),
@@ -116,6 +122,24 @@ class Oracle:
     def dot(self, x, y):
         x, y = _c64(x), _c64(y)
         return self._l.orc_dot(x.size, _ptr(x), _ptr(y))
+
+    def sum(self, x, absolute=False):
+        """cmatrix_solver.cpp:244-263 sum / ABSsum in the tile order."""
+        x = _c64(x)
+        return self._l.orc_sum(x.size, _ptr(x), int(bool(absolute)))
+
+    def product(self, x, y):
+        x, y = _c64(x), _c64(y)
+        out = np.zeros(x.size)
+        self._l.orc_product(x.size, _ptr(x), _ptr(y), _ptr(out))
+        return out
+
+    def axpy(self, a, x, b=0.0, y=None):
+        x = _c64(x)
+        yy = None if y is None else _c64(y)
+        out = np.zeros(x.size)
+        self._l.orc_axpy(x.size, float(a), _ptr(x), float(b), _ptr(yy), _ptr(out))
+        return out
 
     def dot_seq(self, x, y):
         x, y = _c64(x), _c64(y)
@@ -199,7 +223,7 @@ class Oracle:
                                  tol, maxit, C.byref(it), C.byref(rr))
         return x, rc, it.value, rr.value
 
-    def bicgstab_ir32(self, rp, col, val, b, x0, tol=1e-10, maxit=2000, inner_tol=1e-4,
+    def bicgstab_ir32(self, rp, col, val, b, x0, tol=1e-10, maxit=2000, inner_tol=1e-5,
                       inner_maxit=200, sweeps=3):
         rp, col = self._csr(rp, col)
         val, b = _c64(val), _c64(b)
@@ -315,6 +339,23 @@ class Reference:
         self._l.refh_gemv(n, nnz, _ptr(rp), _ptr(col), _ptr(val), a, _ptr(x), bcoef, _ptr(z),
                           _ptr(y))
         return y
+
+    def sum(self, x, absolute=False):
+        x = _c64(x)
+        return self._l.refh_sum(x.size, _ptr(x), int(bool(absolute)))
+
+    def product(self, x, y):
+        x, y = _c64(x), _c64(y)
+        out = np.zeros(x.size)
+        self._l.refh_product(x.size, _ptr(x), _ptr(y), _ptr(out))
+        return out
+
+    def axpy(self, a, x, b=0.0, y=None):
+        x = _c64(x)
+        yy = None if y is None else _c64(y)
+        out = np.zeros(x.size)
+        self._l.refh_axpy(x.size, float(a), _ptr(x), float(b), _ptr(yy), _ptr(out))
+        return out
 
     def norm(self, x, y):
         x, y = _c64(x), _c64(y)

@@ -89,6 +89,40 @@ void refh_gemv(size_t n, size_t nnz, const uint64_t* rp, const uint64_t* col,
 }
 
 // cmatrix_solver.cpp:233 norm (a dot product).
+// cmatrix_solver.cpp:244-263 (static members)
+double refh_sum(size_t n, const double* x, int absolute)
+{
+    CMatrix_solver::Cvector vx(n);
+    load_vec(vx, n, x);
+    return absolute ? CMatrix_solver::ABSsum(vx) : CMatrix_solver::sum(vx);
+}
+
+// :266-272 product
+void refh_product(size_t n, const double* x, const double* y, double* out)
+{
+    CMatrix_solver s(n, n, 0);
+    CMatrix_solver::Cvector vx(n), vy(n), vo(n);
+    load_vec(vx, n, x);
+    load_vec(vy, n, y);
+    s.product(vx, vy, vo);
+    std::memcpy(out, vo.value.data(), n * sizeof(double));
+}
+
+// :275-335 axpy (y == NULL: the one-vector overload)
+void refh_axpy(size_t n, double a, const double* x, double b, const double* y, double* out)
+{
+    CMatrix_solver s(n, n, 0);
+    CMatrix_solver::Cvector vx(n), vy(n), vo(n);
+    load_vec(vx, n, x);
+    if (y) {
+        load_vec(vy, n, y);
+        s.axpy(a, vx, b, vy, vo);
+    } else {
+        s.axpy(a, vx, vo);
+    }
+    std::memcpy(out, vo.value.data(), n * sizeof(double));
+}
+
 double refh_norm(size_t n, const double* x, const double* y)
 {
     CMatrix_solver s(n, n, 0);

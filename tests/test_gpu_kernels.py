@@ -181,3 +181,28 @@ def test_structured_kernel_refused_for_unstructured(ctx):
 
     with pytest.raises(ocsl.OcslError):
         ctx.set_sweep_kernel(2)
+
+
+AXPY_CASES = [(1.0, 1.0), (-1.0, 1.0), (0.3, 1.0), (1.0, -1.0), (-1.0, -1.0), (0.3, -1.0),
+              (0.3, 0.7), (2.5, None)]
+
+
+@pytest.mark.parametrize("n", [1, 2047, 2048, 100003, 3_000_000])
+def test_vector_routines_bit_exact(ctx, torch_cuda, oracle, n):
+    """sum / ABSsum / product / axpy entry points against the oracle."""
+    rng = np.random.default_rng(n)
+    x, y = rng.standard_normal(n), rng.standard_normal(n)
+    X, Y = dev(torch_cuda, x), dev(torch_cuda, y)
+    assert ctx.sum_device(X) == oracle.sum(x)
+    assert ctx.sum_device(X, absolute=True) == oracle.sum(x, absolute=True)
+    O = torch_cuda.empty_like(X)
+    ctx.product_device(X, Y, O)
+    assert np.array_equal(host(O), oracle.product(x, y))
+    for a, b in AXPY_CASES:
+        if b is None:
+            ctx.axpy_device(a, X, O)
+            want = oracle.axpy(a, x)
+        else:
+            ctx.axpy_device(a, X, O, b, Y)
+            want = oracle.axpy(a, x, b, y)
+        assert np.array_equal(host(O), want), (a, b)
