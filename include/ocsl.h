@@ -213,13 +213,18 @@ int ocsl_pattern_outer_device(ocsl_ctx* ctx, double alpha, const double* d_u, co
  * CFlow_face::stress_explicit_part (cflow_solver_cell_face_loops.cpp:25-35),
  * is an input.
  * ---------------------------------------------------------------------- */
-typedef enum { OCSL_EQ_MOMENTUM = 0, OCSL_EQ_PRESSURE = 1, OCSL_EQ_ENTHALPY = 2 } ocsl_equation;
+typedef enum {
+    OCSL_EQ_MOMENTUM = 0, OCSL_EQ_PRESSURE = 1, OCSL_EQ_ENTHALPY = 2,
+    OCSL_EQ_HEAT = 3  /* heat conduction, cheat_solver.cpp:32-65 */
+} ocsl_equation;
 /* Boundary kinds: the values of enums::Eflow_BC_type and Ewall_BC_type (enums.h:39-41). */
 typedef enum {
     OCSL_BC_EMPTY = 0, OCSL_BC_SYMMETRY = 1, OCSL_BC_WALL = 2, OCSL_BC_VELOCITY_INLET = 3,
     OCSL_BC_SUPERSONIC_INLET = 4, OCSL_BC_PRESSURE_OUTLET = 5
 } ocsl_bc_type;
 typedef enum { OCSL_WALL_NO_SLIP = 0, OCSL_WALL_SLIP = 1 } ocsl_wall_type;
+/* enums::Ethermal_BC_type */
+typedef enum { OCSL_THERMAL_CONSTANT_TEMPERATURE = 0, OCSL_THERMAL_ADIABATIC = 1 } ocsl_thermal_type;
 
 typedef struct {
     int equation;       /* ocsl_equation                                          */
@@ -229,6 +234,7 @@ typedef struct {
     int transient;      /* Etimestepping_type::Transient (else steady)            */
     double implicit_underrelaxation;  /* CFlow_solver::implicit_underrelaxation  */
     double R_specific, gamma, sutherland[2], prandtl;  /* Cfluid_properties      */
+    double thermal_diffusivity;  /* Cconfiguration::thermal_diffusivity (heat)    */
 } ocsl_assembly;
 
 /* Per-assembly state, DEVICE pointers.  Face arrays follow the order given to
@@ -271,6 +277,7 @@ typedef struct {
     const double* temperature;
     const double* enthalpy;
     const double* enthalpy_last;
+    const int32_t* bc_thermal;    /* ocsl_thermal_type (heat conduction)          */
 } ocsl_flow_state;
 
 /* The mesh's face-to-cell connectivity (host arrays, once per mesh, after

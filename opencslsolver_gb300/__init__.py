@@ -179,8 +179,9 @@ class Context:
         for k in ("equation", "dimension", "viscous", "blended", "transient"):
             setattr(q, k, int(eq.get(k, 0)))
         for k in ("implicit_underrelaxation", "R_specific", "gamma", "prandtl"):
-            setattr(q, k, float(eq[k]))
-        q.sutherland[0], q.sutherland[1] = (float(v) for v in eq["sutherland"])
+            setattr(q, k, float(eq.get(k, 0.0)))
+        q.thermal_diffusivity = float(eq.get("thermal_diffusivity", 0.0))
+        q.sutherland[0], q.sutherland[1] = (float(v) for v in eq.get("sutherland", (0.0, 0.0)))
         return q
 
     def assemble_device(self, eq: dict, state: dict, value, b, x0, ap=None, total_mdot=None):

@@ -55,7 +55,8 @@ _P = C.c_void_p
 _SZ = C.c_size_t
 
 # ocsl_assembly / ocsl_flow_state (include/ocsl.h), in declaration order.
-EQ_MOMENTUM, EQ_PRESSURE, EQ_ENTHALPY = 0, 1, 2
+EQ_MOMENTUM, EQ_PRESSURE, EQ_ENTHALPY, EQ_HEAT = 0, 1, 2, 3
+THERMAL_CONSTANT_TEMPERATURE, THERMAL_ADIABATIC = 0, 1
 BC_EMPTY, BC_SYMMETRY, BC_WALL, BC_VELOCITY_INLET, BC_SUPERSONIC_INLET, BC_PRESSURE_OUTLET = range(6)
 WALL_NO_SLIP, WALL_SLIP = 0, 1
 
@@ -64,7 +65,8 @@ class Assembly(C.Structure):
     _fields_ = [("equation", C.c_int), ("dimension", C.c_int), ("viscous", C.c_int),
                 ("blended", C.c_int), ("transient", C.c_int),
                 ("implicit_underrelaxation", C.c_double), ("R_specific", C.c_double),
-                ("gamma", C.c_double), ("sutherland", C.c_double * 2), ("prandtl", C.c_double)]
+                ("gamma", C.c_double), ("sutherland", C.c_double * 2), ("prandtl", C.c_double),
+                ("thermal_diffusivity", C.c_double)]
 
 
 FLOW_STATE_FIELDS = (
@@ -74,8 +76,8 @@ FLOW_STATE_FIELDS = (
     "bc_velocity", "bc_value",
     "volume", "delta_t", "velocity", "velocity_last", "pressure_grad", "density_c",
     "density_last", "pressure", "pressure_last", "pressure_corr", "temperature", "enthalpy",
-    "enthalpy_last")
-INT_FIELDS = ("bc_type", "bc_wall", "bc_supersonic")
+    "enthalpy_last", "bc_thermal")
+INT_FIELDS = ("bc_type", "bc_wall", "bc_supersonic", "bc_thermal")
 
 
 class BatchSystem(C.Structure):

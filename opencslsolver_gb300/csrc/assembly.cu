@@ -1,5 +1,7 @@
-// Face-loop coefficient assembly of the flow solver on the GPU
-// (cflow_solver_cell_face_loops.cpp:37-446, solvers_common.h:32-151).
+// Face-loop coefficient assembly on the GPU: the flow solver's momentum,
+// pressure-correction and enthalpy equations (cflow_solver_cell_face_loops.cpp:37-446,
+// solvers_common.h:32-151) and the heat solver's conduction equation
+// (cheat_solver.cpp:32-65).
 //
 // The reference scatters every face's contributions into the CSR with atomic
 // adds from an OpenMP face loop, then a boundary-face loop, then a cell loop.
@@ -99,6 +101,10 @@ __device__ __forceinline__ void diffusive(Ops& o, double D)
 __device__ void face_ops(const ocsl_assembly& q, const ocsl_flow_state& st, int n, int nf, int f,
                          int L, int R, Ops& o)
 {
+    if (q.equation == OCSL_EQ_HEAT) {  // cheat_solver.cpp:32-37 (reads no flow state)
+        diffusive(o, q.thermal_diffusivity * st.ksi_A[f]);
+        return;
+    }
     const double g = st.geo_aver[f], m = st.mdot[f];
     if (q.equation == OCSL_EQ_MOMENTUM) {  // :37-57
         const double* u = st.velocity + (size_t)q.dimension * n;
@@ -150,6 +156,14 @@ __device__ __forceinline__ void neumann_zero(Acc& c, double m)  // solvers_commo
 __device__ void bc_apply(const ocsl_assembly& q, const ocsl_flow_state& st, int n, int nb, int k,
                          int P, Acc& c)
 {
+    if (q.equation == OCSL_EQ_HEAT) {  // cheat_solver.cpp:39-56
+        if (st.bc_thermal[k] == OCSL_THERMAL_CONSTANT_TEMPERATURE) {
+            const double D = q.thermal_diffusivity * st.bc_ksi_A[k];
+            c.a += D;
+            c.b += D * st.bc_temperature[k];
+        }
+        return;
+    }
     const int type = st.bc_type[k];
     const double m = st.bc_mdot[k];
     const double bv = st.bc_value ? st.bc_value[k] : 0.0;
@@ -272,6 +286,12 @@ assemble_kernel(DevPattern P, DevFaces F, ocsl_assembly q, ocsl_flow_state st, d
             c.b += dum;
         }
         xi = st.velocity[(size_t)d * n + i];
+        c.tm = 0.0;
+    } else if (q.equation == OCSL_EQ_HEAT) {  // cheat_solver.cpp:58-66
+        const double dum = vol / st.delta_t[i];
+        c.a += dum;
+        c.b += st.temperature[i] * dum;
+        xi = st.temperature[i];
         c.tm = 0.0;
     } else if (q.equation == OCSL_EQ_PRESSURE) {
         if (q.transient) {

@@ -823,16 +823,17 @@ const char* missing_state_field(const ocsl_assembly& q, const ocsl_flow_state& s
         bool want;
     };
     const bool mom = q.equation == OCSL_EQ_MOMENTUM, pre = q.equation == OCSL_EQ_PRESSURE,
-               ent = q.equation == OCSL_EQ_ENTHALPY, tr = q.transient != 0, vis = q.viscous != 0;
+               ent = q.equation == OCSL_EQ_ENTHALPY, heat = q.equation == OCSL_EQ_HEAT,
+               flow = !heat, tr = q.transient != 0 || heat, vis = q.viscous != 0;
     const Need need[] = {
-        {s.geo_aver, "geo_aver", has_nf},
-        {s.mdot, "mdot", has_nf},
-        {s.ksi_A, "ksi_A", has_nf && ((mom && vis) || ent)},
+        {s.geo_aver, "geo_aver", has_nf && flow},
+        {s.mdot, "mdot", has_nf && flow},
+        {s.ksi_A, "ksi_A", has_nf && ((mom && vis) || ent || heat)},
         {s.stress, "stress", has_nf && mom && vis},
         {s.density, "density", has_nf && pre},
         {s.qy, "qy", has_nf && pre},
-        {s.bc_type, "bc_type", has_nb},
-        {s.bc_mdot, "bc_mdot", has_nb},
+        {s.bc_type, "bc_type", has_nb && flow},
+        {s.bc_mdot, "bc_mdot", has_nb && flow},
         {s.bc_wall, "bc_wall", has_nb && mom && vis},
         {s.bc_area, "bc_area", has_nb && mom && vis},
         {s.bc_area_vector, "bc_area_vector", has_nb && mom && vis},
@@ -841,18 +842,18 @@ const char* missing_state_field(const ocsl_assembly& q, const ocsl_flow_state& s
         {s.bc_supersonic, "bc_supersonic", has_nb && pre},
         {s.bc_qy, "bc_qy", has_nb && pre},
         {s.bc_density, "bc_density", has_nb && pre},
-        {s.bc_temperature, "bc_temperature", has_nb && (pre || ent)},
+        {s.bc_temperature, "bc_temperature", has_nb && (pre || ent || heat)},
         {s.bc_enthalpy, "bc_enthalpy", has_nb && ent},
-        {s.bc_ksi_A, "bc_ksi_A", has_nb && ent},
+        {s.bc_ksi_A, "bc_ksi_A", has_nb && (ent || heat)},
+        {s.bc_thermal, "bc_thermal", has_nb && heat},
         {s.volume, "volume", true},
         {s.delta_t, "delta_t", tr},
         {s.velocity, "velocity", mom},
         {s.velocity_last, "velocity_last", mom},
         {s.pressure_grad, "pressure_grad", mom},
-        {s.density_c, "density_c", (mom && tr) || pre || ent || (has_nb && pre)},
+        {s.density_c, "density_c", (mom && tr) || pre || ent},
         {s.density_last, "density_last", tr && (mom || pre || ent)},
-        {s.temperature, "temperature", (mom && vis) || pre},
-        {s.temperature, "temperature", ent},
+        {s.temperature, "temperature", (mom && vis) || pre || ent || heat},
         {s.pressure_corr, "pressure_corr", pre},
         {s.enthalpy, "enthalpy", ent},
         {s.enthalpy_last, "enthalpy_last", ent},
@@ -1385,7 +1386,7 @@ static int check_assembly(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_s
     if (rc) return rc;
     if (!c->has_faces) return fail(c, OCSL_BAD_ARGUMENT, "ocsl_set_faces has not been called");
     if (!q || !s) return fail(c, OCSL_BAD_ARGUMENT, "null assembly or state");
-    if (q->equation < OCSL_EQ_MOMENTUM || q->equation > OCSL_EQ_ENTHALPY)
+    if (q->equation < OCSL_EQ_MOMENTUM || q->equation > OCSL_EQ_HEAT)
         return fail(c, OCSL_BAD_ARGUMENT, "unknown equation");
     if (q->equation == OCSL_EQ_MOMENTUM && (q->dimension < 0 || q->dimension > 2))
         return fail(c, OCSL_BAD_ARGUMENT, "momentum dimension must be 0, 1 or 2");

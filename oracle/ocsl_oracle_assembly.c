@@ -1,9 +1,9 @@
 /* TEST INFRASTRUCTURE ONLY -- oracle restatement of the flow solver's
  * face-loop coefficient assembly (cflow_solver_cell_face_loops.cpp:37-446,
- * solvers_common.h:32-151), in the order the reference's loops run on one
- * thread: clear, interior faces ascending, boundary faces ascending, cells
- * ascending (cflow_solver.cpp:258-290 momentum, 319-349 pressure correction,
- * 431-460 enthalpy).  Each entry of the matrix and of b is a running sum
+ * solvers_common.h:32-151) and of the heat solver's (cheat_solver.cpp:32-65),
+ * in the order the reference's loops run on one thread: clear, interior faces
+ * ascending, boundary faces ascending, cells ascending (cflow_solver.cpp:258-290
+ * momentum, 319-349 pressure correction, 431-460 enthalpy; cheat_solver.cpp:112-136).  Each entry of the matrix and of b is a running sum
  * from 0.0 in exactly that order.
  *
  * Rounding: the reference is compiled with -ffast-math, so a product that is
@@ -112,10 +112,15 @@ void orc_assemble(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
     memset(value, 0, rp[n] * sizeof(double));
     memset(b, 0, n * sizeof(double));
     if (total_mdot) memset(total_mdot, 0, n * sizeof(double));
-    const double* u = st->velocity + (size_t)d * n;
+    const double* u = st->velocity ? st->velocity + (size_t)d * n : NULL;
     /* interior faces */
     for (int64_t f = 0; f < nf; ++f) {
         const int64_t L = left[f], R = right[f];
+        if (eq == OCSL_EQ_HEAT) { /* cheat_solver.cpp:32-37 */
+            const double D = q->thermal_diffusivity * st->ksi_A[f];
+            diffusive(&s, L, R, D);
+            continue;
+        }
         const double g = st->geo_aver[f], m = st->mdot[f];
         if (eq == OCSL_EQ_MOMENTUM) { /* :37-57 */
             convective(&s, q->blended, g, L, R, m, u[L], u[R]);
@@ -153,6 +158,14 @@ void orc_assemble(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
     /* boundary faces */
     for (int64_t k = 0; k < nb; ++k) {
         const int64_t P = bc_left[k];
+        if (eq == OCSL_EQ_HEAT) { /* cheat_solver.cpp:39-56: constant-temperature faces */
+            if (st->bc_thermal[k] == OCSL_THERMAL_CONSTANT_TEMPERATURE) {
+                const double D = q->thermal_diffusivity * st->bc_ksi_A[k];
+                addA(&s, P, P, D);
+                b[P] += D * st->bc_temperature[k];
+            }
+            continue;
+        }
         const int type = st->bc_type[k];
         const double m = st->bc_mdot[k];
         const double bv = st->bc_value ? st->bc_value[k] : 0.0;
@@ -237,6 +250,11 @@ void orc_assemble(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
                 b[i] += dum;
             }
             x0[i] = u[i];
+        } else if (eq == OCSL_EQ_HEAT) { /* cheat_solver.cpp:58-66 (global dt per cell) */
+            const double dum = vol / st->delta_t[i];
+            value[dg] += dum;
+            b[i] += st->temperature[i] * dum;
+            x0[i] = st->temperature[i];
         } else if (eq == OCSL_EQ_PRESSURE) { /* :273-296 */
             if (q->transient) {
                 const double dum = vol / st->delta_t[i];

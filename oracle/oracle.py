@@ -248,8 +248,10 @@ def _assembly_struct(eq: dict):
     for k in ("equation", "dimension", "viscous", "blended", "transient"):
         setattr(q, k, int(eq.get(k, 0)))
     for k in ("implicit_underrelaxation", "R_specific", "gamma", "prandtl"):
-        setattr(q, k, float(eq[k]))
-    q.sutherland[0], q.sutherland[1] = float(eq["sutherland"][0]), float(eq["sutherland"][1])
+        setattr(q, k, float(eq.get(k, 0.0)))
+    q.thermal_diffusivity = float(eq.get("thermal_diffusivity", 0.0))
+    su = eq.get("sutherland", (0.0, 0.0))
+    q.sutherland[0], q.sutherland[1] = float(su[0]), float(su[1])
     return q
 
 

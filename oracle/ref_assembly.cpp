@@ -17,6 +17,8 @@
 //                     no-slip side walls, pressure outlet
 //          steady     200 cells, viscous, blended, steady with implicit
 //                     under-relaxation, supersonic inlet, slip walls, outlet
+//          heat       100-cell heat conduction (cheat_solver.cpp), fixed
+//                     temperatures at both ends, adiabatic sides
 // File format: repeated [u32 name length][name][u8 kind 'd'|'i'|'u'][u64 count][data].
 #include "croot.h"
 
@@ -155,6 +157,39 @@ void record(CMatrix_solver* s, int eq)
     w.d("cell_total_mdot", col(fl.cells, [](const Fc& c) { return c.total_mdot; }));
 }
 
+// Heat conduction (cheat_solver.cpp:32-65): the equation's inputs are the
+// cell temperatures, the boundary faces' thermal kind and temperature, the
+// diffusivity and the global time step.
+void record_heat(CMatrix_solver* s)
+{
+    const auto& fvm = *root.FVM;
+    const auto& hs = *root.Heat_solver;
+    const auto& cfg = *root.configuration;
+    char name[512];
+    std::snprintf(name, sizeof name, "%s/call_%05ld.bin", g_out.c_str(), g_call);
+    Writer w(name);
+    w.i("meta", {5, 0, 0, 1});
+    w.d("fluid", {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, cfg.thermal_diffusivity, cfg.global_delta_t});
+    w.i("face_left", coli(fvm.faces, [](const CFVM::CFVM_face& f) { return f.left_cell_index; }));
+    w.i("face_right", coli(fvm.faces, [](const CFVM::CFVM_face& f) { return f.right_cell_index; }));
+    w.d("face_ksi_A", col(fvm.faces, [](const CFVM::CFVM_face& f) { return f.diffusion_ksi_A; }));
+    w.i("bc_left", coli(fvm.BC_faces, [](const CFVM::CFVM_BC_face& f) { return f.left_cell_index; }));
+    w.d("bc_ksi_A", col(fvm.BC_faces, [](const CFVM::CFVM_BC_face& f) { return f.diffusion_ksi_A; }));
+    w.d("cell_volume", col(fvm.cells, [](const CFVM::CFVM_cell& c) { return c.volume; }));
+    using Hc = CHeat_solver::CHeat_cell;
+    using Hb = CHeat_solver::CHeat_BC_face;
+    w.i("bc_thermal", coli(hs.BC_faces, [](const Hb& f) { return (int)f.ethermal_BC_type; }));
+    w.d("bc_temperature", col(hs.BC_faces, [](const Hb& f) { return f.Temperature; }));
+    w.d("cell_temperature", col(hs.cells, [](const Hc& c) { return c.Temperature; }));
+    std::vector<uint64_t> rp(s->matrix.row_ptr.begin(), s->matrix.row_ptr.end());
+    std::vector<uint64_t> ci(s->matrix.column_index.begin(), s->matrix.column_index.end());
+    w.u("row_ptr", rp);
+    w.u("column_index", ci);
+    w.d("value", s->matrix.value);
+    w.d("b", s->b_vector.value);
+    w.d("x0", s->x_vector.value);
+}
+
 void base_1d(Cconfiguration& c, int cells)
 {
     c.openmp_number_of_threads = 1;
@@ -172,8 +207,14 @@ void base_1d(Cconfiguration& c, int cells)
 
 extern "C" void __wrap__ZN14CMatrix_solver5solveEv(CMatrix_solver* self)
 {
+    const bool heat = root.configuration->eproblem_type == enums::Eproblem_type::Heat_conduction;
     const int eq = int(g_call % 5);  // x, y, z momentum, p', enthalpy (cflow_solver.cpp)
-    if (g_call >= g_first && g_call < g_first + g_count) record(self, eq);
+    if (g_call >= g_first && g_call < g_first + g_count) {
+        if (heat)
+            record_heat(self);
+        else
+            record(self, eq);
+    }
     __real__ZN14CMatrix_solver5solveEv(self);
     ++g_call;
 }
@@ -243,6 +284,19 @@ int main(int argc, char** argv)
         c.boundary_conditions[2].Pressure = 1.0e5;
         c.max_iteration = steady ? 4 : 2;
         c.max_inner_iteration = steady ? 1 : 3;
+    } else if (kase == "heat") {
+        base_1d(c, 100);
+        c.eproblem_type = enums::Eproblem_type::Heat_conduction;
+        c.global_delta_t = 50.0;
+        c.thermal_diffusivity = 2.0e-3;
+        ic.Temperature = 300.0;
+        c.boundary_conditions[0].ethermal_BC_type = enums::Ethermal_BC_type::constant_temperature;
+        c.boundary_conditions[0].Temperature = 250.0;
+        c.boundary_conditions[1].ethermal_BC_type = enums::Ethermal_BC_type::adiabatic;
+        c.boundary_conditions[2].ethermal_BC_type = enums::Ethermal_BC_type::constant_temperature;
+        c.boundary_conditions[2].Temperature = 450.0;
+        c.max_iteration = 6;
+        c.max_inner_iteration = 1;
     } else {
         std::fprintf(stderr, "unknown case %s\n", kase.c_str());
         return 1;

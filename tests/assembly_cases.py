@@ -6,8 +6,8 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("shocktube", "channel", "steady")
-EQUATIONS = ("momentum_x", "momentum_y", "momentum_z", "pressure", "enthalpy")
+CASES = ("shocktube", "channel", "steady", "heat")
+EQUATIONS = ("momentum_x", "momentum_y", "momentum_z", "pressure", "enthalpy", "heat")
 
 # state field of the C ABI <- recorded array name
 STATE_MAP = {
@@ -23,7 +23,7 @@ STATE_MAP = {
     "density_last": "cell_density_last", "pressure": "cell_pressure",
     "pressure_last": "cell_pressure_last", "pressure_corr": "cell_pressure_corr",
     "temperature": "cell_temperature", "enthalpy": "cell_enthalpy",
-    "enthalpy_last": "cell_enthalpy_last",
+    "enthalpy_last": "cell_enthalpy_last", "bc_thermal": "bc_thermal",
 }
 
 
@@ -35,17 +35,24 @@ class Call:
         meta, fluid = g("meta"), g("fluid")
         eq = int(meta[0])
         self.name = EQUATIONS[eq]
-        self.eq = {
-            "equation": 0 if eq < 3 else (1 if eq == 3 else 2),
-            "dimension": eq if eq < 3 else 0,
-            "viscous": int(meta[1]), "blended": int(meta[2]), "transient": int(meta[3]),
-            "R_specific": fluid[0], "gamma": fluid[1], "sutherland": (fluid[2], fluid[3]),
-            "prandtl": fluid[4], "implicit_underrelaxation": fluid[5],
-        }
-        self.state = {k_: g(v) for k_, v in STATE_MAP.items()}
-        self.value, self.b, self.x0 = g("value"), g("b"), g("x0")
-        self.ap_vec, self.total_mdot = g("cell_ap_vec"), g("cell_total_mdot")
         self.n = self.row_ptr.size - 1
+        has = lambda key: key in z.files or f"c{k}_{key}" in z.files
+        if self.name == "heat":
+            self.eq = {"equation": 3, "transient": 1, "thermal_diffusivity": fluid[6]}
+            self.state = {k_: g(v) for k_, v in STATE_MAP.items() if has(v)}
+            self.state["delta_t"] = np.full(self.n, fluid[7])
+            self.ap_vec = self.total_mdot = None
+        else:
+            self.eq = {
+                "equation": 0 if eq < 3 else (1 if eq == 3 else 2),
+                "dimension": eq if eq < 3 else 0,
+                "viscous": int(meta[1]), "blended": int(meta[2]), "transient": int(meta[3]),
+                "R_specific": fluid[0], "gamma": fluid[1], "sutherland": (fluid[2], fluid[3]),
+                "prandtl": fluid[4], "implicit_underrelaxation": fluid[5],
+            }
+            self.state = {k_: g(v) for k_, v in STATE_MAP.items()}
+            self.ap_vec, self.total_mdot = g("cell_ap_vec"), g("cell_total_mdot")
+        self.value, self.b, self.x0 = g("value"), g("b"), g("x0")
 
     @property
     def ap_expected(self):

@@ -26,8 +26,10 @@ then writes:
   (inviscid, blended, transient, slip walls), a 200-cell viscous channel
   (upwind, transient, velocity inlet, no-slip walls, pressure outlet) and a
   200-cell steady case (viscous, blended, implicit under-relaxation,
-  supersonic inlet, slip walls, outlet).  Mesh arrays are stored once per
-  case, state and outputs per call with the prefix c<k>_.
+  supersonic inlet, slip walls, outlet), and three time steps of a 100-cell
+  heat-conduction run (fixed temperatures at the ends, adiabatic sides).
+  Mesh arrays are stored once per case, state and outputs per call with the
+  prefix c<k>_.
 
 All reference calls use one OpenMP thread (deterministic reduction order).
 """
@@ -143,8 +145,9 @@ def make_small(ref, out):
     np.savez_compressed(out, **arrays)
 
 
-# (case, first recorded solve call): the last inner iteration of each run.
-ASSEMBLY_CASES = [("shocktube", 25), ("channel", 25), ("steady", 15)]
+# (case, first recorded solve call, calls): the last inner iteration of each
+# flow run (5 equations), three time steps of the heat run.
+ASSEMBLY_CASES = [("shocktube", 25, 5), ("channel", 25, 5), ("steady", 15, 5), ("heat", 3, 3)]
 MESH_KEYS = ("face_left", "face_right", "face_geo_aver", "face_ksi_A", "bc_left", "bc_area",
              "bc_area_vector", "bc_perp_dist", "bc_ksi_A", "cell_volume", "row_ptr",
              "column_index", "bc_type", "bc_wall", "bc_thermal")
@@ -166,13 +169,13 @@ def read_named_arrays(path):
 
 def make_assembly(out_dir):
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_assembly")
-    for case, first in ASSEMBLY_CASES:
+    for case, first, count in ASSEMBLY_CASES:
         arrays = {}
         with tempfile.TemporaryDirectory() as d:
-            subprocess.run([exe, d, case, str(first), "5"], cwd=d, check=True,
+            subprocess.run([exe, d, case, str(first), str(count)], cwd=d, check=True,
                            stdout=subprocess.DEVNULL)
             calls = sorted(f for f in os.listdir(d) if f.startswith("call_"))
-            assert len(calls) == 5, calls
+            assert len(calls) == count, calls
             for k, f in enumerate(calls):
                 z = read_named_arrays(os.path.join(d, f))
                 for key, v in z.items():
@@ -182,7 +185,7 @@ def make_assembly(out_dir):
                         arrays[key] = v
                     else:
                         arrays[f"c{k}_{key}"] = v
-        arrays["count"] = np.array(5)
+        arrays["count"] = np.array(count)
         np.savez_compressed(os.path.join(out_dir, f"assembly_{case}.npz"), **arrays)
 
 
