@@ -222,17 +222,13 @@ def run_ours(args):
     import opencslsolver_gb300 as ocsl
     from opencslsolver_gb300 import workloads as W
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
+    from opencslsolver_gb300.replicas import ReplicaGroup
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    group = ReplicaGroup("nccl", device=dev)
+    world, rank = group.world, group.rank
 
     t_gen = time.perf_counter()
     s = W.hex_pprime(args.size, peclet=10.0)
@@ -256,16 +252,8 @@ def run_ours(args):
             raise RuntimeError(f"solve failed: {r}")
         return r
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(v):
-        if dist is None:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier = group.barrier
+    max_over_ranks = group.max_over_ranks
 
     def timed(method, steps, profile=False):
         for _ in range(args.warmup):
@@ -296,7 +284,7 @@ def run_ours(args):
     clocks.start()
     ms_ir, its_ir, prof_ir = timed(ocsl.ILU_BICGSTAB_IR32, args.steps, profile=True)
     clk = clocks.stop()
-    value = world * 1000.0 / ms_ir
+    value = group.job_rate(ms_ir)
 
     # ---- plain FP64 GPU solve, same system and tolerance
     ms_64, its_64, prof_64 = timed(ocsl.ILU_BICGSTAB, max(3, args.steps // 2), profile=True)
@@ -381,8 +369,7 @@ def run_ours(args):
         }
         print(json.dumps(line))
     ctx.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    group.close()
     return 0
 
 
