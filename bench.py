@@ -136,17 +136,19 @@ def algorithmic_bytes(n, nnz_real, nnz_l, nnz_u, structured):
     """Bytes each kernel must move per launch, by category.
 
     SpMV (int32 CSR): values and columns once, row pointers, x once, y, and
-    the one vector its fused dot reads.  Level-scheduled sweeps (CSR): strict
-    lower / upper values and columns, row pointers, diagonal positions (and
-    the reciprocal diagonal backward), rhs, result.  Structured sweeps read
-    no indices: the strict lower / upper values, rhs, result (and the
-    reciprocal diagonal backward).
+    the one vector its fused dot reads; on a box pattern (stencil records) no
+    index at all: values, x, y and the dot's vector.  Level-scheduled sweeps
+    (CSR): strict lower / upper values and columns, row pointers, diagonal
+    positions (and the reciprocal diagonal backward), rhs, result.
+    Structured sweeps read no indices: the strict lower / upper values, rhs,
+    result (and the reciprocal diagonal backward).
     """
     out = {
         "spmv_f32": 8 * nnz_real + 4 * (n + 1) + 12 * n,
         "spmv_f64": 12 * nnz_real + 4 * (n + 1) + 24 * n,
     }
     if structured:
+        out.update({"spmv_f32": 4 * nnz_real + 12 * n, "spmv_f64": 8 * nnz_real + 24 * n})
         out.update({"fw_sweep_f32": 4 * nnz_l + 8 * n, "bw_sweep_f32": 4 * nnz_u + 12 * n,
                     "fw_sweep_f64": 8 * nnz_l + 16 * n, "bw_sweep_f64": 8 * nnz_u + 24 * n})
     else:

@@ -356,6 +356,97 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
     }
 }
 
+// SpMV on the packed stencil records of a natural-order 7-point box pattern
+// (the layout of the structured sweeps: [2][n][4] = (z-, y-, x-, 0) and
+// (x+, y+, z+, diagonal) per row, absent neighbours exact 0).  Same tile and
+// row assignment, same fused dots and epilogues as spmv_kernel, and the same
+// fma chain in the row's CSR order (z-, y-, x-, diagonal, x+, y+, z+): an
+// absent neighbour multiplies an exact 0 by a finite x from a clamped address
+// and adds nothing, so y equals the CSR kernel's bit for bit while no column
+// index is read and every load is coalesced (32 or 64 B of records per row,
+// x at seven shifted, contiguous offsets).
+template <typename T>
+struct BoxSpmvParams {
+    int n, sy, sz;  // rows, y and z strides (nx, nx*ny)
+    const T* rec;   // [2][n][4]
+    const T* x;
+    T* y;
+    const T* z;
+    T* y_copy;
+    const T* w;
+    T a;
+    ReduceState R;
+    Scalars* sc;
+    int epi, it, maxit;
+};
+
+template <typename T>
+struct Rec4;
+template <>
+struct Rec4<float> {
+    using V = float4;
+};
+template <>
+struct Rec4<double> {
+    using V = double4;
+};
+
+template <typename T, int MODE, int DOTS>
+__global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
+{
+    if (p.sc && p.sc->done) return;
+    constexpr int ND = DotCount<DOTS>::value;
+    using V = typename Rec4<T>::V;
+    __shared__ double s_red[kMaxDots * 8];
+    __shared__ int s_last;
+    const int tile = blockIdx.x;
+    const int n = p.n;
+    const V* lo = reinterpret_cast<const V*>(p.rec);
+    const V* hi = lo + n;
+    DotAcc<T> acc[ND > 0 ? ND : 1];
+#pragma unroll 2
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
+        if (row >= n) continue;
+        const V l = lo[row], h = hi[row];
+        const T* x = p.x;
+        const T xzm = __ldg(x + max(row - p.sz, 0)), xym = __ldg(x + max(row - p.sy, 0));
+        const T xxm = __ldg(x + max(row - 1, 0)), xc = __ldg(x + row);
+        const T xxp = __ldg(x + min(row + 1, n - 1)), xyp = __ldg(x + min(row + p.sy, n - 1));
+        const T xzp = __ldg(x + min(row + p.sz, n - 1));
+        T dum = fma_t(l.x, xzm, T(0));
+        dum = fma_t(l.y, xym, dum);
+        dum = fma_t(l.z, xxm, dum);
+        dum = fma_t(h.w, xc, dum);
+        dum = fma_t(h.x, xxp, dum);
+        dum = fma_t(h.y, xyp, dum);
+        dum = fma_t(h.z, xzp, dum);
+        T y, zv = T(0);
+        if constexpr (MODE == 0) {
+            y = dum;
+        } else if constexpr (MODE == 1) {
+            zv = p.z[row];
+            y = zv - dum;
+        } else {
+            zv = p.z[row];
+            y = fma_t(p.a, dum, zv);
+        }
+        p.y[row] = y;
+        if (MODE == 1 && p.y_copy) p.y_copy[row] = y;
+        int k = 0;
+        if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
+        if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
+        if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(p.w[row], y);
+        (void)k;
+    }
+    if constexpr (ND > 0) {
+        double v[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) v[k] = acc[k].value();
+        finish_reduction<ND>(v, tile, gridDim.x, p.R, p.sc, p.epi, p.it, p.maxit, s_red, &s_last);
+    }
+}
+
 template <int OP>
 struct OpDots {
     static constexpr int value =
@@ -533,6 +624,27 @@ void spmv_dots(cudaStream_t st, const SpmvParams<T>& p, int dots)
     }
 }
 
+template <typename T, int MODE, int DOTS>
+void box_spmv_dispatch(cudaStream_t st, const BoxSpmvParams<T>& p)
+{
+    const int nt = ntiles_of(p.n);
+    if (nt == 0) return;
+    box_spmv_kernel<T, MODE, DOTS><<<nt, kThreads, 0, st>>>(p);
+}
+
+template <typename T, int MODE>
+void box_spmv_dots(cudaStream_t st, const BoxSpmvParams<T>& p, int dots)
+{
+    switch (dots) {
+    case 0: box_spmv_dispatch<T, MODE, 0>(st, p); break;
+    case DOT_YY: box_spmv_dispatch<T, MODE, DOT_YY>(st, p); break;
+    case DOT_YY | DOT_ZZ: box_spmv_dispatch<T, MODE, DOT_YY | DOT_ZZ>(st, p); break;
+    case DOT_WY: box_spmv_dispatch<T, MODE, DOT_WY>(st, p); break;
+    case DOT_YY | DOT_WY: box_spmv_dispatch<T, MODE, DOT_YY | DOT_WY>(st, p); break;
+    default: break;
+    }
+}
+
 template <typename T, int OP>
 void vec_dispatch(cudaStream_t st, const VecParams& P)
 {
@@ -568,6 +680,34 @@ void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x,
     case 0: spmv_dots<T, 0>(st, p, dots); break;
     case 1: spmv_dots<T, 1>(st, p, dots); break;
     default: spmv_dots<T, 2>(st, p, dots); break;
+    }
+}
+
+template <typename T>
+void launch_box_spmv(cudaStream_t st, int n, const int* dims, const T* rec, const T* x, T* y,
+                     int mode, double a_const, const T* z, T* y_copy, const T* w, int dots,
+                     const ReduceState& R, Scalars* sc, int epi, int it, int maxit)
+{
+    BoxSpmvParams<T> p;
+    p.n = n;
+    p.sy = dims[0];
+    p.sz = dims[0] * dims[1];
+    p.rec = rec;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.y_copy = y_copy;
+    p.w = w;
+    p.a = (T)a_const;
+    p.R = R;
+    p.sc = sc;
+    p.epi = epi;
+    p.it = it;
+    p.maxit = maxit;
+    switch (mode) {
+    case 0: box_spmv_dots<T, 0>(st, p, dots); break;
+    case 1: box_spmv_dots<T, 1>(st, p, dots); break;
+    default: box_spmv_dots<T, 2>(st, p, dots); break;
     }
 }
 
@@ -623,6 +763,13 @@ template void launch_spmv<double>(cudaStream_t, const DevPattern&, const double*
 template void launch_spmv<float>(cudaStream_t, const DevPattern&, const float*, const float*,
                                  float*, int, const double*, double, const float*, float*,
                                  const float*, int, const ReduceState&, Scalars*, int, int, int);
+template void launch_box_spmv<double>(cudaStream_t, int, const int*, const double*,
+                                      const double*, double*, int, double, const double*,
+                                      double*, const double*, int, const ReduceState&, Scalars*,
+                                      int, int, int);
+template void launch_box_spmv<float>(cudaStream_t, int, const int*, const float*, const float*,
+                                     float*, int, double, const float*, float*, const float*, int,
+                                     const ReduceState&, Scalars*, int, int, int);
 template void launch_vec<double>(cudaStream_t, int, int, const VecPtrs&, const ReduceState&,
                                  Scalars*, const Scalars*, int, int, int);
 template void launch_vec<float>(cudaStream_t, int, int, const VecPtrs&, const ReduceState&,

@@ -124,6 +124,13 @@ void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x,
                  const T* w, int dots, const ReduceState& R, Scalars* sc, int epi, int it,
                  int maxit);
 
+// SpMV on packed stencil records ([2][n][4], the structured sweeps' layout, of A
+// itself) for natural-order 7-point box patterns; dims = (nx, ny, nz).
+template <typename T>
+void launch_box_spmv(cudaStream_t st, int n, const int* dims, const T* rec, const T* x, T* y,
+                     int mode, double a_const, const T* z, T* y_copy, const T* w, int dots,
+                     const ReduceState& R, Scalars* sc, int epi, int it, int maxit);
+
 // Vector kernels: the op decides which pointers it uses.
 enum VecOp : int {
     V_RB_P = 0,   // dum = fma(-w, v, p); p = fma(w, dum, r)

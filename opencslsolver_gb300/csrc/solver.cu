@@ -87,6 +87,8 @@ struct ocsl_ctx {
     float* v32[NVEC32] = {};
     double* d_soa64 = nullptr;  // stencil-SoA factor copies (7-point box patterns)
     float* d_soa32 = nullptr;
+    double* d_recA64 = nullptr;  // stencil records of A itself, for the box SpMV
+    float* d_recA32 = nullptr;
 
     ReduceState R{};
     Scalars* d_sc = nullptr;  // [0] main / outer, [1] inner, [2] utility
@@ -147,7 +149,9 @@ void ocsl_ctx::free_pattern()
     double** d64[] = {&d_A, &d_b, &d_x, &d_Ma, &d_Mb, &d_dinv};
     for (auto pp : d64) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     for (auto& v : v64) { if (v) cudaFree(v); v = nullptr; }
-    float** d32[] = {&d_A32, &d_M32, &d_dinv32, &d_soa32};
+    float** d32[] = {&d_A32, &d_M32, &d_dinv32, &d_soa32, &d_recA32};
+    if (d_recA64) cudaFree(d_recA64);
+    d_recA64 = nullptr;
     if (d_soa64) cudaFree(d_soa64);
     d_soa64 = nullptr;
     for (auto pp : d32) { if (*pp) cudaFree(*pp); *pp = nullptr; }
@@ -308,6 +312,11 @@ struct Solve {
     const double* soa64 = nullptr;  // stencil-SoA copy of the current factor
     const float* soa32 = nullptr;
     bool reuse = false;  // the factor of the previous solve on the same values is still valid
+    // SpMV through the stencil records of A (box patterns), for the matrix
+    // the records were built from
+    const double* matA64 = nullptr;
+    const double* recA64 = nullptr;
+    const float* recA32 = nullptr;
 
     Scalars* sc(int k) const { return c->d_sc + k; }
 
@@ -339,8 +348,39 @@ struct Solve {
               int dots, int k, int epi, int it = 0, int maxit = 0)
     {
         ProfScope ps(c, st, is_f64<TT>() ? PC_SPMV64 : PC_SPMV32);
-        launch_spmv<TT>(st, P, val, x, y, mode, nullptr, 0.0, z, ycopy, w, dots, c->R,
-                        k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+        const TT* rec = nullptr;
+        if constexpr (sizeof(TT) == 8) {
+            if (recA64 && val == matA64) rec = recA64;
+        } else {
+            if (recA32 && val == c->d_A32) rec = recA32;
+        }
+        if (rec)
+            launch_box_spmv<TT>(st, P.n, c->hp.box.dim, rec, x, y, mode, 0.0, z, ycopy, w, dots,
+                                c->R, k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+        else
+            launch_spmv<TT>(st, P, val, x, y, mode, nullptr, 0.0, z, ycopy, w, dots, c->R,
+                            k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+    }
+    // Stencil records of A for the box SpMV (7-point box patterns); built
+    // from the FP64 values, so the FP32 records equal (float)A like A32.
+    void prepare_spmv(const double* A, bool want64, bool want32)
+    {
+        matA64 = A;
+        recA64 = nullptr;
+        recA32 = nullptr;
+        if (!c->hp.box.ok) return;
+        if (want64 && !c->d_recA64) c->d_recA64 = dalloc<double>(8 * (size_t)P.n);
+        if (want32 && !c->d_recA32) c->d_recA32 = dalloc<float>(8 * (size_t)P.n);
+        const bool have = reuse && c->fac_M;  // same values as the previous solve
+        ProfScope ps(c, st, PC_ILU);
+        if (want64) {
+            if (!have) launch_box_to_soa<double>(st, c->hp.box.dim, P.n, P.rp, A, c->d_recA64, 0);
+            recA64 = c->d_recA64;
+        }
+        if (want32) {
+            if (!have) launch_box_to_soa<float>(st, c->hp.box.dim, P.n, P.rp, A, c->d_recA32, 0);
+            recA32 = c->d_recA32;
+        }
     }
     template <typename TT>
     void vec(int op, std::initializer_list<const void*> ptrs, int k, int epi, int it = 0,
@@ -473,6 +513,7 @@ void run_cg_ref(Solve& s, const double* A, const double* b, double* x)
 {
     double** v = s.c->v64;
     s.reset_scalars(0, 0.0);
+    s.prepare_spmv(A, true, false);
     // r = b - A x (:652), p = r (:655), rr = <r,r>
     s.spmv<double>(A, x, v[R], 1, b, v[P], nullptr, DOT_YY, 0, EP_RC_INIT);
     double* r = v[R];
@@ -499,6 +540,7 @@ void run_bicgstab_ref(Solve& s, const double* A, const double* b, double* x, int
     CK(cudaMemsetAsync(v[P], 0, bytes, s.st));  // Cvector(n) starts at 0 (:690-700)
     CK(cudaMemsetAsync(v[V], 0, bytes, s.st));
     const double* M = s.factored(A, sweeps, false, false, 0, true, false, false);  // :702-704
+    s.prepare_spmv(A, true, false);
     // r = b - A x (:708), r0 = r (:710), iteration 0's rhon and res
     s.spmv<double>(A, x, v[R], 1, b, v[R0], nullptr, DOT_YY | DOT_ZZ, 0, EP_RB_INIT);
     for (int it = 0; it < kRefBicgIters; ++it) {
@@ -623,6 +665,7 @@ TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x
 {
     double** v = s.c->v64;
     const double* M = s.factored(A, o.ilu_sweeps, true, false, -1, true, true, false);
+    s.prepare_spmv(A, true, false);
     return run_restarted(
         s, A, b, x, o, [&] { s.vec<double>(V_COPY2, {v[RH], v[P], v[R]}, 0, EP_STORE); },
         [&](int) {
@@ -636,6 +679,7 @@ TolResult run_pcg_tol(Solve& s, const double* A, const double* b, double* x, con
 {
     double** v = s.c->v64;
     s.factored(A, 0, true, false, -1, false, false, false);  // Jacobi: dinv = 1 / A_ii
+    s.prepare_spmv(A, true, false);
     return run_restarted(
         s, A, b, x, o,
         [&] { s.vec<double>(V_PC_INIT, {v[Z], v[P], v[R], s.c->d_dinv}, 0, EP_PC_INIT); },
@@ -660,6 +704,7 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
     TolResult res;
     const double tol2 = o.tol * o.tol;
     const double* M = s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+    s.prepare_spmv(A, true, true);
     int total = 0;
     s.reset_scalars(0, tol2);
     for (int outer = 0;; ++outer) {
