@@ -106,6 +106,15 @@ int ocsl_set_pattern(ocsl_ctx* ctx, size_t n, const size_t* row_ptr, const size_
 int ocsl_check_pattern(size_t n, const size_t* row_ptr, const size_t* column_index,
                        int64_t* nnz_real, int32_t* fw_levels, int32_t* bw_levels,
                        int32_t* box_dims, char* err, size_t err_len);
+/* Build the reference's pattern from the mesh's face connectivity in
+ * O(n + faces), host-only: row i = i and its face neighbours ascending, plus
+ * one phantom column (size_t)-1 when cell i has a boundary face -- the matrix
+ * structure CFVM::define_matrix_structure (cfvm.cpp:74-98) builds with
+ * quadratic insert_element calls.  Call with row_ptr = NULL to get *nnz, then
+ * with row_ptr[n+1] and column_index[*nnz]. */
+int ocsl_build_pattern(size_t n, int64_t n_faces, const int32_t* left, const int32_t* right,
+                       int64_t n_bc, const int32_t* bc_left, size_t* row_ptr,
+                       size_t* column_index, size_t* nnz);
 /* Pattern facts: n, stored nnz (with phantoms), real nnz, forward and
  * backward level counts. */
 int ocsl_pattern_info(const ocsl_ctx* ctx, int64_t* n, int64_t* nnz, int64_t* nnz_real,

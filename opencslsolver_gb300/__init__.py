@@ -27,7 +27,7 @@ from ._abi import (BICGSTAB_REF, CG_REF, ILU_BICGSTAB, ILU_BICGSTAB_IR32, METHOD
 
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
-__all__ = ["Context", "Batch", "CMatrix_solver", "check_pattern", "LibraryMissing", "OcslError",
+__all__ = ["Context", "Batch", "CMatrix_solver", "build_pattern", "check_pattern", "LibraryMissing", "OcslError",
            "CG_REF", "BICGSTAB_REF", "PCG", "ILU_BICGSTAB", "ILU_BICGSTAB_IR32", "METHODS",
            "PHANTOM"]
 
@@ -306,6 +306,28 @@ class Context:
     def backsub_device(self, M, y, x):
         self._check(self._L.ocsl_backsub_device(self._h, _dptr(M), _dptr(y), _dptr(x)),
                     "backsub")
+
+
+def build_pattern(n, left, right, bc_left):
+    """The reference's CSR pattern (row_ptr, column_index as uint64, phantom
+    2**64-1 on boundary cells) from face connectivity, in O(n + faces)
+    (ocsl_build_pattern; replaces cfvm.cpp:74-98).  Host only."""
+    L = _abi.lib()
+    l = np.ascontiguousarray(left, dtype=np.int32)
+    r = np.ascontiguousarray(right, dtype=np.int32)
+    b = np.ascontiguousarray(bc_left, dtype=np.int32)
+    nnz = C.c_size_t(0)
+    st = L.ocsl_build_pattern(int(n), l.size, _ptr(l), _ptr(r), b.size, _ptr(b), None, None,
+                              C.byref(nnz))
+    if st != 0:
+        raise OcslError(st, "build_pattern: bad face connectivity")
+    rp = np.zeros(int(n) + 1, dtype=np.uint64)
+    col = np.zeros(nnz.value, dtype=np.uint64)
+    st = L.ocsl_build_pattern(int(n), l.size, _ptr(l), _ptr(r), b.size, _ptr(b), _ptr(rp),
+                              _ptr(col), C.byref(nnz))
+    if st != 0:
+        raise OcslError(st, "build_pattern")
+    return rp, col
 
 
 class Batch:

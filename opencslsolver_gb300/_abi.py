@@ -112,6 +112,8 @@ _PROTOS = {
     "ocsl_check_pattern": (C.c_int, [_SZ, _P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_char_p,
                                      _SZ]),
+    "ocsl_build_pattern": (C.c_int, [_SZ, C.c_int64, _P, _P, C.c_int64, _P, _P, _P,
+                                     C.POINTER(_SZ)]),
     "ocsl_pattern_info": (C.c_int, [_CTX, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_int32)]),

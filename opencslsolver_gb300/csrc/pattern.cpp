@@ -245,4 +245,46 @@ bool build_face_tables(int n, const std::vector<int>& rp, const std::vector<int>
     return true;
 }
 
+bool build_pattern_from_faces(size_t n, long long nf, const int32_t* left, const int32_t* right,
+                              long long nb, const int32_t* bc_left, std::vector<size_t>& row_ptr,
+                              std::vector<size_t>& column_index, std::string& err)
+{
+    if (n >= (size_t)INT_MAX) return fail(err, "n = %lld exceeds the int32 limit", (long long)n);
+    const long long N = (long long)n;
+    std::vector<int> deg(n + 1, 0);
+    std::vector<char> boundary(n, 0);
+    for (long long f = 0; f < nf; ++f) {
+        if (left[f] < 0 || left[f] >= N || right[f] < 0 || right[f] >= N)
+            return fail(err, "interior face %lld names a cell out of range", f);
+        ++deg[left[f] + 1];
+        ++deg[right[f] + 1];
+    }
+    for (long long g = 0; g < nb; ++g) {
+        if (bc_left[g] < 0 || bc_left[g] >= N)
+            return fail(err, "boundary face %lld names a cell out of range", g);
+        boundary[bc_left[g]] = 1;
+    }
+    for (size_t i = 0; i < n; ++i) deg[i + 1] += deg[i];
+    std::vector<int> nbr(deg[n]);
+    std::vector<int> next(deg.begin(), deg.end() - 1);
+    for (long long f = 0; f < nf; ++f) {
+        nbr[next[left[f]]++] = right[f];
+        nbr[next[right[f]]++] = left[f];
+    }
+    row_ptr.assign(n + 1, 0);
+    column_index.clear();
+    column_index.reserve((size_t)deg[n] + 2 * n);
+    std::vector<int> cols;
+    for (size_t i = 0; i < n; ++i) {
+        cols.assign(nbr.begin() + deg[i], nbr.begin() + deg[i + 1]);
+        cols.push_back((int)i);
+        std::sort(cols.begin(), cols.end());
+        cols.erase(std::unique(cols.begin(), cols.end()), cols.end());  // repeated pairs merge
+        for (int c : cols) column_index.push_back((size_t)c);
+        if (boundary[i]) column_index.push_back(~size_t(0));  // one phantom per boundary cell
+        row_ptr[i + 1] = column_index.size();
+    }
+    return true;
+}
+
 }  // namespace ocsl

@@ -51,4 +51,14 @@ bool build_face_tables(int n, const std::vector<int>& rp, const std::vector<int>
                        long long nf, const int32_t* left, const int32_t* right, long long nb,
                        const int32_t* bc_left, FaceTables& ft, std::string& err);
 
+// The reference's CSR pattern built from the mesh's face connectivity in
+// O(n + faces): row i holds i, its face neighbours in ascending order, and one
+// phantom column (SIZE_MAX) when the cell has a boundary face -- what
+// CFVM::define_matrix_structure (cfvm.cpp:74-98) builds with repeated
+// insert_element calls (cmatrix_solver.cpp:57-103, quadratic).  Returns false
+// with a message on a face naming a cell out of range.
+bool build_pattern_from_faces(size_t n, long long nf, const int32_t* left, const int32_t* right,
+                              long long nb, const int32_t* bc_left, std::vector<size_t>& row_ptr,
+                              std::vector<size_t>& column_index, std::string& err);
+
 }  // namespace ocsl

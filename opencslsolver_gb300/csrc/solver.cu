@@ -1098,6 +1098,26 @@ int ocsl_check_pattern(size_t n, const size_t* rp, const size_t* col, int64_t* n
     return OCSL_OK;
 }
 
+int ocsl_build_pattern(size_t n, int64_t n_faces, const int32_t* left, const int32_t* right,
+                       int64_t n_bc, const int32_t* bc_left, size_t* row_ptr,
+                       size_t* column_index, size_t* nnz)
+{
+    if (!nnz || (n_faces > 0 && (!left || !right)) || (n_bc > 0 && !bc_left) || n_faces < 0 ||
+        n_bc < 0)
+        return OCSL_BAD_ARGUMENT;
+    std::vector<size_t> rp, col;
+    std::string err;
+    if (!build_pattern_from_faces(n, n_faces, left, right, n_bc, bc_left, rp, col, err))
+        return OCSL_BAD_ARGUMENT;
+    const size_t have = *nnz;
+    *nnz = col.size();
+    if (!row_ptr) return OCSL_OK;
+    if (!column_index || have < col.size()) return OCSL_BAD_ARGUMENT;
+    std::memcpy(row_ptr, rp.data(), rp.size() * sizeof(size_t));
+    if (!col.empty()) std::memcpy(column_index, col.data(), col.size() * sizeof(size_t));
+    return OCSL_OK;
+}
+
 int ocsl_pattern_info(const ocsl_ctx* c, int64_t* n, int64_t* nnz, int64_t* nnz_real,
                       int32_t* fw_levels, int32_t* bw_levels)
 {

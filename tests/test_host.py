@@ -180,3 +180,28 @@ def test_box_detection():
     rp2[63:] -= 1
     st, info = ocsl.check_pattern(rp2, col2)
     assert st == 0 and info["box"] == (0, 0, 0)
+
+
+def test_build_pattern_matches_reference_patterns(lib_built):
+    """ocsl_build_pattern (O(n + faces)) reproduces the matrix structure the
+    reference builds with insert_element (cfvm.cpp:74-98) on every recorded
+    mesh: 1000-cell shock tube, 200-cell channel and steady cases, heat."""
+    import assembly_cases as AC
+    import opencslsolver_gb300 as ocsl
+
+    for case in AC.CASES:
+        c = AC.load(case)[0]
+        rp, col = ocsl.build_pattern(c.n, c.left, c.right, c.bc_left)
+        assert np.array_equal(rp, c.row_ptr) and np.array_equal(col, c.column_index), case
+
+
+def test_build_pattern_hex_box_and_errors(lib_built):
+    import opencslsolver_gb300 as ocsl
+
+    f = W.hex_flow_state(9, 7, 5)
+    rp, col = ocsl.build_pattern(f.n, f.left, f.right, f.bc_left)
+    assert np.array_equal(rp, f.row_ptr) and np.array_equal(col, f.column_index)
+    with pytest.raises(ocsl.OcslError):
+        ocsl.build_pattern(f.n, f.left, np.full_like(f.right, f.n), f.bc_left)
+    rp, col = ocsl.build_pattern(4, [], [], [])  # isolated cells: diagonal only
+    assert rp.tolist() == [0, 1, 2, 3, 4] and col.tolist() == [0, 1, 2, 3]
