@@ -241,6 +241,9 @@ def run_ours(args):
     t_pat = time.perf_counter()
     ctx.set_pattern(s.row_ptr, s.column_index)
     t_pat = time.perf_counter() - t_pat
+    # a created stream (not the legacy default one), so the library can replay
+    # its iteration batches from CUDA graphs; torch works on the same stream
+    torch.cuda.set_stream(torch.cuda.Stream(device=dev))
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     A = torch.from_numpy(s.value).to(dev)

@@ -342,6 +342,12 @@ int ocsl_dot_noalloc(size_t n, const double* d_x, const double* d_y, double* d_r
 /* Message of the last failed ocsl_dot_noalloc on this thread. */
 const char* ocsl_noalloc_last_error(void);
 
+/* Tolerance-mode solves replay each batch of Krylov iterations after the
+ * first from a CUDA graph captured on the context's stream (not on the legacy
+ * default stream, not while profiling).  enable = 0 launches every kernel
+ * directly; results are identical either way. */
+int ocsl_set_graphs(ocsl_ctx* ctx, int enable);
+
 /* Kernel timing.  While enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream and accounted to a category:
  *   0 spmv_f64  1 spmv_f32  2 fw_sweep_f64  3 bw_sweep_f64  4 fw_sweep_f32

@@ -90,6 +90,7 @@ class Context:
         self._h = h
         self.n = None
         self.nnz = None
+        self._explicit_stream = False
 
     # -- lifetime
     def close(self):
@@ -115,8 +116,23 @@ class Context:
                                 f"{self._L.ocsl_last_error(self._h).decode()}")
 
     def set_stream(self, stream_handle: int | None):
+        """Run on a caller-owned cudaStream_t (None: back to following torch's
+        current stream for the device entry points)."""
+        self._explicit_stream = stream_handle is not None
         self._check(self._L.ocsl_set_stream(self._h, C.c_void_p(stream_handle or 0)),
                     "set_stream")
+
+    def _follow_torch(self):
+        """Device entry points run on torch's current stream unless a stream
+        was set explicitly, so they are ordered after the torch work that
+        produced their inputs (the legacy default stream is passed as
+        cudaStreamLegacy)."""
+        if self._explicit_stream:
+            return
+        import torch
+
+        h = torch.cuda.current_stream().cuda_stream
+        self._L.ocsl_set_stream(self._h, C.c_void_p(h if h else 1))
 
     def synchronize(self):
         self._check(self._L.ocsl_synchronize(self._h), "synchronize")
@@ -155,6 +171,7 @@ class Context:
 
     def solve_device(self, method, value, b, x, *, raise_on_status=False, **opts):
         """Resident-data solve (ocsl_solve_device) on CUDA tensors; x in/out."""
+        self._follow_torch()
         o = _abi.default_opts(**opts)
         r = Result()
         st = self._L.ocsl_solve_device(self._h, _method(method), _dptr(value), _dptr(b), _dptr(x),
@@ -188,6 +205,7 @@ class Context:
         """Assemble one equation on the device.  ``state`` maps the fields of
         ocsl_flow_state to CUDA tensors (float64; bc_type, bc_wall,
         bc_supersonic int32); outputs are CUDA float64 tensors."""
+        self._follow_torch()
         q = self._assembly(eq)
         st = _abi.flow_state(state, lambda t: _dptr(t).value)
         self._check(self._L.ocsl_assemble_device(self._h, C.byref(q), C.byref(st), _dptr(value),
@@ -196,6 +214,7 @@ class Context:
 
     def bc_value_grad_device(self, eq: dict, state: dict, lam, grad):
         """grad[g] = lam[cell of g] * D_g for the Dirichlet p' boundary faces."""
+        self._follow_torch()
         q = self._assembly(eq)
         st = _abi.flow_state(state, lambda t: _dptr(t).value)
         self._check(self._L.ocsl_bc_value_grad_device(self._h, C.byref(q), C.byref(st),
@@ -219,6 +238,7 @@ class Context:
 
     def solve_transpose_device(self, method, value, g, lam, *, raise_on_status=False, **opts):
         """Resident-data adjoint solve A^T lam = g on CUDA tensors; lam in/out."""
+        self._follow_torch()
         o = _abi.default_opts(**opts)
         r = Result()
         st = self._L.ocsl_solve_transpose_device(self._h, _method(method), _dptr(value), _dptr(g),
@@ -230,12 +250,14 @@ class Context:
 
     def pattern_outer_device(self, u, v, out, alpha=-1.0):
         """out[k] = alpha * u[i] * v[j] on the pattern (dL/dA = -lam_i x_j)."""
+        self._follow_torch()
         self._check(self._L.ocsl_pattern_outer_device(self._h, float(alpha), _dptr(u), _dptr(v),
                                                       _dptr(out)), "pattern_outer")
 
     def solve_multi_device(self, method, value, B, X, **opts):
         """Several right-hand sides sharing the matrix: B, X are [nrhs, n] CUDA
         tensors; the factor is built once.  Returns a list of result dicts."""
+        self._follow_torch()
         nrhs = int(B.shape[0])
         o = _abi.default_opts(**opts)
         res = (Result * nrhs)()
@@ -257,6 +279,10 @@ class Context:
         self._check(self._L.ocsl_sweep_info(self._h, C.byref(kind), dims, tiles), "sweep_info")
         return {"kind": kind.value, "dims": tuple(dims), "tiles": tuple(tiles)}
 
+    def set_graphs(self, enable: bool = True):
+        """Replay iteration batches from CUDA graphs (default on)."""
+        self._check(self._L.ocsl_set_graphs(self._h, int(bool(enable))), "set_graphs")
+
     # -- kernel timing (ocsl_profile_*)
     def profile(self, enable: bool = True):
         self._check(self._L.ocsl_profile_enable(self._h, int(bool(enable))), "profile_enable")
@@ -272,10 +298,12 @@ class Context:
 
     # -- kernel-level entry points (device tensors)
     def gemv_device(self, value, x, y, mode=0, a=0.0, z=None):
+        self._follow_torch()
         self._check(self._L.ocsl_gemv_device(self._h, mode, a, _dptr(value), _dptr(x), _dptr(z),
                                              _dptr(y)), "gemv")
 
     def dot_device(self, x, y):
+        self._follow_torch()
         out = C.c_double()
         self._check(self._L.ocsl_dot_device(self._h, x.numel(), _dptr(x), _dptr(y),
                                             C.byref(out)), "dot")
@@ -283,27 +311,33 @@ class Context:
 
     def sum_device(self, x, absolute=False):
         """cmatrix_solver.cpp:244-263 sum / ABSsum (tile order)."""
+        self._follow_torch()
         out = C.c_double()
         self._check(self._L.ocsl_sum_device(self._h, x.numel(), _dptr(x), int(bool(absolute)),
                                             C.byref(out)), "sum")
         return out.value
 
     def product_device(self, x, y, out):
+        self._follow_torch()
         self._check(self._L.ocsl_product_device(self._h, x.numel(), _dptr(x), _dptr(y),
                                                 _dptr(out)), "product")
 
     def axpy_device(self, a, x, out, b=0.0, y=None):
         """out = a x + b y (the reference's axpy, :275-335); y None: out = a x."""
+        self._follow_torch()
         self._check(self._L.ocsl_axpy_device(self._h, x.numel(), float(a), _dptr(x), float(b),
                                              _dptr(y), _dptr(out)), "axpy")
 
     def ilu_device(self, A, M, sweeps=3):
+        self._follow_torch()
         self._check(self._L.ocsl_ilu_device(self._h, _dptr(A), _dptr(M), sweeps), "ilu")
 
     def forsub_device(self, M, b, y):
+        self._follow_torch()
         self._check(self._L.ocsl_forsub_device(self._h, _dptr(M), _dptr(b), _dptr(y)), "forsub")
 
     def backsub_device(self, M, y, x):
+        self._follow_torch()
         self._check(self._L.ocsl_backsub_device(self._h, _dptr(M), _dptr(y), _dptr(x)),
                     "backsub")
 
@@ -369,7 +403,11 @@ class Batch:
 
     def solve_device(self, method, values, Bs, Xs, **opts):
         """values[i], Bs[i] ([nrhs_i, n_i]) and Xs[i] are CUDA tensors; returns
-        (status, list of per-right-hand-side result dicts)."""
+        (status, list of per-right-hand-side result dicts).  The batch's workers
+        run on their own streams: pending torch work is finished first."""
+        import torch
+
+        torch.cuda.synchronize()
         k = len(values)
         P = C.c_void_p * k
         pv = P(*[_dptr(t).value for t in values])

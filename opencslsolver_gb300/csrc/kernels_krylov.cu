@@ -391,6 +391,11 @@ struct Rec4<double> {
     using V = double4;
 };
 
+#ifndef OCSL_BOX_SPMV_UNROLL
+#define OCSL_BOX_SPMV_UNROLL 2
+#endif
+constexpr int kBoxSpmvUnroll = OCSL_BOX_SPMV_UNROLL;
+
 template <typename T, int MODE, int DOTS>
 __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
 {
@@ -404,7 +409,7 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
     const V* lo = reinterpret_cast<const V*>(p.rec);
     const V* hi = lo + n;
     DotAcc<T> acc[ND > 0 ? ND : 1];
-#pragma unroll 2
+#pragma unroll kBoxSpmvUnroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
         if (row >= n) continue;

@@ -104,6 +104,13 @@ struct ocsl_ctx {
     int sweep_kernel = 0;
     int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
 
+    // CUDA graph of one batch of Krylov iterations, reused while its key
+    // (method and the pointers the iterations read) stays the same
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graphs_on = true;
+    int graph_kind = 0;
+    const void* graph_ptr[6] = {};
+
     // factor of the last solve (buffer and SoA copies), for solves that reuse it
     const double* fac_M = nullptr;
     const double* fac_soa64 = nullptr;
@@ -177,6 +184,8 @@ void ocsl_ctx::free_all()
     for (auto& e : ev_batch) { if (e) cudaEventDestroy(e); e = nullptr; }
     for (auto& e : prof_ev) cudaEventDestroy(e);
     prof_ev.clear();
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = stream = nullptr;
 }
@@ -498,6 +507,52 @@ struct Solve {
             launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S,
                                 k >= 0 ? done(k) : nullptr);
     }
+    // Enqueue `fn` (a fixed sequence of launches) through a CUDA graph keyed by
+    // (kind, ptrs): captured on first use, replayed afterwards.  Returns false
+    // (nothing enqueued) when graphs are off (profiling, legacy default
+    // stream) or the capture failed; the caller then launches directly.
+    template <typename Fn>
+    bool graph_launch(int kind, std::initializer_list<const void*> ptrs, Fn&& fn)
+    {
+        if (!c->graphs_on || c->prof_on || st == nullptr || st == cudaStreamLegacy ||
+            st == cudaStreamPerThread)
+            return false;
+        const void* key[6] = {};
+        int i = 0;
+        for (const void* q : ptrs)
+            if (i < 6) key[i++] = q;
+        bool hit = c->graph_exec && c->graph_kind == kind;
+        for (int j = 0; hit && j < 6; ++j) hit = c->graph_ptr[j] == key[j];
+        if (!hit) {
+            if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+            if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            cudaGraph_t g = nullptr;
+            try {
+                fn();
+            } catch (...) {
+                cudaStreamEndCapture(st, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            cudaGraphExec_t exec = nullptr;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            c->graph_exec = exec;
+            c->graph_kind = kind;
+            for (int j = 0; j < 6; ++j) c->graph_ptr[j] = key[j];
+        }
+        CK(cudaGraphLaunch(c->graph_exec, st));
+        return true;
+    }
     int device_error()
     {
         CK(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -574,15 +629,24 @@ constexpr int kBatch = 2;  // iterations enqueued between looks at the scalars
 // scalars block k reports done.  Two batches are kept in flight: while the GPU
 // runs one, the host inspects the scalars copied after the previous one.
 // Batches enqueued after convergence cost only no-op launches.
+// A full batch after the first is replayed from a CUDA graph when graph_kind
+// is non-zero (the iteration's launches do not depend on `it`).
 template <typename F>
-Scalars run_batches(Solve& s, int k, int budget, F&& enqueue)
+Scalars run_batches(Solve& s, int k, int budget, F&& enqueue, int graph_kind = 0,
+                    std::initializer_list<const void*> graph_ptrs = {})
 {
     Scalars* slot = s.c->h_sc + 6;  // two pinned inspection slots
     int it = 0, issued = 0, inspected = 0;
     while (true) {
         while (issued - inspected < 2 && it < budget) {
             const int m = std::min(kBatch, budget - it);
-            for (int j = 0; j < m; ++j) enqueue(it + j);
+            const bool graphed =
+                graph_kind && m == kBatch && issued > 0 &&
+                s.graph_launch(graph_kind, graph_ptrs, [&] {
+                    for (int j = 0; j < m; ++j) enqueue(it + j);
+                });
+            if (!graphed)
+                for (int j = 0; j < m; ++j) enqueue(it + j);
             it += m;
             CK(cudaMemcpyAsync(slot + (issued & 1), s.c->d_sc + k, sizeof(Scalars),
                                cudaMemcpyDeviceToHost, s.st));
@@ -619,7 +683,8 @@ void bicgstab_iteration(Solve& s, const TT* A, const TT* M, const TT* dinv, TT* 
 // from the current x when they disagree or on breakdown.
 template <typename Init, typename Iter, typename Half>
 TolResult run_restarted(Solve& s, const double* A, const double* b, double* x, const ocsl_opts& o,
-                        Init&& init, Iter&& iteration, Half&& half)
+                        Init&& init, Iter&& iteration, Half&& half, int graph_kind,
+                        std::initializer_list<const void*> graph_ptrs)
 {
     double** v = s.c->v64;
     TolResult res;
@@ -642,7 +707,7 @@ TolResult run_restarted(Solve& s, const double* A, const double* b, double* x, c
         }
         if (st.done) { converged = true; break; }
         if (total >= o.maxit) break;
-        st = run_batches(s, 0, o.maxit - total, iteration);
+        st = run_batches(s, 0, o.maxit - total, iteration, graph_kind, graph_ptrs);
         total += st.iters;
         broke = st.breakdown != 0;
         if (st.status) { res.status = st.status; break; }
@@ -672,7 +737,8 @@ TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x
             bicgstab_iteration<double>(s, A, M, s.c->d_dinv, x, v[R], v[RH], v[P], v[PH], v[V],
                                        v[S], v[SH], v[T], v[TMP], 0);
         },
-        [&] { s.vec<double>(V_TB_HALF, {x, v[PH]}, 0, EP_STORE); });
+        [&] { s.vec<double>(V_TB_HALF, {x, v[PH]}, 0, EP_STORE); }, 1,
+        {A, M, x, s.soa64, s.recA64, s.c->d_dinv});
 }
 
 TolResult run_pcg_tol(Solve& s, const double* A, const double* b, double* x, const ocsl_opts& o)
@@ -688,7 +754,7 @@ TolResult run_pcg_tol(Solve& s, const double* A, const double* b, double* x, con
             s.vec<double>(V_PC_XRZ, {x, v[P], v[R], v[Q], v[Z], s.c->d_dinv}, 0, EP_PC_RUPD);
             s.vec<double>(V_PC_P, {v[P], v[Z]}, 0, EP_STORE);
         },
-        [] {});
+        [] {}, 2, {A, x, s.recA64, s.c->d_dinv});
 }
 
 // FP32 inner ILU-BiCGSTAB (FP32 matrix, factor and vectors; compensated-FP32
@@ -727,10 +793,14 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
         s.reset_scalars(1, itol * itol);
         s.vec<float>(V_IR_SCALE, {v[R], f[F_RI], f[F_RH], f[F_P], f[F_D]}, 1, EP_IR_INNER_INIT);
         const int budget = std::min(o.inner_maxit, o.maxit - total);
-        const Scalars si = run_batches(s, 1, budget, [&](int) {
-            bicgstab_iteration<float>(s, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI], f[F_RH],
-                                      f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH], f[F_T], f[F_TMP], 1);
-        });
+        const Scalars si = run_batches(
+            s, 1, budget,
+            [&](int) {
+                bicgstab_iteration<float>(s, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI],
+                                          f[F_RH], f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH],
+                                          f[F_T], f[F_TMP], 1);
+            },
+            3, {c->d_A32, c->d_M32, s.soa32, s.recA32, c->d_dinv32});
         total += si.iters;
         s.vec<float>(V_TB_HALF, {f[F_D], f[F_PH]}, 1, EP_STORE);
         s.vec<float>(V_IR_UPDATE, {x, f[F_D]}, -1, EP_STORE);
@@ -841,6 +911,7 @@ int ensure_transpose(ocsl_ctx* c)
     int rc = ocsl_create(&t, c->device);
     if (rc != OCSL_OK) return fail(c, rc, "adjoint context: " + g_create_error);
     ocsl_set_sweep_kernel(t, c->sweep_kernel, c->box_tile[0], c->box_tile[1]);
+    t->graphs_on = c->graphs_on;
     rc = ocsl_set_pattern(t, (size_t)n, trp.data(), tcol.data());
     if (rc != OCSL_OK) {
         const std::string msg = t->last_error;
@@ -1361,6 +1432,18 @@ int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
         tiles[0] = c->P.box_ok ? c->P.box.TA : 0;
         tiles[1] = c->P.box_ok ? c->P.box.TB : 0;
     }
+    return OCSL_OK;
+}
+
+int ocsl_set_graphs(ocsl_ctx* c, int enable)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    c->graphs_on = enable != 0;
+    if (!c->graphs_on && c->graph_exec) {
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+    }
+    if (c->tctx) ocsl_set_graphs(c->tctx, enable);
     return OCSL_OK;
 }
 
