@@ -134,8 +134,10 @@ int ocsl_solve_device(ocsl_ctx* ctx, int method, const double* d_value, const do
 /* Several right-hand sides that share one matrix (the three momentum
  * components of an inviscid or slip case, cflow_solver.cpp:258-290):
  * d_b and d_x are [nrhs][n]; the factor is built once and reused by every
- * right-hand side.  result[nrhs].  No reference counterpart (the reference
- * assembles and solves each component separately). */
+ * right-hand side; with OCSL_ILU_BICGSTAB_IR32 they are solved in lockstep
+ * groups of up to four (ocsl_set_col_batching).  result[nrhs].  No reference
+ * counterpart (the reference assembles and solves each component
+ * separately). */
 int ocsl_solve_multi_device(ocsl_ctx* ctx, int method, const double* d_value, int nrhs,
                             const double* d_b, double* d_x, const ocsl_opts* opts,
                             ocsl_result* result);
@@ -347,6 +349,13 @@ const char* ocsl_noalloc_last_error(void);
  * default stream, not while profiling).  enable = 0 launches every kernel
  * directly; results are identical either way. */
 int ocsl_set_graphs(ocsl_ctx* ctx, int enable);
+
+/* ocsl_solve_multi_device with OCSL_ILU_BICGSTAB_IR32 runs its right-hand
+ * sides in lockstep, up to four per pass: every SpMV, vector and sweep launch
+ * serves all of them, and each keeps its own scalars, inner tolerance and
+ * stopping test, so every column's result is bit-identical to solving it
+ * alone with the same factor.  enable = 0 solves them one after another. */
+int ocsl_set_col_batching(ocsl_ctx* ctx, int enable);
 
 /* Kernel timing.  While enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream and accounted to a category:

@@ -283,6 +283,11 @@ class Context:
         """Replay iteration batches from CUDA graphs (default on)."""
         self._check(self._L.ocsl_set_graphs(self._h, int(bool(enable))), "set_graphs")
 
+    def set_col_batching(self, enable: bool = True):
+        """Solve the right-hand sides of solve_multi_device with the FP32-inner
+        solver in lockstep groups of up to four (default on)."""
+        self._check(self._L.ocsl_set_col_batching(self._h, int(bool(enable))), "set_col_batching")
+
     # -- kernel timing (ocsl_profile_*)
     def profile(self, enable: bool = True):
         self._check(self._L.ocsl_profile_enable(self._h, int(bool(enable))), "profile_enable")

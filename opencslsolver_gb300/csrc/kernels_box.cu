@@ -21,6 +21,7 @@
 // first, so waits cannot deadlock.  The output was filled with an all-ones
 // pattern, so a face value is its own ready flag (bounded wait, OCSL_TIMEOUT
 // on expiry).
+#include <algorithm>
 #include "ocsl_internal.cuh"
 
 namespace ocsl {
@@ -137,13 +138,20 @@ struct BoxParams {
     const T* rhs;
     T* out;
     SweepSync S;
-    const int* done;
+    const int* done;   // column q's flag at done[q * done_stride]
+    int done_stride;
+    long long ld;      // elements between the columns of rhs and out
 };
 
 // FWD: y = L^-1 rhs (unit L); !FWD: x = U^-1 rhs, DIV: divide by the
 // diagonal (the reference), else multiply by the stored reciprocal.
 // SPAN: which of x (0), y (1), z (2) the canonical s dimension is; a and b
 // are the other two in ascending stride.
+//
+// NC: right-hand sides carried through the same wavefront pass (column q's
+// rhs and output ld elements after column q-1's); each row's stencil record
+// is staged once and applied to all of them, and every column's arithmetic
+// is exactly that of a one-column sweep.
 //
 // One CTA (TA x TB threads, 16 x 8 by default) sweeps one tile of columns,
 // walking the wavefronts W = a + b + s of its tile with one __syncthreads per
@@ -171,7 +179,8 @@ struct BoxParams {
 constexpr int kPF = OCSL_BOX_PF;
 constexpr int kDF = OCSL_BOX_DF;
 static_assert(kPF % kDF == 0, "the face ring must tile the record ring");
-// shared memory of a 256-thread CTA in FP64 must fit the 227 KB opt-in limit
+// shared memory of a 256-thread CTA, one column in FP64, must fit the 227 KB
+// opt-in limit (several columns: the host narrows the tile)
 static_assert((32 * kPF + 8 * (2 + kPF)) * 256 <= 227 * 1024, "staging too deep for FP64");
 
 template <typename T>
@@ -185,17 +194,22 @@ struct Vec4<double> {
     double v[4];
 };
 
-template <typename T, bool FWD, bool DIV, int SPAN>
+template <typename T, bool FWD, bool DIV, int SPAN, int NC>
 __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
 {
-    if (p.done && *p.done) return;
+    if (p.done) {
+        bool all = true;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) all = all && p.done[q * p.done_stride] != 0;
+        if (all) return;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const BoxGeom& g = p.g;
     const int TA = g.TA, TB = g.TB, NT = g.TA * g.TB;
     using V4 = Vec4<T>;
     V4* coef = reinterpret_cast<V4*>(smem_raw);         // [kPF][NT] packed row records
-    T* ring = reinterpret_cast<T*>(coef + kPF * NT);    // [2][NT]
-    T* srhs = ring + 2 * NT;                            // [kPF][NT] rhs
+    T* ring = reinterpret_cast<T*>(coef + kPF * NT);    // [2][NC][NT]
+    T* srhs = ring + 2 * NC * NT;                       // [kPF][NC][NT] rhs
     __shared__ int s_tile;
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
     __syncthreads();
@@ -226,13 +240,21 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
         const int off_a = dstep * g.S[0], off_b = dstep * g.S[1];
         const int c0 = ca + cb;  // the thread sweeps row cs = W - c0 at wavefront W
         const V4* pack = reinterpret_cast<const V4*>(p.soa) + (FWD ? 0 : p.n);
-        const T* out_c = p.out;
+        // the columns' right-hand sides and outputs, ld elements apart
+        const T* rhs_q[NC];
+        T* out_q[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            rhs_q[q] = p.rhs + (size_t)q * p.ld;
+            out_q[q] = p.out + (size_t)q * p.ld;
+        }
         auto in_range = [&](int cs) { return col_ok && cs >= 0 && cs < Ds; };
         auto refill = [&](int cs, int j) {
             if (in_range(cs)) {
                 const int r = row0 + cs * sstep;
                 cp_async_vec<T>(&coef[j * NT + tid], pack + r);
-                cp_async(&srhs[j * NT + tid], p.rhs + r);
+#pragma unroll
+                for (int q = 0; q < NC; ++q) cp_async(&srhs[(j * NC + q) * NT + tid], rhs_q[q] + r);
             }
             cp_async_commit();
         };
@@ -243,22 +265,27 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
         // Start behind the upstream tiles: thread (0, 0) waits for the first
         // face row of each (their row at s = 0 next to this tile's corner).
         if (tid == 0) {
-            if (face_a) (void)wait_value(out_c + row0 + off_a, p.S.err);
-            if (face_b) (void)wait_value(out_c + row0 + off_b, p.S.err);
+            if (face_a) (void)wait_value(out_q[0] + row0 + off_a, p.S.err);
+            if (face_b) (void)wait_value(out_q[0] + row0 + off_b, p.S.err);
         }
         __syncthreads();
 
-        U fa[kDF], fb[kDF];
+        U fa[kDF][NC], fb[kDF][NC];
 #pragma unroll
         for (int j = 0; j < kDF; ++j) {
             const int cs = Wbase + j - c0;
-            fa[j] = B::kSentinel;
-            fb[j] = B::kSentinel;
-            if (face_a && in_range(cs)) fa[j] = B::load(out_c + row0 + cs * sstep + off_a);
-            if (face_b && in_range(cs)) fb[j] = B::load(out_c + row0 + cs * sstep + off_b);
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                fa[j][q] = B::kSentinel;
+                fb[j][q] = B::kSentinel;
+                if (face_a && in_range(cs)) fa[j][q] = B::load(out_q[q] + row0 + cs * sstep + off_a);
+                if (face_b && in_range(cs)) fb[j][q] = B::load(out_q[q] + row0 + cs * sstep + off_b);
+            }
         }
 
-        T prev = T(0);
+        T prev[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) prev[q] = T(0);
         for (int Wb = Wbase; Wb <= W1; Wb += kPF) {
 #pragma unroll
             for (int j = 0; j < kPF; ++j) {
@@ -268,44 +295,54 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
                 const int cs = W - c0;
                 cp_async_wait<kPF - 1>();
                 if (W >= W0 && in_range(cs)) {
-                    const V4 c = coef[j * NT + tid];
-                    const T* rd = ring + ((W - 1) & 1) * NT;
+                    const V4 cf = coef[j * NT + tid];
                     const int r = row0 + cs * sstep;
-                    T va = T(0), vb = T(0);
-                    if (has_a) {
-                        if (la > 0)
-                            va = rd[tid - 1];
-                        else
-                            va = fa[jf] != B::kSentinel ? B::from(fa[jf])
-                                                        : wait_value(out_c + r + off_a, p.S.err);
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) {
+                        const T* rd = ring + (((W - 1) & 1) * NC + q) * NT;
+                        T va = T(0), vb = T(0);
+                        if (has_a) {
+                            if (la > 0)
+                                va = rd[tid - 1];
+                            else
+                                va = fa[jf][q] != B::kSentinel
+                                         ? B::from(fa[jf][q])
+                                         : wait_value(out_q[q] + r + off_a, p.S.err);
+                        }
+                        if (has_b) {
+                            if (lb > 0)
+                                vb = rd[tid - TA];
+                            else
+                                vb = fb[jf][q] != B::kSentinel
+                                         ? B::from(fb[jf][q])
+                                         : wait_value(out_q[q] + r + off_b, p.S.err);
+                        }
+                        const T vs = cs > 0 ? prev[q] : T(0);
+                        const T vx = SPAN == 0 ? vs : va;
+                        const T vy = SPAN == 0 ? va : (SPAN == 1 ? vs : vb);
+                        const T vz = SPAN == 2 ? vs : vb;
+                        // packed record: z-, y-, x-, (unused) | x+, y+, z+, diagonal term;
+                        // the fma order is the row's CSR order
+                        T sum = fma_t(cf.v[0], FWD ? vz : vx, T(0));
+                        sum = fma_t(cf.v[1], vy, sum);
+                        sum = fma_t(cf.v[2], FWD ? vx : vz, sum);
+                        const T num = srhs[(j * NC + q) * NT + tid] - sum;
+                        const T y = FWD ? num : (DIV ? num / cf.v[3] : num * cf.v[3]);
+                        ring[((W & 1) * NC + q) * NT + tid] = y;
+                        publish(out_q[q] + r, y);
+                        prev[q] = y;
                     }
-                    if (has_b) {
-                        if (lb > 0)
-                            vb = rd[tid - TA];
-                        else
-                            vb = fb[jf] != B::kSentinel ? B::from(fb[jf])
-                                                        : wait_value(out_c + r + off_b, p.S.err);
-                    }
-                    const T vs = cs > 0 ? prev : T(0);
-                    const T vx = SPAN == 0 ? vs : va;
-                    const T vy = SPAN == 0 ? va : (SPAN == 1 ? vs : vb);
-                    const T vz = SPAN == 2 ? vs : vb;
-                    // packed record: z-, y-, x-, (unused) | x+, y+, z+, diagonal term;
-                    // the fma order is the row's CSR order
-                    T sum = fma_t(c.v[0], FWD ? vz : vx, T(0));
-                    sum = fma_t(c.v[1], vy, sum);
-                    sum = fma_t(c.v[2], FWD ? vx : vz, sum);
-                    const T num = srhs[j * NT + tid] - sum;
-                    const T y = FWD ? num : (DIV ? num / c.v[3] : num * c.v[3]);
-                    ring[(W & 1) * NT + tid] = y;
-                    publish(p.out + r, y);
-                    prev = y;
                 }
                 // next face words of this ring slot: wavefront W + kDF
                 {
                     const int csn = cs + kDF;
-                    if (face_a && in_range(csn)) fa[jf] = B::load(out_c + row0 + csn * sstep + off_a);
-                    if (face_b && in_range(csn)) fb[jf] = B::load(out_c + row0 + csn * sstep + off_b);
+#pragma unroll
+                    for (int q = 0; q < NC; ++q) {
+                        if (face_a && in_range(csn))
+                            fa[jf][q] = B::load(out_q[q] + row0 + csn * sstep + off_a);
+                        if (face_b && in_range(csn))
+                            fb[jf][q] = B::load(out_q[q] + row0 + csn * sstep + off_b);
+                    }
                 }
                 refill(cs + kPF, j);
                 if (W >= W0) __syncthreads();  // uniform over the CTA
@@ -353,37 +390,55 @@ __global__ void box_to_soa_kernel(int n, int nx, int ny, int nz, const int* rp, 
     hi[3] = (TO)v[3];
 }
 
-template <typename T, bool FWD, bool DIV, int SPAN>
+template <typename T, bool FWD, bool DIV, int SPAN, int NC>
 void launch_one(cudaStream_t st, const BoxParams<T>& p)
 {
     const int grid = p.g.nta * p.g.ntb;
     const int threads = p.g.TA * p.g.TB;
-    const size_t per = sizeof(Vec4<T>) * kPF + sizeof(T) * (2 + kPF);
-    const size_t smem = per * threads;
+    const size_t smem = box_sweep_smem(threads, (int)sizeof(T), NC);
     static bool attr_set = false;  // one opt-in per instantiation
     if (!attr_set) {
-        cudaFuncSetAttribute(box_cta_kernel<T, FWD, DIV, SPAN>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(per * 256));
+        const size_t most = std::min(box_sweep_smem(256, (int)sizeof(T), NC), kBoxSmemLimit);
+        cudaFuncSetAttribute(box_cta_kernel<T, FWD, DIV, SPAN, NC>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
         attr_set = true;
     }
-    box_cta_kernel<T, FWD, DIV, SPAN><<<grid, threads, smem, st>>>(p);
+    box_cta_kernel<T, FWD, DIV, SPAN, NC><<<grid, threads, smem, st>>>(p);
 }
 
-template <typename T, bool FWD, bool DIV>
+template <typename T, bool FWD, bool DIV, int NC>
 void launch_span(cudaStream_t st, int span, const BoxParams<T>& p)
 {
     switch (span) {
-    case 0: launch_one<T, FWD, DIV, 0>(st, p); break;
-    case 1: launch_one<T, FWD, DIV, 1>(st, p); break;
-    default: launch_one<T, FWD, DIV, 2>(st, p); break;
+    case 0: launch_one<T, FWD, DIV, 0, NC>(st, p); break;
+    case 1: launch_one<T, FWD, DIV, 1, NC>(st, p); break;
+    default: launch_one<T, FWD, DIV, 2, NC>(st, p); break;
+    }
+}
+
+template <typename T, bool FWD>
+void launch_cols(cudaStream_t st, int ncols, const BoxParams<T>& p)
+{
+    switch (ncols) {
+    case 1: launch_span<T, FWD, false, 1>(st, p.g.span, p); break;
+    case 2: launch_span<T, FWD, false, 2>(st, p.g.span, p); break;
+    case 3: launch_span<T, FWD, false, 3>(st, p.g.span, p); break;
+    default: launch_span<T, FWD, false, 4>(st, p.g.span, p); break;
     }
 }
 
 }  // namespace
 
+size_t box_sweep_smem(int threads, int elem_size, int ncols)
+{
+    const size_t per = (size_t)4 * elem_size * kPF + (size_t)elem_size * ncols * (2 + kPF);
+    return per * (size_t)threads;
+}
+
 template <typename T>
 void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, const T* rhs, T* out,
-                      bool forward, int divmode, const SweepSync& S, const int* done)
+                      bool forward, int divmode, const SweepSync& S, const int* done,
+                      const Cols& cols, int done_stride)
 {
     BoxParams<T> p;
     p.g = g;
@@ -393,12 +448,15 @@ void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, co
     p.out = out;
     p.S = S;
     p.done = done;
-    if (forward)
-        launch_span<T, true, false>(st, g.span, p);
-    else if (divmode == 0)
-        launch_span<T, false, true>(st, g.span, p);
+    p.done_stride = done_stride;
+    p.ld = cols.ld;
+    const int nc = std::max(1, std::min(cols.n, kMaxCols));
+    if (divmode == 0 && !forward)
+        launch_span<T, false, true, 1>(st, g.span, p);  // the reference's division: one column
+    else if (forward)
+        launch_cols<T, true>(st, nc, p);
     else
-        launch_span<T, false, false>(st, g.span, p);
+        launch_cols<T, false>(st, nc, p);
 }
 
 template <typename TO>
@@ -415,10 +473,10 @@ void launch_box_to_soa(cudaStream_t st, const int* dims, int n, const int* rp, c
 
 template void launch_box_sweep<double>(cudaStream_t, const BoxGeom&, int, const double*,
                                        const double*, double*, bool, int, const SweepSync&,
-                                       const int*);
+                                       const int*, const Cols&, int);
 template void launch_box_sweep<float>(cudaStream_t, const BoxGeom&, int, const float*,
                                       const float*, float*, bool, int, const SweepSync&,
-                                      const int*);
+                                      const int*, const Cols&, int);
 template void launch_box_to_soa<double>(cudaStream_t, const int*, int, const int*, const double*,
                                         double*, int);
 template void launch_box_to_soa<float>(cudaStream_t, const int*, int, const int*, const double*,

@@ -263,9 +263,14 @@ __global__ void factor_outputs_kernel(int n, const int* rp, const int* diag, con
 // stores, then `tail` words.
 __global__ void __launch_bounds__(kThreads) fill_ones_kernel(unsigned* out, int head,
                                                             long long n16, int tail,
-                                                            const int* done)
+                                                            const int* done, int ndone,
+                                                            int done_stride)
 {
-    if (done && *done) return;
+    if (done) {  // skipped once every listed flag is set
+        bool all = true;
+        for (int q = 0; q < ndone; ++q) all = all && done[q * done_stride] != 0;
+        if (all) return;
+    }
     const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (gid < head) out[gid] = ~0u;
     uint4* body = reinterpret_cast<uint4*>(out + head);
@@ -343,7 +348,8 @@ void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T*
     ilu_sweep_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(p);
 }
 
-void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done)
+void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done, int ndone,
+                      int done_stride)
 {
     // `out` is element-aligned (4 or 8 bytes); the entry points check that.
     const size_t words = bytes / 4;
@@ -357,7 +363,7 @@ void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done)
     if (blocks < 1) blocks = 1;
     if (blocks > 4096) blocks = 4096;
     fill_ones_kernel<<<(int)blocks, kThreads, 0, st>>>(static_cast<unsigned*>(out), (int)head,
-                                                       n16, tail, done);
+                                                       n16, tail, done, ndone, done_stride);
 }
 
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,

@@ -235,18 +235,21 @@ __device__ void apply_epilogue(int epi, const double* s, int nd, Scalars* sc, in
 
 // Store this CTA's tile partials; if it is the last CTA, reduce all tiles and
 // apply the epilogue.  Must be reached by every thread of every CTA.
+// Column `col` of a column-batched launch has its own partials and counter.
 template <int ND>
-__device__ __forceinline__ void finish_reduction(double (&v)[ND], int tile, int ntiles,
+__device__ __forceinline__ void finish_reduction(double (&v)[ND], int tile, int ntiles, int col,
                                                  const ReduceState& R, Scalars* sc, int epi,
                                                  int it, int maxit, double* s_red, int* s_last)
 {
+    double* partials = R.partials + (size_t)col * kMaxDots * R.max_tiles;
+    unsigned* counter = R.counter + col;
     cta_sum<ND>(v, s_red);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < ND; ++k) R.partials[k * R.max_tiles + tile] = v[k];
+        for (int k = 0; k < ND; ++k) partials[k * R.max_tiles + tile] = v[k];
         __threadfence();
-        const unsigned prev = atomicAdd(R.counter, 1u);
-        *s_last = (prev == gridDim.x - 1);
+        const unsigned prev = atomicAdd(counter, 1u);
+        *s_last = (prev == (unsigned)ntiles - 1u);
     }
     __syncthreads();
     if (!*s_last) return;
@@ -255,14 +258,34 @@ __device__ __forceinline__ void finish_reduction(double (&v)[ND], int tile, int 
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
         double a = 0.0;
-        for (int t = threadIdx.x; t < ntiles; t += kThreads) a = a + __ldcg(R.partials + k * R.max_tiles + t);
+        for (int t = threadIdx.x; t < ntiles; t += kThreads) a = a + __ldcg(partials + k * R.max_tiles + t);
         acc[k] = a;
     }
     cta_sum<ND>(acc, s_red);
     if (threadIdx.x == 0) {
         if (sc) apply_epilogue(epi, acc, ND, sc, it, maxit);
-        *R.counter = 0u;
+        *counter = 0u;
     }
+}
+
+// Column and tile of this CTA in a launch of ntiles * cols.n CTAs.
+struct ColTile {
+    int col, tile, ntiles;
+    size_t off;  // element offset of the column's vectors
+};
+__device__ __forceinline__ ColTile col_tile(const Cols& c)
+{
+    ColTile t;
+    t.col = (int)(blockIdx.x % (unsigned)c.n);
+    t.tile = (int)(blockIdx.x / (unsigned)c.n);
+    t.ntiles = (int)(gridDim.x / (unsigned)c.n);
+    t.off = (size_t)t.col * (size_t)c.ld;
+    return t;
+}
+template <typename P>
+__device__ __forceinline__ P* at(P* p, size_t off)
+{
+    return p ? p + off : p;
 }
 
 template <typename T>
@@ -280,6 +303,7 @@ struct SpmvParams {
     ReduceState R;
     Scalars* sc;
     int epi, it, maxit;
+    Cols cols;
 };
 
 // y = A x (MODE 0), y = z - A x (MODE 1), y = fma(a, A x, z) (MODE 2);
@@ -289,14 +313,21 @@ struct SpmvParams {
 template <typename T, int MODE, int DOTS>
 __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
 {
-    if (p.sc && p.sc->done) return;
+    const ColTile ct = col_tile(p.cols);
+    Scalars* const sc = at(p.sc, ct.col);
+    if (sc && sc->done) return;
     constexpr int ND = DotCount<DOTS>::value;
     __shared__ T s_val[kSpmvCap];
     __shared__ int s_col[kSpmvCap];
     __shared__ double s_red[kMaxDots * 8];
     __shared__ int s_last;
-    const int tile = blockIdx.x;
+    const int tile = ct.tile;
     const int n = p.n;
+    const T* const xv = p.x + ct.off;
+    T* const yv = p.y + ct.off;
+    const T* const zvec = at(p.z, ct.off);
+    T* const ycp = at(p.y_copy, ct.off);
+    const T* const wv = at(p.w, ct.off);
     DotAcc<T> acc[ND > 0 ? ND : 1];
 
 #pragma unroll 1
@@ -320,30 +351,30 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
             if (staged) {
                 for (int q = b - q0; q < e - q0; ++q) {
                     const int c = s_col[q];
-                    if (c >= 0) dum = fma_t(s_val[q], __ldg(p.x + c), dum);
+                    if (c >= 0) dum = fma_t(s_val[q], __ldg(xv + c), dum);
                 }
             } else {
                 for (int q = b; q < e; ++q) {
                     const int c = __ldg(p.col + q);
-                    if (c >= 0) dum = fma_t(__ldg(p.val + q), __ldg(p.x + c), dum);
+                    if (c >= 0) dum = fma_t(__ldg(p.val + q), __ldg(xv + c), dum);
                 }
             }
             T y, zv = T(0);
             if constexpr (MODE == 0) {
                 y = dum;
             } else if constexpr (MODE == 1) {
-                zv = p.z[row];
+                zv = zvec[row];
                 y = zv - dum;
             } else {
-                zv = p.z[row];
+                zv = zvec[row];
                 y = fma_t(p.a, dum, zv);
             }
-            p.y[row] = y;
-            if (MODE == 1 && p.y_copy) p.y_copy[row] = y;
+            yv[row] = y;
+            if (MODE == 1 && ycp) ycp[row] = y;
             int k = 0;
             if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
             if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
-            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(p.w[row], y);
+            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(wv[row], y);
             (void)k;
         }
         __syncthreads();
@@ -352,7 +383,8 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
         double v[ND];
 #pragma unroll
         for (int k = 0; k < ND; ++k) v[k] = acc[k].value();
-        finish_reduction<ND>(v, tile, gridDim.x, p.R, p.sc, p.epi, p.it, p.maxit, s_red, &s_last);
+        finish_reduction<ND>(v, tile, ct.ntiles, ct.col, p.R, sc, p.epi, p.it, p.maxit, s_red,
+                             &s_last);
     }
 }
 
@@ -378,6 +410,7 @@ struct BoxSpmvParams {
     ReduceState R;
     Scalars* sc;
     int epi, it, maxit;
+    Cols cols;
 };
 
 template <typename T>
@@ -399,13 +432,20 @@ constexpr int kBoxSpmvUnroll = OCSL_BOX_SPMV_UNROLL;
 template <typename T, int MODE, int DOTS>
 __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
 {
-    if (p.sc && p.sc->done) return;
+    const ColTile ct = col_tile(p.cols);
+    Scalars* const sc = at(p.sc, ct.col);
+    if (sc && sc->done) return;
     constexpr int ND = DotCount<DOTS>::value;
     using V = typename Rec4<T>::V;
     __shared__ double s_red[kMaxDots * 8];
     __shared__ int s_last;
-    const int tile = blockIdx.x;
+    const int tile = ct.tile;
     const int n = p.n;
+    const T* const xv = p.x + ct.off;
+    T* const yv = p.y + ct.off;
+    const T* const zvec = at(p.z, ct.off);
+    T* const ycp = at(p.y_copy, ct.off);
+    const T* const wv = at(p.w, ct.off);
     const V* lo = reinterpret_cast<const V*>(p.rec);
     const V* hi = lo + n;
     DotAcc<T> acc[ND > 0 ? ND : 1];
@@ -414,7 +454,7 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
         const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
         if (row >= n) continue;
         const V l = lo[row], h = hi[row];
-        const T* x = p.x;
+        const T* x = xv;
         const T xzm = __ldg(x + max(row - p.sz, 0)), xym = __ldg(x + max(row - p.sy, 0));
         const T xxm = __ldg(x + max(row - 1, 0)), xc = __ldg(x + row);
         const T xxp = __ldg(x + min(row + 1, n - 1)), xyp = __ldg(x + min(row + p.sy, n - 1));
@@ -430,25 +470,26 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
         if constexpr (MODE == 0) {
             y = dum;
         } else if constexpr (MODE == 1) {
-            zv = p.z[row];
+            zv = zvec[row];
             y = zv - dum;
         } else {
-            zv = p.z[row];
+            zv = zvec[row];
             y = fma_t(p.a, dum, zv);
         }
-        p.y[row] = y;
-        if (MODE == 1 && p.y_copy) p.y_copy[row] = y;
+        yv[row] = y;
+        if (MODE == 1 && ycp) ycp[row] = y;
         int k = 0;
         if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
         if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
-        if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(p.w[row], y);
+        if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(wv[row], y);
         (void)k;
     }
     if constexpr (ND > 0) {
         double v[ND];
 #pragma unroll
         for (int k = 0; k < ND; ++k) v[k] = acc[k].value();
-        finish_reduction<ND>(v, tile, gridDim.x, p.R, p.sc, p.epi, p.it, p.maxit, s_red, &s_last);
+        finish_reduction<ND>(v, tile, ct.ntiles, ct.col, p.R, sc, p.epi, p.it, p.maxit, s_red,
+                             &s_last);
     }
 }
 
@@ -468,29 +509,41 @@ struct VecParams {
     Scalars* sc;
     const Scalars* outer;
     int epi, it, maxit;
+    Cols cols;
 };
 
 template <typename T, int OP>
 __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
 {
+    const ColTile ct = col_tile(P.cols);
+    Scalars* const sc = at(P.sc, ct.col);
+    const Scalars* const outer = at(P.outer, ct.col);
     if constexpr (OP == V_TB_HALF) {
-        if (!P.sc->half) return;
+        if (!sc->half) return;
     } else if constexpr (OP == V_IR_SCALE || OP == V_IR_UPDATE) {
-        if (P.outer->done) return;
-    } else if (P.sc && P.sc->done) {
+        if (outer->done) return;
+    } else if (sc && sc->done) {
         return;
     }
     constexpr int ND = OpDots<OP>::value;
     __shared__ double s_red[kMaxDots * 8];
     __shared__ int s_last;
-    const int tile = blockIdx.x;
+    const int tile = ct.tile;
     const int n = P.n;
-    T* const* v = reinterpret_cast<T* const*>(P.p.v);
+    // this column's vectors (element offsets in each pointer's own type)
+    T* v[8];
+    double* v64[2];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const size_t o = ((P.cols.shared >> i) & 1u) ? 0 : ct.off;
+        v[i] = at(reinterpret_cast<T*>(P.p.v[i]), o);
+        if (i < 2) v64[i] = at(reinterpret_cast<double*>(P.p.v[i]), o);
+    }
 
     // Scalars of this step, read once per thread (written by earlier kernels).
-    const double alpha = P.sc ? P.sc->alpha : 0.0;
-    const double omega = P.sc ? P.sc->omega : 0.0;
-    const double beta = P.sc ? P.sc->beta : 0.0;
+    const double alpha = sc ? sc->alpha : 0.0;
+    const double omega = sc ? sc->omega : 0.0;
+    const double beta = sc ? sc->beta : 0.0;
     const T a = (T)alpha, w = (T)omega, be = (T)beta;
     DotAcc<T> acc[ND > 0 ? ND : 1];
 
@@ -557,18 +610,16 @@ __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
             acc[1].add(r, z);
         } else if constexpr (OP == V_PC_P) {
             v[0][e] = fma_t(be, v[0][e], v[1][e]);
-        } else if constexpr (OP == V_IR_SCALE) {
-            const double* r = reinterpret_cast<const double*>(P.p.v[0]);
-            const float f = (float)(r[e] * P.outer->sum[3]);
-            reinterpret_cast<float*>(P.p.v[1])[e] = f;
-            reinterpret_cast<float*>(P.p.v[2])[e] = f;
-            reinterpret_cast<float*>(P.p.v[3])[e] = f;
-            reinterpret_cast<float*>(P.p.v[4])[e] = 0.0f;
+        } else if constexpr (OP == V_IR_SCALE) {  // v[0] is FP64
+            const float f = (float)(v64[0][e] * outer->sum[3]);
+            v[1][e] = f;
+            v[2][e] = f;
+            v[3][e] = f;
+            v[4][e] = 0.0f;
             acc[0].add(f, f);
-        } else if constexpr (OP == V_IR_UPDATE) {
-            double* x = reinterpret_cast<double*>(P.p.v[0]);
-            const float d = reinterpret_cast<const float*>(P.p.v[1])[e];
-            x[e] = fma((double)d, P.outer->rnorm, x[e]);
+        } else if constexpr (OP == V_IR_UPDATE) {  // v[0] is FP64
+            const float d = v[1][e];
+            v64[0][e] = fma((double)d, outer->rnorm, v64[0][e]);
         } else if constexpr (OP == V_SUM) {  // fma(x, 1, s) == s + x exactly
             acc[0].add(v[0][e], T(1));
         } else if constexpr (OP == V_ABSSUM) {
@@ -595,7 +646,7 @@ __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
         double vals[ND];
 #pragma unroll
         for (int k = 0; k < ND; ++k) vals[k] = acc[k].value();
-        finish_reduction<ND>(vals, tile, gridDim.x, P.R, P.sc, P.epi, P.it, P.maxit, s_red,
+        finish_reduction<ND>(vals, tile, ct.ntiles, ct.col, P.R, sc, P.epi, P.it, P.maxit, s_red,
                              &s_last);
     }
 }
@@ -613,7 +664,7 @@ void spmv_dispatch(cudaStream_t st, const SpmvParams<T>& p)
 {
     const int nt = ntiles_of(p.n);
     if (nt == 0) return;
-    spmv_kernel<T, MODE, DOTS><<<nt, kThreads, 0, st>>>(p);
+    spmv_kernel<T, MODE, DOTS><<<nt * p.cols.n, kThreads, 0, st>>>(p);
 }
 
 template <typename T, int MODE>
@@ -634,7 +685,7 @@ void box_spmv_dispatch(cudaStream_t st, const BoxSpmvParams<T>& p)
 {
     const int nt = ntiles_of(p.n);
     if (nt == 0) return;
-    box_spmv_kernel<T, MODE, DOTS><<<nt, kThreads, 0, st>>>(p);
+    box_spmv_kernel<T, MODE, DOTS><<<nt * p.cols.n, kThreads, 0, st>>>(p);
 }
 
 template <typename T, int MODE>
@@ -655,7 +706,7 @@ void vec_dispatch(cudaStream_t st, const VecParams& P)
 {
     const int nt = ntiles_of(P.n);
     if (nt == 0) return;
-    vec_kernel<T, OP><<<nt, kThreads, 0, st>>>(P);
+    vec_kernel<T, OP><<<nt * P.cols.n, kThreads, 0, st>>>(P);
 }
 
 }  // namespace
@@ -663,9 +714,11 @@ void vec_dispatch(cudaStream_t st, const VecParams& P)
 template <typename T>
 void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x, T* y, int mode,
                  const double* /*scal_a*/, double a_const, const T* z, T* y_copy, const T* w,
-                 int dots, const ReduceState& R, Scalars* sc, int epi, int it, int maxit)
+                 int dots, const ReduceState& R, Scalars* sc, int epi, int it, int maxit,
+                 const Cols& cols)
 {
     SpmvParams<T> p;
+    p.cols = cols;
     p.n = P.n;
     p.rp = P.rp;
     p.col = P.col;
@@ -691,9 +744,11 @@ void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x,
 template <typename T>
 void launch_box_spmv(cudaStream_t st, int n, const int* dims, const T* rec, const T* x, T* y,
                      int mode, double a_const, const T* z, T* y_copy, const T* w, int dots,
-                     const ReduceState& R, Scalars* sc, int epi, int it, int maxit)
+                     const ReduceState& R, Scalars* sc, int epi, int it, int maxit,
+                     const Cols& cols)
 {
     BoxSpmvParams<T> p;
+    p.cols = cols;
     p.n = n;
     p.sy = dims[0];
     p.sz = dims[0] * dims[1];
@@ -718,9 +773,11 @@ void launch_box_spmv(cudaStream_t st, int n, const int* dims, const T* rec, cons
 
 template <typename T>
 void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& ptrs, const ReduceState& R,
-                Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit)
+                Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit,
+                const Cols& cols)
 {
     VecParams P;
+    P.cols = cols;
     P.n = n;
     P.p = ptrs;
     P.R = R;
@@ -764,20 +821,22 @@ void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out
 
 template void launch_spmv<double>(cudaStream_t, const DevPattern&, const double*, const double*,
                                   double*, int, const double*, double, const double*, double*,
-                                  const double*, int, const ReduceState&, Scalars*, int, int, int);
+                                  const double*, int, const ReduceState&, Scalars*, int, int, int,
+                                  const Cols&);
 template void launch_spmv<float>(cudaStream_t, const DevPattern&, const float*, const float*,
                                  float*, int, const double*, double, const float*, float*,
-                                 const float*, int, const ReduceState&, Scalars*, int, int, int);
+                                 const float*, int, const ReduceState&, Scalars*, int, int, int,
+                                 const Cols&);
 template void launch_box_spmv<double>(cudaStream_t, int, const int*, const double*,
                                       const double*, double*, int, double, const double*,
                                       double*, const double*, int, const ReduceState&, Scalars*,
-                                      int, int, int);
+                                      int, int, int, const Cols&);
 template void launch_box_spmv<float>(cudaStream_t, int, const int*, const float*, const float*,
                                      float*, int, double, const float*, float*, const float*, int,
-                                     const ReduceState&, Scalars*, int, int, int);
+                                     const ReduceState&, Scalars*, int, int, int, const Cols&);
 template void launch_vec<double>(cudaStream_t, int, int, const VecPtrs&, const ReduceState&,
-                                 Scalars*, const Scalars*, int, int, int);
+                                 Scalars*, const Scalars*, int, int, int, const Cols&);
 template void launch_vec<float>(cudaStream_t, int, int, const VecPtrs&, const ReduceState&,
-                                Scalars*, const Scalars*, int, int, int);
+                                Scalars*, const Scalars*, int, int, int, const Cols&);
 
 }  // namespace ocsl

@@ -28,6 +28,7 @@ constexpr int kRowsPerThread = 8;      // rows / elements per thread per tile
 constexpr int kTile = kThreads * kRowsPerThread;  // 2048 rows per tile
 constexpr int kSpmvCap = 2560;         // staged nnz per 256-row slab
 constexpr int kMaxDots = 3;
+constexpr int kMaxCols = 4;            // right-hand sides of one column-batched launch
 
 // Scalars of one Krylov iteration, resident on the device.  Reduction
 // epilogues write them, vector kernels read them; the host reads the block
@@ -62,9 +63,21 @@ enum EpiOp : int {
 enum DotSel : int { DOT_YY = 1, DOT_ZZ = 2, DOT_WY = 4 };
 
 struct ReduceState {
-    double* partials;    // [kMaxDots][max_tiles]
-    unsigned* counter;   // CTAs finished (reset by the last one)
+    double* partials;    // [kMaxCols][kMaxDots][max_tiles]
+    unsigned* counter;   // [kMaxCols] CTAs finished (reset by the last one)
     int max_tiles;
+};
+
+// Column batching of the tile kernels: `n` right-hand sides (columns) whose
+// vectors lie `ld` elements apart run in one launch of ntiles * n CTAs.  CTA
+// b works on column b % n and tile b / n, so the CTAs reading the same rows
+// of A run together and A comes from DRAM once; column c uses scalars block
+// sc + c and its own reduction partials and counter.  `shared` marks the
+// vector arguments (bit i = pointer i) that all columns share (dinv).
+struct Cols {
+    int n = 1;
+    long long ld = 0;
+    unsigned shared = 0;
 };
 
 // Geometry of the structured sweep (7-point box patterns): canonical dims
@@ -122,14 +135,15 @@ template <typename T>
 void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x, T* y,
                  int mode, const double* scal_a, double a_const, const T* z, T* y_copy,
                  const T* w, int dots, const ReduceState& R, Scalars* sc, int epi, int it,
-                 int maxit);
+                 int maxit, const Cols& cols = Cols{});
 
 // SpMV on packed stencil records ([2][n][4], the structured sweeps' layout, of A
 // itself) for natural-order 7-point box patterns; dims = (nx, ny, nz).
 template <typename T>
 void launch_box_spmv(cudaStream_t st, int n, const int* dims, const T* rec, const T* x, T* y,
                      int mode, double a_const, const T* z, T* y_copy, const T* w, int dots,
-                     const ReduceState& R, Scalars* sc, int epi, int it, int maxit);
+                     const ReduceState& R, Scalars* sc, int epi, int it, int maxit,
+                     const Cols& cols = Cols{});
 
 // Vector kernels: the op decides which pointers it uses.
 enum VecOp : int {
@@ -163,7 +177,8 @@ struct VecPtrs {
 
 template <typename T>
 void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& p, const ReduceState& R,
-                Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit);
+                Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit,
+                const Cols& cols = Cols{});
 
 template <typename T>
 void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
@@ -182,17 +197,28 @@ void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out
 // Structured sweep on the packed stencil factor ([2][n][4]: (z-, y-, x-, 0),
 // (x+, y+, z+, diagonal term)); divmode 0 divides by the diagonal term, 1
 // multiplies by it.
+// Column-batched form: cols.n (<= kMaxCols) right-hand sides cols.ld apart in
+// one wavefront pass; `done` then points at column 0's flag, the others
+// follow every done_stride ints, and the launch is skipped once all are set.
 template <typename T>
 void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, const T* rhs, T* out,
-                      bool forward, int divmode, const SweepSync& S, const int* done);
+                      bool forward, int divmode, const SweepSync& S, const int* done,
+                      const Cols& cols = Cols{}, int done_stride = 0);
+// Dynamic shared memory of one structured-sweep CTA of `threads` threads
+// (records and rhs staged kPF wavefronts ahead, a two-slot ring per column);
+// a launch needs it <= kBoxSmemLimit.
+size_t box_sweep_smem(int threads, int elem_size, int ncols);
+constexpr size_t kBoxSmemLimit = 227 * 1024;
 // CSR factor (FP64) -> packed stencil records in TO; diagonal term =
 // diagonal, or 1/diagonal with recip.
 template <typename TO>
 void launch_box_to_soa(cudaStream_t st, const int* dims, int n, const int* rp, const double* M,
                        TO* soa, int recip);
 
-// All-ones fill of a sweep output (skipped once the solve is done).
-void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done);
+// All-ones fill of a sweep output, skipped once the solve is done: once all
+// of the ndone flags done[q * done_stride] are set.
+void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done, int ndone = 1,
+                      int done_stride = 0);
 
 // Factor side outputs without a sweep: dinv = 1 / M_ii and FP32 copies.
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,

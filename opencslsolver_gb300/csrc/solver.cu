@@ -61,6 +61,19 @@ constexpr int kRefBicgIters = 3;
 enum Vec64 { R, P, Q, RN, V, R0, S, DUM, H, T, Y, Z, DUM2, PH, SH, RH, TMP, NVEC64 };
 enum Vec32 { F_RI, F_RH, F_P, F_PH, F_V, F_S, F_SH, F_T, F_TMP, F_D, NVEC32 };
 
+// Scalars blocks on the device: 0 main / outer, 1 inner, 2 utility; the
+// column-batched solve uses kMaxCols outer blocks from kScOuterCols and
+// kMaxCols inner blocks from kScInnerCols.
+constexpr int kScOuterCols = 3;
+constexpr int kScInnerCols = kScOuterCols + kMaxCols;
+constexpr int kScBlocks = kScInnerCols + kMaxCols;
+// Pinned host mirrors: read copies [0, 16), upload staging [16, 32),
+// two inspection slots of kMaxCols blocks from 32.
+constexpr int kHostStage = 16;
+constexpr int kHostInspect = 32;
+constexpr int kHostSlots = kHostInspect + 2 * kMaxCols;
+static_assert(kScBlocks <= kHostStage, "host mirror layout");
+
 }  // namespace
 
 struct ocsl_ctx {
@@ -85,14 +98,17 @@ struct ocsl_ctx {
     float* d_M32 = nullptr;
     float* d_dinv32 = nullptr;
     float* v32[NVEC32] = {};
+    // column-batched solves: [kMaxCols][n] work vectors (allocated on first use)
+    double* v64c = nullptr;           // FP64 residuals
+    float* v32c[NVEC32] = {};         // FP32 inner vectors
     double* d_soa64 = nullptr;  // stencil-SoA factor copies (7-point box patterns)
     float* d_soa32 = nullptr;
     double* d_recA64 = nullptr;  // stencil records of A itself, for the box SpMV
     float* d_recA32 = nullptr;
 
     ReduceState R{};
-    Scalars* d_sc = nullptr;  // [0] main / outer, [1] inner, [2] utility
-    Scalars* h_sc = nullptr;  // pinned mirrors, 2 slots x 3 blocks
+    Scalars* d_sc = nullptr;  // [kScBlocks]: main / outer, inner, utility, column blocks
+    Scalars* h_sc = nullptr;  // [kHostSlots] pinned mirrors
     SweepSync S{};
     unsigned* d_sync = nullptr;
     int* d_err = nullptr;
@@ -109,6 +125,8 @@ struct ocsl_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     bool graphs_on = true;
     int graph_kind = 0;
+    // several right-hand sides of the FP32-inner solver in lockstep (else one by one)
+    bool col_batching = true;
     const void* graph_ptr[6] = {};
 
     // factor of the last solve (buffer and SoA copies), for solves that reuse it
@@ -137,6 +155,7 @@ struct ocsl_ctx {
     void free_all();
     void ensure_reduce(int ntiles);
     void ensure_fp32();
+    void ensure_cols();
 };
 
 void ocsl_ctx::free_pattern()
@@ -163,6 +182,9 @@ void ocsl_ctx::free_pattern()
     d_soa64 = nullptr;
     for (auto pp : d32) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     for (auto& v : v32) { if (v) cudaFree(v); v = nullptr; }
+    if (v64c) cudaFree(v64c);
+    v64c = nullptr;
+    for (auto& v : v32c) { if (v) cudaFree(v); v = nullptr; }
     has_pattern = false;
     P = DevPattern{};
 }
@@ -195,11 +217,11 @@ void ocsl_ctx::ensure_reduce(int ntiles)
     ntiles = std::max(ntiles, 1);
     if (R.partials && R.max_tiles >= ntiles) return;
     if (R.partials) CK(cudaFree(R.partials));
-    R.partials = dalloc<double>((size_t)kMaxDots * ntiles);
+    R.partials = dalloc<double>((size_t)kMaxCols * kMaxDots * ntiles);
     R.max_tiles = ntiles;
     if (!R.counter) {
-        R.counter = dalloc<unsigned>(1);
-        CK(cudaMemset(R.counter, 0, sizeof(unsigned)));
+        R.counter = dalloc<unsigned>(kMaxCols);
+        CK(cudaMemset(R.counter, 0, sizeof(unsigned) * kMaxCols));
     }
 }
 
@@ -212,6 +234,14 @@ void ocsl_ctx::ensure_fp32()
     d_dinv32 = dalloc<float>(n);
     for (auto& v : v32) v = dalloc<float>(n);
     if (hp.box.ok) d_soa32 = dalloc<float>(8 * n);
+}
+
+void ocsl_ctx::ensure_cols()
+{
+    if (v64c) return;
+    const size_t n = (size_t)P.n;
+    v64c = dalloc<double>(kMaxCols * n);
+    for (auto& v : v32c) v = dalloc<float>(kMaxCols * n);
 }
 
 namespace {
@@ -326,31 +356,56 @@ struct Solve {
     const double* matA64 = nullptr;
     const double* recA64 = nullptr;
     const float* recA32 = nullptr;
+    // Column batching: every spmv / vec / sweep of this solve serves cols.n
+    // right-hand sides n elements apart, column q with scalars block k + q;
+    // outer_k is the scalars block the refinement-loop vector ops read.
+    Cols cols{};
+    int outer_k = 0;
 
     Scalars* sc(int k) const { return c->d_sc + k; }
 
+    // Blocks k .. k + count - 1 from the host: tol2[q] (one value when
+    // tol2 has one entry) and the done flag done[q] (none when null).
+    void reset_scalars_n(int k, int count, const double* tol2, const int* done_q,
+                         double omega0 = 1.0)
+    {
+        CK(cudaStreamSynchronize(st));  // the staging slots may still be in flight
+        for (int q = 0; q < count; ++q) {
+            Scalars& s = c->h_sc[kHostStage + k + q];
+            std::memset(&s, 0, sizeof s);
+            s.tol2 = tol2[q];
+            s.alpha = 1.0;
+            s.omega = omega0;
+            s.rhon = 1.0;
+            s.rho = 1.0;
+            s.done = done_q ? done_q[q] : 0;
+        }
+        CK(cudaMemcpyAsync(c->d_sc + k, c->h_sc + kHostStage + k, count * sizeof(Scalars),
+                           cudaMemcpyHostToDevice, st));
+    }
     void reset_scalars(int k, double tol2, double omega0 = 1.0)
     {
-        Scalars s;
-        std::memset(&s, 0, sizeof s);
-        s.tol2 = tol2;
-        s.alpha = 1.0;
-        s.omega = omega0;
-        s.rhon = 1.0;
-        s.rho = 1.0;
-        // pinned staging slots 3..5 are private to these uploads
-        Scalars* stage = c->h_sc + 3 + k;
-        CK(cudaStreamSynchronize(st));  // the staging slot may still be in flight
-        *stage = s;
-        CK(cudaMemcpyAsync(c->d_sc + k, stage, sizeof(Scalars), cudaMemcpyHostToDevice, st));
+        reset_scalars_n(k, 1, &tol2, nullptr, omega0);
     }
-    Scalars read_scalars(int k)
+    const Scalars* read_scalars_n(int k, int count)
     {
-        CK(cudaMemcpyAsync(c->h_sc + k, c->d_sc + k, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(c->h_sc + k, c->d_sc + k, count * sizeof(Scalars),
+                           cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        return c->h_sc[k];
+        return c->h_sc + k;
+    }
+    Scalars read_scalars(int k) { return *read_scalars_n(k, 1); }
+    // Set block k's done flag alone.
+    void mark_done(int k)
+    {
+        CK(cudaStreamSynchronize(st));  // the staging slot may still be in flight
+        Scalars& stage = c->h_sc[kHostStage + k];
+        stage.done = 1;
+        CK(cudaMemcpyAsync(&c->d_sc[k].done, &stage.done, sizeof(int), cudaMemcpyHostToDevice,
+                           st));
     }
     const int* done(int k) const { return &c->d_sc[k].done; }
+    static constexpr int kDoneStride = (int)(sizeof(Scalars) / sizeof(int));
 
     template <typename TT>
     void spmv(const TT* val, const TT* x, TT* y, int mode, const TT* z, TT* ycopy, const TT* w,
@@ -365,10 +420,10 @@ struct Solve {
         }
         if (rec)
             launch_box_spmv<TT>(st, P.n, c->hp.box.dim, rec, x, y, mode, 0.0, z, ycopy, w, dots,
-                                c->R, k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+                                c->R, k >= 0 ? sc(k) : nullptr, epi, it, maxit, cols);
         else
             launch_spmv<TT>(st, P, val, x, y, mode, nullptr, 0.0, z, ycopy, w, dots, c->R,
-                            k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+                            k >= 0 ? sc(k) : nullptr, epi, it, maxit, cols);
     }
     // Stencil records of A for the box SpMV (7-point box patterns); built
     // from the FP64 values, so the FP32 records equal (float)A like A32.
@@ -399,7 +454,8 @@ struct Solve {
         int i = 0;
         for (const void* p : ptrs) vp.v[i++] = const_cast<void*>(p);
         ProfScope ps(c, st, is_f64<TT>() ? PC_VEC64 : PC_VEC32);
-        launch_vec<TT>(st, op, n, vp, c->R, k >= 0 ? sc(k) : nullptr, sc(0), epi, it, maxit);
+        launch_vec<TT>(st, op, n, vp, c->R, k >= 0 ? sc(k) : nullptr, sc(outer_k), epi, it, maxit,
+                       cols);
     }
     // Fixed-point ILU factor (cmatrix_solver.cpp:702-704): M starts as A,
     // `sweeps` Jacobi sweeps; returns the buffer holding the factor.  The
@@ -441,10 +497,24 @@ struct Solve {
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
         if (use_box() && soa<TT>())
-            launch_box_sweep<TT>(st, P.box, P.n, soa<TT>(), rhs, out, true, 0, c->S,
-                                 k >= 0 ? done(k) : nullptr);
+            launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, true, 0, c->S,
+                                 k >= 0 ? done(k) : nullptr, cols, kDoneStride);
         else
-            launch_fw_sweep<TT>(st, P, M, rhs, out, c->S, k >= 0 ? done(k) : nullptr);
+            for (int q = 0; q < cols.n; ++q)  // level-scheduled: one launch per column
+                launch_fw_sweep<TT>(st, P, M, rhs + q * cols.ld, out + q * cols.ld, c->S,
+                                    k >= 0 ? done(k + q) : nullptr);
+    }
+    // The box geometry, narrowed while a CTA's staging for cols.n columns
+    // exceeds the shared-memory limit.
+    template <typename TT>
+    BoxGeom sweep_geom() const
+    {
+        BoxGeom g = P.box;
+        while (box_sweep_smem(g.TA * g.TB, (int)sizeof(TT), cols.n) > kBoxSmemLimit &&
+               g.TA * g.TB > 32)
+            g = g.TB > 1 ? make_box_geom(c->hp.box, g.TA, (g.TB + 1) / 2)
+                         : make_box_geom(c->hp.box, (g.TA + 1) / 2, 1);
+        return g;
     }
     bool use_box() const { return P.box_ok && c->sweep_kernel != 1; }
     // After a factorisation: the structured sweeps read the factor in the
@@ -487,10 +557,22 @@ struct Solve {
         if constexpr (sizeof(TT) == 8) return soa64;
         else return soa32;
     }
+    // A sweep output is filled exactly when the sweep that follows runs, so a
+    // finished column keeps its last vectors (the half step reads them): the
+    // column-batched box sweep runs all columns (a finished column's inputs
+    // no longer change, so it recomputes the same values) until every column
+    // is done; the level-scheduled sweep runs per column.
     template <typename TT>
     void fill_sentinel(TT* out, int k)
     {
-        launch_fill_ones(st, out, sizeof(TT) * (size_t)P.n, k >= 0 ? done(k) : nullptr);
+        const size_t bytes = sizeof(TT) * (size_t)P.n;
+        if (cols.n == 1 || (use_box() && soa<TT>())) {
+            launch_fill_ones(st, out, bytes * cols.n, k >= 0 ? done(k) : nullptr, cols.n,
+                             kDoneStride);
+        } else {
+            for (int q = 0; q < cols.n; ++q)
+                launch_fill_ones(st, out + q * cols.ld, bytes, k >= 0 ? done(k + q) : nullptr);
+        }
     }
     template <typename TT>
     void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k)
@@ -501,11 +583,12 @@ struct Solve {
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
         if (use_box() && soa<TT>())
-            launch_box_sweep<TT>(st, P.box, P.n, soa<TT>(), rhs, out, false, divmode, c->S,
-                                 k >= 0 ? done(k) : nullptr);
+            launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, false, divmode,
+                                 c->S, k >= 0 ? done(k) : nullptr, cols, kDoneStride);
         else
-            launch_bw_sweep<TT>(st, P, M, dinv, rhs, out, divmode, c->S,
-                                k >= 0 ? done(k) : nullptr);
+            for (int q = 0; q < cols.n; ++q)
+                launch_bw_sweep<TT>(st, P, M, dinv, rhs + q * cols.ld, out + q * cols.ld, divmode,
+                                    c->S, k >= 0 ? done(k + q) : nullptr);
     }
     // Enqueue `fn` (a fixed sequence of launches) through a CUDA graph keyed by
     // (kind, ptrs): captured on first use, replayed afterwards.  Returns false
@@ -635,7 +718,8 @@ template <typename F>
 Scalars run_batches(Solve& s, int k, int budget, F&& enqueue, int graph_kind = 0,
                     std::initializer_list<const void*> graph_ptrs = {})
 {
-    Scalars* slot = s.c->h_sc + 6;  // two pinned inspection slots
+    Scalars* slot = s.c->h_sc + kHostInspect;  // two pinned inspection slots of kMaxCols blocks
+    const int nc = s.cols.n;
     int it = 0, issued = 0, inspected = 0;
     while (true) {
         while (issued - inspected < 2 && it < budget) {
@@ -648,14 +732,15 @@ Scalars run_batches(Solve& s, int k, int budget, F&& enqueue, int graph_kind = 0
             if (!graphed)
                 for (int j = 0; j < m; ++j) enqueue(it + j);
             it += m;
-            CK(cudaMemcpyAsync(slot + (issued & 1), s.c->d_sc + k, sizeof(Scalars),
+            CK(cudaMemcpyAsync(slot + (issued & 1) * kMaxCols, s.c->d_sc + k, nc * sizeof(Scalars),
                                cudaMemcpyDeviceToHost, s.st));
             CK(cudaEventRecord(s.c->ev_batch[issued & 1], s.st));
             ++issued;
         }
         if (inspected == issued) break;
         CK(cudaEventSynchronize(s.c->ev_batch[inspected & 1]));
-        const bool done = slot[inspected & 1].done != 0;
+        bool done = true;
+        for (int q = 0; q < nc; ++q) done = done && slot[(inspected & 1) * kMaxCols + q].done != 0;
         ++inspected;
         if (done) break;
     }
@@ -810,6 +895,98 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
         s.reset_scalars(0, tol2);
     }
     res.iters = total;
+    return res;
+}
+
+// Column-batched form of run_bicgstab_ir32: nc (<= kMaxCols) right-hand
+// sides b, x ([nc][n]) of one matrix in lockstep.  Every launch serves all
+// columns -- the SpMV and vector kernels run nc column slices in one grid,
+// the structured sweeps carry nc right-hand sides through one wavefront
+// pass -- while each column keeps its own scalars, adaptive inner tolerance,
+// iteration count and status; a finished column's kernels return at once.
+std::vector<TolResult> run_bicgstab_ir32_cols(Solve& s, const double* A, const double* b,
+                                              double* x, int nc, const ocsl_opts& o)
+{
+    ocsl_ctx* c = s.c;
+    c->ensure_fp32();
+    c->ensure_cols();
+    double* R64 = c->v64c;
+    float** f = c->v32c;
+    const int n = s.n;
+    s.cols = Cols{nc, (long long)n, 0u};
+    s.outer_k = kScOuterCols;
+    const int KO = kScOuterCols, KI = kScInnerCols;
+    std::vector<TolResult> res(nc);
+    std::vector<int> fin(nc, 0), total(nc, 0);
+    std::vector<double> tol2(nc, o.tol * o.tol), itol2(nc, 0.0);
+    s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+    s.prepare_spmv(A, true, true);
+    s.reset_scalars_n(KO, nc, tol2.data(), nullptr);
+    for (int outer = 0;; ++outer) {
+        s.spmv<double>(A, x, R64, 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, KO, EP_TB_INIT);
+        const Scalars* so = s.read_scalars_n(KO, nc);
+        int active = 0, most = 0;
+        for (int q = 0; q < nc; ++q) {
+            if (fin[q]) continue;
+            TolResult& r = res[q];
+            r.relres = so[q].res;
+            r.outer = outer;
+            if (so[q].status) {
+                r.status = so[q].status;
+                fin[q] = 1;
+            } else if (so[q].bb == 0.0) {
+                CK(cudaMemsetAsync(x + (size_t)q * n, 0, sizeof(double) * (size_t)n, s.st));
+                r.relres = 0.0;
+                fin[q] = 1;
+            } else if (so[q].done) {
+                fin[q] = 1;
+            } else if (total[q] >= o.maxit || outer >= 1000) {
+                r.status = OCSL_NOT_CONVERGED;
+                fin[q] = 1;
+            } else {
+                ++active;
+                most = std::max(most, total[q]);
+                itol2[q] = std::max(o.inner_tol, 0.5 * o.tol / so[q].res);
+                itol2[q] *= itol2[q];
+            }
+        }
+        if (active == 0) break;
+        // finished columns: outer and inner blocks done, so every kernel skips
+        // them (the outer blocks keep this residual's norms for the scaling)
+        for (int q = 0; q < nc; ++q)
+            if (fin[q] && !so[q].done) s.mark_done(KO + q);
+        s.reset_scalars_n(KI, nc, itol2.data(), fin.data());
+        s.vec<float>(V_IR_SCALE, {R64, f[F_RI], f[F_RH], f[F_P], f[F_D]}, KI, EP_IR_INNER_INIT);
+        const int budget = std::min(o.inner_maxit, o.maxit - most);
+        run_batches(
+            s, KI, budget,
+            [&](int) {
+                bicgstab_iteration<float>(s, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI],
+                                          f[F_RH], f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH],
+                                          f[F_T], f[F_TMP], KI);
+            },
+            5, {c->d_A32, c->d_M32, s.soa32, s.recA32, c->d_dinv32, (const void*)(intptr_t)nc});
+        const Scalars* sp = s.read_scalars_n(KI, nc);
+        const std::vector<Scalars> si(sp, sp + nc);
+        s.vec<float>(V_TB_HALF, {f[F_D], f[F_PH]}, KI, EP_STORE);
+        s.vec<float>(V_IR_UPDATE, {x, f[F_D]}, -1, EP_STORE);
+        for (int q = 0; q < nc; ++q) {
+            if (fin[q]) continue;
+            total[q] += si[q].iters;
+            if (si[q].status == OCSL_NONFINITE) {
+                res[q].status = OCSL_NONFINITE;
+                fin[q] = 1;
+            } else if (si[q].iters == 0 && !si[q].done) {
+                res[q].status = OCSL_BREAKDOWN;
+                fin[q] = 1;
+            }
+        }
+        // the next residuals reuse the outer blocks: clear done, keep tol2
+        s.reset_scalars_n(KO, nc, tol2.data(), fin.data());
+    }
+    for (int q = 0; q < nc; ++q) res[q].iters = total[q];
+    s.cols = Cols{};
+    s.outer_k = 0;
     return res;
 }
 
@@ -1043,9 +1220,9 @@ int ocsl_create(ocsl_ctx** out, int device)
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
         c->stream = c->own_stream;
-        c->d_sc = dalloc<Scalars>(3);
-        CK(cudaMemset(c->d_sc, 0, 3 * sizeof(Scalars)));
-        CK(cudaMallocHost(&c->h_sc, 8 * sizeof(Scalars)));
+        c->d_sc = dalloc<Scalars>(kScBlocks);
+        CK(cudaMemset(c->d_sc, 0, kScBlocks * sizeof(Scalars)));
+        CK(cudaMallocHost(&c->h_sc, kHostSlots * sizeof(Scalars)));
         c->d_sync = dalloc<unsigned>(2);
         CK(cudaMemset(c->d_sync, 0, 2 * sizeof(unsigned)));
         c->S.ticket = c->d_sync;
@@ -1211,6 +1388,53 @@ int ocsl_solve_device(ocsl_ctx* c, int method, const double* A, const double* b,
     return solve_device_impl(c, method, A, b, x, opts, out);
 }
 
+// nc (2..kMaxCols) right-hand sides of the FP32-inner / FP64-refined solver
+// in lockstep (run_bicgstab_ir32_cols); out[nc].
+int solve_cols_impl(ocsl_ctx* c, const double* A, const double* b, double* x, int nc,
+                    const ocsl_opts* opts, ocsl_result* out, bool reuse_factor)
+{
+    const ocsl_opts o = resolve(opts);
+    if (!A || !b || !x) return fail(c, OCSL_BAD_ARGUMENT, "null value, b or x pointer");
+    if (!aligned8(A) || !aligned8(b) || !aligned8(x))
+        return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
+    Solve s{c, c->stream, c->P, c->P.n};
+    s.reuse = reuse_factor;
+    if (!reuse_factor) c->fac_M = nullptr;
+    int status = OCSL_OK;
+    std::vector<TolResult> t;
+    float ms = 0.f;
+    try {
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+        CK(cudaEventRecord(c->ev_start, c->stream));
+        t = run_bicgstab_ir32_cols(s, A, b, x, nc, o);
+        CK(cudaEventRecord(c->ev_stop, c->stream));
+        CK(cudaEventSynchronize(c->ev_stop));
+        CK(cudaEventElapsedTime(&ms, c->ev_start, c->ev_stop));
+        const int derr = s.device_error();
+        if (derr) status = derr;
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        status = from_cuda(c, e);
+    }
+    for (int q = 0; q < nc; ++q) {
+        ocsl_result r;
+        std::memset(&r, 0, sizeof r);
+        if (q < (int)t.size()) {
+            r.residual = t[q].relres;
+            r.iterations = t[q].iters;
+            r.outer_iterations = t[q].outer;
+            r.status = status != OCSL_OK ? status : t[q].status;
+        } else {
+            r.status = status;
+        }
+        r.solve_ms = ms;
+        if (out) out[q] = r;
+        if (status == OCSL_OK && r.status != OCSL_OK) status = r.status;
+    }
+    if (status == OCSL_TIMEOUT) c->last_error = "a triangular-sweep wait hit its bound";
+    return status;
+}
+
 int ocsl_solve_multi_device(ocsl_ctx* c, int method, const double* A, int nrhs, const double* b,
                             double* x, const ocsl_opts* opts, ocsl_result* out)
 {
@@ -1219,6 +1443,21 @@ int ocsl_solve_multi_device(ocsl_ctx* c, int method, const double* A, int nrhs, 
     if (nrhs < 1) return fail(c, OCSL_BAD_ARGUMENT, "nrhs must be >= 1");
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, OCSL_CUDA_ERROR, "cudaSetDevice");
     const size_t n = (size_t)c->P.n;
+    if (method == OCSL_ILU_BICGSTAB_IR32 && nrhs > 1 && n > 0 && c->col_batching) {
+        // groups of up to kMaxCols columns in lockstep; the factor is built once
+        int first = OCSL_OK;
+        for (int r0 = 0; r0 < nrhs; r0 += kMaxCols) {
+            const int nc = std::min(kMaxCols, nrhs - r0);
+            const double* bq = b ? b + r0 * n : nullptr;
+            double* xq = x ? x + r0 * n : nullptr;
+            ocsl_result* oq = out ? out + r0 : nullptr;
+            const int st = nc == 1 ? solve_device_impl(c, method, A, bq, xq, opts, oq, r0 > 0)
+                                   : solve_cols_impl(c, A, bq, xq, nc, opts, oq, r0 > 0);
+            if (st == OCSL_CUDA_ERROR || st == OCSL_BAD_ARGUMENT) return st;
+            if (first == OCSL_OK) first = st;
+        }
+        return first;
+    }
     int first = OCSL_OK;
     for (int r = 0; r < nrhs; ++r) {
         ocsl_result one;
@@ -1322,7 +1561,7 @@ static int vector_entry(ocsl_ctx* c, size_t n, std::initializer_list<const void*
         Solve s{c, c->stream, c->P, (int)n};
         s.reset_scalars(2, 0.0);
         if (!result) {  // elementwise: a and b ride in the scalars block
-            Scalars* stage = c->h_sc + 5;
+            Scalars* stage = c->h_sc + kHostStage + 2;
             CK(cudaStreamSynchronize(c->stream));
             stage->alpha = a;
             stage->beta = b;
@@ -1444,6 +1683,13 @@ int ocsl_set_graphs(ocsl_ctx* c, int enable)
         c->graph_exec = nullptr;
     }
     if (c->tctx) ocsl_set_graphs(c->tctx, enable);
+    return OCSL_OK;
+}
+
+int ocsl_set_col_batching(ocsl_ctx* c, int enable)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    c->col_batching = enable != 0;
     return OCSL_OK;
 }
 

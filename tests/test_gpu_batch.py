@@ -36,6 +36,66 @@ def test_multi_rhs_equals_separate_solves(ctx, torch_cuda, method):
         assert res[r]["status"] == one["status"] and res[r]["iterations"] == one["iterations"]
 
 
+def _lockstep_vs_one_by_one(ctx, torch, s, B, **opts):
+    """Solve B's columns with the FP32-inner solver in lockstep and one by one;
+    return both results."""
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = torch.from_numpy(s.value).cuda()
+    X1 = torch.zeros_like(B)
+    res1 = ctx.solve_multi_device(ocsl.ILU_BICGSTAB_IR32, A, B, X1, **opts)
+    ctx.set_col_batching(False)
+    X2 = torch.zeros_like(B)
+    res2 = ctx.solve_multi_device(ocsl.ILU_BICGSTAB_IR32, A, B, X2, **opts)
+    ctx.set_col_batching(True)
+    return X1, res1, X2, res2
+
+
+@pytest.mark.parametrize("kind,nrhs", [("hex", 2), ("hex", 3), ("hex", 4), ("hex", 6),
+                                       ("tet", 3)])
+def test_lockstep_columns_equal_one_by_one(ctx, oracle, torch_cuda, kind, nrhs):
+    """Lockstep groups of up to four columns (structured sweeps on the box,
+    one level-scheduled launch per column on tets) give every column the
+    bits and iteration counts of solving it alone."""
+    torch = torch_cuda
+    s = W.hex_pprime(17, 12, 11, peclet=50.0) if kind == "hex" else W.tet_pprime(6, 5, 5)
+    rng = np.random.default_rng(40 + nrhs)
+    B = torch.from_numpy(rng.uniform(-1, 1, (nrhs, s.n))).cuda()
+    X1, res1, X2, res2 = _lockstep_vs_one_by_one(ctx, torch, s, B, tol=1e-10)
+    assert torch.equal(X1, X2)
+    for q in range(nrhs):
+        assert res1[q]["status"] == res2[q]["status"] == 0, (q, res1[q])
+        assert res1[q]["iterations"] == res2[q]["iterations"], q
+        assert res1[q]["outer_iterations"] == res2[q]["outer_iterations"], q
+        rr = oracle.true_relres(s.row_ptr, s.column_index, s.value, B[q].cpu().numpy(),
+                                X1[q].cpu().numpy())
+        assert rr <= 1e-10, (q, rr)
+
+
+def test_lockstep_uneven_columns(ctx, torch_cuda):
+    """Columns that finish at different points: b = 0 (x = 0 at once), a tiny
+    and a large right-hand side, a column with a NaN (its own status only)."""
+    torch = torch_cuda
+    s = W.hex_pprime(15, 13, 10, peclet=10.0)
+    rng = np.random.default_rng(7)
+    B = torch.from_numpy(rng.uniform(-1, 1, (4, s.n))).cuda()
+    B[0].zero_()
+    B[1] *= 1e-12
+    B[2] *= 1e6
+    X1, res1, X2, res2 = _lockstep_vs_one_by_one(ctx, torch, s, B, tol=1e-10)
+    assert torch.equal(X1, X2)
+    assert torch.count_nonzero(X1[0]) == 0 and res1[0]["residual"] == 0.0
+    for q in range(4):
+        assert res1[q]["status"] == res2[q]["status"] == 0
+        assert res1[q]["iterations"] == res2[q]["iterations"]
+    B[3, 17] = float("nan")
+    X3 = torch.zeros_like(B)
+    A = torch.from_numpy(s.value).cuda()
+    res3 = ctx.solve_multi_device(ocsl.ILU_BICGSTAB_IR32, A, B, X3, tol=1e-10)
+    assert res3[3]["status"] == _abi.NONFINITE
+    assert all(res3[q]["status"] == 0 for q in range(3))
+    assert torch.equal(X3[:3], X1[:3])
+
+
 def small_batch():
     return W.batch_systems(4, min_cells=1500, max_cells=25_000)
 
