@@ -324,6 +324,16 @@ int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
 /* The sweep kernel in use (1 level-scheduled, 2 structured), the detected box
  * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB). */
 int ocsl_sweep_info(const ocsl_ctx* ctx, int* kind, int* dims, int* tiles);
+/* Autotuner of the structured sweep's column tile (block shape) for this
+ * pattern and matrix: factors d_value as a solve of `method` would, times a
+ * forward + backward sweep for each candidate tile (16x8, 16x16, 32x4, 32x8,
+ * 8x16, 8x8, 64x2, 64x4, 128x1, 128x2, as clipped to the box) with CUDA
+ * events, and keeps the fastest for later solves (as ocsl_set_sweep_kernel
+ * would).  Reports the tile and its sweep-pair time in microseconds; zeros,
+ * and no change, when the structured kernel does not apply.  The tile does
+ * not change any result. */
+int ocsl_autotune_device(ocsl_ctx* ctx, int method, const double* d_value, int* tile_a,
+                         int* tile_b, double* sweep_us);
 
 /* Allocation-free dot product.  This entry point has no counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc -- code that

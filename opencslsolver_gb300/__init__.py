@@ -279,6 +279,17 @@ class Context:
         self._check(self._L.ocsl_sweep_info(self._h, C.byref(kind), dims, tiles), "sweep_info")
         return {"kind": kind.value, "dims": tuple(dims), "tiles": tuple(tiles)}
 
+    def autotune(self, method, value):
+        """Pick the structured sweep's column tile for this matrix by timing the
+        candidates (value: CUDA tensor of A); returns {"tiles": (TA, TB),
+        "sweep_us": t}, tiles (0, 0) when nothing applies."""
+        self._follow_torch()
+        ta, tb, us = C.c_int(), C.c_int(), C.c_double()
+        self._check(self._L.ocsl_autotune_device(self._h, _method(method), _dptr(value),
+                                                 C.byref(ta), C.byref(tb), C.byref(us)),
+                    "autotune")
+        return {"tiles": (ta.value, tb.value), "sweep_us": us.value}
+
     def set_graphs(self, enable: bool = True):
         """Replay iteration batches from CUDA graphs (default on)."""
         self._check(self._L.ocsl_set_graphs(self._h, int(bool(enable))), "set_graphs")

@@ -153,6 +153,8 @@ _PROTOS = {
     "ocsl_noalloc_last_error": (C.c_char_p, []),
     "ocsl_set_graphs": (C.c_int, [_CTX, C.c_int]),
     "ocsl_set_col_batching": (C.c_int, [_CTX, C.c_int]),
+    "ocsl_autotune_device": (C.c_int, [_CTX, C.c_int, C.c_void_p, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "ocsl_profile_enable": (C.c_int, [_CTX, C.c_int]),
     "ocsl_profile_read": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "ocsl_profile_category_name": (C.c_char_p, [C.c_int]),

@@ -1661,6 +1661,92 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
     return OCSL_OK;
 }
 
+int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, int* tile_b,
+                         double* sweep_us)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (tile_a) *tile_a = 0;
+    if (tile_b) *tile_b = 0;
+    if (sweep_us) *sweep_us = 0.0;
+    if (method < OCSL_CG_REF || method > OCSL_ILU_BICGSTAB_IR32)
+        return fail(c, OCSL_BAD_ARGUMENT, "unknown method");
+    if (!A || !aligned8(A)) return fail(c, OCSL_BAD_ARGUMENT, "null or misaligned value pointer");
+    if (!c->hp.box.ok || c->sweep_kernel == 1 || c->P.n == 0 || method == OCSL_CG_REF ||
+        method == OCSL_PCG)
+        return OCSL_OK;  // no structured sweep to tune
+    const bool fp32 = method == OCSL_ILU_BICGSTAB_IR32;
+    const bool ref = method == OCSL_CG_REF || method == OCSL_BICGSTAB_REF;
+    const ocsl_opts o = resolve(nullptr);
+    // candidate column tiles (one thread per column, at most 256)
+    static const int kCand[][2] = {{16, 8}, {16, 16}, {32, 4}, {32, 8}, {8, 16},
+                                   {8, 8},  {64, 2},  {64, 4}, {128, 1}, {128, 2}};
+    const BoxGeom keep = c->P.box;
+    try {
+        CK(cudaSetDevice(c->device));
+        Solve s{c, c->stream, c->P, c->P.n};
+        c->fac_M = nullptr;
+        if (fp32) c->ensure_fp32();
+        // the factor and stencil records a solve of `method` sweeps with
+        s.factored(A, o.ilu_sweeps, !ref, fp32, -1, !fp32, !ref, fp32);
+        const size_t n = (size_t)c->P.n;
+        auto pair = [&] {  // one forward + backward sweep of a zero rhs
+            if (fp32) {
+                s.fw<float>(c->d_M32, c->v32[F_P], c->v32[F_TMP], -1);
+                s.bw<float>(c->d_M32, c->d_dinv32, c->v32[F_TMP], c->v32[F_PH], 1, -1);
+            } else {
+                s.fw<double>(c->fac_M, c->v64[P], c->v64[TMP], -1);
+                s.bw<double>(c->fac_M, c->d_dinv, c->v64[TMP], c->v64[PH], ref ? 0 : 1, -1);
+            }
+        };
+        if (fp32)
+            CK(cudaMemsetAsync(c->v32[F_P], 0, sizeof(float) * n, c->stream));
+        else
+            CK(cudaMemsetAsync(c->v64[P], 0, sizeof(double) * n, c->stream));
+        double best = 1e300;
+        BoxGeom bestg = keep;
+        std::vector<std::pair<int, int>> tried;
+        for (const auto& cd : kCand) {
+            const BoxGeom g = make_box_geom(c->hp.box, cd[0], cd[1]);
+            const std::pair<int, int> key{g.TA, g.TB};
+            if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
+            tried.push_back(key);
+            c->P.box = g;
+            pair();  // warm-up
+            double t = 1e300;
+            for (int rep = 0; rep < 3; ++rep) {
+                CK(cudaEventRecord(c->ev_start, c->stream));
+                pair();
+                CK(cudaEventRecord(c->ev_stop, c->stream));
+                CK(cudaEventSynchronize(c->ev_stop));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, c->ev_start, c->ev_stop));
+                t = std::min(t, 1000.0 * ms);
+            }
+            if (s.device_error()) {
+                c->P.box = keep;
+                return fail(c, OCSL_TIMEOUT, "a triangular-sweep wait hit its bound");
+            }
+            if (t < best) {
+                best = t;
+                bestg = g;
+            }
+        }
+        c->P.box = bestg;
+        c->box_tile[0] = bestg.TA;
+        c->box_tile[1] = bestg.TB;
+        c->fac_M = nullptr;
+        if (tile_a) *tile_a = bestg.TA;
+        if (tile_b) *tile_b = bestg.TB;
+        if (sweep_us) *sweep_us = best;
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        c->P.box = keep;
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
 int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
 {
     if (!c) return OCSL_BAD_ARGUMENT;

@@ -292,3 +292,26 @@ def test_graph_replay_gives_identical_solves(ctx, torch_cuda, method):
             out[graphs] = res
     for (x1, i1), (x2, i2) in zip(out[True], out[False]):
         assert i1 == i2 and np.array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("method", [ocsl.ILU_BICGSTAB_IR32, ocsl.ILU_BICGSTAB, ocsl.BICGSTAB_REF])
+def test_autotuned_tile_gives_identical_solves(ctx, torch_cuda, method):
+    """ocsl_autotune_device picks one of its candidate tiles, keeps it for the
+    next solves, and the solve's bits do not depend on it."""
+    torch = torch_cuda
+    s = W.hex_pprime(40, 36, 33)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = torch.from_numpy(s.value).cuda()
+    B = torch.from_numpy(s.b).cuda()
+    X0 = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    r0 = ctx.solve_device(method, A, B, X0)
+    t = ctx.autotune(method, A)
+    assert t["sweep_us"] > 0 and t["tiles"][0] * t["tiles"][1] <= 256, t
+    assert ctx.sweep_info()["tiles"] == t["tiles"]
+    X1 = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    r1 = ctx.solve_device(method, A, B, X1)
+    assert torch.equal(X0, X1) and r0["iterations"] == r1["iterations"]
+    # nothing to tune: Jacobi PCG, level-scheduled sweeps
+    assert ctx.autotune(ocsl.PCG, A)["tiles"] == (0, 0)
+    ctx.set_sweep_kernel(1)
+    assert ctx.autotune(method, A)["tiles"] == (0, 0)
