@@ -336,10 +336,12 @@ int ocsl_autotune_device(ocsl_ctx* ctx, int method, const double* d_value, int* 
                          int* tile_b, double* sweep_us);
 
 /* Allocation-free dot product.  This entry point has no counterpart in the
- * reference: it exists for callers that cannot call cudaMalloc -- code that
- * runs while a CUDA stream is being captured in global mode (where
- * cudaMalloc is a prohibited call) and programs whose device memory is
- * reserved up front by another allocator, so that a cudaMalloc would fail.
+ * reference: it exists for callers that cannot call cudaMalloc -- programs
+ * whose device memory is reserved up front by another allocator (a
+ * framework's caching pool, a fixed budget taken at start-up), so that a
+ * cudaMalloc would fail, and hosts whose plugins may not allocate or free
+ * device memory while they run, because cudaMalloc and cudaFree can
+ * synchronise the device and stall the host's other streams.
  * It needs no context and allocates nothing: its scratch is a fixed
  * 32,832-byte device array that every GPU loading this library keeps until
  * exit.  Computes <x, y> over n <= 8,388,608 elements (larger n:

@@ -1,10 +1,10 @@
 // ocsl_dot_noalloc: the dot product of ocsl_dot_device without any device
-// allocation, for callers that cannot call cudaMalloc -- code that runs
-// while a CUDA stream is being captured in global mode (where cudaMalloc is
-// a prohibited, potentially synchronising call), and host programs whose
-// device memory is entirely reserved up front by another allocator (a
+// allocation, for callers that cannot call cudaMalloc -- host programs
+// whose device memory is entirely reserved up front by another allocator (a
 // framework's caching pool, a fixed embedded budget), where a cudaMalloc
-// would fail.  No context is needed either.
+// would fail, and hosts whose plugins may not allocate or free device memory
+// while they run, because cudaMalloc and cudaFree can synchronise the device
+// and stall the host's other streams.  No context is needed either.
 //
 // The per-tile partial sums and the completion counter live in one
 // file-scope __device__ array of fixed size, so every GPU that loads this

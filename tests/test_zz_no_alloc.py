@@ -1,9 +1,9 @@
 """The allocation-free entry point, ocsl_dot_noalloc.
 
-It serves callers that cannot call cudaMalloc (code running under a
-global-mode stream capture, or hosts whose device memory another allocator
-has already reserved): its scratch is a fixed device array inside the
-library.  This test calls it through the C ABI twice in a row on the same
+It serves callers that cannot call cudaMalloc (hosts whose device memory
+another allocator has already reserved, or whose plugins may not allocate
+because cudaMalloc and cudaFree can synchronise the device): its scratch is a
+fixed device array inside the library.  This test calls it through the C ABI twice in a row on the same
 inputs and checks each result against the context-based ocsl_dot_device.
 Both use the same fixed reduction order, so the tolerance is 0 (bit-equal).
 The file name makes pytest collect it last; it passes alone or after the
