@@ -321,15 +321,28 @@ int ocsl_bc_value_grad_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
  * tile, one thread per column, at most 256 (0 = default 16 x 8).  All
  * kernels give bit-identical results. */
 int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
+/* Thread-block clusters of the structured sweep: cx x cy neighbouring column
+ * tiles (cx * cy <= 16; 1 x 1 = none, the default) run as one cluster and
+ * pass their face values through distributed shared memory instead of global
+ * memory.  Clipped to the tile grid; a shape the device cannot schedule, or
+ * whose face buffers (columns x s-extent x (TA + TB) values) do not fit the
+ * shared memory, runs as single tiles.  Results are bit-identical for every
+ * shape.  No reference counterpart (the reference sweeps serially,
+ * cmatrix_solver.cpp:555-611). */
+int ocsl_set_sweep_cluster(ocsl_ctx* ctx, int cx, int cy);
+/* The cluster shape in use (after clipping; 0 x 0 when no structured sweep). */
+int ocsl_sweep_cluster_info(const ocsl_ctx* ctx, int* cx, int* cy);
 /* The sweep kernel in use (1 level-scheduled, 2 structured), the detected box
  * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB). */
 int ocsl_sweep_info(const ocsl_ctx* ctx, int* kind, int* dims, int* tiles);
 /* Autotuner of the structured sweep's column tile (block shape) for this
  * pattern and matrix: factors d_value as a solve of `method` would, times a
  * forward + backward sweep for each candidate tile (16x8, 16x16, 32x4, 32x8,
- * 8x16, 8x8, 64x2, 64x4, 128x1, 128x2, as clipped to the box) with CUDA
- * events, and keeps the fastest for later solves (as ocsl_set_sweep_kernel
- * would).  Reports the tile and its sweep-pair time in microseconds; zeros,
+ * 8x16, 8x8, 64x2, 64x4, 128x1, 128x2, as clipped to the box), each alone
+ * and in clusters of 2x2, 4x2, 2x4 and 4x4 tiles, with CUDA events, and
+ * keeps the fastest for later solves (as ocsl_set_sweep_kernel and
+ * ocsl_set_sweep_cluster would; ocsl_sweep_cluster_info reports the cluster).
+ * Reports the tile and its sweep-pair time in microseconds; zeros,
  * and no change, when the structured kernel does not apply.  The tile does
  * not change any result. */
 int ocsl_autotune_device(ocsl_ctx* ctx, int method, const double* d_value, int* tile_a,

@@ -272,12 +272,21 @@ class Context:
         """0 automatic, 1 level-scheduled, 2 structured (7-point box patterns)."""
         self._check(self._L.ocsl_set_sweep_kernel(self._h, kind, tile_a, tile_b), "sweep kernel")
 
+    def set_sweep_cluster(self, cx: int = 1, cy: int = 1):
+        """Run the structured sweep's column tiles in thread-block clusters of
+        cx x cy tiles (faces through distributed shared memory); 1 x 1 = none."""
+        self._check(self._L.ocsl_set_sweep_cluster(self._h, cx, cy), "sweep cluster")
+
     def sweep_info(self):
         kind = C.c_int()
         dims = (C.c_int * 3)()
         tiles = (C.c_int * 2)()
         self._check(self._L.ocsl_sweep_info(self._h, C.byref(kind), dims, tiles), "sweep_info")
-        return {"kind": kind.value, "dims": tuple(dims), "tiles": tuple(tiles)}
+        cx, cy = C.c_int(), C.c_int()
+        self._check(self._L.ocsl_sweep_cluster_info(self._h, C.byref(cx), C.byref(cy)),
+                    "sweep_cluster_info")
+        return {"kind": kind.value, "dims": tuple(dims), "tiles": tuple(tiles),
+                "cluster": (cx.value, cy.value)}
 
     def autotune(self, method, value):
         """Pick the structured sweep's column tile for this matrix by timing the
@@ -288,7 +297,8 @@ class Context:
         self._check(self._L.ocsl_autotune_device(self._h, _method(method), _dptr(value),
                                                  C.byref(ta), C.byref(tb), C.byref(us)),
                     "autotune")
-        return {"tiles": (ta.value, tb.value), "sweep_us": us.value}
+        return {"tiles": (ta.value, tb.value), "sweep_us": us.value,
+                "cluster": self.sweep_info()["cluster"]}
 
     def set_graphs(self, enable: bool = True):
         """Replay iteration batches from CUDA graphs (default on)."""

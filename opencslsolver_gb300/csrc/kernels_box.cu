@@ -21,7 +21,21 @@
 // first, so waits cannot deadlock.  The output was filled with an all-ones
 // pattern, so a face value is its own ready flag (bounded wait, OCSL_TIMEOUT
 // on expiry).
+//
+// Clusters.  With BoxGeom CX x CY > 1 the tiles are grouped into
+// thread-block clusters of CX x CY neighbouring tiles (one CTA each, all
+// co-resident by the hardware's guarantee).  Inside a cluster a tile hands
+// its face values to its downstream neighbours through distributed shared
+// memory: the producing thread stores each value straight into the
+// consumer's face buffer (one slot per s row, sentinel-initialised before a
+// cluster barrier), and the consumer polls its own shared memory, so a hop
+// costs a DSMEM store instead of an L2 store plus L2 polls.  Faces between
+// clusters keep the global value-as-flag path, and clusters take tickets in
+// the same dependency order as single tiles.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "ocsl_internal.cuh"
 
 namespace ocsl {
@@ -51,6 +65,17 @@ struct Bits<double> {
     {
         asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v));
     }
+    // own shared memory written by cluster peers / a peer's shared memory
+    static __device__ __forceinline__ U load_local(unsigned saddr)
+    {
+        U v;
+        asm volatile("ld.relaxed.cluster.shared::cta.b64 %0, [%1];" : "=l"(v) : "r"(saddr));
+        return v;
+    }
+    static __device__ __forceinline__ void store_remote(unsigned caddr, U v)
+    {
+        asm volatile("st.relaxed.cluster.shared::cluster.b64 [%0], %1;" ::"r"(caddr), "l"(v));
+    }
     static __device__ __forceinline__ U to(double x) { return (U)__double_as_longlong(x); }
     static __device__ __forceinline__ double from(U u) { return __longlong_as_double((long long)u); }
 };
@@ -68,6 +93,16 @@ struct Bits<float> {
     static __device__ __forceinline__ void store(float* p, U v)
     {
         asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v));
+    }
+    static __device__ __forceinline__ U load_local(unsigned saddr)
+    {
+        U v;
+        asm volatile("ld.relaxed.cluster.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(saddr));
+        return v;
+    }
+    static __device__ __forceinline__ void store_remote(unsigned caddr, U v)
+    {
+        asm volatile("st.relaxed.cluster.shared::cluster.b32 [%0], %1;" ::"r"(caddr), "r"(v));
     }
     static __device__ __forceinline__ U to(float x) { return __float_as_uint(x); }
     static __device__ __forceinline__ float from(U u) { return __uint_as_float(u); }
@@ -101,6 +136,60 @@ __device__ __forceinline__ void publish(T* p, T v)
     typename B::U u = B::to(v);
     if (u == B::kSentinel) u = B::kCanonicalNaN;
     B::store(p, u);
+}
+
+// Face value from the cluster peer upstream: poll this CTA's own slot
+// (bounded; OCSL_TIMEOUT and a NaN on expiry).
+template <typename T>
+__device__ __noinline__ T wait_local_slow(unsigned saddr, int* err)
+{
+    using B = Bits<T>;
+    for (long it = 0; it < kSpinLimit; ++it) {
+        const typename B::U u = B::load_local(saddr);
+        if (u != B::kSentinel) return B::from(u);
+        if ((it & 255) == 255 && *((volatile int*)err) != 0) break;
+    }
+    atomicCAS(err, 0, (int)OCSL_TIMEOUT);
+    return B::from(B::kCanonicalNaN);
+}
+template <typename T>
+__device__ __forceinline__ T wait_local(const T* slot, int* err)
+{
+    using B = Bits<T>;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(slot);
+    const typename B::U u = B::load_local(a);
+    return u != B::kSentinel ? B::from(u) : wait_local_slow<T>(a, err);
+}
+__device__ __forceinline__ unsigned cluster_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// Every thread of every CTA of the cluster; release / acquire order shared
+// memory writes before it against peers' accesses after it.
+__device__ __forceinline__ void cluster_barrier()
+{
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+// The shared::cluster address of `local` (this CTA's shared memory) in CTA `rank`.
+__device__ __forceinline__ unsigned peer_addr(const void* local, unsigned rank)
+{
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(r)
+                 : "r"((unsigned)__cvta_generic_to_shared(local)), "r"(rank));
+    return r;
+}
+// Hand value v (the sentinel bit pattern mapped to a NaN, as publish does)
+// to the same slot of CTA `rank`.
+template <typename T>
+__device__ __forceinline__ void push_peer(const T* local_slot, unsigned rank, T v)
+{
+    using B = Bits<T>;
+    typename B::U u = B::to(v);
+    if (u == B::kSentinel) u = B::kCanonicalNaN;
+    B::store_remote(peer_addr(local_slot, rank), u);
 }
 
 // Asynchronous global -> shared copies (one element per lane).  `.ca` may
@@ -206,17 +295,44 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const BoxGeom& g = p.g;
     const int TA = g.TA, TB = g.TB, NT = g.TA * g.TB;
+    const bool clus = g.CX * g.CY > 1;  // uniform over the grid
     using V4 = Vec4<T>;
     V4* coef = reinterpret_cast<V4*>(smem_raw);         // [kPF][NT] packed row records
     T* ring = reinterpret_cast<T*>(coef + kPF * NT);    // [2][NC][NT]
     T* srhs = ring + 2 * NC * NT;                       // [kPF][NC][NT] rhs
+    // clusters only: values of the upstream tiles' faces, one slot per s row
+    T* faceA = srhs + kPF * NC * NT;                    // [NC][Ds][TB] from tile (ta - 1, tb)
+    T* faceB = faceA + (clus ? NC * g.D[2] * TB : 0);   // [NC][Ds][TA] from tile (ta, tb - 1)
     __shared__ int s_tile;
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
-    __syncthreads();
-    const int tile = s_tile;
-    if (tile >= g.nta * g.ntb) {
-        if (threadIdx.x == 0) atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
+    int tile = -1;  // ta + tb * nta; -1: a CTA of a partial cluster with no tile
+    bool overflow = false;
+    unsigned rank = 0;
+    if (!clus) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
+        __syncthreads();
+        tile = s_tile;
+        overflow = tile >= g.nta * g.ntb;
     } else {
+        rank = cluster_rank();
+        if (rank == 0 && threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
+        using U = typename Bits<T>::U;
+        U* fu = reinterpret_cast<U*>(faceA);
+        const int nface = NC * g.D[2] * (TA + TB);
+        for (int i = threadIdx.x; i < nface; i += blockDim.x) fu[i] = Bits<T>::kSentinel;
+        // faces initialised and rank 0's ticket written before any peer access
+        cluster_barrier();
+        int blk;
+        asm volatile("ld.shared::cluster.b32 %0, [%1];" : "=r"(blk) : "r"(peer_addr(&s_tile, 0)));
+        overflow = blk >= g.nca * g.ncb;
+        if (!overflow) {
+            const int ta = (blk % g.nca) * g.CX + (int)rank % g.CX;
+            const int tb = (blk / g.nca) * g.CY + (int)rank / g.CX;
+            if (ta < g.nta && tb < g.ntb) tile = ta + tb * g.nta;
+        }
+    }
+    if (overflow) {
+        if (threadIdx.x == 0) atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
+    } else if (tile >= 0) {
         using B = Bits<T>;
         using U = typename B::U;
         const int tid = threadIdx.x;
@@ -224,6 +340,10 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
         const int la = tid % TA, lb = tid / TA;
         const int ca = ta * TA + la, cb = tb * TB + lb;
         const int Da = g.D[0], Db = g.D[1], Ds = g.D[2];
+        // cluster position; an upstream / downstream tile inside the cluster
+        // exchanges faces through shared memory
+        const int rx = (int)rank % g.CX, ry = (int)rank / g.CX;
+        const bool loc_a = clus && rx > 0, loc_b = clus && ry > 0;
         const bool col_ok = ca < Da && cb < Db;
         const int a = FWD ? ca : Da - 1 - ca;
         const int b = FWD ? cb : Db - 1 - cb;
@@ -235,8 +355,12 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
         const int W0 = ta * TA + tb * TB;
         const int W1 = (ta_end - 1) + (tb_end - 1) + Ds - 1;
         const bool has_a = ca > 0, has_b = cb > 0;
-        const bool face_a = col_ok && has_a && la == 0;
-        const bool face_b = col_ok && has_b && lb == 0;
+        // face_*: the neighbour is in the upstream tile, read through global memory
+        const bool face_a = col_ok && has_a && la == 0 && !loc_a;
+        const bool face_b = col_ok && has_b && lb == 0 && !loc_b;
+        // push_*: this column is the face of a downstream tile of the cluster
+        const bool push_a = clus && col_ok && la == TA - 1 && rx < g.CX - 1 && ta + 1 < g.nta;
+        const bool push_b = clus && col_ok && lb == TB - 1 && ry < g.CY - 1 && tb + 1 < g.ntb;
         const int off_a = dstep * g.S[0], off_b = dstep * g.S[1];
         const int c0 = ca + cb;  // the thread sweeps row cs = W - c0 at wavefront W
         const V4* pack = reinterpret_cast<const V4*>(p.soa) + (FWD ? 0 : p.n);
@@ -304,6 +428,8 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
                         if (has_a) {
                             if (la > 0)
                                 va = rd[tid - 1];
+                            else if (loc_a)
+                                va = wait_local(faceA + (q * Ds + cs) * TB + lb, p.S.err);
                             else
                                 va = fa[jf][q] != B::kSentinel
                                          ? B::from(fa[jf][q])
@@ -312,6 +438,8 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
                         if (has_b) {
                             if (lb > 0)
                                 vb = rd[tid - TA];
+                            else if (loc_b)
+                                vb = wait_local(faceB + (q * Ds + cs) * TA + la, p.S.err);
                             else
                                 vb = fb[jf][q] != B::kSentinel
                                          ? B::from(fb[jf][q])
@@ -329,6 +457,8 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
                         const T num = srhs[(j * NC + q) * NT + tid] - sum;
                         const T y = FWD ? num : (DIV ? num / cf.v[3] : num * cf.v[3]);
                         ring[((W & 1) * NC + q) * NT + tid] = y;
+                        if (push_a) push_peer(faceA + (q * Ds + cs) * TB + lb, rank + 1, y);
+                        if (push_b) push_peer(faceB + (q * Ds + cs) * TA + la, rank + g.CX, y);
                         publish(out_q[q] + r, y);
                         prev[q] = y;
                     }
@@ -351,6 +481,8 @@ __global__ void __launch_bounds__(256) box_cta_kernel(BoxParams<T> p)
         cp_async_wait<0>();
     }
     __syncthreads();
+    // no CTA leaves while a peer may still store into its faces
+    if (clus) cluster_barrier();
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(p.S.finished, 1u) == gridDim.x - 1) {
@@ -390,20 +522,91 @@ __global__ void box_to_soa_kernel(int n, int nx, int ny, int nz, const int* rp, 
     hi[3] = (TO)v[3];
 }
 
-template <typename T, bool FWD, bool DIV, int SPAN, int NC>
-void launch_one(cudaStream_t st, const BoxParams<T>& p)
+// Whether a cluster launch of `kern` with this shape can run on the device
+// at all (cudaOccupancyMaxActiveClusters > 0), cached per shape.
+template <typename K>
+bool cluster_fits(K kern, int grid, int threads, size_t smem, int csize)
 {
-    const int grid = p.g.nta * p.g.ntb;
-    const int threads = p.g.TA * p.g.TB;
-    const size_t smem = box_sweep_smem(threads, (int)sizeof(T), NC);
-    static bool attr_set = false;  // one opt-in per instantiation
-    if (!attr_set) {
-        const size_t most = std::min(box_sweep_smem(256, (int)sizeof(T), NC), kBoxSmemLimit);
-        cudaFuncSetAttribute(box_cta_kernel<T, FWD, DIV, SPAN, NC>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
-        attr_set = true;
+    static std::mutex mu;
+    static std::map<std::tuple<int, size_t, int>, bool> seen;
+    const auto key = std::make_tuple(threads, smem, csize);
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = seen.find(key);
+    if (it != seen.end()) return it->second;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, kern, &cfg);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();  // a refused query leaves no sticky error
+        return false;              // not cached: the query may succeed later
     }
-    box_cta_kernel<T, FWD, DIV, SPAN, NC><<<grid, threads, smem, st>>>(p);
+    seen[key] = n > 0;
+    return n > 0;
+}
+
+// Dynamic shared memory above half of an SM's 228 KB (less the 1 KB each CTA
+// reserves): no second CTA fits beside it.
+constexpr size_t kBoxSmemOneCta = 116 * 1024;
+
+template <typename T, bool FWD, bool DIV, int SPAN, int NC>
+void launch_one(cudaStream_t st, BoxParams<T> p)
+{
+    auto kern = box_cta_kernel<T, FWD, DIV, SPAN, NC>;
+    static std::once_flag once;  // one opt-in per instantiation
+    std::call_once(once, [&] {
+        // static + dynamic shared memory must stay within the opt-in limit
+        cudaFuncAttributes fa{};
+        size_t stat = 1024;
+        bool failed = cudaFuncGetAttributes(&fa, kern) != cudaSuccess;
+        if (!failed) stat = fa.sharedSizeBytes;
+        failed |= cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(kBoxSmemOptin - stat)) != cudaSuccess;
+        failed |= cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                  cudaSuccess;
+        if (failed) (void)cudaGetLastError();  // the launch itself reports what matters
+    });
+    const int threads = p.g.TA * p.g.TB;
+    int csize = p.g.CX * p.g.CY;
+    size_t smem = box_sweep_smem(p.g, (int)sizeof(T), NC);
+    if (csize > 1) {
+        // one CTA per SM: a cluster's CTAs may otherwise be packed two to an
+        // SM, which doubles that SM's work per wavefront
+        smem = std::max(smem, kBoxSmemOneCta);
+        const int grid = p.g.nca * p.g.ncb * csize;
+        if (smem > kBoxSmemLimit || !cluster_fits(kern, grid, threads, smem, csize)) {
+            p.g = box_with_cluster(p.g, 1, 1);  // the shape cannot run: single tiles
+            csize = 1;
+            smem = box_sweep_smem(p.g, (int)sizeof(T), NC);
+        }
+    }
+    const int grid = p.g.nca * p.g.ncb * csize;
+    if (csize == 1) {
+        kern<<<grid, threads, smem, st>>>(p);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, p);
 }
 
 template <typename T, bool FWD, bool DIV, int NC>
@@ -433,6 +636,30 @@ size_t box_sweep_smem(int threads, int elem_size, int ncols)
 {
     const size_t per = (size_t)4 * elem_size * kPF + (size_t)elem_size * ncols * (2 + kPF);
     return per * (size_t)threads;
+}
+
+size_t box_sweep_smem(const BoxGeom& g, int elem_size, int ncols)
+{
+    size_t b = box_sweep_smem(g.TA * g.TB, elem_size, ncols);
+    if (g.CX * g.CY > 1) b += (size_t)elem_size * ncols * g.D[2] * (g.TA + g.TB);
+    return b;
+}
+
+BoxGeom box_with_cluster(BoxGeom g, int cx, int cy)
+{
+    cx = std::max(1, std::min(cx, g.nta));
+    cy = std::max(1, std::min(cy, g.ntb));
+    while (cx * cy > kMaxClusterTiles) {
+        if (cx >= cy)
+            --cx;
+        else
+            --cy;
+    }
+    g.CX = cx;
+    g.CY = cy;
+    g.nca = (g.nta + cx - 1) / cx;
+    g.ncb = (g.ntb + cy - 1) / cy;
+    return g;
 }
 
 template <typename T>

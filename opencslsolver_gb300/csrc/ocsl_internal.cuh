@@ -88,6 +88,10 @@ struct BoxGeom {
     int order[3];  // dims by descending stride = CSR order of the lower entries
     int span;      // which of x (0), y (1), z (2) is the spanned dimension s
     int TA, TB, nta, ntb;
+    // Thread-block clusters of CX x CY neighbouring tiles (1 x 1: none).  A
+    // tile hands its face values to a downstream tile of the same cluster
+    // through distributed shared memory; nca x ncb clusters cover the tiles.
+    int CX, CY, nca, ncb;
 };
 
 struct DevPattern {
@@ -208,7 +212,15 @@ void launch_box_sweep(cudaStream_t st, const BoxGeom& g, int n, const T* soa, co
 // (records and rhs staged kPF wavefronts ahead, a two-slot ring per column);
 // a launch needs it <= kBoxSmemLimit.
 size_t box_sweep_smem(int threads, int elem_size, int ncols);
-constexpr size_t kBoxSmemLimit = 227 * 1024;
+constexpr size_t kBoxSmemOptin = 227 * 1024;            // per-block opt-in maximum
+constexpr size_t kBoxSmemLimit = kBoxSmemOptin - 1024;   // dynamic part, static kept below 1 KB
+// The same for geometry g, including a clustered tile's two face buffers
+// (ncols x s-extent x (TA + TB) values).
+size_t box_sweep_smem(const BoxGeom& g, int elem_size, int ncols);
+constexpr int kMaxClusterTiles = 16;
+// g with clusters of cx x cy tiles (clipped to the tile grid and to 16
+// tiles; 1 x 1 = no clusters).
+BoxGeom box_with_cluster(BoxGeom g, int cx, int cy);
 // CSR factor (FP64) -> packed stencil records in TO; diagonal term =
 // diagonal, or 1/diagonal with recip.
 template <typename TO>

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -119,6 +120,7 @@ struct ocsl_ctx {
     // sweep kernel choice (ocsl_set_sweep_kernel): 0 auto, 1 level-scheduled, 2 structured
     int sweep_kernel = 0;
     int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
+    int box_cluster[2] = {1, 1};  // tiles per thread-block cluster (ocsl_set_sweep_cluster)
 
     // CUDA graph of one batch of Krylov iterations, reused while its key
     // (method and the pointers the iterations read) stays the same
@@ -340,7 +342,7 @@ BoxGeom make_box_geom(const BoxShape& bs, int TA_req, int TB_req)
     g.TB = std::min(tb_, std::max(1, g.D[1]));
     g.nta = (g.D[0] + g.TA - 1) / g.TA;
     g.ntb = (g.D[1] + g.TB - 1) / g.TB;
-    return g;
+    return box_with_cluster(g, 1, 1);
 }
 
 struct Solve {
@@ -510,6 +512,8 @@ struct Solve {
     BoxGeom sweep_geom() const
     {
         BoxGeom g = P.box;
+        if (box_sweep_smem(g, (int)sizeof(TT), cols.n) > kBoxSmemLimit)
+            g = box_with_cluster(g, 1, 1);  // face buffers first
         while (box_sweep_smem(g.TA * g.TB, (int)sizeof(TT), cols.n) > kBoxSmemLimit &&
                g.TA * g.TB > 32)
             g = g.TB > 1 ? make_box_geom(c->hp.box, g.TA, (g.TB + 1) / 2)
@@ -1088,6 +1092,7 @@ int ensure_transpose(ocsl_ctx* c)
     int rc = ocsl_create(&t, c->device);
     if (rc != OCSL_OK) return fail(c, rc, "adjoint context: " + g_create_error);
     ocsl_set_sweep_kernel(t, c->sweep_kernel, c->box_tile[0], c->box_tile[1]);
+    ocsl_set_sweep_cluster(t, c->box_cluster[0], c->box_cluster[1]);
     t->graphs_on = c->graphs_on;
     rc = ocsl_set_pattern(t, (size_t)n, trp.data(), tcol.data());
     if (rc != OCSL_OK) {
@@ -1301,7 +1306,9 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         P.bw_chunk = c->d_pat[9];
         P.bw_nchunks = (int)hp.bw_chunk.size() - 1;
         P.box_ok = hp.box.ok && c->sweep_kernel != 1;
-        if (hp.box.ok) P.box = make_box_geom(hp.box, c->box_tile[0], c->box_tile[1]);
+        if (hp.box.ok)
+            P.box = box_with_cluster(make_box_geom(hp.box, c->box_tile[0], c->box_tile[1]),
+                                     c->box_cluster[0], c->box_cluster[1]);
         c->hp.box = hp.box;
         const size_t nn = (size_t)hp.n, nz = (size_t)hp.nnz;
         c->d_A = dalloc<double>(nz);
@@ -1656,8 +1663,29 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
     c->box_tile[1] = tile_b;
     if (c->has_pattern) {
         c->P.box_ok = c->hp.box.ok && kind != 1;
-        if (c->hp.box.ok) c->P.box = make_box_geom(c->hp.box, tile_a, tile_b);
+        if (c->hp.box.ok)
+            c->P.box = box_with_cluster(make_box_geom(c->hp.box, tile_a, tile_b),
+                                        c->box_cluster[0], c->box_cluster[1]);
     }
+    return OCSL_OK;
+}
+
+int ocsl_set_sweep_cluster(ocsl_ctx* c, int cx, int cy)
+{
+    if (!c || cx < 1 || cy < 1 || cx * cy > kMaxClusterTiles) return OCSL_BAD_ARGUMENT;
+    c->box_cluster[0] = cx;
+    c->box_cluster[1] = cy;
+    if (c->has_pattern && c->hp.box.ok) c->P.box = box_with_cluster(c->P.box, cx, cy);
+    return OCSL_OK;
+}
+
+int ocsl_sweep_cluster_info(const ocsl_ctx* c, int* cx, int* cy)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (!c->has_pattern) return OCSL_NO_PATTERN;
+    const bool on = c->P.box_ok;
+    if (cx) *cx = on ? c->P.box.CX : 0;
+    if (cy) *cy = on ? c->P.box.CY : 0;
     return OCSL_OK;
 }
 
@@ -1681,6 +1709,8 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
     // candidate column tiles (one thread per column, at most 256)
     static const int kCand[][2] = {{16, 8}, {16, 16}, {32, 4}, {32, 8}, {8, 16},
                                    {8, 8},  {64, 2},  {64, 4}, {128, 1}, {128, 2}};
+    // tiles per thread-block cluster (1 x 1: none)
+    static const int kClus[][2] = {{1, 1}, {2, 2}, {4, 2}, {2, 4}, {4, 4}};
     const BoxGeom keep = c->P.box;
     try {
         CK(cudaSetDevice(c->device));
@@ -1705,10 +1735,12 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
             CK(cudaMemsetAsync(c->v64[P], 0, sizeof(double) * n, c->stream));
         double best = 1e300;
         BoxGeom bestg = keep;
-        std::vector<std::pair<int, int>> tried;
-        for (const auto& cd : kCand) {
-            const BoxGeom g = make_box_geom(c->hp.box, cd[0], cd[1]);
-            const std::pair<int, int> key{g.TA, g.TB};
+        std::vector<std::array<int, 4>> tried;
+        for (const auto& cd : kCand)
+        for (const auto& cl : kClus) {
+            const BoxGeom g =
+                box_with_cluster(make_box_geom(c->hp.box, cd[0], cd[1]), cl[0], cl[1]);
+            const std::array<int, 4> key{g.TA, g.TB, g.CX, g.CY};
             if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
             tried.push_back(key);
             c->P.box = g;
@@ -1735,6 +1767,8 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         c->P.box = bestg;
         c->box_tile[0] = bestg.TA;
         c->box_tile[1] = bestg.TB;
+        c->box_cluster[0] = bestg.CX;
+        c->box_cluster[1] = bestg.CY;
         c->fac_M = nullptr;
         if (tile_a) *tile_a = bestg.TA;
         if (tile_b) *tile_b = bestg.TB;

@@ -23,6 +23,8 @@ def main(argv=None):
     ap.add_argument("--tet", action="store_true", help="tetrahedral (6 per hex) system")
     ap.add_argument("--dims", type=int, nargs=3, default=None, help="hex box nx ny nz")
     ap.add_argument("--tiles", type=int, nargs=2, default=(0, 0), help="structured sweep tile")
+    ap.add_argument("--cluster", type=int, nargs=2, default=(1, 1),
+                    help="structured sweep tiles per thread-block cluster")
     ap.add_argument("--inner-tol", type=float, default=None, help="IR32 inner tolerance")
     ap.add_argument("--profile", action="store_true",
                     help="print CUDA-event time per launch by kernel category (last solve)")
@@ -42,6 +44,7 @@ def main(argv=None):
     ctx = ocsl.Context(0)
     ctx.set_pattern(s.row_ptr, s.column_index)
     ctx.set_sweep_kernel(a.sweep_kernel, *a.tiles)
+    ctx.set_sweep_cluster(*a.cluster)
     A = torch.from_numpy(s.value).cuda()
     B = torch.from_numpy(s.b).cuda()
     X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
@@ -60,7 +63,7 @@ def main(argv=None):
         for name, (ms, count) in ctx.profile_read().items():
             if count:
                 print(f"{name:14s} {count:5d} launches  {1000.0 * ms / count:9.1f} us/launch")
-    print(f"{s.name}: {a.solves} x {a.method}: {r}")
+    print(f"{s.name}: {a.solves} x {a.method}: {r} sweep {ctx.sweep_info()}")
     ctx.close()
     return 0
 

@@ -173,6 +173,58 @@ def test_structured_sweeps_bit_exact(ctx, torch_cuda, oracle, dims, tiles):
     assert torch_cuda.equal(X, X2)
 
 
+CLUSTER_CASES = [
+    ((20, 20, 20), (4, 4), (2, 2)),
+    ((20, 20, 20), (4, 4), (4, 4)),
+    ((20, 20, 20), (3, 5), (4, 2)),
+    ((13, 7, 9), (2, 2), (4, 1)),
+    ((13, 7, 9), (2, 2), (1, 4)),
+    ((64, 48, 40), (8, 8), (4, 4)),   # partial clusters: 6 x 5 tiles in 4 x 4 clusters
+    ((64, 48, 40), (16, 8), (2, 4)),
+    ((9, 12, 1), (4, 1), (2, 2)),     # one tile row: the cluster is clipped to 2 x 1
+]
+
+
+@pytest.mark.parametrize("dims,tiles,cluster", CLUSTER_CASES)
+def test_clustered_sweeps_bit_exact(ctx, torch_cuda, oracle, dims, tiles, cluster):
+    """Structured sweeps whose tiles run in thread-block clusters (faces
+    through distributed shared memory) equal the oracle bit for bit."""
+    s = W.hex_pprime(*dims)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    ctx.set_sweep_kernel(2, *tiles)
+    ctx.set_sweep_cluster(*cluster)
+    info = ctx.sweep_info()
+    assert info["kind"] == 2 and info["tiles"] == tiles
+    cx, cy = info["cluster"]
+    assert 1 <= cx <= cluster[0] and 1 <= cy <= cluster[1]
+    rng = np.random.default_rng(11)
+    b = rng.standard_normal(s.n)
+    Mh = oracle.ilu(s.row_ptr, s.column_index, s.value)
+    M, B = dev(torch_cuda, Mh), dev(torch_cuda, b)
+    Y, X = torch_cuda.empty_like(B), torch_cuda.empty_like(B)
+    for _ in range(2):  # the tickets and counters of the first launches reset
+        ctx.forsub_device(M, B, Y)
+        y = oracle.forsub(s.row_ptr, s.column_index, Mh, b)
+        assert np.array_equal(host(Y), y)
+        ctx.backsub_device(M, Y, X)
+        assert np.array_equal(host(X), oracle.backsub(s.row_ptr, s.column_index, Mh, y))
+
+
+def test_cluster_shape_is_clipped(ctx):
+    import opencslsolver_gb300 as ocsl
+
+    s = W.hex_pprime(20, 20, 20)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    ctx.set_sweep_kernel(2, 16, 16)          # 2 x 2 tiles
+    ctx.set_sweep_cluster(4, 4)
+    assert ctx.sweep_info()["cluster"] == (2, 2)
+    ctx.set_sweep_cluster(1, 1)
+    assert ctx.sweep_info()["cluster"] == (1, 1)
+    for bad in [(0, 1), (1, 0), (4, 5), (17, 1)]:
+        with pytest.raises(ocsl.OcslError):
+            ctx.set_sweep_cluster(*bad)
+
+
 def test_structured_kernel_refused_for_unstructured(ctx):
     s = W.tet_pprime(3)
     ctx.set_pattern(s.row_ptr, s.column_index)

@@ -262,6 +262,44 @@ def test_sweep_kernels_give_identical_solves(ctx, method):
         assert np.array_equal(out[0][0], x) and out[0][1] == it
 
 
+@pytest.mark.parametrize("method", [ocsl.BICGSTAB_REF, ocsl.ILU_BICGSTAB, ocsl.ILU_BICGSTAB_IR32])
+def test_clustered_sweeps_give_identical_solves(ctx, torch_cuda, method):
+    """Sweeps with tiles in thread-block clusters give the bits and
+    iteration counts of single-tile sweeps, on the legacy stream (direct
+    launches) and on a created stream (graph replay), and for lockstep
+    right-hand sides."""
+    torch = torch_cuda
+    s = W.hex_pprime(40, 36, 33)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = torch.from_numpy(s.value).cuda()
+    rng = np.random.default_rng(21)
+    B = torch.from_numpy(rng.uniform(-1, 1, (3, s.n))).cuda()
+    side = torch.cuda.Stream()
+    out = {}
+    for cl in [(1, 1), (2, 2), (4, 4), (2, 4)]:
+        ctx.set_sweep_kernel(2, 8, 8)
+        ctx.set_sweep_cluster(*cl)
+        assert ctx.sweep_info()["cluster"] == cl
+        X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        r = ctx.solve_device(method, A, B[0], X, tol=1e-10)
+        assert r["status"] == 0, r
+        with torch.cuda.stream(side):
+            X2 = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            r2 = ctx.solve_device(method, A, B[0], X2, tol=1e-10)
+            XM = torch.zeros_like(B)
+            rm = ctx.solve_multi_device(method, A, B, XM, tol=1e-10) \
+                if method != ocsl.BICGSTAB_REF else None
+        torch.cuda.synchronize()
+        assert torch.equal(X, X2) and r["iterations"] == r2["iterations"]
+        out[cl] = (X, r["iterations"], XM if rm is not None else None)
+    X0, it0, XM0 = out[(1, 1)]
+    for cl, (X, it, XM) in out.items():
+        assert torch.equal(X, X0) and it == it0, cl
+        if XM0 is not None:
+            assert torch.equal(XM, XM0), cl
+            assert torch.equal(XM[0], X0), cl
+
+
 @pytest.mark.parametrize("method", [ocsl.PCG, ocsl.ILU_BICGSTAB, ocsl.ILU_BICGSTAB_IR32])
 def test_graph_replay_gives_identical_solves(ctx, torch_cuda, method):
     """Iteration batches replayed from CUDA graphs give the same bits as
@@ -308,6 +346,7 @@ def test_autotuned_tile_gives_identical_solves(ctx, torch_cuda, method):
     t = ctx.autotune(method, A)
     assert t["sweep_us"] > 0 and t["tiles"][0] * t["tiles"][1] <= 256, t
     assert ctx.sweep_info()["tiles"] == t["tiles"]
+    assert ctx.sweep_info()["cluster"] == t["cluster"]
     X1 = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     r1 = ctx.solve_device(method, A, B, X1)
     assert torch.equal(X0, X1) and r0["iterations"] == r1["iterations"]
