@@ -330,18 +330,24 @@ int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
  * shape.  No reference counterpart (the reference sweeps serially,
  * cmatrix_solver.cpp:555-611). */
 int ocsl_set_sweep_cluster(ocsl_ctx* ctx, int cx, int cy);
-/* The cluster shape in use (after clipping; 0 x 0 when no structured sweep). */
-int ocsl_sweep_cluster_info(const ocsl_ctx* ctx, int* cx, int* cy);
+/* The structured-sweep geometry of the FP64 (fp32 = 0) or FP32 (fp32 = 1)
+ * sweeps: tiles[2] = (TA, TB), cluster[2] = (cx, cy) after clipping; zeros
+ * when no structured sweep applies.  ocsl_set_sweep_kernel and
+ * ocsl_set_sweep_cluster set both precisions, ocsl_autotune_device the one
+ * its method sweeps in. */
+int ocsl_sweep_geometry(const ocsl_ctx* ctx, int fp32, int* tiles, int* cluster);
 /* The sweep kernel in use (1 level-scheduled, 2 structured), the detected box
- * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB). */
+ * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB)
+ * of the FP64 sweeps (ocsl_sweep_geometry: either precision). */
 int ocsl_sweep_info(const ocsl_ctx* ctx, int* kind, int* dims, int* tiles);
 /* Autotuner of the structured sweep's column tile (block shape) for this
  * pattern and matrix: factors d_value as a solve of `method` would, times a
  * forward + backward sweep for each candidate tile (16x8, 16x16, 32x4, 32x8,
  * 8x16, 8x8, 64x2, 64x4, 128x1, 128x2, as clipped to the box), each alone
  * and in clusters of 2x2, 4x2, 2x4 and 4x4 tiles, with CUDA events, and
- * keeps the fastest for later solves (as ocsl_set_sweep_kernel and
- * ocsl_set_sweep_cluster would; ocsl_sweep_cluster_info reports the cluster).
+ * keeps the fastest for later solves of the same precision: the FP32
+ * geometry for OCSL_ILU_BICGSTAB_IR32, the FP64 one for the FP64 methods
+ * (ocsl_sweep_geometry reports both, with the cluster shape).
  * Reports the tile and its sweep-pair time in microseconds; zeros,
  * and no change, when the structured kernel does not apply.  The tile does
  * not change any result. */

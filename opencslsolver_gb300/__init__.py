@@ -282,11 +282,13 @@ class Context:
         dims = (C.c_int * 3)()
         tiles = (C.c_int * 2)()
         self._check(self._L.ocsl_sweep_info(self._h, C.byref(kind), dims, tiles), "sweep_info")
-        cx, cy = C.c_int(), C.c_int()
-        self._check(self._L.ocsl_sweep_cluster_info(self._h, C.byref(cx), C.byref(cy)),
-                    "sweep_cluster_info")
-        return {"kind": kind.value, "dims": tuple(dims), "tiles": tuple(tiles),
-                "cluster": (cx.value, cy.value)}
+        out = {"kind": kind.value, "dims": tuple(dims)}
+        for fp32, suffix in ((0, ""), (1, "32")):
+            t, cl = (C.c_int * 2)(), (C.c_int * 2)()
+            self._check(self._L.ocsl_sweep_geometry(self._h, fp32, t, cl), "sweep_geometry")
+            out["tiles" + suffix] = tuple(t)
+            out["cluster" + suffix] = tuple(cl)
+        return out
 
     def autotune(self, method, value):
         """Pick the structured sweep's column tile for this matrix by timing the
@@ -297,8 +299,9 @@ class Context:
         self._check(self._L.ocsl_autotune_device(self._h, _method(method), _dptr(value),
                                                  C.byref(ta), C.byref(tb), C.byref(us)),
                     "autotune")
+        fp32 = _method(method) == ILU_BICGSTAB_IR32
         return {"tiles": (ta.value, tb.value), "sweep_us": us.value,
-                "cluster": self.sweep_info()["cluster"]}
+                "cluster": self.sweep_info()["cluster32" if fp32 else "cluster"]}
 
     def set_graphs(self, enable: bool = True):
         """Replay iteration batches from CUDA graphs (default on)."""

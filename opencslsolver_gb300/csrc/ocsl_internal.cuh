@@ -96,7 +96,8 @@ struct BoxGeom {
 
 struct DevPattern {
     bool box_ok;
-    BoxGeom box;
+    BoxGeom box;    // geometry of the FP64 structured sweeps
+    BoxGeom box32;  // and of the FP32 ones (tuned separately)
     int n;
     int nnz;
     const int* rp;

@@ -77,6 +77,10 @@ static_assert(kScBlocks <= kHostStage, "host mirror layout");
 
 }  // namespace
 
+namespace {
+BoxGeom make_box_geom(const BoxShape& bs, int TA_req, int TB_req);
+}
+
 struct ocsl_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -119,8 +123,19 @@ struct ocsl_ctx {
 
     // sweep kernel choice (ocsl_set_sweep_kernel): 0 auto, 1 level-scheduled, 2 structured
     int sweep_kernel = 0;
-    int box_tile[2] = {0, 0};  // TA, TB override (0 = heuristic)
-    int box_cluster[2] = {1, 1};  // tiles per thread-block cluster (ocsl_set_sweep_cluster)
+    // structured-sweep geometry requests per precision ([0] FP64, [1] FP32):
+    // TA, TB (0 = heuristic) and tiles per thread-block cluster
+    int box_tile[2][2] = {{0, 0}, {0, 0}};
+    int box_cluster[2][2] = {{1, 1}, {1, 1}};
+    // P.box / P.box32 from the requests (box patterns only)
+    void rebuild_box_geoms()
+    {
+        if (!hp.box.ok) return;
+        P.box = box_with_cluster(make_box_geom(hp.box, box_tile[0][0], box_tile[0][1]),
+                                 box_cluster[0][0], box_cluster[0][1]);
+        P.box32 = box_with_cluster(make_box_geom(hp.box, box_tile[1][0], box_tile[1][1]),
+                                   box_cluster[1][0], box_cluster[1][1]);
+    }
 
     // CUDA graph of one batch of Krylov iterations, reused while its key
     // (method and the pointers the iterations read) stays the same
@@ -511,7 +526,7 @@ struct Solve {
     template <typename TT>
     BoxGeom sweep_geom() const
     {
-        BoxGeom g = P.box;
+        BoxGeom g = is_f64<TT>() ? P.box : P.box32;
         if (box_sweep_smem(g, (int)sizeof(TT), cols.n) > kBoxSmemLimit)
             g = box_with_cluster(g, 1, 1);  // face buffers first
         while (box_sweep_smem(g.TA * g.TB, (int)sizeof(TT), cols.n) > kBoxSmemLimit &&
@@ -1091,8 +1106,9 @@ int ensure_transpose(ocsl_ctx* c)
     ocsl_ctx* t = nullptr;
     int rc = ocsl_create(&t, c->device);
     if (rc != OCSL_OK) return fail(c, rc, "adjoint context: " + g_create_error);
-    ocsl_set_sweep_kernel(t, c->sweep_kernel, c->box_tile[0], c->box_tile[1]);
-    ocsl_set_sweep_cluster(t, c->box_cluster[0], c->box_cluster[1]);
+    ocsl_set_sweep_kernel(t, c->sweep_kernel, 0, 0);
+    std::memcpy(t->box_tile, c->box_tile, sizeof(c->box_tile));
+    std::memcpy(t->box_cluster, c->box_cluster, sizeof(c->box_cluster));
     t->graphs_on = c->graphs_on;
     rc = ocsl_set_pattern(t, (size_t)n, trp.data(), tcol.data());
     if (rc != OCSL_OK) {
@@ -1306,10 +1322,8 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         P.bw_chunk = c->d_pat[9];
         P.bw_nchunks = (int)hp.bw_chunk.size() - 1;
         P.box_ok = hp.box.ok && c->sweep_kernel != 1;
-        if (hp.box.ok)
-            P.box = box_with_cluster(make_box_geom(hp.box, c->box_tile[0], c->box_tile[1]),
-                                     c->box_cluster[0], c->box_cluster[1]);
         c->hp.box = hp.box;
+        c->rebuild_box_geoms();
         const size_t nn = (size_t)hp.n, nz = (size_t)hp.nnz;
         c->d_A = dalloc<double>(nz);
         c->d_b = dalloc<double>(nn);
@@ -1659,13 +1673,13 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
     if (kind == 2 && c->has_pattern && !c->hp.box.ok)
         return fail(c, OCSL_BAD_ARGUMENT, "the pattern is not a 7-point box stencil");
     c->sweep_kernel = kind;
-    c->box_tile[0] = tile_a;
-    c->box_tile[1] = tile_b;
+    for (int k = 0; k < 2; ++k) {
+        c->box_tile[k][0] = tile_a;
+        c->box_tile[k][1] = tile_b;
+    }
     if (c->has_pattern) {
         c->P.box_ok = c->hp.box.ok && kind != 1;
-        if (c->hp.box.ok)
-            c->P.box = box_with_cluster(make_box_geom(c->hp.box, tile_a, tile_b),
-                                        c->box_cluster[0], c->box_cluster[1]);
+        c->rebuild_box_geoms();
     }
     return OCSL_OK;
 }
@@ -1673,19 +1687,28 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
 int ocsl_set_sweep_cluster(ocsl_ctx* c, int cx, int cy)
 {
     if (!c || cx < 1 || cy < 1 || cx * cy > kMaxClusterTiles) return OCSL_BAD_ARGUMENT;
-    c->box_cluster[0] = cx;
-    c->box_cluster[1] = cy;
-    if (c->has_pattern && c->hp.box.ok) c->P.box = box_with_cluster(c->P.box, cx, cy);
+    for (int k = 0; k < 2; ++k) {
+        c->box_cluster[k][0] = cx;
+        c->box_cluster[k][1] = cy;
+    }
+    if (c->has_pattern) c->rebuild_box_geoms();
     return OCSL_OK;
 }
 
-int ocsl_sweep_cluster_info(const ocsl_ctx* c, int* cx, int* cy)
+int ocsl_sweep_geometry(const ocsl_ctx* c, int fp32, int* tiles, int* cluster)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
     if (!c->has_pattern) return OCSL_NO_PATTERN;
     const bool on = c->P.box_ok;
-    if (cx) *cx = on ? c->P.box.CX : 0;
-    if (cy) *cy = on ? c->P.box.CY : 0;
+    const BoxGeom& g = fp32 ? c->P.box32 : c->P.box;
+    if (tiles) {
+        tiles[0] = on ? g.TA : 0;
+        tiles[1] = on ? g.TB : 0;
+    }
+    if (cluster) {
+        cluster[0] = on ? g.CX : 0;
+        cluster[1] = on ? g.CY : 0;
+    }
     return OCSL_OK;
 }
 
@@ -1711,7 +1734,9 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
                                    {8, 8},  {64, 2},  {64, 4}, {128, 1}, {128, 2}};
     // tiles per thread-block cluster (1 x 1: none)
     static const int kClus[][2] = {{1, 1}, {2, 2}, {4, 2}, {2, 4}, {4, 4}};
-    const BoxGeom keep = c->P.box;
+    const int pi = fp32 ? 1 : 0;
+    BoxGeom& geo = fp32 ? c->P.box32 : c->P.box;  // the geometry this method's sweeps use
+    const BoxGeom keep = geo;
     try {
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
@@ -1743,7 +1768,7 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
             const std::array<int, 4> key{g.TA, g.TB, g.CX, g.CY};
             if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
             tried.push_back(key);
-            c->P.box = g;
+            geo = g;
             pair();  // warm-up
             double t = 1e300;
             for (int rep = 0; rep < 3; ++rep) {
@@ -1756,7 +1781,7 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
                 t = std::min(t, 1000.0 * ms);
             }
             if (s.device_error()) {
-                c->P.box = keep;
+                geo = keep;
                 return fail(c, OCSL_TIMEOUT, "a triangular-sweep wait hit its bound");
             }
             if (t < best) {
@@ -1764,18 +1789,18 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
                 bestg = g;
             }
         }
-        c->P.box = bestg;
-        c->box_tile[0] = bestg.TA;
-        c->box_tile[1] = bestg.TB;
-        c->box_cluster[0] = bestg.CX;
-        c->box_cluster[1] = bestg.CY;
+        geo = bestg;
+        c->box_tile[pi][0] = bestg.TA;
+        c->box_tile[pi][1] = bestg.TB;
+        c->box_cluster[pi][0] = bestg.CX;
+        c->box_cluster[pi][1] = bestg.CY;
         c->fac_M = nullptr;
         if (tile_a) *tile_a = bestg.TA;
         if (tile_b) *tile_b = bestg.TB;
         if (sweep_us) *sweep_us = best;
         CK(cudaGetLastError());
     } catch (const CudaError& e) {
-        c->P.box = keep;
+        geo = keep;
         return from_cuda(c, e);
     }
     return OCSL_OK;

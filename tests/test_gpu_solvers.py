@@ -345,11 +345,21 @@ def test_autotuned_tile_gives_identical_solves(ctx, torch_cuda, method):
     r0 = ctx.solve_device(method, A, B, X0)
     t = ctx.autotune(method, A)
     assert t["sweep_us"] > 0 and t["tiles"][0] * t["tiles"][1] <= 256, t
-    assert ctx.sweep_info()["tiles"] == t["tiles"]
-    assert ctx.sweep_info()["cluster"] == t["cluster"]
+    sfx = "32" if method == ocsl.ILU_BICGSTAB_IR32 else ""
+    info = ctx.sweep_info()
+    assert info["tiles" + sfx] == t["tiles"] and info["cluster" + sfx] == t["cluster"], (info, t)
     X1 = torch.zeros(s.n, dtype=torch.float64, device="cuda")
     r1 = ctx.solve_device(method, A, B, X1)
     assert torch.equal(X0, X1) and r0["iterations"] == r1["iterations"]
+    # the other precision's geometry is tuned on its own
+    other = ocsl.ILU_BICGSTAB if method == ocsl.ILU_BICGSTAB_IR32 else ocsl.ILU_BICGSTAB_IR32
+    t2 = ctx.autotune(other, A)
+    info2 = ctx.sweep_info()
+    assert info2["tiles" + sfx] == t["tiles"] and info2["cluster" + sfx] == t["cluster"]
+    X2 = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    r2 = ctx.solve_device(method, A, B, X2)
+    assert torch.equal(X0, X2) and r0["iterations"] == r2["iterations"]
+    assert t2["sweep_us"] > 0
     # nothing to tune: Jacobi PCG, level-scheduled sweeps
     assert ctx.autotune(ocsl.PCG, A)["tiles"] == (0, 0)
     ctx.set_sweep_kernel(1)
