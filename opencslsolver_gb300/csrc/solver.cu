@@ -170,6 +170,14 @@ struct ocsl_ctx {
 
     void free_pattern();
     void free_all();
+    // Forget the captured iteration graph: its kernels and launch shapes belong
+    // to the pattern, sweep kernel and geometry it was captured with.
+    void drop_graph()
+    {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+        graph_kind = 0;
+    }
     void ensure_reduce(int ntiles);
     void ensure_fp32();
     void ensure_cols();
@@ -177,6 +185,7 @@ struct ocsl_ctx {
 
 void ocsl_ctx::free_pattern()
 {
+    drop_graph();
     fac_M = nullptr;
     fac_soa64 = nullptr;
     fac_soa32 = nullptr;
@@ -1672,6 +1681,7 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
     if (!c || kind < 0 || kind > 2 || tile_a < 0 || tile_b < 0) return OCSL_BAD_ARGUMENT;
     if (kind == 2 && c->has_pattern && !c->hp.box.ok)
         return fail(c, OCSL_BAD_ARGUMENT, "the pattern is not a 7-point box stencil");
+    c->drop_graph();
     c->sweep_kernel = kind;
     for (int k = 0; k < 2; ++k) {
         c->box_tile[k][0] = tile_a;
@@ -1687,6 +1697,7 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
 int ocsl_set_sweep_cluster(ocsl_ctx* c, int cx, int cy)
 {
     if (!c || cx < 1 || cy < 1 || cx * cy > kMaxClusterTiles) return OCSL_BAD_ARGUMENT;
+    c->drop_graph();
     for (int k = 0; k < 2; ++k) {
         c->box_cluster[k][0] = cx;
         c->box_cluster[k][1] = cy;
@@ -1790,6 +1801,7 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
             }
         }
         geo = bestg;
+        c->drop_graph();
         c->box_tile[pi][0] = bestg.TA;
         c->box_tile[pi][1] = bestg.TB;
         c->box_cluster[pi][0] = bestg.CX;
@@ -1823,10 +1835,7 @@ int ocsl_set_graphs(ocsl_ctx* c, int enable)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
     c->graphs_on = enable != 0;
-    if (!c->graphs_on && c->graph_exec) {
-        cudaGraphExecDestroy(c->graph_exec);
-        c->graph_exec = nullptr;
-    }
+    if (!c->graphs_on) c->drop_graph();
     if (c->tctx) ocsl_set_graphs(c->tctx, enable);
     return OCSL_OK;
 }
@@ -1834,6 +1843,7 @@ int ocsl_set_graphs(ocsl_ctx* c, int enable)
 int ocsl_set_col_batching(ocsl_ctx* c, int enable)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
+    c->drop_graph();
     c->col_batching = enable != 0;
     return OCSL_OK;
 }

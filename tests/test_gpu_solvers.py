@@ -332,6 +332,32 @@ def test_graph_replay_gives_identical_solves(ctx, torch_cuda, method):
         assert i1 == i2 and np.array_equal(x1, x2)
 
 
+def test_new_pattern_drops_captured_graph(ctx, torch_cuda):
+    """A context that replayed iteration graphs for one box and then gets a
+    box of the same size but another shape (same buffer sizes, so the
+    allocator may hand back the same addresses) solves the new system exactly
+    as a fresh context does: captured graphs go with the old pattern."""
+    torch = torch_cuda
+    s1, s2 = W.hex_pprime(40, 36, 33), W.hex_pprime(33, 40, 36)
+    assert s1.n == s2.n and s1.value.size == s2.value.size
+    side = torch.cuda.Stream()
+    fresh = ocsl.Context(0)
+    with torch.cuda.stream(side):
+        out = []
+        for c, systems in ((ctx, (s1, s2)), (fresh, (s2,))):
+            for s in systems:
+                c.set_pattern(s.row_ptr, s.column_index)
+                A = torch.from_numpy(s.value).cuda()
+                B = torch.from_numpy(s.b).cuda()
+                X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+                r = c.solve_device(ocsl.ILU_BICGSTAB_IR32, A, B, X, tol=1e-10)
+                assert r["status"] == 0, r
+            out.append((X, r["iterations"]))
+    torch.cuda.synchronize()
+    fresh.close()
+    assert torch.equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
 @pytest.mark.parametrize("method", [ocsl.ILU_BICGSTAB_IR32, ocsl.ILU_BICGSTAB, ocsl.BICGSTAB_REF])
 def test_autotuned_tile_gives_identical_solves(ctx, torch_cuda, method):
     """ocsl_autotune_device picks one of its candidate tiles, keeps it for the
