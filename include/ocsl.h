@@ -322,7 +322,9 @@ int ocsl_bc_value_grad_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
  * kernels give bit-identical results. */
 int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
 /* Thread-block clusters of the structured sweep: cx x cy neighbouring column
- * tiles (cx * cy <= 16; 1 x 1 = none, the default) run as one cluster and
+ * tiles (cx * cy <= 16; 1 x 1 = none; 0 x 0 = automatic, the default: 2 x 4
+ * when the box has at least 64 column tiles, none below; batch contexts use
+ * 1 x 1) run as one cluster and
  * pass their face values through distributed shared memory instead of global
  * memory.  Clipped to the tile grid; a shape the device cannot schedule, or
  * whose face buffers (columns x s-extent x (TA + TB) values) do not fit the

@@ -274,7 +274,8 @@ class Context:
 
     def set_sweep_cluster(self, cx: int = 1, cy: int = 1):
         """Run the structured sweep's column tiles in thread-block clusters of
-        cx x cy tiles (faces through distributed shared memory); 1 x 1 = none."""
+        cx x cy tiles (faces through distributed shared memory); 1 x 1 = none,
+        0 x 0 = automatic (the default: 2 x 4 on a grid of at least 64 tiles)."""
         self._check(self._L.ocsl_set_sweep_cluster(self._h, cx, cy), "sweep cluster")
 
     def sweep_info(self):

@@ -66,6 +66,9 @@ int ocsl_batch_create(ocsl_batch** out, int device, int count, const ocsl_batch_
             return OCSL_BAD_ARGUMENT;
         }
         int rc = ocsl_create(&b->ctx[i], device);
+        // single-tile sweeps: the systems run concurrently on several streams,
+        // and clustered sweeps would hold whole SMs per CTA
+        if (rc == OCSL_OK) rc = ocsl_set_sweep_cluster(b->ctx[i], 1, 1);
         if (rc == OCSL_OK) rc = ocsl_set_pattern(b->ctx[i], sys[i].n, sys[i].row_ptr,
                                                  sys[i].column_index);
         if (rc != OCSL_OK) {

@@ -81,6 +81,8 @@ namespace {
 BoxGeom make_box_geom(const BoxShape& bs, int TA_req, int TB_req);
 }
 
+constexpr int kAutoClusterTiles = 64;  // tiles from which clusters pay by default
+
 struct ocsl_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -126,15 +128,24 @@ struct ocsl_ctx {
     // structured-sweep geometry requests per precision ([0] FP64, [1] FP32):
     // TA, TB (0 = heuristic) and tiles per thread-block cluster
     int box_tile[2][2] = {{0, 0}, {0, 0}};
-    int box_cluster[2][2] = {{1, 1}, {1, 1}};
+    // 0 x 0 = automatic: 2 x 4 tiles per cluster on a grid of at least
+    // kAutoClusterTiles tiles, single tiles below (few tile hops to save)
+    int box_cluster[2][2] = {{0, 0}, {0, 0}};
     // P.box / P.box32 from the requests (box patterns only)
     void rebuild_box_geoms()
     {
         if (!hp.box.ok) return;
-        P.box = box_with_cluster(make_box_geom(hp.box, box_tile[0][0], box_tile[0][1]),
-                                 box_cluster[0][0], box_cluster[0][1]);
-        P.box32 = box_with_cluster(make_box_geom(hp.box, box_tile[1][0], box_tile[1][1]),
-                                   box_cluster[1][0], box_cluster[1][1]);
+        BoxGeom* geo[2] = {&P.box, &P.box32};
+        for (int k = 0; k < 2; ++k) {
+            const BoxGeom g = make_box_geom(hp.box, box_tile[k][0], box_tile[k][1]);
+            int cx = box_cluster[k][0], cy = box_cluster[k][1];
+            if (cx == 0) {
+                const bool big = g.nta * g.ntb >= kAutoClusterTiles;
+                cx = big ? 2 : 1;
+                cy = big ? 4 : 1;
+            }
+            *geo[k] = box_with_cluster(g, cx, cy);
+        }
     }
 
     // CUDA graph of one batch of Krylov iterations, reused while its key
@@ -1696,7 +1707,9 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
 
 int ocsl_set_sweep_cluster(ocsl_ctx* c, int cx, int cy)
 {
-    if (!c || cx < 1 || cy < 1 || cx * cy > kMaxClusterTiles) return OCSL_BAD_ARGUMENT;
+    const bool automatic = cx == 0 && cy == 0;
+    if (!c || (!automatic && (cx < 1 || cy < 1 || cx * cy > kMaxClusterTiles)))
+        return OCSL_BAD_ARGUMENT;
     c->drop_graph();
     for (int k = 0; k < 2; ++k) {
         c->box_cluster[k][0] = cx;

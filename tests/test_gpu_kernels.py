@@ -220,6 +220,14 @@ def test_cluster_shape_is_clipped(ctx):
     assert ctx.sweep_info()["cluster"] == (2, 2)
     ctx.set_sweep_cluster(1, 1)
     assert ctx.sweep_info()["cluster"] == (1, 1)
+    ctx.set_sweep_cluster(0, 0)                   # automatic: 4 tiles, no clusters
+    assert ctx.sweep_info()["cluster"] == (1, 1)
+    big = W.hex_pprime(40, 36, 33)                 # 16 x 8 tiles: 3 x 5, still below 64
+    ctx.set_pattern(big.row_ptr, big.column_index)
+    ctx.set_sweep_kernel(2, 8, 4)                 # 5 x 9 = 45 tiles
+    assert ctx.sweep_info()["cluster"] == (1, 1)
+    ctx.set_sweep_kernel(2, 4, 4)                 # 9 x 9 = 81 tiles: 2 x 4 clusters
+    assert ctx.sweep_info()["cluster"] == (2, 4)
     for bad in [(0, 1), (1, 0), (4, 5), (17, 1)]:
         with pytest.raises(ocsl.OcslError):
             ctx.set_sweep_cluster(*bad)
