@@ -14,6 +14,8 @@
 #include <cfloat>
 #include <cstdio>
 
+#include <type_traits>
+
 #include "ocsl_internal.cuh"
 
 namespace ocsl {
@@ -512,6 +514,17 @@ struct VecParams {
     Cols cols;
 };
 
+// V_TB_S / V_TB_P also leave the all-ones sweep sentinel in up to two dead
+// vectors (v[6], v[7]: the outputs of the two sweeps that follow), in place
+// of separate fill launches.
+template <typename T>
+__device__ __forceinline__ void fill_sentinels(T* f0, T* f1, int e)
+{
+    using U = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned>::type;
+    if (f0) reinterpret_cast<U*>(f0)[e] = ~U(0);
+    if (f1) reinterpret_cast<U*>(f1)[e] = ~U(0);
+}
+
 template <typename T, int OP>
 __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
 {
@@ -580,6 +593,7 @@ __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
             const T s = fma_t(-a, v[1][e], v[2][e]);
             v[0][e] = s;
             acc[0].add(s, s);
+            fill_sentinels(v[6], v[7], e);
         } else if constexpr (OP == V_TB_XR) {
             v[0][e] = fma_t(w, v[2][e], fma_t(a, v[1][e], v[0][e]));
             const T r = fma_t(-w, v[4][e], v[5][e]);
@@ -588,6 +602,7 @@ __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
             acc[1].add(v[6][e], r);
         } else if constexpr (OP == V_TB_P) {
             v[0][e] = fma_t(be, fma_t(-w, v[1][e], v[0][e]), v[2][e]);
+            fill_sentinels(v[6], v[7], e);
         } else if constexpr (OP == V_TB_HALF) {
             v[0][e] = fma_t(a, v[1][e], v[0][e]);
         } else if constexpr (OP == V_COPY2) {

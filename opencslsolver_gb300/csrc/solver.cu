@@ -525,10 +525,14 @@ struct Solve {
         }
         return src;
     }
+    // The last tolerance-mode iteration's V_TB_P left tmp and p^ filled with
+    // the sweep sentinel (single column only; reset by run_batches).
+    bool tb_prefilled = false;
+    // prefilled: `out` already holds the sentinel (a fused fill upstream).
     template <typename TT>
-    void fw(const TT* M, const TT* rhs, TT* out, int k)
+    void fw(const TT* M, const TT* rhs, TT* out, int k, bool prefilled = false)
     {
-        {
+        if (!prefilled) {
             ProfScope ps(c, st, PC_FILL);
             fill_sentinel(out, k);
         }
@@ -614,9 +618,10 @@ struct Solve {
         }
     }
     template <typename TT>
-    void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k)
+    void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k,
+            bool prefilled = false)
     {
-        {
+        if (!prefilled) {
             ProfScope ps(c, st, PC_FILL);
             fill_sentinel(out, k);
         }
@@ -760,6 +765,7 @@ Scalars run_batches(Solve& s, int k, int budget, F&& enqueue, int graph_kind = 0
     Scalars* slot = s.c->h_sc + kHostInspect;  // two pinned inspection slots of kMaxCols blocks
     const int nc = s.cols.n;
     int it = 0, issued = 0, inspected = 0;
+    s.tb_prefilled = false;  // the first iteration fills its sweep outputs itself
     while (true) {
         while (issued - inspected < 2 && it < budget) {
             const int m = std::min(kBatch, budget - it);
@@ -791,15 +797,24 @@ template <typename TT>
 void bicgstab_iteration(Solve& s, const TT* A, const TT* M, const TT* dinv, TT* x, TT* r, TT* rh,
                         TT* p, TT* ph, TT* vv, TT* ss, TT* sh, TT* t, TT* tmp, int k)
 {
-    s.fw<TT>(M, p, tmp, k);
-    s.bw<TT>(M, dinv, tmp, ph, 1, k);
+    // single column: the vector kernels before each sweep pair fill the
+    // pair's outputs (tmp is dead after each backward sweep, s^ after the x
+    // update, p^ after the p update), so no fill launches inside the loop
+    const bool fuse = s.cols.n == 1;
+    const bool pre = fuse && s.tb_prefilled;
+    TT* f0 = fuse ? tmp : nullptr;
+    s.fw<TT>(M, p, tmp, k, pre);
+    s.bw<TT>(M, dinv, tmp, ph, 1, k, pre);
     s.spmv<TT>(A, ph, vv, 0, nullptr, nullptr, rh, DOT_WY, k, EP_TB_SIGMA);
-    s.vec<TT>(V_TB_S, {ss, vv, r}, k, EP_TB_S);
-    s.fw<TT>(M, ss, tmp, k);
-    s.bw<TT>(M, dinv, tmp, sh, 1, k);
+    s.vec<TT>(V_TB_S, {ss, vv, r, nullptr, nullptr, nullptr, f0, fuse ? sh : nullptr}, k,
+              EP_TB_S);
+    s.fw<TT>(M, ss, tmp, k, fuse);
+    s.bw<TT>(M, dinv, tmp, sh, 1, k, fuse);
     s.spmv<TT>(A, sh, t, 0, nullptr, nullptr, ss, DOT_YY | DOT_WY, k, EP_TB_OMEGA);
     s.vec<TT>(V_TB_XR, {x, ph, sh, r, t, ss, rh}, k, EP_TB_RUPD);
-    s.vec<TT>(V_TB_P, {p, vv, r}, k, EP_STORE);
+    s.vec<TT>(V_TB_P, {p, vv, r, nullptr, nullptr, nullptr, f0, fuse ? ph : nullptr}, k,
+              EP_STORE);
+    s.tb_prefilled = fuse;
 }
 
 // Restarted driver shared by BiCGSTAB and PCG: start from x, iterate until
