@@ -525,6 +525,20 @@ __device__ __forceinline__ void fill_sentinels(T* f0, T* f1, int e)
     if (f1) reinterpret_cast<U*>(f1)[e] = ~U(0);
 }
 
+// Vectors (bit k = v[k]) each op reads, and whether it reads v64[0].
+template <int OP>
+struct VecReads {
+    static constexpr unsigned mask =
+        OP == V_RB_P ? 0x07u : OP == V_RB_HS ? 0x36u : OP == V_RB_XR ? 0x76u
+      : OP == V_DOT2 || OP == V_DOT1 ? 0x03u : OP == V_RC_XR ? 0x1Bu : OP == V_RC_P ? 0x03u
+      : OP == V_TB_S ? 0x06u : OP == V_TB_XR ? 0x77u : OP == V_TB_P ? 0x07u
+      : OP == V_TB_HALF ? 0x03u : OP == V_COPY2 ? 0x04u : OP == V_PC_INIT ? 0x0Cu
+      : OP == V_PC_XRZ ? 0x2Fu : OP == V_PC_P ? 0x03u : OP == V_IR_SCALE ? 0x00u
+      : OP == V_IR_UPDATE ? 0x02u : OP == V_SUM || OP == V_ABSSUM ? 0x01u
+      : OP == V_PRODUCT || OP == V_AXPY ? 0x03u : OP == V_SCALE ? 0x01u : 0xFFu;
+    static constexpr bool f64 = OP == V_IR_SCALE || OP == V_IR_UPDATE;
+};
+
 template <typename T, int OP>
 __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
 {
@@ -560,92 +574,108 @@ __global__ void __launch_bounds__(kThreads) vec_kernel(VecParams P)
     const T a = (T)alpha, w = (T)omega, be = (T)beta;
     DotAcc<T> acc[ND > 0 ? ND : 1];
 
+    // Two phases: every input element of this thread first (all loads in
+    // flight together), then the updates and dot terms in element order, so
+    // results and reduction order are those of one element at a time.  Every
+    // op reads each element of a vector before it writes that element.
+    constexpr unsigned RM = VecReads<OP>::mask;
+    T in[kRowsPerThread][8];
+    double in64[kRowsPerThread];
+#pragma unroll
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int e = tile * kTile + j * kThreads + (int)threadIdx.x;
+        const bool ok = e < n;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if ((RM >> k) & 1u) in[j][k] = ok ? v[k][e] : T(0);
+        if constexpr (VecReads<OP>::f64) in64[j] = ok ? v64[0][e] : 0.0;
+    }
 #pragma unroll
     for (int j = 0; j < kRowsPerThread; ++j) {
         const int e = tile * kTile + j * kThreads + (int)threadIdx.x;
         if (e >= n) continue;
         if constexpr (OP == V_RB_P) {  // :718-720
-            const T dum = fma_t(-w, v[1][e], v[0][e]);
-            v[0][e] = fma_t(w, dum, v[2][e]);
+            const T dum = fma_t(-w, in[j][1], in[j][0]);
+            v[0][e] = fma_t(w, dum, in[j][2]);
         } else if constexpr (OP == V_RB_HS) {  // :731, :738
-            v[0][e] = fma_t(a, v[2][e], v[1][e]);
-            v[3][e] = fma_t(-a, v[4][e], v[5][e]);
+            v[0][e] = fma_t(a, in[j][2], in[j][1]);
+            v[3][e] = fma_t(-a, in[j][4], in[j][5]);
         } else if constexpr (OP == V_RB_XR) {  // :753, :756, next :714 and :733
-            v[0][e] = fma_t(w, v[1][e], v[2][e]);
-            const T r = fma_t(-w, v[4][e], v[5][e]);
+            v[0][e] = fma_t(w, in[j][1], in[j][2]);
+            const T r = fma_t(-w, in[j][4], in[j][5]);
             v[3][e] = r;
-            acc[0].add(v[6][e], r);
+            acc[0].add(in[j][6], r);
             acc[1].add(r, r);
         } else if constexpr (OP == V_DOT2) {
-            const T x = v[0][e];
-            acc[0].add(x, v[1][e]);
+            const T x = in[j][0];
+            acc[0].add(x, in[j][1]);
             acc[1].add(x, x);
         } else if constexpr (OP == V_DOT1) {
-            acc[0].add(v[0][e], v[1][e]);
+            acc[0].add(in[j][0], in[j][1]);
         } else if constexpr (OP == V_RC_XR) {  // :662-667
-            v[0][e] = fma_t(a, v[1][e], v[0][e]);
-            const T rn = fma_t(-a, v[3][e], v[4][e]);
+            v[0][e] = fma_t(a, in[j][1], in[j][0]);
+            const T rn = fma_t(-a, in[j][3], in[j][4]);
             v[2][e] = rn;
             acc[0].add(rn, rn);
         } else if constexpr (OP == V_RC_P) {  // :674
-            v[0][e] = fma_t(be, v[0][e], v[1][e]);
+            v[0][e] = fma_t(be, in[j][0], in[j][1]);
         } else if constexpr (OP == V_TB_S) {
-            const T s = fma_t(-a, v[1][e], v[2][e]);
+            const T s = fma_t(-a, in[j][1], in[j][2]);
             v[0][e] = s;
             acc[0].add(s, s);
             fill_sentinels(v[6], v[7], e);
         } else if constexpr (OP == V_TB_XR) {
-            v[0][e] = fma_t(w, v[2][e], fma_t(a, v[1][e], v[0][e]));
-            const T r = fma_t(-w, v[4][e], v[5][e]);
+            v[0][e] = fma_t(w, in[j][2], fma_t(a, in[j][1], in[j][0]));
+            const T r = fma_t(-w, in[j][4], in[j][5]);
             v[3][e] = r;
             acc[0].add(r, r);
-            acc[1].add(v[6][e], r);
+            acc[1].add(in[j][6], r);
         } else if constexpr (OP == V_TB_P) {
-            v[0][e] = fma_t(be, fma_t(-w, v[1][e], v[0][e]), v[2][e]);
+            v[0][e] = fma_t(be, fma_t(-w, in[j][1], in[j][0]), in[j][2]);
             fill_sentinels(v[6], v[7], e);
         } else if constexpr (OP == V_TB_HALF) {
-            v[0][e] = fma_t(a, v[1][e], v[0][e]);
+            v[0][e] = fma_t(a, in[j][1], in[j][0]);
         } else if constexpr (OP == V_COPY2) {
-            const T r = v[2][e];
+            const T r = in[j][2];
             v[0][e] = r;
             v[1][e] = r;
         } else if constexpr (OP == V_PC_INIT) {
-            const T r = v[2][e];
-            const T z = r * v[3][e];
+            const T r = in[j][2];
+            const T z = r * in[j][3];
             v[0][e] = z;
             v[1][e] = z;
             acc[0].add(r, z);
         } else if constexpr (OP == V_PC_XRZ) {
-            v[0][e] = fma_t(a, v[1][e], v[0][e]);
-            const T r = fma_t(-a, v[3][e], v[2][e]);
+            v[0][e] = fma_t(a, in[j][1], in[j][0]);
+            const T r = fma_t(-a, in[j][3], in[j][2]);
             v[2][e] = r;
-            const T z = r * v[5][e];
+            const T z = r * in[j][5];
             v[4][e] = z;
             acc[0].add(r, r);
             acc[1].add(r, z);
         } else if constexpr (OP == V_PC_P) {
-            v[0][e] = fma_t(be, v[0][e], v[1][e]);
+            v[0][e] = fma_t(be, in[j][0], in[j][1]);
         } else if constexpr (OP == V_IR_SCALE) {  // v[0] is FP64
-            const float f = (float)(v64[0][e] * outer->sum[3]);
+            const float f = (float)(in64[j] * outer->sum[3]);
             v[1][e] = f;
             v[2][e] = f;
             v[3][e] = f;
             v[4][e] = 0.0f;
             acc[0].add(f, f);
         } else if constexpr (OP == V_IR_UPDATE) {  // v[0] is FP64
-            const float d = v[1][e];
-            v64[0][e] = fma((double)d, outer->rnorm, v64[0][e]);
+            const float d = in[j][1];
+            v64[0][e] = fma((double)d, outer->rnorm, in64[j]);
         } else if constexpr (OP == V_SUM) {  // fma(x, 1, s) == s + x exactly
-            acc[0].add(v[0][e], T(1));
+            acc[0].add(in[j][0], T(1));
         } else if constexpr (OP == V_ABSSUM) {
-            acc[0].add(fabs(v[0][e]), T(1));
+            acc[0].add(fabs(in[j][0]), T(1));
         } else if constexpr (OP == V_PRODUCT) {
-            v[2][e] = v[0][e] * v[1][e];
+            v[2][e] = in[j][0] * in[j][1];
         } else if constexpr (OP == V_SCALE) {
-            v[2][e] = a * v[0][e];
+            v[2][e] = a * in[j][0];
         } else if constexpr (OP == V_AXPY) {
             // a = alpha, b = beta of the scalars block; the reference's branches
-            const T x = v[0][e], y = v[1][e];
+            const T x = in[j][0], y = in[j][1];
             T o;
             if (be == T(1)) {
                 o = a == T(1) ? x + y : (a == T(-1) ? y - x : fma_t(a, x, y));
