@@ -365,10 +365,10 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
             if constexpr (MODE == 0) {
                 y = dum;
             } else if constexpr (MODE == 1) {
-                zv = zvec[row];
+                zv = __ldg(zvec + row);
                 y = zv - dum;
             } else {
-                zv = zvec[row];
+                zv = __ldg(zvec + row);
                 y = fma_t(p.a, dum, zv);
             }
             yv[row] = y;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
             int k = 0;
             if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
             if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
-            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(wv[row], y);
+            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(wv + row), y);
             (void)k;
         }
         __syncthreads();
@@ -399,6 +399,10 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
 // and adds nothing, so y equals the CSR kernel's bit for bit while no column
 // index is read and every load is coalesced (32 or 64 B of records per row,
 // x at seven shifted, contiguous offsets).
+// In both SpMV kernels z and w are read through the read-only path: no
+// launch writes them (y may equal z only element-wise, each row's z read
+// coming before its y store in the same thread), so later rows' loads can be
+// issued ahead of earlier rows' stores.
 template <typename T>
 struct BoxSpmvParams {
     int n, sy, sz;  // rows, y and z strides (nx, nx*ny)
@@ -427,7 +431,7 @@ struct Rec4<double> {
 };
 
 #ifndef OCSL_BOX_SPMV_UNROLL
-#define OCSL_BOX_SPMV_UNROLL 2
+#define OCSL_BOX_SPMV_UNROLL 4
 #endif
 constexpr int kBoxSpmvUnroll = OCSL_BOX_SPMV_UNROLL;
 
@@ -472,10 +476,10 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
         if constexpr (MODE == 0) {
             y = dum;
         } else if constexpr (MODE == 1) {
-            zv = zvec[row];
+            zv = __ldg(zvec + row);
             y = zv - dum;
         } else {
-            zv = zvec[row];
+            zv = __ldg(zvec + row);
             y = fma_t(p.a, dum, zv);
         }
         yv[row] = y;
@@ -483,7 +487,7 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
         int k = 0;
         if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
         if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
-        if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(wv[row], y);
+        if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(wv + row), y);
         (void)k;
     }
     if constexpr (ND > 0) {
