@@ -210,8 +210,8 @@ def run_reference(args):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": "one step = one full reference ILU_BICGSTAB_solve() call "
                                    "(ILU + 3 fixed iterations, the reference's own solve; it "
-                                   "cannot reach 1e-10) on the 128^3 system, OpenMP port of "
-                                   "cmatrix_solver.cpp:682-762"},
+                                   f"cannot reach 1e-10) on the {args.size}^3 system, OpenMP "
+                                   "port of cmatrix_solver.cpp:682-762"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

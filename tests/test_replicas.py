@@ -84,3 +84,25 @@ def test_reference_arm_non_root_rank_exits_without_work():
                        capture_output=True, text=True, timeout=120)
     assert p.returncode == 0, p.stderr
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_prints_its_line():
+    """Rank 0 of the reference arm times the reference algorithm (the oracle's
+    OpenMP port of ILU_BICGSTAB_solve) on the host and prints one JSON line
+    with the contract's keys (small box here; the default is 128^3)."""
+    import json
+
+    env = dict(os.environ, RANK="0", LOCAL_RANK="0", WORLD_SIZE="1")
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--size", "12", "--steps", "2", "--warmup", "1"], env=env, cwd=ROOT,
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    line = json.loads(p.stdout.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+                "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0 and line["steps"] == 2
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["config"]["n"] == 12 ** 3
+    assert "12^3" in line["cpu_baseline"]["sample"]
