@@ -33,7 +33,10 @@ typedef struct ocsl_ctx ocsl_ctx;
 typedef enum {
     OCSL_OK = 0,
     OCSL_NOT_CONVERGED = 1, /* tolerance mode hit maxit (x holds the last iterate) */
-    OCSL_ZERO_PIVOT = 2,    /* a zero or non-finite pivot in the ILU factor       */
+    OCSL_ZERO_PIVOT = 2,    /* a zero or non-finite pivot in the factor: mode R
+                               still computes exactly as the reference (which has
+                               no check) and reports it; mode T runs no iteration
+                               and leaves x unchanged                               */
     OCSL_NONFINITE = 3,     /* NaN/Inf met in the iteration                       */
     OCSL_BAD_PATTERN = 4,   /* pattern rejected by ocsl_set_pattern               */
     OCSL_TIMEOUT = 5,       /* a bounded device wait gave up (triangular sweep)   */
@@ -184,7 +187,9 @@ int ocsl_product_device(ocsl_ctx* ctx, size_t n, const double* d_x, const double
  * (:284-335); d_y = NULL gives out = a x (:275-281). */
 int ocsl_axpy_device(ocsl_ctx* ctx, size_t n, double a, const double* d_x, double b,
                      const double* d_y, double* d_out);
-/* M = `sweeps` fixed-point ILU sweeps of A; cmatrix_solver.cpp:472-552. */
+/* M = `sweeps` fixed-point ILU sweeps of A; cmatrix_solver.cpp:472-552.
+ * M is always written; OCSL_ZERO_PIVOT reports a zero or non-finite diagonal
+ * of it (the reference's commented-out check, :495-500). */
 int ocsl_ilu_device(ocsl_ctx* ctx, const double* d_A, double* d_M, int sweeps);
 /* y = L^-1 b, cmatrix_solver.cpp:555-572 ILU_forsub. */
 int ocsl_forsub_device(ocsl_ctx* ctx, const double* d_M, const double* d_b, double* d_y);
@@ -370,12 +375,31 @@ int ocsl_autotune_device(ocsl_ctx* ctx, int method, const double* d_value, int* 
  * the result to the device double *d_result, asynchronously on `stream`
  * (a cudaStream_t, NULL for the legacy default stream).  The first call on a
  * device resolves the scratch address with cudaGetSymbolAddress, so make it
- * before any stream capture.  All calls share the scratch: calls that overlap
- * on the GPU (concurrent streams) race and must be serialised by the caller. */
+ * before any stream capture.  That address belongs to the device's primary
+ * context and is kept for the life of the process: it is not valid after a
+ * cudaDeviceReset, nor under another driver context made current on that
+ * device.  All calls share the scratch: calls that overlap on the GPU
+ * (concurrent streams) race and must be serialised by the caller.  A null
+ * pointer, or one not aligned to 8 bytes, is OCSL_BAD_ARGUMENT before any
+ * CUDA call. */
 int ocsl_dot_noalloc(size_t n, const double* d_x, const double* d_y, double* d_result,
                      void* stream);
 /* Message of the last failed ocsl_dot_noalloc on this thread. */
 const char* ocsl_noalloc_last_error(void);
+
+/* Failure injection for tests of the bounded waits (no reference
+ * counterpart: the reference's sweeps are serial and never wait).  With
+ * OCSL_FAULT_SKIP_FIRST_TILE the next triangular sweep this context launches
+ * leaves out the first unit of its schedule -- tile (or cluster of tiles) 0
+ * of the structured sweep, chunk 0 of the level-scheduled one -- by starting
+ * its work dispenser at 1 with one unit fewer in the grid.  Nothing computes
+ * those rows, every wait on them runs out after its bound (about a second),
+ * the waiting rows store NaN and the call reports OCSL_TIMEOUT; no kernel
+ * faults or traps, and the context solves normally afterwards.  The
+ * injection is consumed by that one sweep; OCSL_FAULT_NONE cancels it. */
+#define OCSL_FAULT_NONE 0
+#define OCSL_FAULT_SKIP_FIRST_TILE 1
+int ocsl_inject_fault(ocsl_ctx* ctx, int kind);
 
 /* Tolerance-mode solves replay each batch of Krylov iterations after the
  * first from a CUDA graph captured on the context's stream (not on the legacy

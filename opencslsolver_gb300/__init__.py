@@ -308,6 +308,12 @@ class Context:
         """Replay iteration batches from CUDA graphs (default on)."""
         self._check(self._L.ocsl_set_graphs(self._h, int(bool(enable))), "set_graphs")
 
+    def inject_fault(self, kind: int = 1):
+        """Test hook: the next triangular sweep leaves out the first unit of its
+        schedule, so its bounded waits run out (the call reports OCSL_TIMEOUT);
+        kind 0 cancels a pending injection."""
+        self._check(self._L.ocsl_inject_fault(self._h, int(kind)), "inject_fault")
+
     def set_col_batching(self, enable: bool = True):
         """Solve the right-hand sides of solve_multi_device with the FP32-inner
         solver in lockstep groups of up to four (default on)."""

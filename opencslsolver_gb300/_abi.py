@@ -154,6 +154,7 @@ _PROTOS = {
     "ocsl_dot_noalloc": (C.c_int, [_SZ, _P, _P, _P, _P]),
     "ocsl_noalloc_last_error": (C.c_char_p, []),
     "ocsl_set_graphs": (C.c_int, [_CTX, C.c_int]),
+    "ocsl_inject_fault": (C.c_int, [_CTX, C.c_int]),
     "ocsl_set_col_batching": (C.c_int, [_CTX, C.c_int]),
     "ocsl_autotune_device": (C.c_int, [_CTX, C.c_int, C.c_void_p, C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]),

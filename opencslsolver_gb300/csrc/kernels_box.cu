@@ -589,7 +589,11 @@ void launch_one(cudaStream_t st, BoxParams<T> p)
             smem = box_sweep_smem(p.g, (int)sizeof(T), NC);
         }
     }
-    const int grid = p.g.nca * p.g.ncb * csize;
+    int grid = p.g.nca * p.g.ncb * csize;
+    if (p.S.skip_first && grid > csize) {  // fault injection: tile / cluster 0 never runs
+        preset_ticket_one(st, p.S.ticket);
+        grid -= csize;
+    }
     if (csize == 1) {
         kern<<<grid, threads, smem, st>>>(p);
         return;

@@ -206,7 +206,18 @@ struct IluParams {
     float* dinv32;
     float* A32;
     const int* done;
+    int* pivot_err;  // last sweep: OCSL_ZERO_PIVOT on a zero or non-finite M_ii
 };
+
+// A usable pivot: non-zero and finite (and, for the FP32 inner solver, a
+// finite FP32 reciprocal).  The reference's own check of the sequential
+// factor tests M_ii == 0 (cmatrix_solver.cpp:495-500, commented out there);
+// the fixed-point factor can also carry Inf / NaN from an earlier sweep.
+__device__ __forceinline__ void check_pivot(double m, const float* r32, int* err)
+{
+    const bool bad = !(m != 0.0 && isfinite(m)) || (r32 && !isfinite(*r32));
+    if (bad) atomicCAS(err, 0, (int)OCSL_ZERO_PIVOT);
+}
 
 // One Jacobi sweep of the reference's fixed-point ILU (cmatrix_solver.cpp:525-549):
 //   lower  (col < i):  Mnew_ij = (A_ij - sum_k M_ik M_kj) / M_jj
@@ -232,18 +243,21 @@ __global__ void __launch_bounds__(kThreads) ilu_sweep_kernel(IluParams p)
         if (p.M32) p.M32[j] = (float)m;
         if (p.A32) p.A32[j] = (float)a;
         if (j == di) {
+            float r32 = 0.f;
             if (p.dinv) {
                 const double r = 1.0 / m;
                 p.dinv[i] = r;
-                if (p.dinv32) p.dinv32[i] = (float)r;
+                r32 = (float)r;
+                if (p.dinv32) p.dinv32[i] = r32;
             }
+            if (p.pivot_err) check_pivot(m, p.dinv32 ? &r32 : nullptr, p.pivot_err);
         }
     }
 }
 
 __global__ void factor_outputs_kernel(int n, const int* rp, const int* diag, const double* M,
                                       const double* A, double* dinv, float* M32, float* dinv32,
-                                      float* A32)
+                                      float* A32, int* pivot_err)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -252,9 +266,12 @@ __global__ void factor_outputs_kernel(int n, const int* rp, const int* diag, con
         if (M32) M32[j] = (float)M[j];
         if (A32) A32[j] = (float)A[j];
     }
-    const double r = 1.0 / M[diag[i]];
+    const double m = M[diag[i]];
+    const double r = 1.0 / m;
+    const float r32 = (float)r;
     if (dinv) dinv[i] = r;
-    if (dinv32) dinv32[i] = (float)r;
+    if (dinv32) dinv32[i] = r32;
+    if (pivot_err) check_pivot(m, dinv32 ? &r32 : nullptr, pivot_err);
 }
 
 // Fill a sweep's output with the all-ones pattern, unless the solve is done:
@@ -300,7 +317,23 @@ SweepParams<T> make_sweep(const DevPattern& P, bool forward, const T* M, const T
     return p;
 }
 
+// Fault injection (SweepSync::skip_first): the dispenser starts at 1 and the
+// grid is one chunk short, so chunk 0 is never solved.  Returns the chunks
+// left out (0 when there is only one).
+int skip_chunks(cudaStream_t st, const SweepSync& S, int nchunks)
+{
+    if (!S.skip_first || nchunks < 2) return 0;
+    preset_ticket_one(st, S.ticket);
+    return 1;
+}
+
 }  // namespace
+
+void preset_ticket_one(cudaStream_t st, unsigned* ticket)
+{
+    // little-endian word 0 -> 1: only its lowest byte changes
+    cudaMemsetAsync(ticket, 1, 1, st);
+}
 
 template <typename T>
 void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* rhs, T* out,
@@ -308,7 +341,7 @@ void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 {
     if (P.n == 0) return;  // `out` holds the all-ones pattern (filled by the caller)
     auto p = make_sweep<T>(P, true, M, nullptr, rhs, out, S, done);
-    fw_sweep_kernel<T><<<p.nchunks, kThreads, 0, st>>>(p);
+    fw_sweep_kernel<T><<<p.nchunks - skip_chunks(st, S, p.nchunks), kThreads, 0, st>>>(p);
 }
 
 template <typename T>
@@ -317,15 +350,17 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 {
     if (P.n == 0) return;  // `out` holds the all-ones pattern (filled by the caller)
     auto p = make_sweep<T>(P, false, M, dinv, rhs, out, S, done);
+    const int grid = p.nchunks - skip_chunks(st, S, p.nchunks);
     if (divmode == 0)
-        bw_sweep_kernel<T, true><<<p.nchunks, kThreads, 0, st>>>(p);
+        bw_sweep_kernel<T, true><<<grid, kThreads, 0, st>>>(p);
     else
-        bw_sweep_kernel<T, false><<<p.nchunks, kThreads, 0, st>>>(p);
+        bw_sweep_kernel<T, false><<<grid, kThreads, 0, st>>>(p);
 }
 
 template <typename T>
 void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
-                      double* dinv, float* M32, float* dinv32, float* A32, const int* done)
+                      double* dinv, float* M32, float* dinv32, float* A32, const int* done,
+                      int* pivot_err)
 {
     static_assert(sizeof(T) == 8, "the ILU factor is computed in FP64");
     if (P.n == 0) return;
@@ -345,6 +380,7 @@ void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T*
     p.dinv32 = dinv32;
     p.A32 = A32;
     p.done = done;
+    p.pivot_err = pivot_err;
     ilu_sweep_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(p);
 }
 
@@ -367,11 +403,11 @@ void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done,
 }
 
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
-                           double* dinv, float* M32, float* dinv32, float* A32)
+                           double* dinv, float* M32, float* dinv32, float* A32, int* pivot_err)
 {
     if (P.n == 0) return;
     factor_outputs_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-        P.n, P.rp, P.diag, M, A, dinv, M32, dinv32, A32);
+        P.n, P.rp, P.diag, M, A, dinv, M32, dinv32, A32, pivot_err);
 }
 
 template void launch_fw_sweep<double>(cudaStream_t, const DevPattern&, const double*,
@@ -385,6 +421,6 @@ template void launch_bw_sweep<float>(cudaStream_t, const DevPattern&, const floa
                                      const float*, float*, int, const SweepSync&, const int*);
 template void launch_ilu_sweep<double>(cudaStream_t, const DevPattern&, const double*,
                                        const double*, double*, double*, float*, float*, float*,
-                                       const int*);
+                                       const int*, int*);
 
 }  // namespace ocsl

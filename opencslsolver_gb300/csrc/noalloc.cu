@@ -18,6 +18,7 @@
 // same over the tile sums), so the result equals ocsl_dot_device bit for bit.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -95,6 +96,8 @@ dot_noalloc_kernel(int n, const double* __restrict__ x, const double* __restrict
     }
 }
 
+bool aligned8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
+
 // Address of the scratch array on the current device; resolved once per device.
 int scratch_for_current_device(double** out)
 {
@@ -131,6 +134,12 @@ int ocsl_dot_noalloc(size_t n, const double* d_x, const double* d_y, double* d_r
 {
     if (!d_result || (n > 0 && (!d_x || !d_y))) {
         g_noalloc_error = "null pointer";
+        return OCSL_BAD_ARGUMENT;
+    }
+    // the kernel loads and stores whole doubles: a pointer off an 8-byte
+    // boundary would fault in the caller's context, so it is refused here
+    if (!aligned8(d_result) || (n > 0 && (!aligned8(d_x) || !aligned8(d_y)))) {
+        g_noalloc_error = "pointer not aligned to 8 bytes";
         return OCSL_BAD_ARGUMENT;
     }
     if (n > kMaxN) {

@@ -131,7 +131,15 @@ struct SweepSync {
     unsigned* ticket;    // chunk dispenser (reset by the last CTA)
     unsigned* finished;
     int* err;            // ocsl_status of a bounded wait that gave up
+    // Host side only (ocsl_inject_fault): the launcher starts the dispenser at
+    // 1 and launches one tile / cluster / chunk fewer, so the first unit of
+    // the schedule is never computed and the waits on it run out.
+    int skip_first;
 };
+
+// Sets the dispenser to 1 on `st` (its only word is 0 between launches: the
+// last CTA of every sweep resets it).
+void preset_ticket_one(cudaStream_t st, unsigned* ticket);
 
 // ------------------------------------------------------------------ host-side launchers
 // All launchers enqueue on `st` and never synchronise.
@@ -185,9 +193,12 @@ void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& p, const ReduceSt
                 Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit,
                 const Cols& cols = Cols{});
 
+// pivot_err (last sweep only): set to OCSL_ZERO_PIVOT when a diagonal of the
+// factor is zero or non-finite (or its FP32 reciprocal is not finite)
 template <typename T>
 void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
-                      double* dinv, float* M32, float* dinv32, float* A32, const int* done);
+                      double* dinv, float* M32, float* dinv32, float* A32, const int* done,
+                      int* pivot_err = nullptr);
 
 template <typename T>
 void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* rhs, T* out,
@@ -235,7 +246,8 @@ void launch_fill_ones(cudaStream_t st, void* out, size_t bytes, const int* done,
 
 // Factor side outputs without a sweep: dinv = 1 / M_ii and FP32 copies.
 void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M, const double* A,
-                           double* dinv, float* M32, float* dinv32, float* A32);
+                           double* dinv, float* M32, float* dinv32, float* A32,
+                           int* pivot_err = nullptr);
 
 // assembly.cu
 void launch_assemble(cudaStream_t st, const DevPattern& P, const DevFaces& F,

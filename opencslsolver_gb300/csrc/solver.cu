@@ -125,6 +125,16 @@ struct ocsl_ctx {
 
     // sweep kernel choice (ocsl_set_sweep_kernel): 0 auto, 1 level-scheduled, 2 structured
     int sweep_kernel = 0;
+    // ocsl_inject_fault: the next sweep leaves out the first unit of its schedule
+    bool fault_skip_pending = false;
+    // the sync block of the next sweep launch (consumes a pending injection)
+    SweepSync next_sync()
+    {
+        SweepSync s = S;
+        s.skip_first = fault_skip_pending ? 1 : 0;
+        fault_skip_pending = false;
+        return s;
+    }
     // structured-sweep geometry requests per precision ([0] FP64, [1] FP32):
     // TA, TB (0 = heuristic) and tiles per thread-block cluster
     int box_tile[2][2] = {{0, 0}, {0, 0}};
@@ -161,6 +171,8 @@ struct ocsl_ctx {
     const double* fac_M = nullptr;
     const double* fac_soa64 = nullptr;
     const float* fac_soa32 = nullptr;
+    bool fac_checked = false;  // fac_status holds the pivot check of fac_M
+    int fac_status = OCSL_OK;
 
     // face-loop assembly: the mesh's face incidence (ocsl_set_faces)
     DevFaces F{};
@@ -505,11 +517,11 @@ struct Solve {
         float* M32 = want_fp32 ? c->d_M32 : nullptr;
         float* dinv32 = want_fp32 ? c->d_dinv32 : nullptr;
         float* A32 = want_fp32 ? c->d_A32 : nullptr;
+        // every factor's diagonal is checked on the device (OCSL_ZERO_PIVOT
+        // into the context's error word, read by pivot_status / at the end)
         if (sweeps == 0) {
-            if (want_dinv || want_fp32) {
-                ProfScope ps(c, st, PC_ILU);
-                launch_factor_outputs(st, P, A, A, dinv, M32, dinv32, A32);
-            }
+            ProfScope ps(c, st, PC_ILU);
+            launch_factor_outputs(st, P, A, A, dinv, M32, dinv32, A32, c->d_err);
             return A;
         }
         const double* src = A;
@@ -520,7 +532,7 @@ struct Solve {
             ProfScope ps(c, st, PC_ILU);
             launch_ilu_sweep<double>(st, P, A, src, dst, last ? dinv : nullptr,
                                      last ? M32 : nullptr, last ? dinv32 : nullptr,
-                                     last ? A32 : nullptr, dn);
+                                     last ? A32 : nullptr, dn, last ? c->d_err : nullptr);
             src = dst;
         }
         return src;
@@ -538,12 +550,12 @@ struct Solve {
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
         if (use_box() && soa<TT>())
-            launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, true, 0, c->S,
-                                 k >= 0 ? done(k) : nullptr, cols, kDoneStride);
+            launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, true, 0,
+                                 c->next_sync(), k >= 0 ? done(k) : nullptr, cols, kDoneStride);
         else
             for (int q = 0; q < cols.n; ++q)  // level-scheduled: one launch per column
-                launch_fw_sweep<TT>(st, P, M, rhs + q * cols.ld, out + q * cols.ld, c->S,
-                                    k >= 0 ? done(k + q) : nullptr);
+                launch_fw_sweep<TT>(st, P, M, rhs + q * cols.ld, out + q * cols.ld,
+                                    c->next_sync(), k >= 0 ? done(k + q) : nullptr);
     }
     // The box geometry, narrowed while a CTA's staging for cols.n columns
     // exceeds the shared-memory limit.
@@ -589,6 +601,7 @@ struct Solve {
         }
         const double* M = factor(A, sweeps, want_dinv, want_fp32, k);
         prepare_box(M, want64, recip64, want32);
+        c->fac_checked = false;
         c->fac_M = M;
         c->fac_soa64 = soa64;
         c->fac_soa32 = soa32;
@@ -628,11 +641,11 @@ struct Solve {
         ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
         if (use_box() && soa<TT>())
             launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, false, divmode,
-                                 c->S, k >= 0 ? done(k) : nullptr, cols, kDoneStride);
+                                 c->next_sync(), k >= 0 ? done(k) : nullptr, cols, kDoneStride);
         else
             for (int q = 0; q < cols.n; ++q)
                 launch_bw_sweep<TT>(st, P, M, dinv, rhs + q * cols.ld, out + q * cols.ld, divmode,
-                                    c->S, k >= 0 ? done(k + q) : nullptr);
+                                    c->next_sync(), k >= 0 ? done(k + q) : nullptr);
     }
     // Enqueue `fn` (a fixed sequence of launches) through a CUDA graph keyed by
     // (kind, ptrs): captured on first use, replayed afterwards.  Returns false
@@ -641,8 +654,8 @@ struct Solve {
     template <typename Fn>
     bool graph_launch(int kind, std::initializer_list<const void*> ptrs, Fn&& fn)
     {
-        if (!c->graphs_on || c->prof_on || st == nullptr || st == cudaStreamLegacy ||
-            st == cudaStreamPerThread)
+        if (!c->graphs_on || c->prof_on || c->fault_skip_pending || st == nullptr ||
+            st == cudaStreamLegacy || st == cudaStreamPerThread)
             return false;
         const void* key[6] = {};
         int i = 0;
@@ -679,6 +692,16 @@ struct Solve {
         }
         CK(cudaGraphLaunch(c->graph_exec, st));
         return true;
+    }
+    // OCSL_ZERO_PIVOT when the current factor has a zero or non-finite
+    // diagonal (synchronises once per factor; a reused factor keeps its verdict)
+    int pivot_status()
+    {
+        if (!c->fac_checked) {
+            c->fac_status = device_error() == OCSL_ZERO_PIVOT ? OCSL_ZERO_PIVOT : OCSL_OK;
+            c->fac_checked = true;
+        }
+        return c->fac_status;
     }
     int device_error()
     {
@@ -749,6 +772,15 @@ struct TolResult {
     double relres = 0.0;
     int status = OCSL_OK;
 };
+
+// A factor with a zero or non-finite pivot: no iteration runs, x is unchanged.
+TolResult zero_pivot_result()
+{
+    TolResult r;
+    r.relres = NAN;
+    r.status = OCSL_ZERO_PIVOT;
+    return r;
+}
 
 constexpr int kBatch = 2;  // iterations enqueued between looks at the scalars
 
@@ -869,6 +901,7 @@ TolResult run_bicgstab_tol(Solve& s, const double* A, const double* b, double* x
 {
     double** v = s.c->v64;
     const double* M = s.factored(A, o.ilu_sweeps, true, false, -1, true, true, false);
+    if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
     s.prepare_spmv(A, true, false);
     return run_restarted(
         s, A, b, x, o, [&] { s.vec<double>(V_COPY2, {v[RH], v[P], v[R]}, 0, EP_STORE); },
@@ -884,6 +917,7 @@ TolResult run_pcg_tol(Solve& s, const double* A, const double* b, double* x, con
 {
     double** v = s.c->v64;
     s.factored(A, 0, true, false, -1, false, false, false);  // Jacobi: dinv = 1 / A_ii
+    if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
     s.prepare_spmv(A, true, false);
     return run_restarted(
         s, A, b, x, o,
@@ -909,6 +943,7 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
     TolResult res;
     const double tol2 = o.tol * o.tol;
     const double* M = s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+    if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
     s.prepare_spmv(A, true, true);
     int total = 0;
     s.reset_scalars(0, tol2);
@@ -974,6 +1009,12 @@ std::vector<TolResult> run_bicgstab_ir32_cols(Solve& s, const double* A, const d
     std::vector<int> fin(nc, 0), total(nc, 0);
     std::vector<double> tol2(nc, o.tol * o.tol), itol2(nc, 0.0);
     s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+    if (s.pivot_status() != OCSL_OK) {
+        for (auto& r : res) r = zero_pivot_result();
+        s.cols = Cols{};
+        s.outer_k = 0;
+        return res;
+    }
     s.prepare_spmv(A, true, true);
     s.reset_scalars_n(KO, nc, tol2.data(), nullptr);
     for (int outer = 0;; ++outer) {
@@ -1112,6 +1153,7 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
     r.status = status;
     if (out) *out = r;
     if (status == OCSL_TIMEOUT) c->last_error = "a triangular-sweep wait hit its bound";
+    if (status == OCSL_ZERO_PIVOT) c->last_error = "the factor has a zero or non-finite pivot";
     return status;
 }
 
@@ -1667,11 +1709,15 @@ int ocsl_ilu_device(ocsl_ctx* c, const double* A, double* M, int sweeps)
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
         c->fac_M = nullptr;
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
         const double* F = s.factor(A, sweeps, false, false, -1);
         CK(cudaMemcpyAsync(M, F, sizeof(double) * (size_t)c->P.nnz, cudaMemcpyDeviceToDevice,
                            c->stream));
         CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(c->stream));
+        // M is written either way (the reference has no check); the status
+        // tells the caller that a diagonal of it is zero or non-finite
+        if (s.device_error() == OCSL_ZERO_PIVOT)
+            return fail(c, OCSL_ZERO_PIVOT, "the factor has a zero or non-finite pivot");
     } catch (const CudaError& e) {
         return from_cuda(c, e);
     }
@@ -1856,6 +1902,13 @@ int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
         tiles[0] = c->P.box_ok ? c->P.box.TA : 0;
         tiles[1] = c->P.box_ok ? c->P.box.TB : 0;
     }
+    return OCSL_OK;
+}
+
+int ocsl_inject_fault(ocsl_ctx* c, int kind)
+{
+    if (!c || kind < OCSL_FAULT_NONE || kind > OCSL_FAULT_SKIP_FIRST_TILE) return OCSL_BAD_ARGUMENT;
+    c->fault_skip_pending = kind == OCSL_FAULT_SKIP_FIRST_TILE;
     return OCSL_OK;
 }
 

@@ -215,10 +215,11 @@ def _kuhn_tets():
     return np.array(tets, np.int64)  # (6, 4)
 
 
-def tet_pprime(nx: int, ny: int | None = None, nz: int | None = None, *, peclet: float = 50.0,
-               seed: int = BASE_SEED, jitter: float = 0.1) -> System:
-    ny = nx if ny is None else ny
-    nz = nx if nz is None else nz
+def _tet_mesh(nx, ny, nz, seed, jitter):
+    """Kuhn-split tet mesh of the jittered box: node coordinates, cell
+    vertices, centroids, the interior faces (L < R, sorted by vertex key) with
+    their area vectors (oriented L -> R) and centres, and the boundary faces
+    (cell, vertex triple)."""
     nh = nx * ny * nz
     n = 6 * nh
     P = _jittered_nodes(nx, ny, nz, np.random.default_rng(seed), jitter)
@@ -233,7 +234,6 @@ def tet_pprime(nx: int, ny: int | None = None, nz: int | None = None, *, peclet:
     tv = corner[:, kt].reshape(n, 4)            # cell = 6*hex + local tet
     X = P.reshape(-1, 3)
     cent = X[tv].mean(axis=1)
-    # faces: each tet face = the 3 vertices other than vertex m
     faces = np.stack([np.sort(np.delete(tv, m, axis=1), axis=1) for m in range(4)], axis=1)
     fkeys = faces.reshape(-1, 3)
     owner = np.repeat(np.arange(n), 4)
@@ -251,6 +251,18 @@ def tet_pprime(nx: int, ny: int | None = None, nz: int | None = None, *, peclet:
     FC = (p0 + p1 + p2) / 3.0
     dvec = cent[R] - cent[L]
     A *= np.sign(np.einsum("ij,ij->i", A, dvec))[:, None]
+    paired = np.zeros(fkeys.shape[0], bool)
+    paired[a_idx] = True
+    paired[b_idx] = True
+    bidx = np.nonzero(~paired)[0]
+    return n, X, tv, cent, L, R, A, FC, dvec, owner[bidx], fkeys[bidx]
+
+
+def tet_pprime(nx: int, ny: int | None = None, nz: int | None = None, *, peclet: float = 50.0,
+               seed: int = BASE_SEED, jitter: float = 0.1) -> System:
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    n, X, tv, cent, L, R, A, FC, dvec, _, _ = _tet_mesh(nx, ny, nz, seed, jitter)
     Amag = np.linalg.norm(A, axis=1)
     dist = np.linalg.norm(dvec, axis=1)
     # boundary cells: tets with fewer than 4 interior faces
@@ -443,6 +455,83 @@ def hex_flow_state(nx: int, ny: int | None = None, nz: int | None = None, *, see
               transient=int(transient), implicit_underrelaxation=0.7)
     return FlowCase(f"hexflow{nx}x{ny}x{nz}", rp, col, left.astype(np.int32),
                     right.astype(np.int32), bc_left.astype(np.int32), state, eq, inlet)
+
+
+def tet_flow_state(nx: int, ny: int | None = None, nz: int | None = None, *,
+                   seed: int = BASE_SEED + 7, jitter: float = 0.1, equation: int = 1,
+                   transient: bool = True, blended: bool = True,
+                   inlet_value: float = 0.0) -> FlowCase:
+    """Seeded flow state on the Kuhn-split tet mesh of a jittered nx*ny*nz box
+    (6 tets per hex), in the same form as hex_flow_state but with general
+    geometry: interior faces in vertex-key order, geo_aver from the face-centre
+    distances (cfvm.cpp:137), ksi_A = |A| / d, tet volumes; boundary faces on
+    x = 0 a supersonic inlet, x = 1 a pressure outlet, walls elsewhere, with
+    outward area vectors and the centroid's distance to the face plane."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    n, X, tv, cent, L, R, A, FC, dvec, bcell, bnodes = _tet_mesh(nx, ny, nz, seed, jitter)
+    rng = np.random.default_rng(seed + 11)
+    Amag = np.linalg.norm(A, axis=1)
+    dist = np.linalg.norm(dvec, axis=1)
+    dL = np.linalg.norm(FC - cent[L], axis=1)
+    dR = np.linalg.norm(cent[R] - FC, axis=1)
+    geo = dR / (dL + dR)
+    vel = 100.0 * (1.0 + 0.2 * _velocity(cent, rng))
+    T = 300.0 + 20.0 * np.sin(2 * np.pi * cent[:, 0]) * np.cos(np.pi * cent[:, 1])
+    p = np.full(n, 1.0e5)
+    rho = p / AIR["R_specific"] / T
+    rho_f = geo * rho[L] + (1.0 - geo) * rho[R]
+    u_f = geo[:, None] * vel[L] + (1.0 - geo[:, None]) * vel[R]
+    mdot = rho_f * np.einsum("ij,ij->i", u_f, A)
+    e1, e2, e3 = (X[tv[:, k]] - X[tv[:, 0]] for k in (1, 2, 3))
+    vol = np.abs(np.einsum("ij,ij->i", e1, np.cross(e2, e3))) / 6.0
+    dt = 1e-4
+    qy = np.random.default_rng(seed + 1).uniform(0.5, 2.0, L.size) * (
+        20.0 / 4.0 * vol.mean() / (dt * AIR["R_specific"] * 300.0 * AIR["gamma"] * rho_f))
+    # boundary faces: outward area vector, plane distance, kind by position
+    q0, q1, q2 = X[bnodes[:, 0]], X[bnodes[:, 1]], X[bnodes[:, 2]]
+    bav = 0.5 * np.cross(q1 - q0, q2 - q0)
+    bfc = (q0 + q1 + q2) / 3.0
+    out = np.einsum("ij,ij->i", bav, bfc - cent[bcell])
+    bav *= np.sign(out)[:, None]
+    bc_area = np.linalg.norm(bav, axis=1)
+    perp = np.abs(np.einsum("ij,ij->i", bav, bfc - cent[bcell])) / bc_area
+    nb = bcell.size
+    bc_type = np.full(nb, _abi_bc("WALL"), np.int32)
+    bc_type[bfc[:, 0] < 1e-12] = _abi_bc("SUPERSONIC_INLET")
+    bc_type[bfc[:, 0] > 1.0 - 1e-12] = _abi_bc("PRESSURE_OUTLET")
+    bc_vel = vel[bcell].T.copy()
+    bc_rho = rho[bcell]
+    bc_mdot = bc_rho * np.einsum("ij,ij->i", vel[bcell], bav)
+    bc_mdot[bc_type == _abi_bc("WALL")] = 0.0
+    inlet = np.nonzero(bc_type == _abi_bc("SUPERSONIC_INLET"))[0]
+    bc_value = np.zeros(nb)
+    bc_value[inlet] = inlet_value
+    # the reference's pattern for this face connectivity (host-only builder)
+    from . import build_pattern
+
+    rp, col = build_pattern(n, L.astype(np.int32), R.astype(np.int32), bcell.astype(np.int32))
+    stress = np.random.default_rng(seed + 3).uniform(-1.0, 1.0, (3, L.size)) * 1e-3
+    state = {
+        "geo_aver": geo, "ksi_A": Amag / dist, "mdot": mdot, "density": rho_f, "qy": qy,
+        "stress": stress, "bc_type": bc_type, "bc_wall": np.full(nb, 1, np.int32),
+        "bc_supersonic": np.zeros(nb, np.int32), "bc_area": bc_area, "bc_area_vector": bav.T.copy(),
+        "bc_perp_dist": perp, "bc_ksi_A": bc_area / perp, "bc_mdot": bc_mdot,
+        "bc_density": bc_rho, "bc_qy": np.full(nb, float(np.mean(qy))),
+        "bc_temperature": T[bcell], "bc_enthalpy": 1005.0 * T[bcell], "bc_velocity": bc_vel,
+        "bc_value": bc_value, "bc_thermal": (np.arange(nb) % 2).astype(np.int32),
+        "volume": vol, "delta_t": np.full(n, dt), "velocity": vel.T.copy(),
+        "velocity_last": (0.99 * vel).T.copy(),
+        "pressure_grad": np.random.default_rng(seed + 4).uniform(-1.0, 1.0, (3, n)),
+        "density_c": rho, "density_last": rho * (1.0 + 1e-4 * np.sin(7.0 * cent[:, 2])),
+        "pressure": p, "pressure_last": p.copy(),
+        "pressure_corr": np.random.default_rng(seed + 5).uniform(-1.0, 1.0, n),
+        "temperature": T, "enthalpy": 1005.0 * T, "enthalpy_last": 1005.0 * T * 0.999,
+    }
+    eq = dict(AIR, equation=equation, dimension=0, viscous=0, blended=int(blended),
+              transient=int(transient), implicit_underrelaxation=0.7)
+    return FlowCase(f"tetflow{nx}x{ny}x{nz}", rp, col, L.astype(np.int32), R.astype(np.int32),
+                    bcell.astype(np.int32), state, eq, inlet)
 
 
 def _abi_bc(name: str) -> int:

@@ -22,7 +22,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libocsl_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liboracle_ref.so")
 REF_SHOCKTUBE = os.path.join(HERE, "_ref", "ref_shocktube")
-REF_DIR = os.environ.get("OCSL_REFERENCE_DIR", "/root/reference")
+# The reference's source directory: OCSL_REFERENCE_DIR, else a checkout named
+# "reference" beside this repository.  Where neither exists, everything that
+# needs the reference skips.
+REF_DIR = os.environ.get("OCSL_REFERENCE_DIR") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference"))
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 _P = C.c_void_p

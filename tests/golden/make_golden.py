@@ -2,7 +2,10 @@
 
 Run in a container where the reference's sources are present:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference <reference source dir>]
+
+(default: OCSL_REFERENCE_DIR, else a checkout named "reference" beside this
+repository).
 
 It builds the reference from its own sources (oracle/Makefile, target `ref`),
 then writes:
@@ -191,7 +194,7 @@ def make_assembly(out_dir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=orc.REF_DIR)
     a = ap.parse_args()
     orc.build(a.reference)
     ref = orc.Reference()

@@ -205,3 +205,21 @@ def test_build_pattern_hex_box_and_errors(lib_built):
         ocsl.build_pattern(f.n, f.left, np.full_like(f.right, f.n), f.bc_left)
     rp, col = ocsl.build_pattern(4, [], [], [])  # isolated cells: diagonal only
     assert rp.tolist() == [0, 1, 2, 3, 4] and col.tolist() == [0, 1, 2, 3]
+
+
+def test_dot_noalloc_refuses_bad_pointers_before_any_cuda_call(lib_built):
+    # null and misaligned pointers are refused on the host, so no kernel could
+    # fault on them; this runs (and must pass) without a GPU
+    L = lib_built
+    buf = (C.c_double * 4)()
+    base = C.addressof(buf)
+    good = C.c_void_p(base)
+    odd = C.c_void_p(base + 4)
+    assert L.ocsl_dot_noalloc(4, None, good, good, None) == _abi.BAD_ARGUMENT
+    assert b"null" in L.ocsl_noalloc_last_error()
+    assert L.ocsl_dot_noalloc(4, good, good, None, None) == _abi.BAD_ARGUMENT
+    for x, y, r in ((odd, good, good), (good, odd, good), (good, good, odd)):
+        assert L.ocsl_dot_noalloc(4, x, y, r, None) == _abi.BAD_ARGUMENT
+        assert b"aligned" in L.ocsl_noalloc_last_error()
+    # with n = 0 the inputs are not read, only the result pointer is checked
+    assert L.ocsl_dot_noalloc(0, odd, odd, odd, None) == _abi.BAD_ARGUMENT

@@ -55,3 +55,31 @@ def test_dot_noalloc_limits(lib_built, torch_cuda):
     assert st == 0
     torch.cuda.synchronize()
     assert out.item() == 0.0
+
+
+def test_dot_noalloc_at_the_limit(lib_built, torch_cuda):
+    # n exactly at the maximum uses all 4,096 tile slots, the counter sits in
+    # the slot right after them; bit-equal to the context-based dot
+    import opencslsolver_gb300 as ocsl
+
+    torch = torch_cuda
+    L = lib_built
+    n = 8_388_608
+    g = torch.Generator(device="cuda").manual_seed(7)
+    X = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    Y = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    with ocsl.Context(0) as ctx:
+        want = ctx.dot_device(X, Y)
+    out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):
+        st = L.ocsl_dot_noalloc(n, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()),
+                                C.c_void_p(out.data_ptr()), C.c_void_p(stream))
+        assert st == 0, L.ocsl_noalloc_last_error()
+        torch.cuda.synchronize()
+        assert out.item() == want
+    # a misaligned device pointer is refused before any launch
+    bad = C.c_void_p(X.data_ptr() + 4)
+    st = L.ocsl_dot_noalloc(16, bad, C.c_void_p(Y.data_ptr()), C.c_void_p(out.data_ptr()),
+                            C.c_void_p(stream))
+    assert st == 7 and b"aligned" in L.ocsl_noalloc_last_error()
