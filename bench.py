@@ -339,7 +339,7 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel in the headline timed region
     peak, peak_kind = load_peaks()
-    structured = ctx.sweep_info()["kind"] == 2
+    structured = ctx.sweep_info()["kind"] in (2, 3)
     algo = algorithmic_bytes(s.n, s.nnz_real, nnz_l, nnz_u, structured)
     per_cat = {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof_ir.items() if v[1]}
     total_ms = sum(v["ms_total"] for k, v in per_cat.items())

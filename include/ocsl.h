@@ -33,7 +33,7 @@ typedef struct ocsl_ctx ocsl_ctx;
 typedef enum {
     OCSL_OK = 0,
     OCSL_NOT_CONVERGED = 1, /* tolerance mode hit maxit (x holds the last iterate) */
-    OCSL_ZERO_PIVOT = 2,    /* a zero or non-finite pivot in the factor: mode R
+    OCSL_ZERO_PIVOT = 2,    /* a zero or infinite pivot in the factor: mode R
                                still computes exactly as the reference (which has
                                no check) and reports it; mode T runs no iteration
                                and leaves x unchanged                               */
@@ -188,7 +188,7 @@ int ocsl_product_device(ocsl_ctx* ctx, size_t n, const double* d_x, const double
 int ocsl_axpy_device(ocsl_ctx* ctx, size_t n, double a, const double* d_x, double b,
                      const double* d_y, double* d_out);
 /* M = `sweeps` fixed-point ILU sweeps of A; cmatrix_solver.cpp:472-552.
- * M is always written; OCSL_ZERO_PIVOT reports a zero or non-finite diagonal
+ * M is always written; OCSL_ZERO_PIVOT reports a zero or infinite diagonal
  * of it (the reference's commented-out check, :495-500). */
 int ocsl_ilu_device(ocsl_ctx* ctx, const double* d_A, double* d_M, int sweeps);
 /* y = L^-1 b, cmatrix_solver.cpp:555-572 ILU_forsub. */
@@ -321,10 +321,16 @@ int ocsl_bc_value_grad_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
 
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
- * level-scheduled kernel, 2 the structured kernel (OCSL_BAD_ARGUMENT if the
- * pattern is not a box).  tile_a / tile_b set the structured kernel's column
- * tile, one thread per column, at most 256 (0 = default 16 x 8).  All
- * kernels give bit-identical results. */
+ * level-scheduled kernel, 2 the structured CTA kernel, 3 the structured
+ * warp-pipelined kernel (2 and 3: OCSL_BAD_ARGUMENT if the pattern is not a
+ * box).  With kind 2, tile_a / tile_b set the CTA kernel's column tile, one
+ * thread per column, at most 256 (0 = default 16 x 8).  With kind 3 they set
+ * the warp-pipelined kernel's warps per CTA (1..8, 0 = default 4) and its
+ * start lag behind an upstream CTA in rows (0 = default 6).  In automatic
+ * mode a single right-hand side uses the warp-pipelined kernel (or, after
+ * ocsl_autotune_device, whichever structured kernel timed faster for that
+ * precision); column-batched solves use the CTA kernel.  All kernels give
+ * bit-identical results. */
 int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
 /* Thread-block clusters of the structured sweep: cx x cy neighbouring column
  * tiles (cx * cy <= 16; 1 x 1 = none; 0 x 0 = automatic, the default: 2 x 4
@@ -337,6 +343,10 @@ int ocsl_set_sweep_kernel(ocsl_ctx* ctx, int kind, int tile_a, int tile_b);
  * shape.  No reference counterpart (the reference sweeps serially,
  * cmatrix_solver.cpp:555-611). */
 int ocsl_set_sweep_cluster(ocsl_ctx* ctx, int cx, int cy);
+/* Whether single-right-hand-side sweeps of the FP64 (fp32 = 0) or FP32
+ * (fp32 = 1) solvers run the warp-pipelined kernel (*on), and its warps per
+ * CTA and start lag; zeros when they do not. */
+int ocsl_wave_geometry(const ocsl_ctx* ctx, int fp32, int* on, int* warps, int* lag);
 /* The structured-sweep geometry of the FP64 (fp32 = 0) or FP32 (fp32 = 1)
  * sweeps: tiles[2] = (TA, TB), cluster[2] = (cx, cy) after clipping; zeros
  * when no structured sweep applies.  ocsl_set_sweep_kernel and

@@ -269,7 +269,9 @@ class Context:
 
     # -- triangular-sweep kernel choice
     def set_sweep_kernel(self, kind: int = 0, tile_a: int = 0, tile_b: int = 0):
-        """0 automatic, 1 level-scheduled, 2 structured (7-point box patterns)."""
+        """0 automatic, 1 level-scheduled, 2 structured CTA kernel (tile_a x
+        tile_b column tile), 3 structured warp-pipelined kernel (tile_a warps
+        per CTA, tile_b start lag); 2 and 3 need a 7-point box pattern."""
         self._check(self._L.ocsl_set_sweep_kernel(self._h, kind, tile_a, tile_b), "sweep kernel")
 
     def set_sweep_cluster(self, cx: int = 1, cy: int = 1):
@@ -289,6 +291,10 @@ class Context:
             self._check(self._L.ocsl_sweep_geometry(self._h, fp32, t, cl), "sweep_geometry")
             out["tiles" + suffix] = tuple(t)
             out["cluster" + suffix] = tuple(cl)
+            on, wa, lag = C.c_int(), C.c_int(), C.c_int()
+            self._check(self._L.ocsl_wave_geometry(self._h, fp32, C.byref(on), C.byref(wa),
+                                                   C.byref(lag)), "wave_geometry")
+            out["wave" + suffix] = {"on": bool(on.value), "warps": wa.value, "lag": lag.value}
         return out
 
     def autotune(self, method, value):
@@ -301,8 +307,10 @@ class Context:
                                                  C.byref(ta), C.byref(tb), C.byref(us)),
                     "autotune")
         fp32 = _method(method) == ILU_BICGSTAB_IR32
+        info = self.sweep_info()
         return {"tiles": (ta.value, tb.value), "sweep_us": us.value,
-                "cluster": self.sweep_info()["cluster32" if fp32 else "cluster"]}
+                "cluster": info["cluster32" if fp32 else "cluster"],
+                "wave": info["wave32" if fp32 else "wave"]}
 
     def set_graphs(self, enable: bool = True):
         """Replay iteration batches from CUDA graphs (default on)."""

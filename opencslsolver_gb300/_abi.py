@@ -151,6 +151,8 @@ _PROTOS = {
                                   C.POINTER(C.c_int)]),
     "ocsl_set_sweep_cluster": (C.c_int, [_CTX, C.c_int, C.c_int]),
     "ocsl_sweep_geometry": (C.c_int, [_CTX, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "ocsl_wave_geometry": (C.c_int, [_CTX, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]),
     "ocsl_dot_noalloc": (C.c_int, [_SZ, _P, _P, _P, _P]),
     "ocsl_noalloc_last_error": (C.c_char_p, []),
     "ocsl_set_graphs": (C.c_int, [_CTX, C.c_int]),

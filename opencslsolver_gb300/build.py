@@ -20,7 +20,8 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libocsl_gb300.so")
 
-SOURCES = ["kernels_krylov.cu", "kernels_ilu.cu", "kernels_box.cu", "solver.cu", "pattern.cpp",
+SOURCES = ["kernels_krylov.cu", "kernels_ilu.cu", "kernels_box.cu", "kernels_wave.cu", "solver.cu",
+           "pattern.cpp",
            "noalloc.cu", "adjoint.cu", "assembly.cu", "batch.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -206,16 +206,18 @@ struct IluParams {
     float* dinv32;
     float* A32;
     const int* done;
-    int* pivot_err;  // last sweep: OCSL_ZERO_PIVOT on a zero or non-finite M_ii
+    int* pivot_err;  // last sweep: OCSL_ZERO_PIVOT on a zero or infinite M_ii
 };
 
-// A usable pivot: non-zero and finite (and, for the FP32 inner solver, a
-// finite FP32 reciprocal).  The reference's own check of the sequential
+// A broken-down pivot: zero or infinite (for the FP32 inner solver also an
+// infinite FP32 reciprocal).  The reference's own check of the sequential
 // factor tests M_ii == 0 (cmatrix_solver.cpp:495-500, commented out there);
-// the fixed-point factor can also carry Inf / NaN from an earlier sweep.
+// the fixed-point factor turns a zero pivot into infinities in the sweeps
+// after it.  A NaN pivot comes from NaN / Inf in the matrix itself, which the
+// iteration reports as OCSL_NONFINITE.
 __device__ __forceinline__ void check_pivot(double m, const float* r32, int* err)
 {
-    const bool bad = !(m != 0.0 && isfinite(m)) || (r32 && !isfinite(*r32));
+    const bool bad = m == 0.0 || isinf(m) || (r32 && isinf(*r32));
     if (bad) atomicCAS(err, 0, (int)OCSL_ZERO_PIVOT);
 }
 

@@ -194,7 +194,7 @@ void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& p, const ReduceSt
                 const Cols& cols = Cols{});
 
 // pivot_err (last sweep only): set to OCSL_ZERO_PIVOT when a diagonal of the
-// factor is zero or non-finite (or its FP32 reciprocal is not finite)
+// factor is zero or infinite (or its FP32 reciprocal is infinite)
 template <typename T>
 void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
                       double* dinv, float* M32, float* dinv32, float* A32, const int* done,
@@ -233,6 +233,30 @@ constexpr int kMaxClusterTiles = 16;
 // g with clusters of cx x cy tiles (clipped to the tile grid and to 16
 // tiles; 1 x 1 = no clusters).
 BoxGeom box_with_cluster(BoxGeom g, int cx, int cy);
+// Warp-pipelined structured sweep (kernels_wave.cu), one right-hand side:
+// each warp solves K (along a) x 32 (along b) columns, K = 4 in FP32 and 2 in
+// FP64; a CTA holds WA warps side by side along a.
+constexpr int kWaveMaxWarps = 8;
+struct WaveGeom {
+    int D[3];      // extents of a, b, s (as BoxGeom)
+    int S[3];      // row strides of a, b, s
+    int span;      // which of x (0), y (1), z (2) is s
+    int WA;        // warps per CTA
+    int nta, ntb;  // CTA tiles along a and b
+    int lag;       // start lag behind an upstream CTA (rows)
+    int lag_sh;    // start lag behind the warp to the left (rows)
+};
+int wave_cols_per_warp(int elem_size);
+// Dynamic shared memory of one CTA (cp.async rings and the face buffers
+// between its warps).
+size_t wave_sweep_smem(const WaveGeom& g, int elem_size);
+// Geometry for `warps` warps per CTA (clipped to the box and to the
+// shared-memory limit); lag 0 = default.
+WaveGeom make_wave_geom(const BoxGeom& box, int elem_size, int warps, int lag = 0);
+template <typename T>
+void launch_wave_sweep(cudaStream_t st, const WaveGeom& g, int n, const T* soa, const T* rhs,
+                       T* out, bool forward, int divmode, const SweepSync& S, const int* done);
+
 // CSR factor (FP64) -> packed stencil records in TO; diagonal term =
 // diagonal, or 1/diagonal with recip.
 template <typename TO>

@@ -141,10 +141,22 @@ struct ocsl_ctx {
     // 0 x 0 = automatic: 2 x 4 tiles per cluster on a grid of at least
     // kAutoClusterTiles tiles, single tiles below (few tile hops to save)
     int box_cluster[2][2] = {{0, 0}, {0, 0}};
-    // P.box / P.box32 from the requests (box patterns only)
+    // Warp-pipelined sweep (kernels_wave.cu) for single right-hand sides, per
+    // precision ([0] FP64, [1] FP32): on / off, warps per CTA and start lag
+    // requests (0 = automatic), and the geometry built from them.
+    bool wave_on[2] = {true, true};
+    int wave_req[2][2] = {{0, 0}, {0, 0}};
+    WaveGeom wave[2] = {};
+    // P.box / P.box32 and the wave geometries from the requests (box patterns only)
     void rebuild_box_geoms()
     {
         if (!hp.box.ok) return;
+        for (int k = 0; k < 2; ++k) {
+            const BoxGeom base = make_box_geom(hp.box, 0, 0);
+            const int elem = k == 0 ? 8 : 4;
+            wave[k] = make_wave_geom(base, elem, wave_req[k][0] > 0 ? wave_req[k][0] : 4,
+                                     wave_req[k][1]);
+        }
         BoxGeom* geo[2] = {&P.box, &P.box32};
         for (int k = 0; k < 2; ++k) {
             const BoxGeom g = make_box_geom(hp.box, box_tile[k][0], box_tile[k][1]);
@@ -549,7 +561,10 @@ struct Solve {
             fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
-        if (use_box() && soa<TT>())
+        if (use_box() && soa<TT>() && use_wave<TT>())
+            launch_wave_sweep<TT>(st, c->wave[is_f64<TT>() ? 0 : 1], P.n, soa<TT>(), rhs, out,
+                                  true, 0, c->next_sync(), k >= 0 ? done(k) : nullptr);
+        else if (use_box() && soa<TT>())
             launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, true, 0,
                                  c->next_sync(), k >= 0 ? done(k) : nullptr, cols, kDoneStride);
         else
@@ -572,6 +587,14 @@ struct Solve {
         return g;
     }
     bool use_box() const { return P.box_ok && c->sweep_kernel != 1; }
+    // the warp-pipelined kernel serves one right-hand side at a time; kind 2
+    // forces the CTA kernel, kind 3 the warp-pipelined one
+    template <typename TT>
+    bool use_wave() const
+    {
+        if (cols.n != 1 || c->sweep_kernel == 2) return false;
+        return c->sweep_kernel == 3 || c->wave_on[is_f64<TT>() ? 0 : 1];
+    }
     // After a factorisation: the structured sweeps read the factor in the
     // stencil-SoA layout (slot 3: diagonal for the reference's division, or
     // its reciprocal for the tolerance-mode multiply).
@@ -639,7 +662,10 @@ struct Solve {
             fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
-        if (use_box() && soa<TT>())
+        if (use_box() && soa<TT>() && use_wave<TT>())
+            launch_wave_sweep<TT>(st, c->wave[is_f64<TT>() ? 0 : 1], P.n, soa<TT>(), rhs, out,
+                                  false, divmode, c->next_sync(), k >= 0 ? done(k) : nullptr);
+        else if (use_box() && soa<TT>())
             launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, false, divmode,
                                  c->next_sync(), k >= 0 ? done(k) : nullptr, cols, kDoneStride);
         else
@@ -693,7 +719,7 @@ struct Solve {
         CK(cudaGraphLaunch(c->graph_exec, st));
         return true;
     }
-    // OCSL_ZERO_PIVOT when the current factor has a zero or non-finite
+    // OCSL_ZERO_PIVOT when the current factor has a zero or infinite
     // diagonal (synchronises once per factor; a reused factor keeps its verdict)
     int pivot_status()
     {
@@ -773,7 +799,7 @@ struct TolResult {
     int status = OCSL_OK;
 };
 
-// A factor with a zero or non-finite pivot: no iteration runs, x is unchanged.
+// A factor with a zero or infinite pivot: no iteration runs, x is unchanged.
 TolResult zero_pivot_result()
 {
     TolResult r;
@@ -1153,7 +1179,7 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
     r.status = status;
     if (out) *out = r;
     if (status == OCSL_TIMEOUT) c->last_error = "a triangular-sweep wait hit its bound";
-    if (status == OCSL_ZERO_PIVOT) c->last_error = "the factor has a zero or non-finite pivot";
+    if (status == OCSL_ZERO_PIVOT) c->last_error = "the factor has a zero or infinite pivot";
     return status;
 }
 
@@ -1715,9 +1741,9 @@ int ocsl_ilu_device(ocsl_ctx* c, const double* A, double* M, int sweeps)
                            c->stream));
         CK(cudaGetLastError());
         // M is written either way (the reference has no check); the status
-        // tells the caller that a diagonal of it is zero or non-finite
+        // tells the caller that a diagonal of it is zero or infinite
         if (s.device_error() == OCSL_ZERO_PIVOT)
-            return fail(c, OCSL_ZERO_PIVOT, "the factor has a zero or non-finite pivot");
+            return fail(c, OCSL_ZERO_PIVOT, "the factor has a zero or infinite pivot");
     } catch (const CudaError& e) {
         return from_cuda(c, e);
     }
@@ -1750,14 +1776,20 @@ static int sweep_entry(ocsl_ctx* c, bool forward, const double* M, const double*
 
 int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
 {
-    if (!c || kind < 0 || kind > 2 || tile_a < 0 || tile_b < 0) return OCSL_BAD_ARGUMENT;
-    if (kind == 2 && c->has_pattern && !c->hp.box.ok)
+    if (!c || kind < 0 || kind > 3 || tile_a < 0 || tile_b < 0) return OCSL_BAD_ARGUMENT;
+    if (kind == 3 && tile_a > kWaveMaxWarps) return OCSL_BAD_ARGUMENT;
+    if (kind >= 2 && c->has_pattern && !c->hp.box.ok)
         return fail(c, OCSL_BAD_ARGUMENT, "the pattern is not a 7-point box stencil");
     c->drop_graph();
     c->sweep_kernel = kind;
     for (int k = 0; k < 2; ++k) {
-        c->box_tile[k][0] = tile_a;
-        c->box_tile[k][1] = tile_b;
+        if (kind == 3) {  // warps per CTA, start lag
+            c->wave_req[k][0] = tile_a;
+            c->wave_req[k][1] = tile_b;
+        } else {
+            c->box_tile[k][0] = tile_a;
+            c->box_tile[k][1] = tile_b;
+        }
     }
     if (c->has_pattern) {
         c->P.box_ok = c->hp.box.ok && kind != 1;
@@ -1797,6 +1829,19 @@ int ocsl_sweep_geometry(const ocsl_ctx* c, int fp32, int* tiles, int* cluster)
     return OCSL_OK;
 }
 
+int ocsl_wave_geometry(const ocsl_ctx* c, int fp32, int* on, int* warps, int* lag)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (!c->has_pattern) return OCSL_NO_PATTERN;
+    const int k = fp32 ? 1 : 0;
+    const bool act = c->P.box_ok && c->sweep_kernel != 2 &&
+                     (c->sweep_kernel == 3 || c->wave_on[k]);
+    if (on) *on = act ? 1 : 0;
+    if (warps) *warps = act ? c->wave[k].WA : 0;
+    if (lag) *lag = act ? c->wave[k].lag : 0;
+    return OCSL_OK;
+}
+
 int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, int* tile_b,
                          double* sweep_us)
 {
@@ -1822,6 +1867,8 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
     const int pi = fp32 ? 1 : 0;
     BoxGeom& geo = fp32 ? c->P.box32 : c->P.box;  // the geometry this method's sweeps use
     const BoxGeom keep = geo;
+    const int kind_keep = c->sweep_kernel;
+    const WaveGeom wkeep = c->wave[pi];
     try {
         CK(cudaSetDevice(c->device));
         Solve s{c, c->stream, c->P, c->P.n};
@@ -1843,17 +1890,7 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
             CK(cudaMemsetAsync(c->v32[F_P], 0, sizeof(float) * n, c->stream));
         else
             CK(cudaMemsetAsync(c->v64[P], 0, sizeof(double) * n, c->stream));
-        double best = 1e300;
-        BoxGeom bestg = keep;
-        std::vector<std::array<int, 4>> tried;
-        for (const auto& cd : kCand)
-        for (const auto& cl : kClus) {
-            const BoxGeom g =
-                box_with_cluster(make_box_geom(c->hp.box, cd[0], cd[1]), cl[0], cl[1]);
-            const std::array<int, 4> key{g.TA, g.TB, g.CX, g.CY};
-            if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
-            tried.push_back(key);
-            geo = g;
+        auto timed_pair = [&]() {
             pair();  // warm-up
             double t = 1e300;
             for (int rep = 0; rep < 3; ++rep) {
@@ -1865,8 +1902,53 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
                 CK(cudaEventElapsedTime(&ms, c->ev_start, c->ev_stop));
                 t = std::min(t, 1000.0 * ms);
             }
+            return t;
+        };
+        // warp-pipelined kernel: warps per CTA x start lag
+        double best_wave = 1e300;
+        WaveGeom bestw = wkeep;
+        if (c->sweep_kernel != 2) {
+            c->sweep_kernel = 3;
+            static const int kWarps[] = {1, 2, 4, 8};
+            static const int kLags[] = {4, 6, 10};
+            const BoxGeom base = make_box_geom(c->hp.box, 0, 0);
+            std::vector<std::array<int, 2>> wtried;
+            for (int wa : kWarps)
+            for (int lg : kLags) {
+                const WaveGeom g = make_wave_geom(base, fp32 ? 4 : 8, wa, lg);
+                const std::array<int, 2> key{g.WA, g.lag};
+                if (std::find(wtried.begin(), wtried.end(), key) != wtried.end()) continue;
+                wtried.push_back(key);
+                c->wave[pi] = g;
+                const double t = timed_pair();
+                if (s.device_error()) {
+                    c->sweep_kernel = kind_keep;
+                    c->wave[pi] = wkeep;
+                    return fail(c, OCSL_TIMEOUT, "a triangular-sweep wait hit its bound");
+                }
+                if (t < best_wave) {
+                    best_wave = t;
+                    bestw = g;
+                }
+            }
+            c->sweep_kernel = 2;  // time the CTA kernel's shapes next
+        }
+        double best = 1e300;
+        BoxGeom bestg = keep;
+        std::vector<std::array<int, 4>> tried;
+        for (const auto& cd : kCand)
+        for (const auto& cl : kClus) {
+            const BoxGeom g =
+                box_with_cluster(make_box_geom(c->hp.box, cd[0], cd[1]), cl[0], cl[1]);
+            const std::array<int, 4> key{g.TA, g.TB, g.CX, g.CY};
+            if (std::find(tried.begin(), tried.end(), key) != tried.end()) continue;
+            tried.push_back(key);
+            geo = g;
+            const double t = timed_pair();
             if (s.device_error()) {
                 geo = keep;
+                c->sweep_kernel = kind_keep;
+                c->wave[pi] = wkeep;
                 return fail(c, OCSL_TIMEOUT, "a triangular-sweep wait hit its bound");
             }
             if (t < best) {
@@ -1880,13 +1962,28 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         c->box_tile[pi][1] = bestg.TB;
         c->box_cluster[pi][0] = bestg.CX;
         c->box_cluster[pi][1] = bestg.CY;
+        c->sweep_kernel = kind_keep;
+        const bool wave_wins = kind_keep != 2 && best_wave < best;
+        // automatic choice: this precision's single-column sweeps use the
+        // faster kernel (a forced kind keeps its kernel)
+        if (kind_keep == 0) c->wave_on[pi] = wave_wins;
+        if (wave_wins || kind_keep == 3) {
+            c->wave[pi] = bestw;
+            c->wave_req[pi][0] = bestw.WA;
+            c->wave_req[pi][1] = bestw.lag;
+        } else {
+            c->wave[pi] = wkeep;
+        }
         c->fac_M = nullptr;
-        if (tile_a) *tile_a = bestg.TA;
-        if (tile_b) *tile_b = bestg.TB;
-        if (sweep_us) *sweep_us = best;
+        const int K = wave_cols_per_warp(fp32 ? 4 : 8);
+        if (tile_a) *tile_a = wave_wins ? bestw.WA * K : bestg.TA;
+        if (tile_b) *tile_b = wave_wins ? 32 : bestg.TB;
+        if (sweep_us) *sweep_us = wave_wins ? best_wave : best;
         CK(cudaGetLastError());
     } catch (const CudaError& e) {
         geo = keep;
+        c->sweep_kernel = kind_keep;
+        c->wave[pi] = wkeep;
         return from_cuda(c, e);
     }
     return OCSL_OK;
@@ -1896,7 +1993,7 @@ int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
     if (!c->has_pattern) return OCSL_NO_PATTERN;
-    if (kind) *kind = c->P.box_ok ? 2 : 1;
+    if (kind) *kind = !c->P.box_ok ? 1 : (c->sweep_kernel == 2 ? 2 : (c->sweep_kernel == 3 || c->wave_on[0] ? 3 : 2));
     if (dims) for (int k = 0; k < 3; ++k) dims[k] = c->hp.box.ok ? c->hp.box.dim[k] : 0;
     if (tiles) {
         tiles[0] = c->P.box_ok ? c->P.box.TA : 0;
