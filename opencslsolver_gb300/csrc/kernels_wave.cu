@@ -1,38 +1,53 @@
 // Warp-pipelined structured sweeps for 7-point box patterns (one right-hand
-// side).
+// side), with every memory access coalesced.
 //
 // The forward sweep of a natural-order 7-point stencil, y = L^-1 rhs
-// (cmatrix_solver.cpp:555-572), is a chain of wavefronts W = a + b + s: row
-// (a, b, s) needs the rows (a-1, b, s), (a, b-1, s) and (a, b, s-1).  The
-// backward sweep (:595-611) is the same with every coordinate mirrored.
+// (cmatrix_solver.cpp:555-572), is a chain of wavefronts: row (a, b, s) needs
+// (a-1, b, s), (a, b-1, s) and (a, b, s-1).  The backward sweep (:595-611) is
+// the same with every coordinate mirrored.  Canonical coordinates here: a = x
+// (unit stride), s = the longer of y and z, b = the other one.
 //
-// Here one warp owns a column tile of K (along a) x 32 (along b, one lane
-// each) columns and walks its own steps t = 0, 1, ...: at step t, column k of
-// lane l solves row s = t - k - l.  Every dependency of that row was solved
-// at step t - 1 inside the same warp:
-//   (a-1, b, s): column k-1 of the same lane         -> a register
-//   (a, b-1, s): column k of lane l-1                 -> one warp shuffle
-//   (a, b, s-1): column k of the same lane            -> a register
-// so a step is K independent fma chains, no barrier and no memory round trip
-// on the critical path.  Only the tile's faces come from outside: column 0's
-// a-neighbour from the warp to the left (same CTA: one shared-memory slot per
-// s row; other CTA: the output vector in global memory) and lane 0's
-// b-neighbours from the tile below (global memory).  Values crossing a CTA
-// use the value-as-flag protocol of the other sweeps -- the output is
-// pre-filled with all-ones, every wait is bounded (OCSL_TIMEOUT and a NaN
-// when it runs out) -- and are fetched a few steps ahead into a register
-// ring; shared-memory faces are filled with the same sentinel at the start.
+// One warp owns a tile of 32 (along a, one lane each) x K (along b) columns
+// and walks steps t = 0 .. T-1, T = Ds + K - 1 + 31: at step t, column k of
+// lane l solves row s = t - k - l.  Every dependency inside the tile was
+// solved at step t - 1 by the same warp:
+//   (a-1, b, s): column k of lane l-1   -> one warp shuffle
+//   (a, b-1, s): column k-1 of lane l   -> a register
+//   (a, b, s-1): column k of lane l     -> a register
+// so a step is K independent fma chains with no barrier.
 //
-// A row's arithmetic is the packed record's fma chain in CSR order (z-, y-,
-// x-), then rhs - sum (and the division by, or the product with the
-// reciprocal of, the diagonal backward), exactly as in box_cta_kernel, so
-// results are bit-identical to the oracle whatever the tile shape.
+// Memory.  Rows solved in the same step lie on a diagonal of the box, so
+// per-lane loads and stores of natural-order vectors would touch a different
+// cache line per lane -- the load/store pipe, not DRAM, then sets the speed.
+// Instead:
+//   * the factor's stencil records are stored in the sweep's own step order
+//     ([tile][t][k][lane], written once per factorisation by
+//     box_to_wave_kernel), so each step reads K contiguous 32-record blocks;
+//   * the right-hand side and the output go through a ring of s-slices in
+//     shared memory: slice s of the tile (K rows of 32 consecutive a) is
+//     loaded with one coalesced access per row kP steps before step s, each
+//     row's result overwrites its right-hand side in place, and the slice is
+//     written back with coalesced stores once its last row is solved (step
+//     s + K - 1 + 31);
+//   * faces between tiles are exchanged through buffers indexed by the
+//     producer's step ([d][k] for the a-face: lane 31 of the tile to the left,
+//     [d][lane] for the b-face: column K-1 of the tile below), so that the
+//     producer's stores and the consumer's loads are contiguous too.  Faces
+//     between the warps of a CTA live in shared memory; faces between CTAs in
+//     global memory, where a value is its own ready flag (all-ones = not
+//     yet), every wait is bounded (OCSL_TIMEOUT and a NaN when it runs out),
+//     values are fetched kDF steps ahead, and the consumer writes the
+//     sentinel back after use, so the buffers are ready for the next launch
+//     without a fill (after a launch that timed out the host refills them).
 //
-// Records and right-hand sides are staged with per-lane cp.async into a
-// P-step ring in shared memory; each lane reads back only what it copied
-// itself, so no barrier is needed there either.  CTAs take tiles from an
-// atomic ticket in row-major tile order (a tile's upstream neighbours come
-// first), so a waiting CTA never waits on an unscheduled one.
+// A row's arithmetic is the record's fma chain in CSR order (z-, y-, x-),
+// then rhs - sum (and the division by, or the product with the reciprocal
+// of, the diagonal backward), exactly as in box_cta_kernel: results are
+// bit-identical to the oracle whatever the tiling.
+//
+// A CTA holds WB warps stacked along b; CTAs take tiles from an atomic ticket
+// in row-major tile order, so a tile's upstream neighbours always hold
+// earlier tickets and a waiting CTA never waits on an unscheduled one.
 #include <algorithm>
 #include <mutex>
 
@@ -43,10 +58,10 @@ namespace ocsl {
 namespace {
 
 constexpr long kSpinLimit = 1L << 21;
-constexpr int kP = 12;   // cp.async ring depth (steps)
-constexpr int kDF = 4;   // global face values fetched this many steps ahead
-constexpr int kWaveLag = kDF + 2;    // default start lag behind an upstream CTA (rows)
-constexpr int kWaveLagShared = 1;    // ... behind the warp to the left
+constexpr int kP = 8;     // prefetch depth of records and right-hand-side slices (steps)
+constexpr int kDF = 4;    // global face values fetched this many steps ahead
+constexpr int kWaveLag = kDF + 2;   // default start lag behind an upstream CTA (rows)
+constexpr int kWaveLagShared = 1;   // ... behind the warp below in the same CTA
 
 template <typename T>
 struct Bits;
@@ -55,13 +70,13 @@ struct Bits<double> {
     using U = unsigned long long;
     static constexpr U kSentinel = ~0ull;
     static constexpr U kCanonicalNaN = 0x7FF8000000000000ull;
-    static __device__ __forceinline__ U load(const double* p)
+    static __device__ __forceinline__ U load(const U* p)
     {
         U v;
         asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
         return v;
     }
-    static __device__ __forceinline__ void store(double* p, U v)
+    static __device__ __forceinline__ void store(U* p, U v)
     {
         asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v));
     }
@@ -73,13 +88,13 @@ struct Bits<float> {
     using U = unsigned int;
     static constexpr U kSentinel = ~0u;
     static constexpr U kCanonicalNaN = 0x7FC00000u;
-    static __device__ __forceinline__ U load(const float* p)
+    static __device__ __forceinline__ U load(const U* p)
     {
         U v;
         asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p));
         return v;
     }
-    static __device__ __forceinline__ void store(float* p, U v)
+    static __device__ __forceinline__ void store(U* p, U v)
     {
         asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v));
     }
@@ -93,19 +108,16 @@ __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(
 template <typename U>
 __device__ __forceinline__ U vload_shared(const U* p)
 {
-    if constexpr (sizeof(U) == 8) {
-        U v;
+    U v;
+    if constexpr (sizeof(U) == 8)
         asm volatile("ld.volatile.shared.b64 %0, [%1];"
                      : "=l"(v)
                      : "r"((unsigned)__cvta_generic_to_shared(p)));
-        return v;
-    } else {
-        U v;
+    else
         asm volatile("ld.volatile.shared.b32 %0, [%1];"
                      : "=r"(v)
                      : "r"((unsigned)__cvta_generic_to_shared(p)));
-        return v;
-    }
+    return v;
 }
 template <typename U>
 __device__ __forceinline__ void vstore_shared(U* p, U v)
@@ -118,10 +130,10 @@ __device__ __forceinline__ void vstore_shared(U* p, U v)
                      "r"(v));
 }
 
-// Bounded polls (OCSL_TIMEOUT and a NaN when they run out, or as soon as
-// another wait of the launch has given up).
+// Bounded polls: OCSL_TIMEOUT and a NaN when they run out, or as soon as
+// another wait of the launch has given up.
 template <typename T>
-__device__ __noinline__ T wait_global(const T* p, int* err)
+__device__ __noinline__ T wait_global(const typename Bits<T>::U* p, int* err)
 {
     using B = Bits<T>;
     unsigned ns = 0;
@@ -151,7 +163,7 @@ template <typename T>
 __device__ __forceinline__ typename Bits<T>::U to_bits(T v)
 {
     using B = Bits<T>;
-    typename B::U u = B::to(v);
+    const typename B::U u = B::to(v);
     return u == B::kSentinel ? B::kCanonicalNaN : u;
 }
 
@@ -191,17 +203,18 @@ __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0
 template <typename T>
 struct WaveParams {
     WaveGeom g;
-    int n;
-    const T* soa;  // packed records [2][n][4]: (z-, y-, x-, 0), (x+, y+, z+, diagonal term)
-    const T* rhs;
-    T* out;
+    const T* rec;   // this direction's records in step order [nwb][nwa][T][K][32]
+    const T* rhs;   // natural order
+    T* out;         // natural order
+    typename Bits<T>::U* faceA;  // [tiles][T][K]  lane 31 of a tile, by producer step
+    typename Bits<T>::U* faceB;  // [tiles][T][32] column K-1 of a tile, by producer step
     SweepSync S;
     const int* done;
 };
 
 // FWD: y = L^-1 rhs (unit L); !FWD: x = U^-1 rhs, DIV: divide by the
-// diagonal (the reference), else multiply by the stored reciprocal.  SPAN:
-// which of x (0), y (1), z (2) the canonical s dimension is.
+// diagonal (the reference), else multiply by the stored reciprocal.
+// SPAN: 2 when s = z (b = y), 1 when s = y (b = z).
 template <typename T, bool FWD, bool DIV, int SPAN, int K>
 __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WaveParams<T> p)
 {
@@ -209,98 +222,103 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
     using B = Bits<T>;
     using U = typename B::U;
     using R = Rec<T>;
+    constexpr int RS = kP + K + 31;  // slice ring: loaded kP steps ahead, kept until flushed
     extern __shared__ __align__(32) unsigned char smem_raw[];
     const WaveGeom& g = p.g;
-    const int WA = g.WA;
+    const int WB = g.WB, T_ = g.T;
     const int w = (int)threadIdx.x >> 5, l = (int)threadIdx.x & 31;
     const int Da = g.D[0], Db = g.D[1], Ds = g.D[2];
-    R* ring = reinterpret_cast<R*>(smem_raw);                 // [WA][kP][K][32]
-    T* rring = reinterpret_cast<T*>(ring + WA * kP * K * 32); // [WA][kP][K][32]
-    U* faceA = reinterpret_cast<U*>(rring + WA * kP * K * 32); // [WA-1][Ds][32]
+    R* rring = reinterpret_cast<R*>(smem_raw);                    // [WB][kP][K][32]
+    T* sring = reinterpret_cast<T*>(rring + WB * kP * K * 32);    // [WB][RS][K][32]
+    U* sface = reinterpret_cast<U*>(sring + WB * RS * K * 32);    // [WB-1][T][32]
     __shared__ int s_tile;
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(p.S.ticket, 1u);
-    for (int i = threadIdx.x; i < (WA - 1) * Ds * 32; i += blockDim.x) faceA[i] = B::kSentinel;
+    for (int i = threadIdx.x; i < (WB - 1) * T_ * 32; i += blockDim.x) sface[i] = B::kSentinel;
     __syncthreads();
     const int tile = s_tile;
+    const int wa = tile % g.nta, tb = tile / g.nta;
+    const int wb = tb * WB + w;
     if (tile >= g.nta * g.ntb) {  // never with a fresh dispenser; keeps every access in bounds
         if (threadIdx.x == 0) atomicCAS(p.S.err, 0, (int)OCSL_TIMEOUT);
-    } else {
-        const int ta = tile % g.nta, tb = tile / g.nta;
-        const int a0 = (ta * WA + w) * K;  // canonical a of column 0
-        const int b = tb * 32 + l;
-        const bool b_ok = b < Db;
-        const int dstep = FWD ? -1 : 1;    // physical offset of an upstream neighbour
-        const int off_a = dstep * g.S[0], off_b = dstep * g.S[1];
+    } else if (wb < g.nwb) {  // uniform over the warp
+        int* err = p.S.err;
+        const int a = wa * 32 + l;
+        const bool a_ok = a < Da;
         const int sstep = FWD ? g.S[2] : -g.S[2];
-        // physical row of column k at s = 0
+        const int pa = FWD ? a : Da - 1 - a;
         int base[K];
         bool ok[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            const int a = a0 + k;
-            ok[k] = b_ok && a < Da;
-            const int pa = FWD ? a : Da - 1 - a;
+            const int b = wb * K + k;
+            ok[k] = a_ok && b < Db;
             const int pb = FWD ? b : Db - 1 - b;
-            base[k] = pa * g.S[0] + pb * g.S[1] + (FWD ? 0 : (Ds - 1) * g.S[2]);
+            base[k] = ok[k] ? pa * g.S[0] + pb * g.S[1] + (FWD ? 0 : (Ds - 1) * g.S[2]) : 0;
         }
-        const bool has_b = b > 0;          // lane l-1 or the tile below holds (a, b-1)
-        const bool face_b = has_b && l == 0;   // ... the tile below (global)
-        const bool has_a = a0 > 0;         // column 0's a-neighbour exists
-        const bool face_a_sh = has_a && w > 0;   // ... in the warp to the left (shared)
-        const bool face_a_gl = has_a && w == 0;  // ... in the CTA to the left (global)
-        const bool push_a = w < WA - 1;    // column K-1 feeds the warp to the right
-        const R* recs = reinterpret_cast<const R*>(p.soa) + (FWD ? 0 : p.n);
-        R* my_ring = ring + w * kP * K * 32;
-        T* my_rr = rring + w * kP * K * 32;
-        const U* fa_in = faceA + (w - 1) * Ds * 32;  // valid when w > 0
-        U* fa_out = faceA + w * Ds * 32;             // valid when w < WA - 1
-        int* err = p.S.err;
+        const int wt = wb * g.nwa + wa;  // tile index of the step-order layouts
+        const R* recs = reinterpret_cast<const R*>(p.rec) + (size_t)wt * T_ * K * 32;
+        R* my_rr = rring + w * kP * K * 32;
+        T* my_sr = sring + w * RS * K * 32;
+        // faces in: a from the tile to the left (another CTA), b from the tile
+        // below (the warp below, or the CTA below for warp 0)
+        const bool has_a = wa > 0;
+        const bool has_b = wb > 0;
+        const U* fa_in = has_a ? p.faceA + (size_t)(wt - 1) * T_ * K : nullptr;
+        const U* fb_in_sh = (has_b && w > 0) ? sface + (w - 1) * T_ * 32 : nullptr;
+        const U* fb_in_gl = (has_b && w == 0) ? p.faceB + (size_t)(wt - g.nwa) * T_ * 32 : nullptr;
+        // faces out
+        const bool push_a = wa + 1 < g.nwa && l == 31;
+        U* fa_out = p.faceA + (size_t)wt * T_ * K;
+        const bool push_b = wb + 1 < g.nwb;
+        U* fb_out_sh = (push_b && w < WB - 1) ? sface + w * T_ * 32 : nullptr;
+        U* fb_out_gl = (push_b && w == WB - 1) ? p.faceB + (size_t)wt * T_ * 32 : nullptr;
 
-        auto refill = [&](int t, int j) {
+        auto issue = [&](int t) {  // records of step t and right-hand-side slice t
+            if (t < T_) {
+                const int j = t % kP;
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const int s = t - k - l;
-                if (ok[k] && s >= 0 && s < Ds) {
-                    const int r = base[k] + s * sstep;
-                    cp_rec<T>(&my_ring[(j * K + k) * 32 + l], recs + r);
-                    cp_val<T>(&my_rr[(j * K + k) * 32 + l], p.rhs + r);
-                }
+                for (int k = 0; k < K; ++k)
+                    cp_rec<T>(&my_rr[(j * K + k) * 32 + l], recs + ((size_t)t * K + k) * 32 + l);
+            }
+            if (t < Ds) {
+                const int j = t % RS;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if (ok[k]) cp_val<T>(&my_sr[(j * K + k) * 32 + l], p.rhs + base[k] + t * sstep);
             }
             cp_commit();
         };
 #pragma unroll
-        for (int j = 0; j < kP; ++j) refill(j, j);
+        for (int j = 0; j < kP; ++j) issue(j);
 
-        // Start behind the upstream tiles: wait for their face values at
-        // s = lag next to this tile (lane 0, column 0), so that the values
-        // fetched kDF steps ahead are normally final; behind the warp to the
-        // left by lag_sh rows.
+        // Start behind the upstream tiles: wait for their face values of row
+        // s = lag next to this tile (lane 0, column 0), so that values fetched
+        // kDF steps ahead are normally final.
         {
             const int sg = min(g.lag, Ds - 1), ss = min(g.lag_sh, Ds - 1);
-            if (face_a_gl && l == 0 && ok[0]) (void)wait_global(p.out + base[0] + sg * sstep + off_a, err);
-            if (face_b && ok[0]) (void)wait_global(p.out + base[0] + sg * sstep + off_b, err);
-            if (face_a_sh && l == 0 && ok[0]) {
-                const U* slot = fa_in + ss * 32;
-                if (vload_shared(slot) == B::kSentinel) (void)wait_shared<T>(slot, err);
+            if (l == 0 && ok[0]) {
+                if (fa_in && B::load(fa_in + (size_t)(sg + 31) * K) == B::kSentinel)
+                    (void)wait_global<T>(fa_in + (size_t)(sg + 31) * K, err);
+                if (fb_in_gl && B::load(fb_in_gl + (size_t)(sg + K - 1) * 32) == B::kSentinel)
+                    (void)wait_global<T>(fb_in_gl + (size_t)(sg + K - 1) * 32, err);
+                if (fb_in_sh && vload_shared(fb_in_sh + (ss + K - 1) * 32) == B::kSentinel)
+                    (void)wait_shared<T>(fb_in_sh + (ss + K - 1) * 32, err);
             }
         }
         __syncwarp();
 
-        // global face values, kDF steps ahead: fa (column 0, a-1), fb (lane 0, b-1)
-        U fa[kDF], fb[kDF][K];
+        // global face values kDF steps ahead: fa (lane 0, the K a-neighbours of
+        // step t at d = t + 31), fb (column 0's b-neighbour at d = t + K - 1)
+        U fa[kDF][K], fb[kDF];
         auto fetch = [&](int t, int j) {
-            fa[j] = B::kSentinel;
-            if (face_a_gl) {
-                const int s = t - l;
-                if (ok[0] && s >= 0 && s < Ds) fa[j] = B::load(p.out + base[0] + s * sstep + off_a);
-            }
 #pragma unroll
-            for (int k = 0; k < K; ++k) {
-                fb[j][k] = B::kSentinel;
-                const int s = t - k;
-                if (face_b && ok[k] && s >= 0 && s < Ds)
-                    fb[j][k] = B::load(p.out + base[k] + s * sstep + off_b);
+            for (int k = 0; k < K; ++k) fa[j][k] = B::kSentinel;
+            fb[j] = B::kSentinel;
+            if (fa_in && l == 0 && t + 31 < T_) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) fa[j][k] = B::load(fa_in + (size_t)(t + 31) * K + k);
             }
+            if (fb_in_gl && t + K - 1 < T_) fb[j] = B::load(fb_in_gl + (size_t)(t + K - 1) * 32 + l);
         };
 #pragma unroll
         for (int j = 0; j < kDF; ++j) fetch(j, j);
@@ -308,50 +326,49 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
         T cur[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) cur[k] = T(0);
-        // one past the last step of the warp's last column in range
-        const int kmax = min(K - 1, max(Da - 1 - a0, 0));
-        const int lmax = min(31, max(Db - 1 - tb * 32, 0));
-        const int T_end = Ds + kmax + lmax;
-        for (int tb0 = 0; tb0 < T_end; tb0 += kP) {
+        for (int t0 = 0; t0 < T_; t0 += kP) {
 #pragma unroll
             for (int j = 0; j < kP; ++j) {
-                const int t = tb0 + j;
-                if (t >= T_end) break;  // uniform over the warp
+                const int t = t0 + j;
+                if (t >= T_) break;  // uniform over the warp
                 const int jf = j % kDF;
                 cp_wait<kP - 1>();
-                T up[K];  // lane l-1's values of the previous step (b-neighbours)
+                T up[K];  // lane l-1's values of the previous step: a-neighbours
 #pragma unroll
                 for (int k = 0; k < K; ++k) up[k] = __shfl_up_sync(0xffffffffu, cur[k], 1);
                 T nv[K];
+                U out_a[K];
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
                     nv[k] = cur[k];
+                    out_a[k] = B::kSentinel;
                     const int s = t - k - l;
                     if (ok[k] && s >= 0 && s < Ds) {
-                        const R cf = my_ring[(j * K + k) * 32 + l];
-                        const T rh = my_rr[(j * K + k) * 32 + l];
+                        const R cf = my_rr[(j * K + k) * 32 + l];
+                        T* slot = &my_sr[((s % RS) * K + k) * 32 + l];
+                        const T rh = *slot;
                         T va = T(0), vb = T(0);
-                        if (k > 0) {
-                            va = cur[k - 1];  // a0 + k > 0 always
-                        } else if (face_a_sh) {
-                            const U* slot = fa_in + s * 32 + l;
-                            const U u = vload_shared(slot);
-                            va = u != B::kSentinel ? B::from(u) : wait_shared<T>(slot, err);
-                        } else if (face_a_gl) {
-                            va = fa[jf] != B::kSentinel
-                                     ? B::from(fa[jf])
-                                     : wait_global(p.out + base[0] + s * sstep + off_a, err);
-                        }
                         if (l > 0) {
-                            vb = up[k];
-                        } else if (face_b) {
-                            vb = fb[jf][k] != B::kSentinel
-                                     ? B::from(fb[jf][k])
-                                     : wait_global(p.out + base[k] + s * sstep + off_b, err);
+                            va = up[k];
+                        } else if (has_a) {
+                            va = fa[jf][k] != B::kSentinel
+                                     ? B::from(fa[jf][k])
+                                     : wait_global<T>(fa_in + (size_t)(t + 31) * K + k, err);
+                        }
+                        if (k > 0) {
+                            vb = cur[k - 1];
+                        } else if (fb_in_sh) {
+                            const U* fs = fb_in_sh + (t + K - 1) * 32 + l;
+                            const U u = vload_shared(fs);
+                            vb = u != B::kSentinel ? B::from(u) : wait_shared<T>(fs, err);
+                        } else if (fb_in_gl) {
+                            vb = fb[jf] != B::kSentinel
+                                     ? B::from(fb[jf])
+                                     : wait_global<T>(fb_in_gl + (size_t)(t + K - 1) * 32 + l, err);
                         }
                         const T vs = s > 0 ? cur[k] : T(0);
-                        const T vx = SPAN == 0 ? vs : va;
-                        const T vy = SPAN == 0 ? va : (SPAN == 1 ? vs : vb);
+                        const T vx = va;
+                        const T vy = SPAN == 2 ? vb : vs;
                         const T vz = SPAN == 2 ? vs : vb;
                         // record: z-, y-, x-, (unused) | x+, y+, z+, diagonal term;
                         // the fma order is the row's CSR order
@@ -361,20 +378,48 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
                         const T num = rh - sum;
                         const T y = FWD ? num : (DIV ? num / cf.v[3] : num * cf.v[3]);
                         nv[k] = y;
+                        *slot = y;  // the slice keeps the result until it is written back
                         const U bits = to_bits(y);
-                        B::store(p.out + base[k] + s * sstep, bits);
-                        if (k == K - 1 && push_a) vstore_shared(fa_out + s * 32 + l, bits);
+                        out_a[k] = bits;
+                        if (k == K - 1) {
+                            if (fb_out_sh) vstore_shared(fb_out_sh + t * 32 + l, bits);
+                            else if (fb_out_gl) B::store(fb_out_gl + (size_t)t * 32 + l, bits);
+                        }
                     }
                 }
+                if (push_a) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        if (out_a[k] != B::kSentinel) B::store(fa_out + (size_t)t * K + k, out_a[k]);
+                }
+                // consumed global faces go back to the sentinel for the next launch
+                if (fa_in && l == 0 && t + 31 < T_) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        if (ok[k] && t - k >= 0 && t - k < Ds)
+                            B::store(const_cast<U*>(fa_in) + (size_t)(t + 31) * K + k, B::kSentinel);
+                }
+                if (fb_in_gl && ok[0] && t - l >= 0 && t - l < Ds && t + K - 1 < T_)
+                    B::store(const_cast<U*>(fb_in_gl) + (size_t)(t + K - 1) * 32 + l, B::kSentinel);
 #pragma unroll
                 for (int k = 0; k < K; ++k) cur[k] = nv[k];
+                // slice t - (K-1) - 31 is complete: write it back, coalesced
+                {
+                    const int sf = t - (K - 1) - 31;
+                    if (sf >= 0 && sf < Ds) {
+                        const int js = sf % RS;
+#pragma unroll
+                        for (int k = 0; k < K; ++k)
+                            if (ok[k]) p.out[base[k] + sf * sstep] = my_sr[(js * K + k) * 32 + l];
+                    }
+                }
                 fetch(t + kDF, jf);
-                refill(t + kP, j);
+                issue(t + kP);
             }
         }
         cp_wait<0>();
     }
-    // every warp of the CTA done with the face buffers before the CTA retires
+    // every warp of the CTA done with the shared faces before the CTA retires
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -383,6 +428,45 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
             *p.S.finished = 0u;
         }
     }
+}
+
+// CSR factor -> stencil records in each direction's step order (see above).
+// Row r's real entries are, in storage order, z-, y-, x-, diagonal, x+, y+,
+// z+ (absent ones skipped), then phantoms; the host verified exactly this
+// pattern.  fw gets (z-, y-, x-, 0), bw gets (x+, y+, z+, diagonal) with the
+// diagonal replaced by 1 / diagonal (computed in FP64) when RECIP.  Absent
+// entries are exact 0.  Slots of the layout that belong to no row (the
+// skewed ends of each tile) are never read as a row's record.
+template <typename TO, int RECIP>
+__global__ void box_to_wave_kernel(int n, int nx, int ny, int nz, const int* rp, const double* M,
+                                   WaveGeom g, TO* fw, TO* bw)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int i = r % nx, j = (r / nx) % ny, kz = r / (nx * ny);
+    const bool present[7] = {kz > 0, j > 0, i > 0, true, i < nx - 1, j < ny - 1, kz < nz - 1};
+    double v[7];
+    int q = rp[r];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) v[d] = present[d] ? M[q++] : 0.0;
+    if (RECIP) v[3] = 1.0 / v[3];
+    const int K = g.K;
+    const int a = i, b = g.span == 2 ? j : kz, s = g.span == 2 ? kz : j;
+    auto index = [&](int ca, int cb, int cs) {
+        const int wa = ca >> 5, l = ca & 31, wb = cb / K, k = cb % K;
+        const size_t wt = (size_t)wb * g.nwa + wa;
+        return ((wt * g.T + (size_t)(cs + k + l)) * K + k) * 32 + l;
+    };
+    TO* lo = fw + 4 * index(a, b, s);
+    TO* hi = bw + 4 * index(g.D[0] - 1 - a, g.D[1] - 1 - b, g.D[2] - 1 - s);
+    lo[0] = (TO)v[0];
+    lo[1] = (TO)v[1];
+    lo[2] = (TO)v[2];
+    lo[3] = (TO)0;
+    hi[0] = (TO)v[4];
+    hi[1] = (TO)v[5];
+    hi[2] = (TO)v[6];
+    hi[3] = (TO)v[3];
 }
 
 template <typename T>
@@ -412,17 +496,16 @@ void launch_wave_one(cudaStream_t st, WaveParams<T> p)
         preset_ticket_one(st, p.S.ticket);
         grid -= 1;
     }
-    kern<<<grid, 32 * p.g.WA, smem, st>>>(p);
+    kern<<<grid, 32 * p.g.WB, smem, st>>>(p);
 }
 
 template <typename T, bool FWD, bool DIV>
-void launch_wave_span(cudaStream_t st, int span, const WaveParams<T>& p)
+void launch_wave_span(cudaStream_t st, const WaveParams<T>& p)
 {
-    switch (span) {
-    case 0: launch_wave_one<T, FWD, DIV, 0>(st, p); break;
-    case 1: launch_wave_one<T, FWD, DIV, 1>(st, p); break;
-    default: launch_wave_one<T, FWD, DIV, 2>(st, p); break;
-    }
+    if (p.g.span == 2)
+        launch_wave_one<T, FWD, DIV, 2>(st, p);
+    else
+        launch_wave_one<T, FWD, DIV, 1>(st, p);
 }
 
 }  // namespace
@@ -432,58 +515,86 @@ int wave_cols_per_warp(int elem_size) { return elem_size == 8 ? wave_k<double>()
 size_t wave_sweep_smem(const WaveGeom& g, int elem_size)
 {
     const int K = wave_cols_per_warp(elem_size);
-    const size_t rec = (size_t)4 * elem_size;
-    return (size_t)g.WA * kP * K * 32 * (rec + elem_size) +
-           (size_t)(g.WA - 1) * g.D[2] * 32 * elem_size;
+    const int RS = kP + K + 31;
+    return (size_t)g.WB * kP * K * 32 * (4 * elem_size) + (size_t)g.WB * RS * K * 32 * elem_size +
+           (size_t)(g.WB - 1) * g.T * 32 * elem_size;
 }
 
-WaveGeom make_wave_geom(const BoxGeom& box, int elem_size, int warps, int lag)
+WaveGeom make_wave_geom(const int* dims, int elem_size, int warps, int lag)
 {
     WaveGeom g{};
-    for (int k = 0; k < 3; ++k) {
-        g.D[k] = box.D[k];
-        g.S[k] = box.S[k];
-    }
-    g.span = box.span;
-    const int K = wave_cols_per_warp(elem_size);
-    const int need = (g.D[0] + K - 1) / K;  // warps to cover a
-    int wa = std::max(1, std::min({warps, kWaveMaxWarps, need}));
-    g.WA = wa;
-    while (g.WA > 1 && wave_sweep_smem(g, elem_size) > kBoxSmemLimit) --g.WA;
-    wa = g.WA;
+    const int nx = dims[0], ny = dims[1], nz = dims[2];
+    g.span = nz >= ny ? 2 : 1;  // s = the longer of y and z
+    g.D[0] = nx;
+    g.D[1] = g.span == 2 ? ny : nz;
+    g.D[2] = g.span == 2 ? nz : ny;
+    g.S[0] = 1;
+    g.S[1] = g.span == 2 ? nx : nx * ny;
+    g.S[2] = g.span == 2 ? nx * ny : nx;
+    g.K = wave_cols_per_warp(elem_size);
+    g.nwa = (g.D[0] + 31) / 32;
+    g.nwb = (g.D[1] + g.K - 1) / g.K;
+    g.T = g.D[2] + g.K - 1 + 31;
+    g.WB = std::max(1, std::min({warps > 0 ? warps : 4, kWaveMaxWarps, g.nwb}));
+    while (g.WB > 1 && wave_sweep_smem(g, elem_size) > kBoxSmemLimit) --g.WB;
+    g.nta = g.nwa;
+    g.ntb = (g.nwb + g.WB - 1) / g.WB;
     g.lag = lag > 0 ? lag : kWaveLag;
     g.lag_sh = kWaveLagShared;
-    g.nta = (g.D[0] + wa * K - 1) / (wa * K);
-    g.ntb = (g.D[1] + 31) / 32;
     return g;
 }
 
-template <typename T>
-void launch_wave_sweep(cudaStream_t st, const WaveGeom& g, int n, const T* soa, const T* rhs,
-                       T* out, bool forward, int divmode, const SweepSync& S, const int* done)
+size_t wave_layout_elems(const WaveGeom& g)
 {
-    if (n == 0) return;
+    return (size_t)g.nwa * g.nwb * g.T * g.K * 32;
+}
+
+template <typename T>
+void launch_wave_sweep(cudaStream_t st, const WaveGeom& g, const T* rec, const T* rhs, T* out,
+                       void* face_a, void* face_b, bool forward, int divmode, const SweepSync& S,
+                       const int* done)
+{
+    if (g.D[0] * g.D[1] * g.D[2] == 0) return;
     WaveParams<T> p;
     p.g = g;
-    p.n = n;
-    p.soa = soa;
+    p.rec = rec;
     p.rhs = rhs;
     p.out = out;
+    p.faceA = static_cast<typename Bits<T>::U*>(face_a);
+    p.faceB = static_cast<typename Bits<T>::U*>(face_b);
     p.S = S;
     p.done = done;
     if (forward)
-        launch_wave_span<T, true, false>(st, g.span, p);
+        launch_wave_span<T, true, false>(st, p);
     else if (divmode == 0)
-        launch_wave_span<T, false, true>(st, g.span, p);
+        launch_wave_span<T, false, true>(st, p);
     else
-        launch_wave_span<T, false, false>(st, g.span, p);
+        launch_wave_span<T, false, false>(st, p);
 }
 
-template void launch_wave_sweep<double>(cudaStream_t, const WaveGeom&, int, const double*,
-                                        const double*, double*, bool, int, const SweepSync&,
-                                        const int*);
-template void launch_wave_sweep<float>(cudaStream_t, const WaveGeom&, int, const float*,
-                                       const float*, float*, bool, int, const SweepSync&,
+template <typename TO>
+void launch_box_to_wave(cudaStream_t st, const int* dims, int n, const int* rp, const double* M,
+                        const WaveGeom& g, TO* fw, TO* bw, int recip)
+{
+    if (n == 0) return;
+    const int blocks = (n + 255) / 256;
+    if (recip)
+        box_to_wave_kernel<TO, 1><<<blocks, 256, 0, st>>>(n, dims[0], dims[1], dims[2], rp, M, g,
+                                                          fw, bw);
+    else
+        box_to_wave_kernel<TO, 0><<<blocks, 256, 0, st>>>(n, dims[0], dims[1], dims[2], rp, M, g,
+                                                          fw, bw);
+}
+
+template void launch_wave_sweep<double>(cudaStream_t, const WaveGeom&, const double*,
+                                        const double*, double*, void*, void*, bool, int,
+                                        const SweepSync&, const int*);
+template void launch_wave_sweep<float>(cudaStream_t, const WaveGeom&, const float*, const float*,
+                                       float*, void*, void*, bool, int, const SweepSync&,
                                        const int*);
+template void launch_box_to_wave<double>(cudaStream_t, const int*, int, const int*, const double*,
+                                         const WaveGeom&, double*, double*, int);
+template void launch_box_to_wave<float>(cudaStream_t, const int*, int, const int*, const double*,
+                                        const WaveGeom&, float*, float*, int);
 
 }  // namespace ocsl

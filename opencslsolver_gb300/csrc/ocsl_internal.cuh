@@ -233,29 +233,45 @@ constexpr int kMaxClusterTiles = 16;
 // g with clusters of cx x cy tiles (clipped to the tile grid and to 16
 // tiles; 1 x 1 = no clusters).
 BoxGeom box_with_cluster(BoxGeom g, int cx, int cy);
-// Warp-pipelined structured sweep (kernels_wave.cu), one right-hand side:
-// each warp solves K (along a) x 32 (along b) columns, K = 4 in FP32 and 2 in
-// FP64; a CTA holds WA warps side by side along a.
+// Warp-pipelined structured sweep (kernels_wave.cu), one right-hand side.
+// Canonical coordinates a = x, s = the longer of y and z, b = the other; a
+// warp solves a tile of 32 (along a, one lane each) x K (along b) columns,
+// K = 4 in FP32 and 2 in FP64; a CTA holds WB warps stacked along b.  The
+// factor's records are stored per direction in the sweep's step order
+// ([nwb][nwa][T][K][32] records, T = Ds + K - 1 + 31), which depends on the
+// box and K only, not on WB or the lag.
 constexpr int kWaveMaxWarps = 8;
 struct WaveGeom {
-    int D[3];      // extents of a, b, s (as BoxGeom)
-    int S[3];      // row strides of a, b, s
-    int span;      // which of x (0), y (1), z (2) is s
-    int WA;        // warps per CTA
+    int D[3];      // extents of a, b, s
+    int S[3];      // physical row strides of a, b, s
+    int span;      // 2: s = z (b = y); 1: s = y (b = z)
+    int K;         // columns per warp along b
+    int nwa, nwb;  // warp tiles along a and b
+    int T;         // steps of a warp tile
+    int WB;        // warps per CTA
     int nta, ntb;  // CTA tiles along a and b
     int lag;       // start lag behind an upstream CTA (rows)
-    int lag_sh;    // start lag behind the warp to the left (rows)
+    int lag_sh;    // start lag behind the warp below (rows)
 };
 int wave_cols_per_warp(int elem_size);
 // Dynamic shared memory of one CTA (cp.async rings and the face buffers
 // between its warps).
 size_t wave_sweep_smem(const WaveGeom& g, int elem_size);
-// Geometry for `warps` warps per CTA (clipped to the box and to the
-// shared-memory limit); lag 0 = default.
-WaveGeom make_wave_geom(const BoxGeom& box, int elem_size, int warps, int lag = 0);
+// Geometry of an nx * ny * nz box for `warps` warps per CTA (0 = default 4;
+// clipped to the box and to the shared-memory limit); lag 0 = default.
+WaveGeom make_wave_geom(const int* dims, int elem_size, int warps, int lag = 0);
+// Records (of 4 elements) in one direction's step-order layout.
+size_t wave_layout_elems(const WaveGeom& g);
+// face_a: [nwa * nwb][T][K], face_b: [nwa * nwb][T][32] elements of the
+// sweep's type, all-ones between launches.
 template <typename T>
-void launch_wave_sweep(cudaStream_t st, const WaveGeom& g, int n, const T* soa, const T* rhs,
-                       T* out, bool forward, int divmode, const SweepSync& S, const int* done);
+void launch_wave_sweep(cudaStream_t st, const WaveGeom& g, const T* rec, const T* rhs, T* out,
+                       void* face_a, void* face_b, bool forward, int divmode, const SweepSync& S,
+                       const int* done);
+// CSR factor (FP64) -> the forward and backward step-order record layouts of g.
+template <typename TO>
+void launch_box_to_wave(cudaStream_t st, const int* dims, int n, const int* rp, const double* M,
+                        const WaveGeom& g, TO* fw, TO* bw, int recip);
 
 // CSR factor (FP64) -> packed stencil records in TO; diagonal term =
 // diagonal, or 1/diagonal with recip.

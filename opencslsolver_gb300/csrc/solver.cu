@@ -147,15 +147,24 @@ struct ocsl_ctx {
     bool wave_on[2] = {true, true};
     int wave_req[2][2] = {{0, 0}, {0, 0}};
     WaveGeom wave[2] = {};
+    // its step-order record layouts ([0] forward, [1] backward) and face
+    // buffers (all-ones between launches; refilled after a wait ran out)
+    double* d_wrec64[2] = {nullptr, nullptr};
+    float* d_wrec32[2] = {nullptr, nullptr};
+    void* d_wface[2] = {nullptr, nullptr};
+    size_t wface_bytes[2] = {0, 0};
+    bool wave_faces_dirty = false;
+    // the warp-pipelined kernel applies to this box (its layout stays within
+    // 16 n records: boxes much thinner than a warp in x are left to the CTA kernel)
+    bool wave_fits[2] = {false, false};
     // P.box / P.box32 and the wave geometries from the requests (box patterns only)
     void rebuild_box_geoms()
     {
         if (!hp.box.ok) return;
         for (int k = 0; k < 2; ++k) {
-            const BoxGeom base = make_box_geom(hp.box, 0, 0);
             const int elem = k == 0 ? 8 : 4;
-            wave[k] = make_wave_geom(base, elem, wave_req[k][0] > 0 ? wave_req[k][0] : 4,
-                                     wave_req[k][1]);
+            wave[k] = make_wave_geom(hp.box.dim, elem, wave_req[k][0], wave_req[k][1]);
+            wave_fits[k] = wave_layout_elems(wave[k]) <= 16 * (size_t)std::max(P.n, 1);
         }
         BoxGeom* geo[2] = {&P.box, &P.box32};
         for (int k = 0; k < 2; ++k) {
@@ -216,6 +225,8 @@ struct ocsl_ctx {
     void ensure_reduce(int ntiles);
     void ensure_fp32();
     void ensure_cols();
+    // step-order records and face buffers of the warp-pipelined sweep (k: 0 FP64, 1 FP32)
+    void ensure_wave(int k);
 };
 
 void ocsl_ctx::free_pattern()
@@ -246,6 +257,17 @@ void ocsl_ctx::free_pattern()
     if (v64c) cudaFree(v64c);
     v64c = nullptr;
     for (auto& v : v32c) { if (v) cudaFree(v); v = nullptr; }
+    for (int k = 0; k < 2; ++k) {
+        if (d_wrec64[k]) cudaFree(d_wrec64[k]);
+        if (d_wrec32[k]) cudaFree(d_wrec32[k]);
+        if (d_wface[k]) cudaFree(d_wface[k]);
+        d_wrec64[k] = nullptr;
+        d_wrec32[k] = nullptr;
+        d_wface[k] = nullptr;
+        wface_bytes[k] = 0;
+        wave_fits[k] = false;
+    }
+    wave_faces_dirty = false;
     has_pattern = false;
     P = DevPattern{};
 }
@@ -295,6 +317,26 @@ void ocsl_ctx::ensure_fp32()
     d_dinv32 = dalloc<float>(n);
     for (auto& v : v32) v = dalloc<float>(n);
     if (hp.box.ok) d_soa32 = dalloc<float>(8 * n);
+}
+
+void ocsl_ctx::ensure_wave(int k)
+{
+    const WaveGeom& g = wave[k];
+    const size_t recs = wave_layout_elems(g);
+    const size_t face = (size_t)g.nwa * g.nwb * g.T * (g.K + 32) * (k == 0 ? 8 : 4);
+    if (k == 0 && !d_wrec64[0]) {
+        d_wrec64[0] = dalloc<double>(4 * recs);
+        d_wrec64[1] = dalloc<double>(4 * recs);
+    }
+    if (k == 1 && !d_wrec32[0]) {
+        d_wrec32[0] = dalloc<float>(4 * recs);
+        d_wrec32[1] = dalloc<float>(4 * recs);
+    }
+    if (!d_wface[k]) {
+        CK(cudaMalloc(&d_wface[k], face));
+        CK(cudaMemset(d_wface[k], 0xFF, face));
+        wface_bytes[k] = face;
+    }
 }
 
 void ocsl_ctx::ensure_cols()
@@ -556,14 +598,14 @@ struct Solve {
     template <typename TT>
     void fw(const TT* M, const TT* rhs, TT* out, int k, bool prefilled = false)
     {
-        if (!prefilled) {
+        const bool wave = use_box() && soa<TT>() && use_wave<TT>();
+        if (!prefilled && !wave) {  // the warp-pipelined sweep keeps its faces apart
             ProfScope ps(c, st, PC_FILL);
             fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
-        if (use_box() && soa<TT>() && use_wave<TT>())
-            launch_wave_sweep<TT>(st, c->wave[is_f64<TT>() ? 0 : 1], P.n, soa<TT>(), rhs, out,
-                                  true, 0, c->next_sync(), k >= 0 ? done(k) : nullptr);
+        if (wave)
+            wave_sweep<TT>(rhs, out, true, 0, k);
         else if (use_box() && soa<TT>())
             launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, true, 0,
                                  c->next_sync(), k >= 0 ? done(k) : nullptr, cols, kDoneStride);
@@ -592,8 +634,36 @@ struct Solve {
     template <typename TT>
     bool use_wave() const
     {
-        if (cols.n != 1 || c->sweep_kernel == 2) return false;
-        return c->sweep_kernel == 3 || c->wave_on[is_f64<TT>() ? 0 : 1];
+        const int k = is_f64<TT>() ? 0 : 1;
+        if (cols.n != 1 || !wave_possible(k)) return false;
+        return c->sweep_kernel == 3 || c->wave_on[k];
+    }
+    // the step-order records are kept for this precision (the CTA kernel is
+    // not forced and the box is not too thin for the warp tiles)
+    bool wave_possible(int k) const
+    {
+        return P.box_ok && c->sweep_kernel != 2 && c->sweep_kernel != 1 && c->wave_fits[k];
+    }
+    template <typename TT>
+    const TT* wave_rec(bool forward) const
+    {
+        if constexpr (sizeof(TT) == 8) return c->d_wrec64[forward ? 0 : 1];
+        else return c->d_wrec32[forward ? 0 : 1];
+    }
+    template <typename TT>
+    void wave_sweep(const TT* rhs, TT* out, bool forward, int divmode, int k)
+    {
+        const int pi = is_f64<TT>() ? 0 : 1;
+        if (c->wave_faces_dirty) {  // a launch gave up waiting: faces to all-ones again
+            for (int q = 0; q < 2; ++q)
+                if (c->d_wface[q]) CK(cudaMemsetAsync(c->d_wface[q], 0xFF, c->wface_bytes[q], st));
+            c->wave_faces_dirty = false;
+        }
+        const WaveGeom& g = c->wave[pi];
+        char* faces = static_cast<char*>(c->d_wface[pi]);
+        const size_t fa_bytes = (size_t)g.nwa * g.nwb * g.T * g.K * sizeof(TT);
+        launch_wave_sweep<TT>(st, g, wave_rec<TT>(forward), rhs, out, faces, faces + fa_bytes,
+                              forward, divmode, c->next_sync(), k >= 0 ? done(k) : nullptr);
     }
     // After a factorisation: the structured sweeps read the factor in the
     // stencil-SoA layout (slot 3: diagonal for the reference's division, or
@@ -607,10 +677,20 @@ struct Solve {
         if (want64) {
             launch_box_to_soa<double>(st, c->hp.box.dim, P.n, P.rp, M, c->d_soa64, recip64 ? 1 : 0);
             soa64 = c->d_soa64;
+            if (wave_possible(0)) {
+                c->ensure_wave(0);
+                launch_box_to_wave<double>(st, c->hp.box.dim, P.n, P.rp, M, c->wave[0],
+                                           c->d_wrec64[0], c->d_wrec64[1], recip64 ? 1 : 0);
+            }
         }
         if (want32) {
             launch_box_to_soa<float>(st, c->hp.box.dim, P.n, P.rp, M, c->d_soa32, 1);
             soa32 = c->d_soa32;
+            if (wave_possible(1)) {
+                c->ensure_wave(1);
+                launch_box_to_wave<float>(st, c->hp.box.dim, P.n, P.rp, M, c->wave[1],
+                                          c->d_wrec32[0], c->d_wrec32[1], 1);
+            }
         }
     }
     // factor() + prepare_box(), or the previous solve's factor when reusing
@@ -657,14 +737,14 @@ struct Solve {
     void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k,
             bool prefilled = false)
     {
-        if (!prefilled) {
+        const bool wave = use_box() && soa<TT>() && use_wave<TT>();
+        if (!prefilled && !wave) {
             ProfScope ps(c, st, PC_FILL);
             fill_sentinel(out, k);
         }
         ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
-        if (use_box() && soa<TT>() && use_wave<TT>())
-            launch_wave_sweep<TT>(st, c->wave[is_f64<TT>() ? 0 : 1], P.n, soa<TT>(), rhs, out,
-                                  false, divmode, c->next_sync(), k >= 0 ? done(k) : nullptr);
+        if (wave)
+            wave_sweep<TT>(rhs, out, false, divmode, k);
         else if (use_box() && soa<TT>())
             launch_box_sweep<TT>(st, sweep_geom<TT>(), P.n, soa<TT>(), rhs, out, false, divmode,
                                  c->next_sync(), k >= 0 ? done(k) : nullptr, cols, kDoneStride);
@@ -733,6 +813,7 @@ struct Solve {
     {
         CK(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        if (*c->h_err == OCSL_TIMEOUT) c->wave_faces_dirty = true;
         return *c->h_err;
     }
 };
@@ -858,7 +939,7 @@ void bicgstab_iteration(Solve& s, const TT* A, const TT* M, const TT* dinv, TT* 
     // single column: the vector kernels before each sweep pair fill the
     // pair's outputs (tmp is dead after each backward sweep, s^ after the x
     // update, p^ after the p update), so no fill launches inside the loop
-    const bool fuse = s.cols.n == 1;
+    const bool fuse = s.cols.n == 1 && !(s.use_box() && s.template use_wave<TT>());
     const bool pre = fuse && s.tb_prefilled;
     TT* f0 = fuse ? tmp : nullptr;
     s.fw<TT>(M, p, tmp, k, pre);
@@ -1781,6 +1862,7 @@ int ocsl_set_sweep_kernel(ocsl_ctx* c, int kind, int tile_a, int tile_b)
     if (kind >= 2 && c->has_pattern && !c->hp.box.ok)
         return fail(c, OCSL_BAD_ARGUMENT, "the pattern is not a 7-point box stencil");
     c->drop_graph();
+    c->fac_M = nullptr;  // the next solve prepares the layouts this kernel reads
     c->sweep_kernel = kind;
     for (int k = 0; k < 2; ++k) {
         if (kind == 3) {  // warps per CTA, start lag
@@ -1834,10 +1916,10 @@ int ocsl_wave_geometry(const ocsl_ctx* c, int fp32, int* on, int* warps, int* la
     if (!c) return OCSL_BAD_ARGUMENT;
     if (!c->has_pattern) return OCSL_NO_PATTERN;
     const int k = fp32 ? 1 : 0;
-    const bool act = c->P.box_ok && c->sweep_kernel != 2 &&
+    const bool act = c->P.box_ok && c->sweep_kernel != 2 && c->wave_fits[k] &&
                      (c->sweep_kernel == 3 || c->wave_on[k]);
     if (on) *on = act ? 1 : 0;
-    if (warps) *warps = act ? c->wave[k].WA : 0;
+    if (warps) *warps = act ? c->wave[k].WB : 0;
     if (lag) *lag = act ? c->wave[k].lag : 0;
     return OCSL_OK;
 }
@@ -1907,16 +1989,15 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         // warp-pipelined kernel: warps per CTA x start lag
         double best_wave = 1e300;
         WaveGeom bestw = wkeep;
-        if (c->sweep_kernel != 2) {
+        if (c->sweep_kernel != 2 && c->wave_fits[pi]) {
             c->sweep_kernel = 3;
-            static const int kWarps[] = {1, 2, 4, 8};
-            static const int kLags[] = {4, 6, 10};
-            const BoxGeom base = make_box_geom(c->hp.box, 0, 0);
+            static const int kWarps[] = {1, 2, 3, 4, 6, 8};
+            static const int kLags[] = {3, 6, 10};
             std::vector<std::array<int, 2>> wtried;
-            for (int wa : kWarps)
+            for (int wb : kWarps)
             for (int lg : kLags) {
-                const WaveGeom g = make_wave_geom(base, fp32 ? 4 : 8, wa, lg);
-                const std::array<int, 2> key{g.WA, g.lag};
+                const WaveGeom g = make_wave_geom(c->hp.box.dim, fp32 ? 4 : 8, wb, lg);
+                const std::array<int, 2> key{g.WB, g.lag};
                 if (std::find(wtried.begin(), wtried.end(), key) != wtried.end()) continue;
                 wtried.push_back(key);
                 c->wave[pi] = g;
@@ -1969,15 +2050,15 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         if (kind_keep == 0) c->wave_on[pi] = wave_wins;
         if (wave_wins || kind_keep == 3) {
             c->wave[pi] = bestw;
-            c->wave_req[pi][0] = bestw.WA;
+            c->wave_req[pi][0] = bestw.WB;
             c->wave_req[pi][1] = bestw.lag;
         } else {
             c->wave[pi] = wkeep;
         }
         c->fac_M = nullptr;
         const int K = wave_cols_per_warp(fp32 ? 4 : 8);
-        if (tile_a) *tile_a = wave_wins ? bestw.WA * K : bestg.TA;
-        if (tile_b) *tile_b = wave_wins ? 32 : bestg.TB;
+        if (tile_a) *tile_a = wave_wins ? 32 : bestg.TA;
+        if (tile_b) *tile_b = wave_wins ? bestw.WB * K : bestg.TB;
         if (sweep_us) *sweep_us = wave_wins ? best_wave : best;
         CK(cudaGetLastError());
     } catch (const CudaError& e) {
@@ -1993,7 +2074,10 @@ int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
     if (!c->has_pattern) return OCSL_NO_PATTERN;
-    if (kind) *kind = !c->P.box_ok ? 1 : (c->sweep_kernel == 2 ? 2 : (c->sweep_kernel == 3 || c->wave_on[0] ? 3 : 2));
+    if (kind)
+        *kind = !c->P.box_ok ? 1
+                : (c->sweep_kernel != 2 && c->wave_fits[0] &&
+                   (c->sweep_kernel == 3 || c->wave_on[0])) ? 3 : 2;
     if (dims) for (int k = 0; k < 3; ++k) dims[k] = c->hp.box.ok ? c->hp.box.dim[k] : 0;
     if (tiles) {
         tiles[0] = c->P.box_ok ? c->P.box.TA : 0;
