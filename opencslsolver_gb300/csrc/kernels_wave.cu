@@ -59,8 +59,8 @@ namespace {
 
 constexpr long kSpinLimit = 1L << 21;
 constexpr int kP = 8;     // prefetch depth of records and right-hand-side slices (steps)
-constexpr int kDF = 4;    // global face values fetched this many steps ahead
-constexpr int kWaveLag = kDF + 2;   // default start lag behind an upstream CTA (rows)
+constexpr int kDF = 6;    // global face values fetched this many steps ahead
+constexpr int kWaveLag = kDF + 3;   // default start lag behind an upstream CTA (rows)
 constexpr int kWaveLagShared = 1;   // ... behind the warp below in the same CTA
 
 template <typename T>
@@ -273,23 +273,29 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
         U* fb_out_sh = (push_b && w < WB - 1) ? sface + w * T_ * 32 : nullptr;
         U* fb_out_gl = (push_b && w == WB - 1) ? p.faceB + (size_t)wt * T_ * 32 : nullptr;
 
-        auto issue = [&](int t) {  // records of step t and right-hand-side slice t
-            if (t < T_) {
-                const int j = t % kP;
+        // Ring slots are tracked incrementally (RS is not a power of two):
+        // rs_l = (t - l) mod RS, so row (k, s = t - k - l) sits in slot
+        // rs_l - k (mod RS); rs_fl = (t - K + 1 - 31) mod RS is the slice that
+        // completes at step t; rs_in = (t + kP) mod RS is the slice issued at t.
+        const T* rhs_k[K];
 #pragma unroll
-                for (int k = 0; k < K; ++k)
-                    cp_rec<T>(&my_rr[(j * K + k) * 32 + l], recs + ((size_t)t * K + k) * 32 + l);
+        for (int k = 0; k < K; ++k) rhs_k[k] = p.rhs + base[k];
+        auto issue = [&](int t, int rs) {  // records of step t and right-hand-side slice t
+            if (t < T_) {  // uniform over the warp
+                const int j = t % kP;
+                const R* src = recs + (size_t)t * K * 32 + l;
+#pragma unroll
+                for (int k = 0; k < K; ++k) cp_rec<T>(&my_rr[(j * K + k) * 32 + l], src + k * 32);
             }
             if (t < Ds) {
-                const int j = t % RS;
 #pragma unroll
                 for (int k = 0; k < K; ++k)
-                    if (ok[k]) cp_val<T>(&my_sr[(j * K + k) * 32 + l], p.rhs + base[k] + t * sstep);
+                    if (ok[k]) cp_val<T>(&my_sr[(rs * K + k) * 32 + l], rhs_k[k] + t * sstep);
             }
             cp_commit();
         };
 #pragma unroll
-        for (int j = 0; j < kP; ++j) issue(j);
+        for (int j = 0; j < kP; ++j) issue(j, j);
 
         // Start behind the upstream tiles: wait for their face values of row
         // s = lag next to this tile (lane 0, column 0), so that values fetched
@@ -309,16 +315,15 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
 
         // global face values kDF steps ahead: fa (lane 0, the K a-neighbours of
         // step t at d = t + 31), fb (column 0's b-neighbour at d = t + K - 1)
+        const bool get_a = fa_in != nullptr && l == 0;
         U fa[kDF][K], fb[kDF];
         auto fetch = [&](int t, int j) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) fa[j][k] = B::kSentinel;
-            fb[j] = B::kSentinel;
-            if (fa_in && l == 0 && t + 31 < T_) {
-#pragma unroll
-                for (int k = 0; k < K; ++k) fa[j][k] = B::load(fa_in + (size_t)(t + 31) * K + k);
-            }
-            if (fb_in_gl && t + K - 1 < T_) fb[j] = B::load(fb_in_gl + (size_t)(t + K - 1) * 32 + l);
+            for (int k = 0; k < K; ++k)
+                fa[j][k] = (get_a && t + 31 < T_) ? B::load(fa_in + (size_t)(t + 31) * K + k)
+                                                  : B::kSentinel;
+            fb[j] = (fb_in_gl && t + K - 1 < T_) ? B::load(fb_in_gl + (size_t)(t + K - 1) * 32 + l)
+                                                 : B::kSentinel;
         };
 #pragma unroll
         for (int j = 0; j < kDF; ++j) fetch(j, j);
@@ -326,6 +331,9 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
         T cur[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) cur[k] = T(0);
+        int rs_l = l == 0 ? 0 : RS - l;
+        int rs_fl = RS - (K - 1) - 31;
+        int rs_in = kP;
         for (int t0 = 0; t0 < T_; t0 += kP) {
 #pragma unroll
             for (int j = 0; j < kP; ++j) {
@@ -333,88 +341,111 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
                 if (t >= T_) break;  // uniform over the warp
                 const int jf = j % kDF;
                 cp_wait<kP - 1>();
+                // rows of this step and their slots
+                bool act[K];
+                int slot_i[K];
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const int s = t - k - l;
+                    act[k] = ok[k] && (unsigned)s < (unsigned)Ds;
+                    const int sk = rs_l - k;
+                    slot_i[k] = ((sk < 0 ? sk + RS : sk) * K + k) * 32 + l;
+                }
+                // faces of this step; a face value that is not there yet is
+                // waited for on the rare slow path
+                T fa_v[K], fb_v = T(0);
+                bool slow = false;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    fa_v[k] = get_a ? B::from(fa[jf][k]) : T(0);
+                    slow |= get_a && act[k] && fa[jf][k] == B::kSentinel;
+                }
+                U fbu = B::kSentinel;
+                if (fb_in_sh) fbu = vload_shared(fb_in_sh + (t + K - 1) * 32 + l);
+                else if (fb_in_gl) fbu = fb[jf];
+                if (fb_in_sh || fb_in_gl) {
+                    fb_v = B::from(fbu);
+                    slow |= act[0] && fbu == B::kSentinel;
+                }
+                if (slow) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        if (get_a && act[k] && fa[jf][k] == B::kSentinel)
+                            fa_v[k] = wait_global<T>(fa_in + (size_t)(t + 31) * K + k, err);
+                    if (act[0] && fbu == B::kSentinel) {
+                        if (fb_in_sh)
+                            fb_v = wait_shared<T>(fb_in_sh + (t + K - 1) * 32 + l, err);
+                        else
+                            fb_v = wait_global<T>(fb_in_gl + (size_t)(t + K - 1) * 32 + l, err);
+                    }
+                }
                 T up[K];  // lane l-1's values of the previous step: a-neighbours
 #pragma unroll
                 for (int k = 0; k < K; ++k) up[k] = __shfl_up_sync(0xffffffffu, cur[k], 1);
+                // K independent rows, straight-line (inactive rows compute on
+                // stale slot contents and are discarded)
                 T nv[K];
-                U out_a[K];
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    nv[k] = cur[k];
-                    out_a[k] = B::kSentinel;
+                    const R cf = my_rr[(j * K + k) * 32 + l];
+                    const T rh = my_sr[slot_i[k]];
                     const int s = t - k - l;
-                    if (ok[k] && s >= 0 && s < Ds) {
-                        const R cf = my_rr[(j * K + k) * 32 + l];
-                        T* slot = &my_sr[((s % RS) * K + k) * 32 + l];
-                        const T rh = *slot;
-                        T va = T(0), vb = T(0);
-                        if (l > 0) {
-                            va = up[k];
-                        } else if (has_a) {
-                            va = fa[jf][k] != B::kSentinel
-                                     ? B::from(fa[jf][k])
-                                     : wait_global<T>(fa_in + (size_t)(t + 31) * K + k, err);
-                        }
-                        if (k > 0) {
-                            vb = cur[k - 1];
-                        } else if (fb_in_sh) {
-                            const U* fs = fb_in_sh + (t + K - 1) * 32 + l;
-                            const U u = vload_shared(fs);
-                            vb = u != B::kSentinel ? B::from(u) : wait_shared<T>(fs, err);
-                        } else if (fb_in_gl) {
-                            vb = fb[jf] != B::kSentinel
-                                     ? B::from(fb[jf])
-                                     : wait_global<T>(fb_in_gl + (size_t)(t + K - 1) * 32 + l, err);
-                        }
-                        const T vs = s > 0 ? cur[k] : T(0);
-                        const T vx = va;
-                        const T vy = SPAN == 2 ? vb : vs;
-                        const T vz = SPAN == 2 ? vs : vb;
-                        // record: z-, y-, x-, (unused) | x+, y+, z+, diagonal term;
-                        // the fma order is the row's CSR order
-                        T sum = fma_t(cf.v[0], FWD ? vz : vx, T(0));
-                        sum = fma_t(cf.v[1], vy, sum);
-                        sum = fma_t(cf.v[2], FWD ? vx : vz, sum);
-                        const T num = rh - sum;
-                        const T y = FWD ? num : (DIV ? num / cf.v[3] : num * cf.v[3]);
-                        nv[k] = y;
-                        *slot = y;  // the slice keeps the result until it is written back
-                        const U bits = to_bits(y);
-                        out_a[k] = bits;
-                        if (k == K - 1) {
-                            if (fb_out_sh) vstore_shared(fb_out_sh + t * 32 + l, bits);
-                            else if (fb_out_gl) B::store(fb_out_gl + (size_t)t * 32 + l, bits);
-                        }
-                    }
+                    const T va = l > 0 ? up[k] : fa_v[k];
+                    const T vb = k > 0 ? cur[k > 0 ? k - 1 : 0] : fb_v;
+                    const T vs = s > 0 ? cur[k] : T(0);
+                    const T vx = va;
+                    const T vy = SPAN == 2 ? vb : vs;
+                    const T vz = SPAN == 2 ? vs : vb;
+                    // record: z-, y-, x-, (unused) | x+, y+, z+, diagonal term;
+                    // the fma order is the row's CSR order
+                    T sum = fma_t(cf.v[0], FWD ? vz : vx, T(0));
+                    sum = fma_t(cf.v[1], vy, sum);
+                    sum = fma_t(cf.v[2], FWD ? vx : vz, sum);
+                    const T num = rh - sum;
+                    T y;
+                    if constexpr (FWD)
+                        y = num;
+                    else if constexpr (DIV)
+                        y = num / (act[k] ? cf.v[3] : T(1));
+                    else
+                        y = num * cf.v[3];
+                    nv[k] = act[k] ? y : cur[k];
+                    if (act[k]) my_sr[slot_i[k]] = y;  // kept until the slice is written back
+                }
+                // faces out: column K-1 to the tile above, lane 31 to the right
+                if (act[K - 1]) {
+                    const U bits = to_bits(nv[K - 1]);
+                    if (fb_out_sh) vstore_shared(fb_out_sh + t * 32 + l, bits);
+                    else if (fb_out_gl) B::store(fb_out_gl + (size_t)t * 32 + l, bits);
                 }
                 if (push_a) {
 #pragma unroll
                     for (int k = 0; k < K; ++k)
-                        if (out_a[k] != B::kSentinel) B::store(fa_out + (size_t)t * K + k, out_a[k]);
+                        if (act[k]) B::store(fa_out + (size_t)t * K + k, to_bits(nv[k]));
                 }
                 // consumed global faces go back to the sentinel for the next launch
-                if (fa_in && l == 0 && t + 31 < T_) {
+                if (get_a) {
 #pragma unroll
                     for (int k = 0; k < K; ++k)
-                        if (ok[k] && t - k >= 0 && t - k < Ds)
+                        if (act[k])
                             B::store(const_cast<U*>(fa_in) + (size_t)(t + 31) * K + k, B::kSentinel);
                 }
-                if (fb_in_gl && ok[0] && t - l >= 0 && t - l < Ds && t + K - 1 < T_)
+                if (fb_in_gl && act[0])
                     B::store(const_cast<U*>(fb_in_gl) + (size_t)(t + K - 1) * 32 + l, B::kSentinel);
 #pragma unroll
                 for (int k = 0; k < K; ++k) cur[k] = nv[k];
                 // slice t - (K-1) - 31 is complete: write it back, coalesced
-                {
+                if (t >= K - 1 + 31 && t - (K - 1) - 31 < Ds) {  // uniform over the warp
                     const int sf = t - (K - 1) - 31;
-                    if (sf >= 0 && sf < Ds) {
-                        const int js = sf % RS;
 #pragma unroll
-                        for (int k = 0; k < K; ++k)
-                            if (ok[k]) p.out[base[k] + sf * sstep] = my_sr[(js * K + k) * 32 + l];
-                    }
+                    for (int k = 0; k < K; ++k)
+                        if (ok[k]) p.out[base[k] + sf * sstep] = my_sr[(rs_fl * K + k) * 32 + l];
                 }
                 fetch(t + kDF, jf);
-                issue(t + kP);
+                issue(t + kP, rs_in);
+                rs_l = rs_l + 1 == RS ? 0 : rs_l + 1;
+                rs_fl = rs_fl + 1 == RS ? 0 : rs_fl + 1;
+                rs_in = rs_in + 1 == RS ? 0 : rs_in + 1;
             }
         }
         cp_wait<0>();
