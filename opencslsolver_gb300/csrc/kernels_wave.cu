@@ -59,8 +59,11 @@ namespace {
 
 constexpr long kSpinLimit = 1L << 21;
 constexpr int kP = 8;     // prefetch depth of records and right-hand-side slices (steps)
-constexpr int kDF = 6;    // global face values fetched this many steps ahead
+constexpr int kDF = 4;    // global face values fetched this many steps ahead
 constexpr int kWaveLag = kDF + 3;   // default start lag behind an upstream CTA (rows)
+// the face ring slot of step t is (t mod kP) mod kDF: equal to t mod kDF only
+// when kDF divides kP
+static_assert(kP % kDF == 0, "the face ring must tile the step ring");
 constexpr int kWaveLagShared = 1;   // ... behind the warp below in the same CTA
 
 template <typename T>
@@ -361,8 +364,11 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
                     slow |= get_a && act[k] && fa[jf][k] == B::kSentinel;
                 }
                 U fbu = B::kSentinel;
-                if (fb_in_sh) fbu = vload_shared(fb_in_sh + (t + K - 1) * 32 + l);
-                else if (fb_in_gl) fbu = fb[jf];
+                if (fb_in_sh) {
+                    if (t + K - 1 < T_) fbu = vload_shared(fb_in_sh + (t + K - 1) * 32 + l);
+                } else if (fb_in_gl) {
+                    fbu = fb[jf];
+                }
                 if (fb_in_sh || fb_in_gl) {
                     fb_v = B::from(fbu);
                     slow |= act[0] && fbu == B::kSentinel;
