@@ -378,7 +378,9 @@ __global__ void __launch_bounds__(32 * kWaveMaxWarps) wave_sweep_kernel(WavePara
                     for (int k = 0; k < K; ++k)
                         if (get_a && act[k] && fa[jf][k] == B::kSentinel)
                             fa_v[k] = wait_global<T>(fa_in + (size_t)(t + 31) * K + k, err);
-                    if (act[0] && fbu == B::kSentinel) {
+                    // only a tile with a b-face waits for one (fbu keeps the
+                    // all-ones default on the bottom tile row)
+                    if ((fb_in_sh || fb_in_gl) && act[0] && fbu == B::kSentinel) {
                         if (fb_in_sh)
                             fb_v = wait_shared<T>(fb_in_sh + (t + K - 1) * 32 + l, err);
                         else
