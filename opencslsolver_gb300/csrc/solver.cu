@@ -144,7 +144,11 @@ struct ocsl_ctx {
     // Warp-pipelined sweep (kernels_wave.cu) for single right-hand sides, per
     // precision ([0] FP64, [1] FP32): on / off, warps per CTA and start lag
     // requests (0 = automatic), and the geometry built from them.
-    bool wave_on[2] = {true, true};
+    // Off by default: on the boxes measured (64^3, 128^3) the CTA kernel's
+    // wavefront is shorter; ocsl_autotune_device switches it on per precision
+    // where it times faster, ocsl_set_sweep_kernel(3, ...) forces it.
+    bool wave_on[2] = {false, false};
+    bool wave_tuning = false;  // the autotuner is timing it: keep its layouts
     int wave_req[2][2] = {{0, 0}, {0, 0}};
     WaveGeom wave[2] = {};
     // its step-order record layouts ([0] forward, [1] backward) and face
@@ -642,7 +646,8 @@ struct Solve {
     // not forced and the box is not too thin for the warp tiles)
     bool wave_possible(int k) const
     {
-        return P.box_ok && c->sweep_kernel != 2 && c->sweep_kernel != 1 && c->wave_fits[k];
+        return P.box_ok && c->sweep_kernel != 2 && c->sweep_kernel != 1 && c->wave_fits[k] &&
+               (c->sweep_kernel == 3 || c->wave_on[k] || c->wave_tuning);
     }
     template <typename TT>
     const TT* wave_rec(bool forward) const
@@ -1957,6 +1962,12 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         c->fac_M = nullptr;
         if (fp32) c->ensure_fp32();
         // the factor and stencil records a solve of `method` sweeps with
+        // the warp-pipelined kernel's layouts are prepared too while timing it
+        struct TuningFlag {
+            bool& f;
+            explicit TuningFlag(bool& x) : f(x) { f = true; }
+            ~TuningFlag() { f = false; }
+        } tuning(c->wave_tuning);
         s.factored(A, o.ilu_sweeps, !ref, fp32, -1, !fp32, !ref, fp32);
         const size_t n = (size_t)c->P.n;
         auto pair = [&] {  // one forward + backward sweep of a zero rhs
