@@ -319,6 +319,66 @@ int ocsl_bc_value_grad_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
                               const ocsl_flow_state* state, const double* d_lambda,
                               double* d_grad);
 
+/* ------------------------------------------------------------------------
+ * The SIMPLE inner iteration on the device: CFlow_solver::iterate
+ * (cflow_solver.cpp:229-476) for an inviscid flow whose boundary faces are
+ * walls, symmetry planes or empty faces -- boundary pressures, the pressure
+ * gradient, the three momentum assemblies and solves, face mass fluxes, the
+ * pressure-correction assembly and solve, the corrections of pressure, mass
+ * fluxes, densities and velocities, and the enthalpy assembly and solve with
+ * the temperature and Mach updates -- all on the context's stream, with no
+ * host round trip between the stages.  The state of ocsl_flow_state is read
+ * AND WRITTEN in place (pressure, velocity, density_c, temperature, enthalpy,
+ * pressure_corr, pressure_grad, mdot, density, qy); its boundary arrays
+ * bc_type, bc_area_vector are read.  Other boundary kinds or eq->viscous give
+ * OCSL_BAD_ARGUMENT.  ocsl_set_faces must have been called.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    /* interior-face metrics (CFVM_face), [3][n_faces] for vectors */
+    const double* face_area_vector;
+    const double* face_alpha;
+    const double* face_distance;   /* cell_center_distance                     */
+    const double* face_unit;       /* cell_center_unit_vector                  */
+    /* boundary-face metrics (CFVM_BC_face), [3][n_bc] for vectors */
+    const double* bc_distance;
+    const double* bc_unit;
+    /* per-iteration fields the iteration writes (DEVICE pointers) */
+    double* bc_pressure;           /* CFlow_BC_face::Pressure (n_bc)             */
+    double* pressure_corr_grad;    /* [3][n]                                     */
+    double* ap;                    /* CFlow_cell::ap (n)                         */
+    double* ap_vec;                /* [3][n]                                     */
+    double* mach;                  /* n                                          */
+    double* total_mdot;            /* n                                          */
+    /* Cfluid_properties and CFlow_solver constants */
+    double cp, Tref, H_formation;
+    double relax_p, relax_u;       /* explicit_underrelaxation_P / _u            */
+} ocsl_flow_iteration;
+
+typedef struct {
+    /* Momentum_global_residual[0..2], Pressure_global_residual (sum |b| of the
+     * pressure-correction system), Enthalpy_global_residual */
+    double residual[5];
+    int iterations[5];             /* of the five solves, in solve order       */
+    int status[5];                 /* ocsl_status of each solve                */
+} ocsl_flow_report;
+
+/* One inner iteration.  methods[0] solves the three momentum components,
+ * methods[1] the pressure correction, methods[2] the enthalpy (the reference
+ * has one switch for all, cconfiguration.cpp:213-228; CG_REF / BICGSTAB_REF
+ * are the reference's CG_solve / ILU_BICGSTAB_solve).  opts applies to the
+ * tolerance-mode methods (NULL = defaults).  Returns the first failing solve's
+ * status (the iteration still runs to the end, as the reference's does), or
+ * OCSL_OK; report (may be NULL) receives the residuals and per-solve results.
+ * The residual sums are taken in the library's tile order, so they may differ
+ * from the reference's serial sums in the last bits. */
+int ocsl_flow_iterate_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
+                             const ocsl_flow_state* state, const ocsl_flow_iteration* it,
+                             const int* methods, const ocsl_opts* opts,
+                             ocsl_flow_report* report);
+/* CFlow_solver::update_timestep for a transient run (cflow_solver.cpp:503-512):
+ * velocity, density, pressure and enthalpy are copied to their *_last fields. */
+int ocsl_flow_end_step_device(ocsl_ctx* ctx, const ocsl_flow_state* state);
+
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured CTA kernel, 3 the structured

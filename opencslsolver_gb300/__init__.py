@@ -220,6 +220,31 @@ class Context:
         self._check(self._L.ocsl_bc_value_grad_device(self._h, C.byref(q), C.byref(st),
                                                       _dptr(lam), _dptr(grad)), "bc_value_grad")
 
+    def flow_iterate_device(self, eq: dict, state: dict, arrays: dict, constants: dict,
+                            methods=(CG_REF, BICGSTAB_REF, BICGSTAB_REF), **opts) -> dict:
+        """One SIMPLE inner iteration on the device (ocsl_flow_iterate_device).
+        ``state`` maps ocsl_flow_state fields to CUDA tensors, updated in place;
+        ``arrays`` the device arrays of ocsl_flow_iteration (metrics and the
+        fields the iteration writes), ``constants`` its cp, Tref, H_formation,
+        relax_p, relax_u.  Returns the report; a failing solve raises."""
+        self._follow_torch()
+        q = self._assembly(eq)
+        st = _abi.flow_state(state, lambda t: _dptr(t).value)
+        it = _abi.flow_iteration(arrays, constants, lambda t: _dptr(t).value)
+        m = (C.c_int * 3)(*(_method(x) for x in methods))
+        o = _abi.default_opts(**opts)
+        rep = _abi.FlowReport()
+        self._check(self._L.ocsl_flow_iterate_device(self._h, C.byref(q), C.byref(st),
+                                                     C.byref(it), m, C.byref(o), C.byref(rep)),
+                    "flow_iterate")
+        return rep.as_dict()
+
+    def flow_end_step_device(self, state: dict) -> None:
+        """Copy velocity, density, pressure and enthalpy to their *_last fields."""
+        self._follow_torch()
+        st = _abi.flow_state(state, lambda t: _dptr(t).value)
+        self._check(self._L.ocsl_flow_end_step_device(self._h, C.byref(st)), "flow_end_step")
+
     # -- adjoint (no reference counterpart)
     def solve_transpose(self, method, value, g, lam, *, raise_on_status=False, **opts):
         """Host-buffer adjoint solve A^T lam = g (ocsl_solve_transpose); ``value``

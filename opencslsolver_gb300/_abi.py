@@ -98,6 +98,39 @@ def flow_state(arrays: dict, ptr) -> FlowState:
         setattr(st, f, None if a is None else ptr(a))
     return st
 
+# ocsl_flow_iteration / ocsl_flow_report (include/ocsl.h)
+FLOW_ITERATION_ARRAYS = (
+    "face_area_vector", "face_alpha", "face_distance", "face_unit", "bc_distance", "bc_unit",
+    "bc_pressure", "pressure_corr_grad", "ap", "ap_vec", "mach", "total_mdot")
+FLOW_ITERATION_CONSTANTS = ("cp", "Tref", "H_formation", "relax_p", "relax_u")
+
+
+class FlowIteration(C.Structure):
+    _fields_ = ([(f, C.c_void_p) for f in FLOW_ITERATION_ARRAYS] +
+                [(f, C.c_double) for f in FLOW_ITERATION_CONSTANTS])
+
+
+class FlowReport(C.Structure):
+    _fields_ = [("residual", C.c_double * 5), ("iterations", C.c_int * 5),
+                ("status", C.c_int * 5)]
+
+    def as_dict(self) -> dict:
+        return {"residual": list(self.residual), "iterations": list(self.iterations),
+                "status": list(self.status)}
+
+
+def flow_iteration(arrays: dict, constants: dict, ptr) -> FlowIteration:
+    """FlowIteration from named arrays (``ptr(a)`` gives each address) and the
+    five constants; missing arrays are NULL."""
+    it = FlowIteration()
+    for f in FLOW_ITERATION_ARRAYS:
+        a = arrays.get(f)
+        setattr(it, f, None if a is None else ptr(a))
+    for f in FLOW_ITERATION_CONSTANTS:
+        setattr(it, f, float(constants[f]))
+    return it
+
+
 _CTX = C.c_void_p
 _PROTOS = {
     "ocsl_default_opts": (None, [C.POINTER(Opts)]),
@@ -146,6 +179,10 @@ _PROTOS = {
                                        _P, _P, _P]),
     "ocsl_bc_value_grad_device": (C.c_int, [_CTX, C.POINTER(Assembly), C.POINTER(FlowState), _P,
                                             _P]),
+    "ocsl_flow_iterate_device": (C.c_int, [_CTX, C.POINTER(Assembly), C.POINTER(FlowState),
+                                           C.POINTER(FlowIteration), C.POINTER(C.c_int),
+                                           C.POINTER(Opts), C.POINTER(FlowReport)]),
+    "ocsl_flow_end_step_device": (C.c_int, [_CTX, C.POINTER(FlowState)]),
     "ocsl_set_sweep_kernel": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_int]),
     "ocsl_sweep_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),

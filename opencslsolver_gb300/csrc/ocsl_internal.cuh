@@ -296,6 +296,63 @@ void launch_assemble(cudaStream_t st, const DevPattern& P, const DevFaces& F,
 void launch_bc_value_grad(cudaStream_t st, const DevFaces& F, const ocsl_assembly& q,
                           const ocsl_flow_state& s, const double* lambda, double* grad);
 
+// flow.cu: the SIMPLE inner iteration around the assembly and the solves.
+// Cell arrays [n] ([3][n] for vectors), face arrays [nf] ([3][nf]), boundary
+// arrays [nb] ([3][nb]); the state is updated in place.
+struct FlowDev {
+    // cells
+    double* pressure;
+    double* velocity;           // [3][n]
+    double* velocity_last;      // [3][n]
+    double* density_c;
+    double* density_last;
+    double* pressure_last;
+    double* temperature;
+    double* enthalpy;
+    double* enthalpy_last;
+    double* pressure_corr;
+    double* pressure_grad;       // [3][n]
+    double* pressure_corr_grad;  // [3][n]
+    double* ap;
+    double* ap_vec;              // [3][n]
+    double* mach;
+    const double* volume;
+    // interior faces
+    const int* left;
+    const int* right;
+    const double* geo_aver;
+    const double* area_vector;   // [3][nf]
+    const double* alpha;         // [3][nf]
+    const double* distance;
+    const double* unit;          // [3][nf]
+    double* mdot;
+    double* face_density;
+    double* qy;
+    // boundary faces
+    const int* bc_type;
+    const int* bc_left;
+    const double* bc_area_vector;  // [3][nb]
+    const double* bc_unit;         // [3][nb]
+    const double* bc_distance;
+    double* bc_pressure;
+    // constants
+    double relax_p, relax_u, cp, Tref, H_formation;
+};
+void launch_flow_bc_pressure(cudaStream_t st, int n, int nb, const FlowDev& f);
+void launch_flow_grad(cudaStream_t st, bool corr, int n, int nf, int nb, const FlowDev& f,
+                      const DevFaces& F);
+void launch_flow_velocity_update(cudaStream_t st, int n, int d, const double* x, const FlowDev& f,
+                                 double* res);
+void launch_flow_face_mdot(cudaStream_t st, int n, int nf, const FlowDev& f, int blended);
+void launch_flow_pcorr(cudaStream_t st, int n, const double* x, const FlowDev& f);
+void launch_flow_correct(cudaStream_t st, int n, int nf, const FlowDev& f, int blended,
+                         double R_specific, double gamma);
+void launch_flow_enthalpy_update(cudaStream_t st, int n, const double* x, const FlowDev& f,
+                                 double* res, double R_specific, double gamma);
+void launch_flow_end_step(cudaStream_t st, int n, const FlowDev& f);
+// *out = sc->sum[0] (on the stream, no host round trip)
+void launch_take_sum(cudaStream_t st, const Scalars* sc, double* out);
+
 // adjoint.cu
 void launch_gather_values(cudaStream_t st, long long nnz, const int* perm, const double* val,
                           double* out);

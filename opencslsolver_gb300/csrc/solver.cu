@@ -67,7 +67,8 @@ enum Vec32 { F_RI, F_RH, F_P, F_PH, F_V, F_S, F_SH, F_T, F_TMP, F_D, NVEC32 };
 // kMaxCols inner blocks from kScInnerCols.
 constexpr int kScOuterCols = 3;
 constexpr int kScInnerCols = kScOuterCols + kMaxCols;
-constexpr int kScBlocks = kScInnerCols + kMaxCols;
+constexpr int kScFlow = kScInnerCols + kMaxCols;  // residual sums of the SIMPLE iteration
+constexpr int kScBlocks = kScFlow + 1;
 // Pinned host mirrors: read copies [0, 16), upload staging [16, 32),
 // two inspection slots of kMaxCols blocks from 32.
 constexpr int kHostStage = 16;
@@ -199,6 +200,16 @@ struct ocsl_ctx {
     bool fac_checked = false;  // fac_status holds the pivot check of fac_M
     int fac_status = OCSL_OK;
 
+    // SIMPLE iteration on the device (ocsl_flow_iterate_device): the system
+    // of the equation being solved, a residual work vector, the five residual
+    // sums, and the boundary-kind check of the last state seen
+    double* d_fval = nullptr;
+    double* d_fb = nullptr;
+    double* d_fx = nullptr;
+    double* d_ftmp = nullptr;
+    double* d_fres = nullptr;
+    const void* flow_bc_checked = nullptr;
+
     // face-loop assembly: the mesh's face incidence (ocsl_set_faces)
     DevFaces F{};
     int* d_faces[8] = {};
@@ -247,6 +258,9 @@ void ocsl_ctx::free_pattern()
     for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
     F = DevFaces{};
     has_faces = false;
+    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp, &d_fres};
+    for (auto pp : dflow) { if (*pp) cudaFree(*pp); *pp = nullptr; }
+    flow_bc_checked = nullptr;
     for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
     double** d64[] = {&d_A, &d_b, &d_x, &d_Ma, &d_Mb, &d_dinv};
     for (auto pp : d64) { if (*pp) cudaFree(*pp); *pp = nullptr; }
@@ -2179,6 +2193,7 @@ int ocsl_set_faces(ocsl_ctx* c, int64_t n_faces, const int32_t* left, const int3
         CK(cudaStreamSynchronize(c->stream));
         for (auto& p : c->d_faces) { if (p) cudaFree(p); p = nullptr; }
         c->has_faces = false;
+        c->flow_bc_checked = nullptr;
         const std::vector<int> l(left, left + n_faces), r(right, right + n_faces),
             bl(bc_left, bc_left + n_bc);
         const std::vector<int>* tabs[8] = {&l, &r, &bl, &ft.cell_ptr, &ft.cell_ent, &ft.cell_slot,
@@ -2227,6 +2242,206 @@ int ocsl_assemble_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_st
     try {
         CK(cudaSetDevice(c->device));
         launch_assemble(c->stream, c->P, c->F, *q, *s, value, b, x0, ap, total_mdot);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+// ------------------------------------------------------------------ SIMPLE iteration
+
+// The state arrays the iteration needs, checked for presence; the FlowDev view.
+static int flow_view(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s,
+                     const ocsl_flow_iteration* it, FlowDev& f)
+{
+    int rc = check_assembly(c, q, s);
+    if (rc) return rc;
+    if (!it) return fail(c, OCSL_BAD_ARGUMENT, "null iteration arguments");
+    if (q->viscous) return fail(c, OCSL_BAD_ARGUMENT, "the device iteration is for inviscid flows");
+    const bool nf = c->F.nf > 0, nb = c->F.nb > 0;
+    for (int e : {OCSL_EQ_MOMENTUM, OCSL_EQ_PRESSURE, OCSL_EQ_ENTHALPY}) {
+        ocsl_assembly qe = *q;
+        qe.equation = e;
+        if (const char* miss = missing_state_field(qe, *s, nf, nb))
+            return fail(c, OCSL_BAD_ARGUMENT, std::string("state field ") + miss + " is NULL");
+    }
+    struct Need {
+        const void* p;
+        const char* name;
+        bool want;
+    };
+    const Need need[] = {
+        {s->density, "density", nf}, {s->qy, "qy", nf}, {s->bc_area_vector, "bc_area_vector", nb},
+        {s->temperature, "temperature", true}, {s->pressure, "pressure", true},
+        {s->pressure_last, "pressure_last", true},
+        {it->face_area_vector, "face_area_vector", nf}, {it->face_alpha, "face_alpha", nf},
+        {it->face_distance, "face_distance", nf}, {it->face_unit, "face_unit", nf},
+        {it->bc_distance, "bc_distance", nb}, {it->bc_unit, "bc_unit", nb},
+        {it->bc_pressure, "bc_pressure", nb}, {it->pressure_corr_grad, "pressure_corr_grad", true},
+        {it->ap, "ap", true}, {it->ap_vec, "ap_vec", true}, {it->mach, "mach", true},
+        {it->total_mdot, "total_mdot", true}};
+    for (const Need& x : need)
+        if (x.want && !x.p) return fail(c, OCSL_BAD_ARGUMENT, std::string(x.name) + " is NULL");
+    // boundary kinds: walls, symmetry and empty faces only (checked once per array)
+    if (nb && c->flow_bc_checked != s->bc_type) {
+        std::vector<int32_t> kind(c->F.nb);
+        CK(cudaMemcpy(kind.data(), s->bc_type, sizeof(int32_t) * kind.size(),
+                      cudaMemcpyDeviceToHost));
+        for (int32_t k : kind)
+            if (k != OCSL_BC_WALL && k != OCSL_BC_SYMMETRY && k != OCSL_BC_EMPTY)
+                return fail(c, OCSL_BAD_ARGUMENT,
+                            "the device iteration supports wall, symmetry and empty boundaries");
+        c->flow_bc_checked = s->bc_type;
+    }
+    auto w = [](const double* p) { return const_cast<double*>(p); };
+    f.pressure = w(s->pressure);
+    f.velocity = w(s->velocity);
+    f.velocity_last = w(s->velocity_last);
+    f.density_c = w(s->density_c);
+    f.density_last = w(s->density_last);
+    f.pressure_last = w(s->pressure_last);
+    f.temperature = w(s->temperature);
+    f.enthalpy = w(s->enthalpy);
+    f.enthalpy_last = w(s->enthalpy_last);
+    f.pressure_corr = w(s->pressure_corr);
+    f.pressure_grad = w(s->pressure_grad);
+    f.pressure_corr_grad = it->pressure_corr_grad;
+    f.ap = it->ap;
+    f.ap_vec = it->ap_vec;
+    f.mach = it->mach;
+    f.volume = s->volume;
+    f.left = c->F.left;
+    f.right = c->F.right;
+    f.geo_aver = s->geo_aver;
+    f.area_vector = it->face_area_vector;
+    f.alpha = it->face_alpha;
+    f.distance = it->face_distance;
+    f.unit = it->face_unit;
+    f.mdot = w(s->mdot);
+    f.face_density = w(s->density);
+    f.qy = w(s->qy);
+    f.bc_type = s->bc_type;
+    f.bc_left = c->F.bc_left;
+    f.bc_area_vector = s->bc_area_vector;
+    f.bc_unit = it->bc_unit;
+    f.bc_distance = it->bc_distance;
+    f.bc_pressure = it->bc_pressure;
+    f.relax_p = it->relax_p;
+    f.relax_u = it->relax_u;
+    f.cp = it->cp;
+    f.Tref = it->Tref;
+    f.H_formation = it->H_formation;
+    return OCSL_OK;
+}
+
+int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s,
+                             const ocsl_flow_iteration* it, const int* methods,
+                             const ocsl_opts* opts, ocsl_flow_report* report)
+{
+    if (report) std::memset(report, 0, sizeof *report);
+    if (!methods) return c ? fail(c, OCSL_BAD_ARGUMENT, "null methods") : OCSL_BAD_ARGUMENT;
+    for (int e = 0; e < 3; ++e)
+        if (methods[e] < OCSL_CG_REF || methods[e] > OCSL_ILU_BICGSTAB_IR32)
+            return c ? fail(c, OCSL_BAD_ARGUMENT, "unknown method") : OCSL_BAD_ARGUMENT;
+    FlowDev f{};
+    int status = OCSL_OK;
+    ocsl_flow_report rep{};
+    try {
+        int rc = flow_view(c, q, s, it, f);
+        if (rc) return rc;
+        CK(cudaSetDevice(c->device));
+        const int n = c->P.n, nf = c->F.nf, nb = c->F.nb;
+        if (n == 0) {
+            if (report) *report = rep;
+            return OCSL_OK;
+        }
+        if (!c->d_fval) {
+            c->d_fval = dalloc<double>((size_t)c->P.nnz);
+            c->d_fb = dalloc<double>((size_t)n);
+            c->d_fx = dalloc<double>((size_t)n);
+            c->d_ftmp = dalloc<double>((size_t)n);
+            c->d_fres = dalloc<double>(5);
+        }
+        cudaStream_t st = c->stream;
+        Solve sv{c, st, c->P, n};
+        CK(cudaMemsetAsync(c->d_sc + kScFlow, 0, sizeof(Scalars), st));
+        auto residual = [&](const double* v, int slot) {  // sum |v| in tile order
+            sv.vec<double>(V_ABSSUM, {v}, kScFlow, EP_STORE);
+            launch_take_sum(st, c->d_sc + kScFlow, c->d_fres + slot);
+        };
+        auto solve = [&](int slot, int method) {
+            ocsl_result r;
+            const int rc2 = solve_device_impl(c, method, c->d_fval, c->d_fb, c->d_fx, opts, &r);
+            rep.iterations[slot] = r.iterations;
+            rep.status[slot] = rc2;
+            if (rc2 != OCSL_OK && status == OCSL_OK) status = rc2;
+        };
+        ocsl_assembly qe = *q;
+        // boundary conditions and the pressure gradient (cflow_solver.cpp:234-241)
+        launch_flow_bc_pressure(st, n, nb, f);
+        launch_flow_grad(st, false, n, nf, nb, f, c->F);
+        CK(cudaMemsetAsync(f.ap, 0, sizeof(double) * n, st));  // :244-247
+        // momentum components (:257-302)
+        for (int d = 0; d < 3; ++d) {
+            qe.equation = OCSL_EQ_MOMENTUM;
+            qe.dimension = d;
+            launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, f.ap_vec + (size_t)d * n,
+                            it->total_mdot);
+            solve(d, methods[0]);
+            launch_flow_velocity_update(st, n, d, c->d_fx, f, c->d_ftmp);
+            residual(c->d_ftmp, d);
+        }
+        // face mass fluxes (:305-309), pressure correction (:316-358)
+        launch_flow_face_mdot(st, n, nf, f, q->blended);
+        qe.equation = OCSL_EQ_PRESSURE;
+        qe.dimension = 0;
+        launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, it->total_mdot);
+        residual(c->d_fb, 3);  // Pressure_global_residual = ABSsum(b), :346
+        solve(3, methods[1]);
+        launch_flow_pcorr(st, n, c->d_fx, f);
+        // corrections (:375-426)
+        launch_flow_grad(st, true, n, nf, nb, f, c->F);
+        launch_flow_correct(st, n, nf, f, q->blended, q->R_specific, q->gamma);
+        // enthalpy (:428-474)
+        qe.equation = OCSL_EQ_ENTHALPY;
+        launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, nullptr);
+        solve(4, methods[2]);
+        launch_flow_enthalpy_update(st, n, c->d_fx, f, c->d_ftmp, q->R_specific, q->gamma);
+        residual(c->d_ftmp, 4);
+        CK(cudaMemcpyAsync(c->h_sc + kHostStage, c->d_fres, 5 * sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::memcpy(rep.residual, c->h_sc + kHostStage, 5 * sizeof(double));
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        status = from_cuda(c, e);
+    }
+    if (report) *report = rep;
+    return status;
+}
+
+int ocsl_flow_end_step_device(ocsl_ctx* c, const ocsl_flow_state* s)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!s || !s->velocity || !s->velocity_last || !s->density_c || !s->density_last ||
+        !s->pressure || !s->pressure_last || !s->enthalpy || !s->enthalpy_last)
+        return fail(c, OCSL_BAD_ARGUMENT, "null state field");
+    try {
+        CK(cudaSetDevice(c->device));
+        FlowDev f{};
+        auto w = [](const double* p) { return const_cast<double*>(p); };
+        f.velocity = w(s->velocity);
+        f.velocity_last = w(s->velocity_last);
+        f.density_c = w(s->density_c);
+        f.density_last = w(s->density_last);
+        f.pressure = w(s->pressure);
+        f.pressure_last = w(s->pressure_last);
+        f.enthalpy = w(s->enthalpy);
+        f.enthalpy_last = w(s->enthalpy_last);
+        launch_flow_end_step(c->stream, c->P.n, f);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(c->stream));
     } catch (const CudaError& e) {

@@ -107,6 +107,39 @@ void orc_bc_value_grad(size_t n, const uint64_t* rp, int64_t nb, const int32_t* 
                        const ocsl_assembly* q, const ocsl_flow_state* st, const double* lambda,
                        double* grad);
 
+/* The SIMPLE inner iteration around the assembly and the solves
+ * (ocsl_oracle_flow.c): `st` and `it` hold HOST pointers and are updated in
+ * place as ocsl_flow_iterate_device updates its device arrays.  methods[3]
+ * as there (OCSL_CG_REF, OCSL_BICGSTAB_REF, and with opts OCSL_PCG and
+ * OCSL_ILU_BICGSTAB, whose tol, maxit, ilu_sweeps are read); given_x (may be NULL)
+ * replaces solve e's result by given_x[e]; sys_* (may be NULL) receive the
+ * five assembled systems (5 x nnz, 5 x n) before each solve.  Returns 0, or -1
+ * for an unsupported method. */
+void orc_flow_bc_pressure(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
+                          const ocsl_flow_iteration* it);
+void orc_flow_grad(int corr, size_t n, int64_t nf, const int32_t* left, const int32_t* right,
+                   int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
+                   const ocsl_flow_iteration* it);
+void orc_flow_velocity_update(size_t n, int d, const double* x, const ocsl_flow_state* st,
+                              const ocsl_flow_iteration* it, double* res);
+void orc_flow_face_mdot(size_t n, int64_t nf, const int32_t* left, const int32_t* right,
+                        int blended, const ocsl_flow_state* st, const ocsl_flow_iteration* it);
+void orc_flow_pcorr(size_t n, const double* x, const ocsl_flow_state* st,
+                    const ocsl_flow_iteration* it);
+void orc_flow_correct(size_t n, int64_t nf, const int32_t* left, const int32_t* right,
+                      const ocsl_assembly* q, const ocsl_flow_state* st,
+                      const ocsl_flow_iteration* it);
+void orc_flow_enthalpy_update(size_t n, const double* x, const ocsl_assembly* q,
+                              const ocsl_flow_state* st, const ocsl_flow_iteration* it,
+                              double* res);
+void orc_flow_end_step(size_t n, const ocsl_flow_state* st);
+int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
+                     const int32_t* left, const int32_t* right, int64_t nb,
+                     const int32_t* bc_left, const ocsl_assembly* q, const ocsl_flow_state* st,
+                     const ocsl_flow_iteration* it, const int* methods, const ocsl_opts* opts,
+                     const double* const* given_x, double* sys_value, double* sys_b,
+                     double* sys_x0, double* residual, int* iterations);
+
 /* Exact relative residual ||b - A x||_2 / ||b||_2 in long double. */
 double orc_true_relres(size_t n, const uint64_t* rp, const uint64_t* col, const double* val,
                        const double* b, const double* x);

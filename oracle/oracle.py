@@ -90,6 +90,9 @@ _ORACLE_PROTOS = {
     "orc_assemble": (None, _CSR + [C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, _P, _P, _P,
                                    _P]),
     "orc_bc_value_grad": (None, [_SZ, _P, C.c_int64, _P, _P, _P, _P, _P]),
+    "orc_flow_iterate": (C.c_int, _CSR + [C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, _P, _P,
+                                          _P, _P, _P, _P, _P, _P]),
+    "orc_flow_end_step": (None, [_SZ, _P]),
 }
 _REF_CSR = [_SZ, _SZ, _P, _P]
 _REF_PROTOS = {
@@ -301,6 +304,69 @@ def bc_value_grad(rp, bc_left, eq: dict, state: dict, lam):
                           C.addressof(st), _ptr(lam), _ptr(g))
     del keep
     return g
+
+
+def _flow_structs(case: dict):
+    """The ocsl_flow_state / ocsl_flow_iteration of a flow case (dict with
+    "state", "arrays", "constants"; arrays updated in place)."""
+    from opencslsolver_gb300 import _abi
+
+    for group in ("state", "arrays"):
+        for k, v in case[group].items():
+            dt = np.int32 if k in _abi.INT_FIELDS else np.float64
+            if not (isinstance(v, np.ndarray) and v.dtype == dt and v.flags.c_contiguous):
+                raise ValueError(f"{group}[{k}] must be a C-contiguous {np.dtype(dt)} array")
+    st = _abi.flow_state(case["state"], lambda a: a.ctypes.data)
+    it = _abi.flow_iteration(case["arrays"], case["constants"], lambda a: a.ctypes.data)
+    return st, it
+
+
+def flow_iterate(case: dict, methods, given_x=None, capture=False, tol=1e-10, maxit=5000,
+                 ilu_sweeps=3):
+    """One SIMPLE inner iteration of the oracle (ocsl_oracle_flow.c) on
+    ``case`` (mesh, eq, state, arrays, constants), in place.  given_x: five
+    solutions used instead of solving; tol / maxit / ilu_sweeps: the
+    tolerance-mode methods' settings (the library's defaults).  Returns
+    residuals[5], iterations[5] and, with capture, the five assembled systems
+    (value, b, x0)."""
+    from opencslsolver_gb300 import _abi
+    lib = Oracle()._l
+    rp = np.ascontiguousarray(case["row_ptr"], np.uint64)
+    col = np.ascontiguousarray(case["column_index"], np.uint64)
+    left = np.ascontiguousarray(case["left"], np.int32)
+    right = np.ascontiguousarray(case["right"], np.int32)
+    bc_left = np.ascontiguousarray(case["bc_left"], np.int32)
+    n = rp.size - 1
+    q = _assembly_struct(case["eq"])
+    st, it = _flow_structs(case)
+    m = (C.c_int * 3)(*[int(v) for v in methods])
+    gx = None
+    if given_x is not None:
+        given = [np.ascontiguousarray(x, np.float64) for x in given_x]
+        gx = (_P * 5)(*[_ptr(x) for x in given])
+    sv = sb = sx = None
+    if capture:
+        sv, sb, sx = np.zeros((5, col.size)), np.zeros((5, n)), np.zeros((5, n))
+    o = _abi.Opts()
+    o.tol, o.maxit, o.ilu_sweeps = float(tol), int(maxit), int(ilu_sweeps)
+    res, its = np.zeros(5), np.zeros(5, np.int32)
+    rc = lib.orc_flow_iterate(n, _ptr(rp), _ptr(col), left.size, _ptr(left), _ptr(right),
+                              bc_left.size, _ptr(bc_left), C.addressof(q), C.addressof(st),
+                              C.addressof(it), m, C.addressof(o), gx, _ptr(sv), _ptr(sb),
+                              _ptr(sx), _ptr(res), _ptr(its))
+    if rc:
+        raise ValueError("the oracle iteration supports CG_REF, BICGSTAB_REF, PCG and "
+                         "ILU_BICGSTAB")
+    out = {"residual": res, "iterations": its}
+    if capture:
+        out.update(value=sv, b=sb, x0=sx)
+    return out
+
+
+def flow_end_step(case: dict) -> None:
+    lib = Oracle()._l
+    st, _ = _flow_structs(case)
+    lib.orc_flow_end_step(np.asarray(case["row_ptr"]).size - 1, C.addressof(st))
 
 
 def reference_available() -> bool:

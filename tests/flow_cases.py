@@ -1,0 +1,151 @@
+"""Flow cases for the SIMPLE-iteration tests: the reference's recorded shock
+tube states (tests/golden/flow_shocktube.npz, written by
+tests/golden/make_golden.py from oracle/ref_flow.cpp's dumps) turned into the
+library's ocsl_flow_state / ocsl_flow_iteration layout."""
+import os
+
+import numpy as np
+
+from opencslsolver_gb300 import _abi
+
+# ocsl_flow_state field <- recorded name
+STATE_FROM = {
+    "geo_aver": "face_geo_aver", "ksi_A": "face_ksi_A", "mdot": "face_mdot",
+    "density": "face_density", "qy": "face_qy", "stress": "face_stress",
+    "bc_type": "bc_type", "bc_wall": "bc_wall", "bc_supersonic": "bc_supersonic",
+    "bc_area": "bc_area", "bc_area_vector": "bc_area_vector", "bc_perp_dist": "bc_perp_dist",
+    "bc_ksi_A": "bc_ksi_A", "bc_mdot": "bc_mdot", "bc_density": "bc_density", "bc_qy": "bc_qy",
+    "bc_temperature": "bc_temperature", "bc_enthalpy": "bc_enthalpy",
+    "bc_velocity": "bc_velocity", "volume": "cell_volume", "delta_t": "cell_delta_t",
+    "velocity": "cell_velocity", "velocity_last": "cell_velocity_last",
+    "pressure_grad": "cell_pressure_grad", "density_c": "cell_density",
+    "density_last": "cell_density_last", "pressure": "cell_pressure",
+    "pressure_last": "cell_pressure_last", "pressure_corr": "cell_pressure_corr",
+    "temperature": "cell_temperature", "enthalpy": "cell_enthalpy",
+    "enthalpy_last": "cell_enthalpy_last", "bc_thermal": "bc_thermal",
+}
+# ocsl_flow_iteration array <- recorded name
+ARRAYS_FROM = {
+    "face_area_vector": "face_area_vector", "face_alpha": "face_alpha",
+    "face_distance": "face_distance", "face_unit": "face_unit", "bc_distance": "bc_distance",
+    "bc_unit": "bc_unit", "bc_pressure": "bc_pressure",
+    "pressure_corr_grad": "cell_pressure_corr_grad", "ap": "cell_ap", "ap_vec": "cell_ap_vec",
+    "mach": "cell_mach", "total_mdot": "cell_total_mdot",
+}
+# geometry: taken from the setup record, never changed by the iteration
+SETUP_ONLY = {"geo_aver", "ksi_A", "bc_area", "bc_area_vector", "bc_perp_dist", "bc_ksi_A",
+              "volume", "face_area_vector", "face_alpha", "face_distance", "face_unit",
+              "bc_distance", "bc_unit"}
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "flow_shocktube.npz")
+# recorded inner iterations (step_iteration) of the fixture
+ITERATIONS = ("0_0", "0_1", "57_2")
+STEPS, INNER = 200, 5
+
+# the fields one inner iteration writes (compared after it)
+WRITTEN_STATE = ("velocity", "density_c", "pressure", "pressure_grad", "pressure_corr",
+                 "temperature", "enthalpy", "mdot", "density", "qy")
+WRITTEN_ARRAYS = ("bc_pressure", "pressure_corr_grad", "ap", "ap_vec", "mach", "total_mdot")
+
+
+def make_case(setup: dict, rec: dict) -> dict:
+    """A flow case: the mesh and constants of ``setup`` with the state of
+    ``rec`` (a state record), every array a fresh contiguous copy."""
+    fl = setup["fluid"]
+    state, arrays = {}, {}
+    for k, name in STATE_FROM.items():
+        src = setup if k in SETUP_ONLY else rec
+        dt = np.int32 if k in _abi.INT_FIELDS else np.float64
+        state[k] = np.ascontiguousarray(src[name], dt).copy()
+    for k, name in ARRAYS_FROM.items():
+        src = setup if k in SETUP_ONLY else rec
+        arrays[k] = np.ascontiguousarray(src[name], np.float64).copy()
+    return {
+        "row_ptr": setup["row_ptr"], "column_index": setup["column_index"],
+        "left": setup["face_left"], "right": setup["face_right"], "bc_left": setup["bc_left"],
+        "eq": {"viscous": 0, "blended": 1, "transient": 1, "R_specific": fl[0], "gamma": fl[1],
+               "sutherland": (fl[2], fl[3]), "prandtl": fl[4],
+               "implicit_underrelaxation": fl[5]},
+        "constants": {"cp": fl[6], "Tref": fl[7], "H_formation": fl[8], "relax_p": fl[9],
+                      "relax_u": fl[10]},
+        "state": state, "arrays": arrays,
+    }
+
+
+def written(case: dict) -> dict:
+    """The fields one inner iteration writes, by name."""
+    out = {k: case["state"][k] for k in WRITTEN_STATE}
+    out.update({k: case["arrays"][k] for k in WRITTEN_ARRAYS})
+    return out
+
+
+def recorded(setup: dict, rec: dict) -> dict:
+    """The same fields from a state record."""
+    c = make_case(setup, rec)
+    return written(c)
+
+
+class Golden:
+    """tests/golden/flow_shocktube.npz, by record."""
+
+    def __init__(self, path: str = GOLDEN):
+        z = np.load(path)
+        self._z = {k: z[k] for k in z.files}
+
+    def record(self, prefix: str) -> dict:
+        p = prefix + "__"
+        return {k[len(p):]: v for k, v in self._z.items() if k.startswith(p)}
+
+    @property
+    def setup(self) -> dict:
+        return self.record("setup")
+
+    def start(self, tag: str) -> dict:
+        return self.setup if tag == "0_0" else self.record(f"start_{tag}")
+
+    def systems(self, tag: str) -> dict:
+        return {k: self._z[f"{k}_{tag}"] for k in ("value", "b", "x0", "x")}
+
+    def case(self, record: dict | None = None) -> dict:
+        return make_case(self.setup, self.setup if record is None else record)
+
+
+def relerr(got, want) -> float:
+    scale = float(np.max(np.abs(want))) if np.size(want) else 0.0
+    return float(np.max(np.abs(np.asarray(got) - np.asarray(want)))) / (scale or 1.0)
+
+
+def field_errors(got: dict, want: dict) -> dict:
+    """Max |got - want| / max |want| per field."""
+    return {k: relerr(got[k], want[k]) for k in want}
+
+
+class DeviceCase:
+    """A flow case's arrays as CUDA tensors, for Context.flow_iterate_device."""
+
+    def __init__(self, torch, case: dict):
+        self.torch = torch
+        self.case = case
+
+        def dev(k, v):
+            dt = torch.int32 if k in _abi.INT_FIELDS else torch.float64
+            return torch.from_numpy(np.ascontiguousarray(v)).to(device="cuda", dtype=dt)
+
+        self.state = {k: dev(k, v) for k, v in case["state"].items()}
+        self.arrays = {k: dev(k, v) for k, v in case["arrays"].items()}
+
+    def bind(self, ctx) -> None:
+        c = self.case
+        ctx.set_pattern(c["row_ptr"], c["column_index"])
+        ctx.set_faces(c["left"], c["right"], c["bc_left"])
+
+    def iterate(self, ctx, methods, **opts) -> dict:
+        return ctx.flow_iterate_device(self.case["eq"], self.state, self.arrays,
+                                       self.case["constants"], methods, **opts)
+
+    def end_step(self, ctx) -> None:
+        ctx.flow_end_step_device(self.state)
+
+    def written(self) -> dict:
+        out = {k: self.state[k].cpu().numpy() for k in WRITTEN_STATE}
+        out.update({k: self.arrays[k].cpu().numpy() for k in WRITTEN_ARRAYS})
+        return out

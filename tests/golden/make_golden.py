@@ -22,6 +22,17 @@ then writes:
 * small_systems.npz -- seeded small systems in the reference layout with the
   reference's gemv, ILU_decompose, ILU_forsub/backsub, CG_solve and
   ILU_BICGSTAB_solve outputs;
+* flow_shocktube.npz -- the reference's SIMPLE loop on the same shock tube,
+  recorded by oracle/ref_flow.cpp one inner iteration at a time: the setup
+  (mesh metrics, fluid constants, initial state; keys setup__*), for the inner
+  iterations 0:0, 0:1 and 57:2 (step:iteration) of the run with every
+  equation through ILU_BICGSTAB_solve the state before the iteration
+  (start_<tag>__*, 0:0 starts from the setup), the five assembled systems and
+  the reference's solutions (value_<tag>, b_<tag>, x0_<tag>, x_<tag>) and the
+  state after it (post_<tag>__*), and the final state after 200 steps x 5
+  inner iterations with every equation through ILU_BICGSTAB_solve
+  (final_bicg__*) and with the momentum equations through CG_solve
+  (final_cg__*);
 * assembly_<case>.npz -- the inputs (cell / face state) and outputs (matrix
   values, b, x0, ap_vec, total_mdot) of the reference's face-loop assembly,
   recorded by oracle/ref_assembly.cpp right before the 5 solve calls of one
@@ -192,17 +203,57 @@ def make_assembly(out_dir):
         np.savez_compressed(os.path.join(out_dir, f"assembly_{case}.npz"), **arrays)
 
 
+# (start record, recorded iteration) of the flow fixture; "setup" = initial state
+FLOW_ITERATIONS = [("setup", "0_0"), ("post_0_0", "0_1"), ("post_57_1", "57_2")]
+
+
+def make_flow(path):
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_flow")
+    arrays = {}
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([exe, d, "bicg", "200", "5", "0:0", "0:1", "57:1", "57:2"], cwd=d,
+                       check=True, stdout=subprocess.DEVNULL)
+        rec = lambda name: read_named_arrays(os.path.join(d, name + ".bin"))  # noqa: E731
+        for k, v in rec("setup").items():
+            arrays[f"setup__{k}"] = v
+        for start, tag in FLOW_ITERATIONS:
+            if start != "setup":
+                for k, v in rec(start).items():
+                    arrays[f"start_{tag}__{k}"] = v
+            for k, v in rec(f"post_{tag}").items():
+                arrays[f"post_{tag}__{k}"] = v
+            pre = [rec(f"pre_{tag}_{e}") for e in range(5)]
+            for key in ("value", "b", "x0", "x"):
+                arrays[f"{key}_{tag}"] = np.stack([p[key] for p in pre])
+        for k, v in rec("final").items():
+            arrays[f"final_bicg__{k}"] = v
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([exe, d, "cg", "200", "5"], cwd=d, check=True, stdout=subprocess.DEVNULL)
+        for k, v in read_named_arrays(os.path.join(d, "final.bin")).items():
+            arrays[f"final_cg__{k}"] = v
+    np.savez_compressed(path, **arrays)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=orc.REF_DIR)
+    ap.add_argument("--only", choices=["kat", "shocktube", "small", "assembly", "flow"],
+                    help="write one fixture (default: all)")
     a = ap.parse_args()
     orc.build(a.reference)
     ref = orc.Reference()
     ref.set_threads(1)
-    make_kat(ref, os.path.join(HERE, "kat_tridiag10.npz"))
-    make_shocktube(os.path.join(HERE, "shocktube_calls.npz"))
-    make_small(ref, os.path.join(HERE, "small_systems.npz"))
-    make_assembly(HERE)
+    want = lambda name: a.only in (None, name)  # noqa: E731
+    if want("kat"):
+        make_kat(ref, os.path.join(HERE, "kat_tridiag10.npz"))
+    if want("shocktube"):
+        make_shocktube(os.path.join(HERE, "shocktube_calls.npz"))
+    if want("small"):
+        make_small(ref, os.path.join(HERE, "small_systems.npz"))
+    if want("assembly"):
+        make_assembly(HERE)
+    if want("flow"):
+        make_flow(os.path.join(HERE, "flow_shocktube.npz"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -1,0 +1,116 @@
+"""The SIMPLE inner iteration on the device (ocsl_flow_iterate_device) on the
+1000-cell shock tube recorded from the reference (tests/golden/flow_shocktube.npz).
+
+* Bit-exact to the oracle restatement, inner iteration by inner iteration
+  (every field the iteration writes, the residual sums and the solves'
+  iteration counts), with the reference's own solvers (momentum CG_solve or
+  ILU_BICGSTAB_solve; p' and enthalpy ILU_BICGSTAB_solve) and with the
+  tolerance-mode ILU-BiCGSTAB.
+* 200 time steps x 5 inner iterations against the reference's final fields:
+  within 1e-9 relative (measured: a few 1e-13, the residue of the
+  reference's -ffast-math build and its serial dot products), for both of
+  the reference's solver choices; with every equation solved by the
+  tolerance-mode ILU-BiCGSTAB to 1e-10, within 1e-9 of the reference run that
+  uses ILU_BICGSTAB_solve everywhere.
+* Unsupported input is refused before anything is written.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import opencslsolver_gb300 as ocsl
+from opencslsolver_gb300 import _abi
+from oracle import oracle as orc
+
+import flow_cases as FC
+
+pytestmark = pytest.mark.gpu
+
+METHODS = {
+    "bicg": (ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF),
+    "cg": (ocsl.CG_REF, ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF),
+    "tol": (ocsl.ILU_BICGSTAB, ocsl.ILU_BICGSTAB, ocsl.ILU_BICGSTAB),
+}
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return FC.Golden()
+
+
+def _same(got: dict, want: dict, where):
+    for k in want:
+        assert np.array_equal(got[k], want[k]), (where, k, FC.relerr(got[k], want[k]))
+
+
+@pytest.mark.parametrize("mode", ["bicg", "cg", "tol"])
+def test_iteration_bit_exact_vs_oracle(ctx, torch_cuda, golden, mode):
+    case = golden.case()
+    dev = FC.DeviceCase(torch_cuda, golden.case())
+    dev.bind(ctx)
+    for step in range(2):
+        for inner in range(FC.INNER):
+            rep = dev.iterate(ctx, METHODS[mode])
+            want = orc.flow_iterate(case, METHODS[mode])
+            _same(dev.written(), FC.written(case), (mode, step, inner))
+            assert rep["residual"] == list(want["residual"]), (mode, step, inner, rep)
+            assert rep["iterations"] == list(want["iterations"]), (mode, step, inner, rep)
+            assert rep["status"] == [0] * 5
+        dev.end_step(ctx)
+        orc.flow_end_step(case)
+    for k in ("velocity_last", "density_last", "pressure_last", "enthalpy_last"):
+        assert np.array_equal(dev.state[k].cpu().numpy(), case["state"][k]), k
+
+
+@pytest.mark.parametrize("mode", ["bicg", "cg", "tol"])
+def test_shocktube_200_steps_vs_reference(ctx, torch_cuda, golden, mode):
+    dev = FC.DeviceCase(torch_cuda, golden.case())
+    dev.bind(ctx)
+    torch_cuda.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(FC.STEPS):
+        for _ in range(FC.INNER):
+            rep = dev.iterate(ctx, METHODS[mode])
+            assert rep["status"] == [0] * 5, rep
+        dev.end_step(ctx)
+    torch_cuda.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / (FC.STEPS * FC.INNER)
+    ref = "final_bicg" if mode in ("bicg", "tol") else "final_cg"
+    errs = FC.field_errors(dev.written(), FC.recorded(golden.setup, golden.record(ref)))
+    print(f"{mode}: {ms:.3f} ms per inner iteration; max field error vs {ref}: "
+          f"{max(errs.values()):.2e} ({max(errs, key=errs.get)})")
+    assert max(errs.values()) <= 1e-9, errs
+    if mode != "tol":
+        assert max(errs.values()) <= 1e-11, errs
+
+
+def test_rejects_unsupported_input(ctx, torch_cuda, golden):
+    dev = FC.DeviceCase(torch_cuda, golden.case())
+    dev.bind(ctx)
+    before = {k: v.clone() for k, v in dev.state.items()}
+    kinds = dev.state["bc_type"].clone()
+    kinds[3] = _abi.BC_VELOCITY_INLET
+    dev.state["bc_type"] = kinds
+    with pytest.raises(ocsl.OcslError) as e:
+        dev.iterate(ctx, METHODS["bicg"])
+    assert e.value.status == _abi.BAD_ARGUMENT
+    dev.state["bc_type"] = before["bc_type"]
+    eq = dict(dev.case["eq"], viscous=1)
+    with pytest.raises(ocsl.OcslError) as e:
+        ctx.flow_iterate_device(eq, dev.state, dev.arrays, dev.case["constants"],
+                                METHODS["bicg"])
+    assert e.value.status == _abi.BAD_ARGUMENT
+    arrays = dict(dev.arrays)
+    del arrays["face_alpha"]
+    with pytest.raises(ocsl.OcslError) as e:
+        ctx.flow_iterate_device(dev.case["eq"], dev.state, arrays, dev.case["constants"],
+                                METHODS["bicg"])
+    assert e.value.status == _abi.BAD_ARGUMENT
+    for k, v in before.items():
+        assert torch_cuda.equal(dev.state[k], v), k
+    # the context still iterates exactly like the oracle
+    case = golden.case()
+    dev.iterate(ctx, METHODS["bicg"])
+    orc.flow_iterate(case, METHODS["bicg"])
+    _same(dev.written(), FC.written(case), "after refusals")
