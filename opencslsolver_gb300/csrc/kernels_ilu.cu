@@ -190,6 +190,120 @@ __global__ void __launch_bounds__(kThreads) bw_sweep_kernel(SweepParams<T> p)
     sweep_epilogue(p.S);
 }
 
+// Tiny systems with a deep schedule (the 1D shock tube's chain: one row per
+// level): a single warp walks the rows in natural order (reverse order for
+// the backward sweep), a topological order of either triangle, so there is
+// nothing to wait for.  Rows are taken 32 at a time: lane k loads row k's
+// triangle entries (up to kSerialK of them), right-hand side, divisor and
+// the divisor's reciprocal into shared memory in one parallel round trip;
+// then lane 0 alone runs the rows' chain (the other lanes would only repeat
+// its FP64 work), with the solution in shared memory and the last row's
+// value in a register (a chain row depends on the row before it).  Sums run
+// over the entries in storage order with fma from 0, and a result with the
+// all-ones pattern is stored as the canonical NaN, as in the level-scheduled
+// kernels: the results are the same bits.
+constexpr int kSerialK = 4;
+
+// a / b, correctly rounded, from y = RN(1/b) by Markstein's method (P.
+// Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): q = RN(a y) is within 1.5 ulp;
+// one residual correction q + (a - b q) y brings it within an ulp, and a
+// second one is, by Markstein's theorem (y within half an ulp of 1/b, q within
+// an ulp of a/b), the correctly rounded quotient.  The residuals a - b q are
+// exact fmas.  Operands outside [2^-500, 2^500] in magnitude (zeros,
+// subnormals, infinities, NaN, values near over- or underflow) take the IEEE
+// division.  Five dependent operations instead of a full division on the
+// serial chain.
+__device__ __forceinline__ bool markstein_range(double v)
+{
+    const int e = (__double2hiint(v) >> 20) & 0x7ff;  // biased exponent
+    return e >= 1023 - 500 && e <= 1023 + 500;
+}
+
+__device__ __forceinline__ double div_rcp(double a, double b, double y, bool b_ok)
+{
+    if (!b_ok || !markstein_range(a)) return a / b;
+    double q = a * y;
+    double r = fma(-b, q, a);
+    q = fma(r, y, q);
+    r = fma(-b, q, a);
+    return fma(r, y, q);
+}
+
+__device__ __forceinline__ float div_rcp(float a, float b, float, bool) { return a / b; }
+
+template <typename T, bool FW, bool DIV>
+__global__ void __launch_bounds__(32) serial_sweep_kernel(SweepParams<T> p)
+{
+    if (p.done && *p.done) return;
+    extern __shared__ __align__(16) unsigned char serial_smem[];
+    T* xs = reinterpret_cast<T*>(serial_smem);
+    __shared__ int s_row[32], s_q0[32], s_q1[32], s_ok[32];
+    __shared__ int s_col[kSerialK][32];
+    __shared__ T s_rhs[32], s_div[32], s_rcp[32];
+    __shared__ T s_m[kSerialK][32];
+    using B = Bits<T>;
+    const int lane = (int)threadIdx.x;
+    const int n = p.n;
+    int last_i = -1;
+    T last = T(0);
+    for (int base = 0; base < n; base += 32) {
+        const int r = base + lane;
+        if (r < n) {
+            const int i = FW ? r : n - 1 - r;
+            const int d = __ldg(p.diag + i);
+            const int q0 = FW ? __ldg(p.rp + i) : d + 1;
+            const int q1 = FW ? d : __ldg(p.rp + i + 1);
+            s_row[lane] = i;
+            s_q0[lane] = q0;
+            s_q1[lane] = q1;
+            s_rhs[lane] = p.rhs[i];
+            if (!FW) {
+                const T dv = DIV ? __ldg(p.M + d) : __ldg(p.dinv + i);
+                s_div[lane] = dv;
+                if (DIV) {
+                    s_rcp[lane] = T(1) / dv;
+                    if constexpr (sizeof(T) == 8) s_ok[lane] = markstein_range(dv) ? 1 : 0;
+                    else s_ok[lane] = 0;
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < kSerialK; ++t) {
+                const bool in = q0 + t < q1;
+                s_col[t][lane] = in ? __ldg(p.col + q0 + t) : -1;
+                s_m[t][lane] = in ? __ldg(p.M + q0 + t) : T(0);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const int cnt = min(32, n - base);
+            for (int k = 0; k < cnt; ++k) {
+                const int ik = s_row[k];
+                T sum = T(0);
+#pragma unroll
+                for (int t = 0; t < kSerialK; ++t) {
+                    const int j = s_col[t][k];
+                    if (j >= 0) sum = fma_t(s_m[t][k], j == last_i ? last : xs[j], sum);
+                }
+                for (int q = s_q0[k] + kSerialK; q < s_q1[k]; ++q) {  // rows with more entries
+                    const int j = __ldg(p.col + q);
+                    if (j < 0) continue;  // phantom: the reference adds 0 * x[-1]
+                    sum = fma_t(__ldg(p.M + q), j == last_i ? last : xs[j], sum);
+                }
+                const T num = s_rhs[k] - sum;
+                T v = num;
+                if (!FW) v = DIV ? div_rcp(num, s_div[k], s_rcp[k], s_ok[k] != 0) : num * s_div[k];
+                if (B::to(v) == B::kSentinel) v = B::from(B::kCanonicalNaN);
+                xs[ik] = v;
+                p.out[ik] = v;
+                last_i = ik;
+                last = v;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 struct IluParams {
     int n;
     const int* rp;
@@ -360,6 +474,22 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 }
 
 template <typename T>
+void launch_serial_sweep(cudaStream_t st, const DevPattern& P, bool forward, const T* M,
+                         const T* dinv, const T* rhs, T* out, int divmode, const int* done)
+{
+    if (P.n == 0) return;
+    SweepSync none{};
+    auto p = make_sweep<T>(P, forward, M, dinv, rhs, out, none, done);
+    const size_t smem = sizeof(T) * (size_t)P.n;
+    if (forward)
+        serial_sweep_kernel<T, true, true><<<1, 32, smem, st>>>(p);
+    else if (divmode == 0)
+        serial_sweep_kernel<T, false, true><<<1, 32, smem, st>>>(p);
+    else
+        serial_sweep_kernel<T, false, false><<<1, 32, smem, st>>>(p);
+}
+
+template <typename T>
 void launch_ilu_sweep(cudaStream_t st, const DevPattern& P, const T* A, const T* Mold, T* Mnew,
                       double* dinv, float* M32, float* dinv32, float* A32, const int* done,
                       int* pivot_err)
@@ -421,6 +551,11 @@ template void launch_bw_sweep<double>(cudaStream_t, const DevPattern&, const dou
                                       const SweepSync&, const int*);
 template void launch_bw_sweep<float>(cudaStream_t, const DevPattern&, const float*, const float*,
                                      const float*, float*, int, const SweepSync&, const int*);
+template void launch_serial_sweep<double>(cudaStream_t, const DevPattern&, bool, const double*,
+                                          const double*, const double*, double*, int,
+                                          const int*);
+template void launch_serial_sweep<float>(cudaStream_t, const DevPattern&, bool, const float*,
+                                         const float*, const float*, float*, int, const int*);
 template void launch_ilu_sweep<double>(cudaStream_t, const DevPattern&, const double*,
                                        const double*, double*, double*, float*, float*, float*,
                                        const int*, int*);

@@ -207,6 +207,14 @@ void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 template <typename T>
 void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
                      const T* rhs, T* out, int divmode, const SweepSync& S, const int* done);
+// One-warp sweep in natural (forward) or reverse (backward) row order for
+// tiny systems with a deep schedule; the solution is staged in n * sizeof(T)
+// bytes of shared memory (at most kSerialMaxBytes, which leaves the kernel's
+// row staging room under the 48 KB a launch may take without opting in).
+constexpr int kSerialMaxBytes = 40 * 1024;
+template <typename T>
+void launch_serial_sweep(cudaStream_t st, const DevPattern& P, bool forward, const T* M,
+                         const T* dinv, const T* rhs, T* out, int divmode, const int* done);
 
 void launch_convert_f64_f32(cudaStream_t st, int n, const double* in, float* out);
 

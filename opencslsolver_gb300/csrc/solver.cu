@@ -200,6 +200,9 @@ struct ocsl_ctx {
     bool fac_checked = false;  // fac_status holds the pivot check of fac_M
     int fac_status = OCSL_OK;
 
+    // the pattern qualifies for the one-warp serial sweep ([0] FP64, [1] FP32)
+    bool serial_ok[2] = {false, false};
+
     // SIMPLE iteration on the device (ocsl_flow_iterate_device): the system
     // of the equation being solved, a residual work vector, the five residual
     // sums, and the boundary-kind check of the last state seen
@@ -616,6 +619,13 @@ struct Solve {
     template <typename TT>
     void fw(const TT* M, const TT* rhs, TT* out, int k, bool prefilled = false)
     {
+        if (use_serial<TT>()) {
+            ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
+            for (int q = 0; q < cols.n; ++q)
+                launch_serial_sweep<TT>(st, P, true, M, nullptr, rhs + q * cols.ld,
+                                        out + q * cols.ld, 0, k >= 0 ? done(k + q) : nullptr);
+            return;
+        }
         const bool wave = use_box() && soa<TT>() && use_wave<TT>();
         if (!prefilled && !wave) {  // the warp-pipelined sweep keeps its faces apart
             ProfScope ps(c, st, PC_FILL);
@@ -647,6 +657,13 @@ struct Solve {
         return g;
     }
     bool use_box() const { return P.box_ok && c->sweep_kernel != 1; }
+    // the one-warp serial sweep (automatic mode, tiny deep patterns; a
+    // pending fault injection exercises the waits of the other kernels)
+    template <typename TT>
+    bool use_serial() const
+    {
+        return c->sweep_kernel == 0 && c->serial_ok[is_f64<TT>() ? 0 : 1] && !c->fault_skip_pending;
+    }
     // the warp-pipelined kernel serves one right-hand side at a time; kind 2
     // forces the CTA kernel, kind 3 the warp-pipelined one
     template <typename TT>
@@ -692,6 +709,8 @@ struct Solve {
         soa64 = nullptr;
         soa32 = nullptr;
         if (!use_box()) return;
+        if (use_serial<double>()) want64 = false;  // the serial sweep reads the CSR factor
+        if (use_serial<float>()) want32 = false;
         ProfScope ps(c, st, PC_ILU);
         if (want64) {
             launch_box_to_soa<double>(st, c->hp.box.dim, P.n, P.rp, M, c->d_soa64, recip64 ? 1 : 0);
@@ -756,6 +775,13 @@ struct Solve {
     void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k,
             bool prefilled = false)
     {
+        if (use_serial<TT>()) {
+            ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
+            for (int q = 0; q < cols.n; ++q)
+                launch_serial_sweep<TT>(st, P, false, M, dinv, rhs + q * cols.ld,
+                                        out + q * cols.ld, divmode, k >= 0 ? done(k + q) : nullptr);
+            return;
+        }
         const bool wave = use_box() && soa<TT>() && use_wave<TT>();
         if (!prefilled && !wave) {
             ProfScope ps(c, st, PC_FILL);
@@ -1527,6 +1553,12 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         P.box_ok = hp.box.ok && c->sweep_kernel != 1;
         c->hp.box = hp.box;
         c->rebuild_box_geoms();
+        // the one-warp sweep: the solution fits its shared memory and the
+        // schedule is at least a quarter as deep as the system is long
+        for (int k = 0; k < 2; ++k)
+            c->serial_ok[k] = (size_t)hp.n * (k ? sizeof(float) : sizeof(double)) <=
+                                  (size_t)kSerialMaxBytes &&
+                              4LL * P.fw_nchunks >= hp.n && 4LL * P.bw_nchunks >= hp.n;
         const size_t nn = (size_t)hp.n, nz = (size_t)hp.nnz;
         c->d_A = dalloc<double>(nz);
         c->d_b = dalloc<double>(nn);
@@ -2100,7 +2132,8 @@ int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
     if (!c) return OCSL_BAD_ARGUMENT;
     if (!c->has_pattern) return OCSL_NO_PATTERN;
     if (kind)
-        *kind = !c->P.box_ok ? 1
+        *kind = c->sweep_kernel == 0 && c->serial_ok[0] ? 4
+                : !c->P.box_ok ? 1
                 : (c->sweep_kernel != 2 && c->wave_fits[0] &&
                    (c->sweep_kernel == 3 || c->wave_on[0])) ? 3 : 2;
     if (dims) for (int k = 0; k < 3; ++k) dims[k] = c->hp.box.ok ? c->hp.box.dim[k] : 0;

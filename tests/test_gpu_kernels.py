@@ -185,6 +185,131 @@ CLUSTER_CASES = [
 ]
 
 
+def _box_system(dims, seed=2):
+    """A box-stencil system; a 1-cell-wide box is the reference's 1D mesh."""
+    if dims[1] == 1 and dims[2] == 1:
+        rp, col = W.pattern_1d(dims[0])
+        rng = np.random.default_rng(seed)
+        val = np.where(col == W.PHANTOM, 0.0, rng.uniform(-1, 0, col.size))
+        rows = np.repeat(np.arange(dims[0]), np.diff(rp.astype(np.int64)))
+        val[col == rows.astype(np.uint64)] = 3.0
+        return W.System(rp, col, val, rng.uniform(-1, 1, dims[0]))
+    return W.hex_pprime(*dims)
+
+
+SERIAL = [(33, 1, 1), (1000, 1, 1), (5120, 1, 1), (2000, 2, 1), (1500, 2, 1)]
+
+
+@pytest.mark.parametrize("dims", SERIAL)
+def test_serial_sweeps_bit_exact(ctx, torch_cuda, oracle, dims):
+    """Tiny systems whose schedule is about as deep as they are long take the
+    one-warp serial sweep in automatic mode (kind 4): sweeps and whole solves
+    equal the oracle bit for bit, FP64 and FP32."""
+    import opencslsolver_gb300 as ocsl
+
+    s = _box_system(dims)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    assert ctx.sweep_info()["kind"] == 4
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(s.n)
+    Mh = oracle.ilu(s.row_ptr, s.column_index, s.value)
+    M, B = dev(torch_cuda, Mh), dev(torch_cuda, b)
+    Y, X = torch_cuda.empty_like(B), torch_cuda.empty_like(B)
+    ctx.forsub_device(M, B, Y)
+    y = oracle.forsub(s.row_ptr, s.column_index, Mh, b)
+    assert np.array_equal(host(Y), y)
+    ctx.backsub_device(M, Y, X)
+    assert np.array_equal(host(X), oracle.backsub(s.row_ptr, s.column_index, Mh, y))
+    x0 = np.zeros(s.n)
+    for method, fn in ((ocsl.BICGSTAB_REF, oracle.bicgstab_ref), (ocsl.CG_REF, oracle.cg_ref)):
+        x = x0.copy()
+        r = ctx.solve(method, s.value, s.b, x)
+        xo, res_o, it_o = fn(s.row_ptr, s.column_index, s.value, s.b, x0)
+        assert np.array_equal(x, xo) and r["residual"] == res_o and r["iterations"] == it_o
+    x = x0.copy()
+    r = ctx.solve(ocsl.ILU_BICGSTAB, s.value, s.b, x, tol=1e-10)
+    xo, rc, it, _ = oracle.bicgstab_tol(s.row_ptr, s.column_index, s.value, s.b, x0, tol=1e-10)
+    assert r["status"] == 0 and np.array_equal(x, xo) and r["iterations"] == it
+    x = x0.copy()
+    r = ctx.solve(ocsl.ILU_BICGSTAB_IR32, s.value, s.b, x, tol=1e-10)
+    assert r["status"] == 0
+    assert oracle.true_relres(s.row_ptr, s.column_index, s.value, s.b, x) <= 1e-10
+    # the other kernels give the same bits
+    ctx.set_sweep_kernel(1)
+    assert ctx.sweep_info()["kind"] == 1
+    Y2 = torch_cuda.empty_like(B)
+    ctx.forsub_device(M, B, Y2)
+    assert torch_cuda.equal(Y, Y2)
+
+
+def _random_doubles(rng, size, emin, emax):
+    """Random signs, exponents in [emin, emax] and 52-bit mantissas, with a
+    share of mantissas near all ones or all zeros (binade edges)."""
+    mant = rng.integers(0, 1 << 52, size, dtype=np.uint64)
+    edge = rng.random(size)
+    mant[edge < 0.1] = np.uint64((1 << 52) - 1) - rng.integers(0, 64, int((edge < 0.1).sum()),
+                                                               dtype=np.uint64)
+    mant[(edge >= 0.1) & (edge < 0.2)] = rng.integers(0, 64, int(((edge >= 0.1) & (edge < 0.2)).sum()),
+                                                      dtype=np.uint64)
+    exp = (rng.integers(emin, emax + 1, size) + 1023).astype(np.uint64)
+    sign = rng.integers(0, 2, size, dtype=np.uint64)
+    return ((sign << np.uint64(63)) | (exp << np.uint64(52)) | mant).view(np.float64)
+
+
+def test_serial_backsub_division_is_correctly_rounded(ctx, torch_cuda):
+    """The serial backward sweep divides by the pivot with Markstein's method
+    (reciprocal + two residual corrections) in the safe exponent range and by
+    the IEEE division elsewhere: on a 1D system whose off-diagonal entries are
+    0, x = y / M_ii must be the correctly rounded quotient, bit for bit, for
+    12M operand pairs -- exponents within +-260 (the fast path), pairs beyond
+    +-500 with a moderate quotient, subnormals and zeros (the IEEE path),
+    mantissas at binade edges.  Quotients stay finite, so no row poisons the
+    next through 0 * inf."""
+    n = 5120
+    rp, col = W.pattern_1d(n)
+    ctx.set_pattern(rp, col)
+    assert ctx.sweep_info()["kind"] == 4
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64))).astype(np.uint64)
+    on_diag = col == rows
+    rng = np.random.default_rng(12)
+    specials = [(0.0, 3.0), (-0.0, 3.0), (5e-324, 0.5), (5e-324, 3.0), (-2.2250738585072014e-308, 3.0),
+                (1.7976931348623157e308, 2.0), (1.7976931348623157e308, np.inf), (1.0, -np.inf),
+                (2.0 ** -500, 2.0 ** 500), (2.0 ** 500, 2.0 ** -500), (1.0, 3.0), (-1.0, 3.0)]
+    val = np.zeros(col.size)
+    Y = torch_cuda.empty(n, dtype=torch_cuda.float64, device="cuda")
+    X = torch_cuda.empty_like(Y)
+    Mt = torch_cuda.empty(col.size, dtype=torch_cuda.float64, device="cuda")
+    bad = 0
+    for it in range(2000):
+        if it % 2 == 0:
+            a = _random_doubles(rng, n, -260, 260)
+            b = _random_doubles(rng, n, -260, 260)
+        else:  # large or small operands, quotient near 1
+            ea = rng.integers(-1020, 1021, n)
+            a = _random_doubles(rng, n, 0, 0) * np.exp2(ea.astype(np.float64))
+            b = _random_doubles(rng, n, 0, 0) * np.exp2((ea + rng.integers(-20, 21, n)).clip(-1022, 1023))
+        if it % 10 == 0:
+            a[:len(specials)] = [p[0] for p in specials]
+            b[:len(specials)] = [p[1] for p in specials]
+        val[on_diag] = b
+        Mt.copy_(torch_cuda.from_numpy(val))
+        Y.copy_(torch_cuda.from_numpy(a))
+        ctx.backsub_device(Mt, Y, X)
+        got = X.cpu().numpy()
+        want = a / b
+        assert np.all(np.isfinite(want))
+        bad += int(np.count_nonzero(got.view(np.uint64) != want.view(np.uint64)))
+    assert bad == 0
+
+
+def test_serial_sweep_limits(ctx):
+    """Larger or shallow patterns keep the level-scheduled / structured kernels."""
+    for dims, kind in (((5121, 1, 1), 2), ((20, 20, 20), 2), ((64, 8, 1), 2)):
+        s = _box_system(dims)
+        ctx.set_pattern(s.row_ptr, s.column_index)
+        assert ctx.sweep_info()["kind"] == kind, dims
+
+
 @pytest.mark.parametrize("dims,tiles,cluster", CLUSTER_CASES)
 def test_clustered_sweeps_bit_exact(ctx, torch_cuda, oracle, dims, tiles, cluster):
     """Structured sweeps whose tiles run in thread-block clusters (faces
