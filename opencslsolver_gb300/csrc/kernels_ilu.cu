@@ -204,33 +204,33 @@ __global__ void __launch_bounds__(kThreads) bw_sweep_kernel(SweepParams<T> p)
 // kernels: the results are the same bits.
 constexpr int kSerialK = 4;
 
-// a / b, correctly rounded, from y = RN(1/b) by Markstein's method (P.
-// Markstein, "Computation of elementary functions on the IBM RISC System/6000
-// processor", IBM J. Res. Dev. 34(1), 1990): q = RN(a y) is within 1.5 ulp;
-// one residual correction q + (a - b q) y brings it within an ulp, and a
-// second one is, by Markstein's theorem (y within half an ulp of 1/b, q within
-// an ulp of a/b), the correctly rounded quotient.  The residuals a - b q are
-// exact fmas.  Operands outside [2^-500, 2^500] in magnitude (zeros,
-// subnormals, infinities, NaN, values near over- or underflow) take the IEEE
-// division.  Five dependent operations instead of a full division on the
-// serial chain.
+// a / b, correctly rounded, by Markstein's method (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990).  Off the chain, per row: y =
+// RN(1/b) and y_lo = RN((1 - b y) y), so y + y_lo is 1/b to about 2^-104
+// (1 - b y is exact in an fma).  On the chain: q = RN(a y + a y_lo) is within
+// an ulp of a/b, and one residual correction q + (a - b q) y is, by
+// Markstein's theorem (y within half an ulp of 1/b, q within an ulp of a/b),
+// the correctly rounded quotient; the residual a - b q is an exact fma.
+// Operands outside [2^-500, 2^500] in magnitude (zeros, subnormals,
+// infinities, NaN, values near over- or underflow) take the IEEE division.
+// Four dependent FP64 operations instead of a division, which costs about
+// nine times one of them on this GPU.
 __device__ __forceinline__ bool markstein_range(double v)
 {
     const int e = (__double2hiint(v) >> 20) & 0x7ff;  // biased exponent
     return e >= 1023 - 500 && e <= 1023 + 500;
 }
 
-__device__ __forceinline__ double div_rcp(double a, double b, double y, bool b_ok)
+__device__ __forceinline__ double div_rcp(double a, double b, double y, double ylo, bool b_ok)
 {
     if (!b_ok || !markstein_range(a)) return a / b;
-    double q = a * y;
-    double r = fma(-b, q, a);
-    q = fma(r, y, q);
-    r = fma(-b, q, a);
+    const double q = fma(a, y, a * ylo);
+    const double r = fma(-b, q, a);
     return fma(r, y, q);
 }
 
-__device__ __forceinline__ float div_rcp(float a, float b, float, bool) { return a / b; }
+__device__ __forceinline__ float div_rcp(float a, float b, float, float, bool) { return a / b; }
 
 template <typename T, bool FW, bool DIV>
 __global__ void __launch_bounds__(32) serial_sweep_kernel(SweepParams<T> p)
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(32) serial_sweep_kernel(SweepParams<T> p)
     T* xs = reinterpret_cast<T*>(serial_smem);
     __shared__ int s_row[32], s_q0[32], s_q1[32], s_ok[32];
     __shared__ int s_col[kSerialK][32];
-    __shared__ T s_rhs[32], s_div[32], s_rcp[32];
+    __shared__ T s_rhs[32], s_div[32], s_rcp[32], s_rlo[32];
     __shared__ T s_m[kSerialK][32];
     using B = Bits<T>;
     const int lane = (int)threadIdx.x;
@@ -262,7 +262,9 @@ __global__ void __launch_bounds__(32) serial_sweep_kernel(SweepParams<T> p)
                 const T dv = DIV ? __ldg(p.M + d) : __ldg(p.dinv + i);
                 s_div[lane] = dv;
                 if (DIV) {
-                    s_rcp[lane] = T(1) / dv;
+                    const T y = T(1) / dv;
+                    s_rcp[lane] = y;
+                    s_rlo[lane] = fma_t(-dv, y, T(1)) * y;
                     if constexpr (sizeof(T) == 8) s_ok[lane] = markstein_range(dv) ? 1 : 0;
                     else s_ok[lane] = 0;
                 }
@@ -292,7 +294,9 @@ __global__ void __launch_bounds__(32) serial_sweep_kernel(SweepParams<T> p)
                 }
                 const T num = s_rhs[k] - sum;
                 T v = num;
-                if (!FW) v = DIV ? div_rcp(num, s_div[k], s_rcp[k], s_ok[k] != 0) : num * s_div[k];
+                if (!FW)
+                    v = DIV ? div_rcp(num, s_div[k], s_rcp[k], s_rlo[k], s_ok[k] != 0)
+                            : num * s_div[k];
                 if (B::to(v) == B::kSentinel) v = B::from(B::kCanonicalNaN);
                 xs[ik] = v;
                 p.out[ik] = v;

@@ -204,14 +204,36 @@ struct ocsl_ctx {
     bool serial_ok[2] = {false, false};
 
     // SIMPLE iteration on the device (ocsl_flow_iterate_device): the system
-    // of the equation being solved, a residual work vector, the five residual
-    // sums, and the boundary-kind check of the last state seen
+    // of the equation being solved, a residual work vector, the per-call
+    // outputs (device and pinned host), and the boundary-kind check of the
+    // last state seen
+    struct FlowOut {
+        double residual[5];
+        int iterations[5];
+        int err[5];
+    };
     double* d_fval = nullptr;
     double* d_fb = nullptr;
     double* d_fx = nullptr;
     double* d_ftmp = nullptr;
-    double* d_fres = nullptr;
+    FlowOut* d_fout = nullptr;
+    FlowOut* h_fout = nullptr;
     const void* flow_bc_checked = nullptr;
+    // the captured inner iteration (reference-faithful solves), replayed while
+    // its key -- every argument of the call and the stream -- stays the same;
+    // the first call with a key runs directly (it allocates), the next captures
+    cudaGraphExec_t flow_exec = nullptr;
+    std::vector<unsigned char> flow_key;
+    int flow_seen = 0;
+    Scalars* d_sc_ref = nullptr;  // the scalars block a reference-faithful solve starts from
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    void drop_flow_graph()
+    {
+        if (flow_exec) cudaGraphExecDestroy(flow_exec);
+        flow_exec = nullptr;
+        flow_key.clear();
+        flow_seen = 0;
+    }
 
     // face-loop assembly: the mesh's face incidence (ocsl_set_faces)
     DevFaces F{};
@@ -239,6 +261,7 @@ struct ocsl_ctx {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
         graph_kind = 0;
+        drop_flow_graph();
     }
     void ensure_reduce(int ntiles);
     void ensure_fp32();
@@ -261,7 +284,7 @@ void ocsl_ctx::free_pattern()
     for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
     F = DevFaces{};
     has_faces = false;
-    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp, &d_fres};
+    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp};
     for (auto pp : dflow) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     flow_bc_checked = nullptr;
     for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
@@ -312,6 +335,15 @@ void ocsl_ctx::free_all()
     prof_ev.clear();
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     graph_exec = nullptr;
+    if (d_fout) cudaFree(d_fout);
+    if (h_fout) cudaFreeHost(h_fout);
+    if (d_sc_ref) cudaFree(d_sc_ref);
+    d_fout = nullptr;
+    h_fout = nullptr;
+    d_sc_ref = nullptr;
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    ev_fork = ev_join = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = stream = nullptr;
 }
@@ -866,10 +898,21 @@ struct Solve {
 // ------------------------------------------------------------------ reference-faithful
 
 // CMatrix_solver::CG_solve (cmatrix_solver.cpp:635-680).
-void run_cg_ref(Solve& s, const double* A, const double* b, double* x)
+// Block 0 as a reference-faithful solve starts it: from the host (a
+// synchronising upload) or, for a captured graph, from the context's device
+// copy of that start state.
+void reset_ref_scalars(Solve& s, bool from_device)
+{
+    if (from_device)
+        CK(cudaMemcpyAsync(s.sc(0), s.c->d_sc_ref, sizeof(Scalars), cudaMemcpyDeviceToDevice, s.st));
+    else
+        s.reset_scalars(0, 0.0);
+}
+
+void run_cg_ref(Solve& s, const double* A, const double* b, double* x, bool device_reset = false)
 {
     double** v = s.c->v64;
-    s.reset_scalars(0, 0.0);
+    reset_ref_scalars(s, device_reset);
     s.prepare_spmv(A, true, false);
     // r = b - A x (:652), p = r (:655), rr = <r,r>
     s.spmv<double>(A, x, v[R], 1, b, v[P], nullptr, DOT_YY, 0, EP_RC_INIT);
@@ -889,11 +932,12 @@ void run_cg_ref(Solve& s, const double* A, const double* b, double* x)
 // CMatrix_solver::ILU_BICGSTAB_solve (cmatrix_solver.cpp:682-762), quirks kept:
 // omega in the direction update, rho never updated, the residual test on the
 // r from the start of the iteration, x not updated on that exit.
-void run_bicgstab_ref(Solve& s, const double* A, const double* b, double* x, int sweeps)
+void run_bicgstab_ref(Solve& s, const double* A, const double* b, double* x, int sweeps,
+                      bool device_reset = false)
 {
     double** v = s.c->v64;
     const size_t bytes = sizeof(double) * (size_t)s.n;
-    s.reset_scalars(0, 0.0);
+    reset_ref_scalars(s, device_reset);
     CK(cudaMemsetAsync(v[P], 0, bytes, s.st));  // Cvector(n) starts at 0 (:690-700)
     CK(cudaMemsetAsync(v[V], 0, bytes, s.st));
     const double* M = s.factored(A, sweeps, false, false, 0, true, false, false);  // :702-704
@@ -2369,15 +2413,186 @@ static int flow_view(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state*
     return OCSL_OK;
 }
 
+}  // extern "C"
+
+// The launches of one inner iteration on `st`, in the reference's order
+// (cflow_solver.cpp:229-476).  solve(slot, method) enqueues the linear solve
+// of equation slot (0-2 momentum, 3 p', 4 enthalpy) on the system in
+// d_fval / d_fb / d_fx.
+template <typename SolveFn>
+static void enqueue_flow(ocsl_ctx* c, cudaStream_t st, const ocsl_assembly* q,
+                         const ocsl_flow_state* s, const ocsl_flow_iteration* it,
+                         const int* methods, const FlowDev& f, SolveFn&& solve)
+{
+    const int n = c->P.n, nf = c->F.nf, nb = c->F.nb;
+    Solve sv{c, st, c->P, n};
+    CK(cudaMemsetAsync(c->d_sc + kScFlow, 0, sizeof(Scalars), st));
+    auto residual = [&](const double* v, int slot) {  // sum |v| in tile order
+        sv.vec<double>(V_ABSSUM, {v}, kScFlow, EP_STORE);
+        launch_take_sum(st, c->d_sc + kScFlow, c->d_fout->residual + slot);
+    };
+    ocsl_assembly qe = *q;
+    // boundary conditions and the pressure gradient (:234-241)
+    launch_flow_bc_pressure(st, n, nb, f);
+    launch_flow_grad(st, false, n, nf, nb, f, c->F);
+    CK(cudaMemsetAsync(f.ap, 0, sizeof(double) * n, st));  // :244-247
+    // momentum components (:257-302)
+    for (int d = 0; d < 3; ++d) {
+        qe.equation = OCSL_EQ_MOMENTUM;
+        qe.dimension = d;
+        launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx,
+                        f.ap_vec + (size_t)d * n, it->total_mdot);
+        solve(d, methods[0]);
+        launch_flow_velocity_update(st, n, d, c->d_fx, f, c->d_ftmp);
+        residual(c->d_ftmp, d);
+    }
+    // face mass fluxes (:305-309), pressure correction (:316-358)
+    launch_flow_face_mdot(st, n, nf, f, q->blended);
+    qe.equation = OCSL_EQ_PRESSURE;
+    qe.dimension = 0;
+    launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, it->total_mdot);
+    residual(c->d_fb, 3);  // Pressure_global_residual = ABSsum(b), :346
+    solve(3, methods[1]);
+    launch_flow_pcorr(st, n, c->d_fx, f);
+    // corrections (:375-426)
+    launch_flow_grad(st, true, n, nf, nb, f, c->F);
+    launch_flow_correct(st, n, nf, f, q->blended, q->R_specific, q->gamma);
+    // enthalpy (:428-474)
+    qe.equation = OCSL_EQ_ENTHALPY;
+    launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, nullptr);
+    solve(4, methods[2]);
+    launch_flow_enthalpy_update(st, n, c->d_fx, f, c->d_ftmp, q->R_specific, q->gamma);
+    residual(c->d_ftmp, 4);
+}
+
+static bool capturable(cudaStream_t st)
+{
+    return st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+}
+
+// Reference-faithful solves only: the whole iteration as one CUDA graph.  The
+// solves start from the device copy of their scalars, their iteration counts
+// and error words are copied aside on the device, and the outputs come back
+// in one copy at the end -- no host round trip inside.  The graph runs on the
+// caller's stream, or (the legacy default stream cannot be captured) on the
+// context's own stream joined to the caller's by events.
+static int flow_iterate_graphed(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s,
+                                const ocsl_flow_iteration* it, const int* methods,
+                                const ocsl_opts& o, const FlowDev& f, ocsl_flow_report& rep)
+{
+    std::vector<unsigned char> key;
+    auto add = [&](const void* p, size_t bytes) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), b, b + bytes);
+    };
+    add(q, sizeof *q);
+    add(s, sizeof *s);
+    add(it, sizeof *it);
+    add(methods, 3 * sizeof(int));
+    add(&o.ilu_sweeps, sizeof o.ilu_sweeps);
+    add(&c->stream, sizeof c->stream);
+    if (key != c->flow_key) {
+        c->drop_flow_graph();
+        c->flow_key = key;
+    }
+    if (!c->d_sc_ref) {
+        Scalars init;
+        std::memset(&init, 0, sizeof init);
+        init.alpha = init.omega = init.rhon = init.rho = 1.0;
+        c->d_sc_ref = dalloc<Scalars>(1);
+        CK(cudaMemcpy(c->d_sc_ref, &init, sizeof init, cudaMemcpyHostToDevice));
+        CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    }
+    const cudaStream_t caller = c->stream;
+    const cudaStream_t work = capturable(caller) ? caller : c->own_stream;
+    if (work != caller) {
+        CK(cudaEventRecord(c->ev_fork, caller));
+        CK(cudaStreamWaitEvent(work, c->ev_fork, 0));
+    }
+    auto enqueue = [&] {
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), work));
+        enqueue_flow(c, work, q, s, it, methods, f, [&](int slot, int method) {
+            Solve sv{c, work, c->P, c->P.n};
+            c->fac_M = nullptr;
+            if (method == OCSL_CG_REF)
+                run_cg_ref(sv, c->d_fval, c->d_fb, c->d_fx, true);
+            else
+                run_bicgstab_ref(sv, c->d_fval, c->d_fb, c->d_fx, o.ilu_sweeps, true);
+            CK(cudaMemcpyAsync(c->d_fout->iterations + slot, &c->d_sc[0].iters, sizeof(int),
+                               cudaMemcpyDeviceToDevice, work));
+            CK(cudaMemcpyAsync(c->d_fout->err + slot, c->d_err, sizeof(int),
+                               cudaMemcpyDeviceToDevice, work));
+            CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), work));
+        });
+        CK(cudaMemcpyAsync(c->h_fout, c->d_fout, sizeof *c->h_fout, cudaMemcpyDeviceToHost, work));
+    };
+    bool launched = false;
+    if (!c->flow_exec && c->flow_seen >= 1) {
+        if (cudaStreamBeginCapture(work, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            cudaGraph_t g = nullptr;
+            try {
+                enqueue();
+            } catch (...) {
+                cudaStreamEndCapture(work, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            cudaError_t e = cudaStreamEndCapture(work, &g);
+            cudaGraphExec_t exec = nullptr;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (e == cudaSuccess)
+                c->flow_exec = exec;
+            else
+                cudaGetLastError();  // capture refused: run directly below
+        } else {
+            cudaGetLastError();
+        }
+    }
+    if (c->flow_exec) {
+        CK(cudaGraphLaunch(c->flow_exec, work));
+        launched = true;
+    }
+    if (!launched) enqueue();
+    ++c->flow_seen;
+    if (work != caller) {
+        CK(cudaEventRecord(c->ev_join, work));
+        CK(cudaStreamWaitEvent(caller, c->ev_join, 0));
+    }
+    CK(cudaStreamSynchronize(work));
+    CK(cudaGetLastError());
+    int status = OCSL_OK;
+    for (int e = 0; e < 5; ++e) {
+        rep.residual[e] = c->h_fout->residual[e];
+        rep.iterations[e] = c->h_fout->iterations[e];
+        rep.status[e] = c->h_fout->err[e];
+        if (rep.status[e] && status == OCSL_OK) status = rep.status[e];
+    }
+    if (status != OCSL_OK) {
+        // host-side choices baked into the graph may no longer hold
+        if (status == OCSL_TIMEOUT) c->wave_faces_dirty = true;
+        c->drop_flow_graph();
+        c->last_error = status == OCSL_TIMEOUT ? "a triangular-sweep wait hit its bound"
+                                               : "the factor has a zero or infinite pivot";
+    }
+    return status;
+}
+
+extern "C" {
+
 int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state* s,
                              const ocsl_flow_iteration* it, const int* methods,
                              const ocsl_opts* opts, ocsl_flow_report* report)
 {
     if (report) std::memset(report, 0, sizeof *report);
     if (!methods) return c ? fail(c, OCSL_BAD_ARGUMENT, "null methods") : OCSL_BAD_ARGUMENT;
-    for (int e = 0; e < 3; ++e)
+    bool ref_only = true;
+    for (int e = 0; e < 3; ++e) {
         if (methods[e] < OCSL_CG_REF || methods[e] > OCSL_ILU_BICGSTAB_IR32)
             return c ? fail(c, OCSL_BAD_ARGUMENT, "unknown method") : OCSL_BAD_ARGUMENT;
+        ref_only = ref_only && (methods[e] == OCSL_CG_REF || methods[e] == OCSL_BICGSTAB_REF);
+    }
     FlowDev f{};
     int status = OCSL_OK;
     ocsl_flow_report rep{};
@@ -2385,7 +2600,7 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
         int rc = flow_view(c, q, s, it, f);
         if (rc) return rc;
         CK(cudaSetDevice(c->device));
-        const int n = c->P.n, nf = c->F.nf, nb = c->F.nb;
+        const int n = c->P.n;
         if (n == 0) {
             if (report) *report = rep;
             return OCSL_OK;
@@ -2395,60 +2610,32 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
             c->d_fb = dalloc<double>((size_t)n);
             c->d_fx = dalloc<double>((size_t)n);
             c->d_ftmp = dalloc<double>((size_t)n);
-            c->d_fres = dalloc<double>(5);
         }
-        cudaStream_t st = c->stream;
-        Solve sv{c, st, c->P, n};
-        CK(cudaMemsetAsync(c->d_sc + kScFlow, 0, sizeof(Scalars), st));
-        auto residual = [&](const double* v, int slot) {  // sum |v| in tile order
-            sv.vec<double>(V_ABSSUM, {v}, kScFlow, EP_STORE);
-            launch_take_sum(st, c->d_sc + kScFlow, c->d_fres + slot);
-        };
-        auto solve = [&](int slot, int method) {
-            ocsl_result r;
-            const int rc2 = solve_device_impl(c, method, c->d_fval, c->d_fb, c->d_fx, opts, &r);
-            rep.iterations[slot] = r.iterations;
-            rep.status[slot] = rc2;
-            if (rc2 != OCSL_OK && status == OCSL_OK) status = rc2;
-        };
-        ocsl_assembly qe = *q;
-        // boundary conditions and the pressure gradient (cflow_solver.cpp:234-241)
-        launch_flow_bc_pressure(st, n, nb, f);
-        launch_flow_grad(st, false, n, nf, nb, f, c->F);
-        CK(cudaMemsetAsync(f.ap, 0, sizeof(double) * n, st));  // :244-247
-        // momentum components (:257-302)
-        for (int d = 0; d < 3; ++d) {
-            qe.equation = OCSL_EQ_MOMENTUM;
-            qe.dimension = d;
-            launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, f.ap_vec + (size_t)d * n,
-                            it->total_mdot);
-            solve(d, methods[0]);
-            launch_flow_velocity_update(st, n, d, c->d_fx, f, c->d_ftmp);
-            residual(c->d_ftmp, d);
+        if (!c->d_fout) {
+            c->d_fout = dalloc<ocsl_ctx::FlowOut>(1);
+            CK(cudaMallocHost(&c->h_fout, sizeof *c->h_fout));
         }
-        // face mass fluxes (:305-309), pressure correction (:316-358)
-        launch_flow_face_mdot(st, n, nf, f, q->blended);
-        qe.equation = OCSL_EQ_PRESSURE;
-        qe.dimension = 0;
-        launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, it->total_mdot);
-        residual(c->d_fb, 3);  // Pressure_global_residual = ABSsum(b), :346
-        solve(3, methods[1]);
-        launch_flow_pcorr(st, n, c->d_fx, f);
-        // corrections (:375-426)
-        launch_flow_grad(st, true, n, nf, nb, f, c->F);
-        launch_flow_correct(st, n, nf, f, q->blended, q->R_specific, q->gamma);
-        // enthalpy (:428-474)
-        qe.equation = OCSL_EQ_ENTHALPY;
-        launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, nullptr);
-        solve(4, methods[2]);
-        launch_flow_enthalpy_update(st, n, c->d_fx, f, c->d_ftmp, q->R_specific, q->gamma);
-        residual(c->d_ftmp, 4);
-        CK(cudaMemcpyAsync(c->h_sc + kHostStage, c->d_fres, 5 * sizeof(double),
-                           cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        std::memcpy(rep.residual, c->h_sc + kHostStage, 5 * sizeof(double));
-        CK(cudaGetLastError());
+        const ocsl_opts o = resolve(opts);
+        if (ref_only && c->graphs_on && !c->prof_on && !c->fault_skip_pending) {
+            status = flow_iterate_graphed(c, q, s, it, methods, o, f, rep);
+        } else {
+            // solves through the ordinary entry (tolerance-mode iterations
+            // look at their scalars between batches)
+            const cudaStream_t st = c->stream;
+            enqueue_flow(c, st, q, s, it, methods, f, [&](int slot, int method) {
+                ocsl_result r;
+                const int rc2 = solve_device_impl(c, method, c->d_fval, c->d_fb, c->d_fx, &o, &r);
+                rep.iterations[slot] = r.iterations;
+                rep.status[slot] = rc2;
+                if (rc2 != OCSL_OK && status == OCSL_OK) status = rc2;
+            });
+            CK(cudaMemcpyAsync(c->h_fout, c->d_fout, sizeof *c->h_fout, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            std::memcpy(rep.residual, c->h_fout->residual, sizeof rep.residual);
+            CK(cudaGetLastError());
+        }
     } catch (const CudaError& e) {
+        c->drop_flow_graph();
         status = from_cuda(c, e);
     }
     if (report) *report = rep;

@@ -14,7 +14,8 @@
   mass fluxes and densities) within 5e-9 of the reference run that uses
   ILU_BICGSTAB_solve everywhere (measured 1.1e-9: the reference's own solves
   stop after a fixed count), the derived p' gradient and cell mass balance
-  within 1e-8.
+  within 1e-8; the same for the FP32-inner / FP64-refined solver, whose p'
+  gradient is within 1e-7 (measured 4.2e-8).
 * Unsupported input is refused before anything is written.
 """
 import time
@@ -34,6 +35,7 @@ METHODS = {
     "bicg": (ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF),
     "cg": (ocsl.CG_REF, ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF),
     "tol": (ocsl.ILU_BICGSTAB, ocsl.ILU_BICGSTAB, ocsl.ILU_BICGSTAB),
+    "ir32": (ocsl.ILU_BICGSTAB_IR32, ocsl.ILU_BICGSTAB_IR32, ocsl.ILU_BICGSTAB_IR32),
 }
 
 
@@ -66,7 +68,7 @@ def test_iteration_bit_exact_vs_oracle(ctx, torch_cuda, golden, mode):
         assert np.array_equal(dev.state[k].cpu().numpy(), case["state"][k]), k
 
 
-@pytest.mark.parametrize("mode", ["bicg", "cg", "tol"])
+@pytest.mark.parametrize("mode", ["bicg", "cg", "tol", "ir32"])
 def test_shocktube_200_steps_vs_reference(ctx, torch_cuda, golden, mode):
     dev = FC.DeviceCase(torch_cuda, golden.case())
     dev.bind(ctx)
@@ -79,17 +81,17 @@ def test_shocktube_200_steps_vs_reference(ctx, torch_cuda, golden, mode):
         dev.end_step(ctx)
     torch_cuda.cuda.synchronize()
     ms = (time.perf_counter() - t0) * 1e3 / (FC.STEPS * FC.INNER)
-    ref = "final_bicg" if mode in ("bicg", "tol") else "final_cg"
+    ref = "final_cg" if mode == "cg" else "final_bicg"
     errs = FC.field_errors(dev.written(), FC.recorded(golden.setup, golden.record(ref)))
     print(f"{mode}: {ms:.3f} ms per inner iteration; max field error vs {ref}: "
           f"{max(errs.values()):.2e} ({max(errs, key=errs.get)})")
-    if mode == "tol":
+    if mode in ("tol", "ir32"):
         # converged solves against the reference's fixed-count ones (measured:
         # state <= 1.1e-9, p' gradient 3.1e-9)
         for k in ("velocity", "pressure", "temperature", "density_c", "enthalpy", "mdot",
                   "density"):
             assert errs[k] <= 5e-9, (k, errs)
-        assert max(errs.values()) <= 1e-8, errs
+        assert max(errs.values()) <= (1e-8 if mode == "tol" else 1e-7), errs
     else:
         assert max(errs.values()) <= 1e-11, errs
 
@@ -123,3 +125,39 @@ def test_rejects_unsupported_input(ctx, torch_cuda, golden):
     dev.iterate(ctx, METHODS["bicg"])
     orc.flow_iterate(case, METHODS["bicg"])
     _same(dev.written(), FC.written(case), "after refusals")
+
+
+def test_graph_replay_matches_direct_launches(ctx, torch_cuda, golden):
+    """Reference-faithful iterations run as one captured CUDA graph from the
+    second call with the same arguments on; the graph (this context), the
+    direct launches (a context with graphs off) and the oracle agree bit for
+    bit, on torch's default stream and on a side stream (a new key each
+    switch), and a changed constant is captured afresh."""
+    torch = torch_cuda
+    case = golden.case()
+    graphed, direct = FC.DeviceCase(torch, golden.case()), FC.DeviceCase(torch, golden.case())
+    graphed.bind(ctx)
+    ctx2 = ocsl.Context(0)
+    try:
+        ctx2.set_graphs(False)
+        direct.bind(ctx2)
+        side = torch.cuda.Stream()
+        for k in range(12):
+            if k == 8:  # a new under-relaxation factor: a new key
+                for c in (case, graphed.case, direct.case):
+                    c["constants"] = dict(c["constants"], relax_u=0.9)
+            if 4 <= k < 8:
+                with torch.cuda.stream(side):
+                    r0 = graphed.iterate(ctx, METHODS["cg"])
+                side.synchronize()
+            else:
+                r0 = graphed.iterate(ctx, METHODS["cg"])
+            r1 = direct.iterate(ctx2, METHODS["cg"])
+            want = orc.flow_iterate(case, METHODS["cg"])
+            _same(graphed.written(), FC.written(case), ("graph", k))
+            _same(direct.written(), FC.written(case), ("direct", k))
+            assert r0 == r1, (k, r0, r1)
+            assert r0["residual"] == list(want["residual"])
+            assert r0["iterations"] == list(want["iterations"])
+    finally:
+        ctx2.close()

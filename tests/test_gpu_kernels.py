@@ -258,7 +258,7 @@ def _random_doubles(rng, size, emin, emax):
 
 def test_serial_backsub_division_is_correctly_rounded(ctx, torch_cuda):
     """The serial backward sweep divides by the pivot with Markstein's method
-    (reciprocal + two residual corrections) in the safe exponent range and by
+    (a two-term reciprocal + one residual correction) in the safe exponent range and by
     the IEEE division elsewhere: on a 1D system whose off-diagonal entries are
     0, x = y / M_ii must be the correctly rounded quotient, bit for bit, for
     12M operand pairs -- exponents within +-260 (the fast path), pairs beyond
