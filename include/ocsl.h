@@ -321,17 +321,20 @@ int ocsl_bc_value_grad_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
 
 /* ------------------------------------------------------------------------
  * The SIMPLE inner iteration on the device: CFlow_solver::iterate
- * (cflow_solver.cpp:229-476) for an inviscid flow whose boundary faces are
- * walls, symmetry planes or empty faces -- boundary pressures, the pressure
- * gradient, the three momentum assemblies and solves, face mass fluxes, the
- * pressure-correction assembly and solve, the corrections of pressure, mass
- * fluxes, densities and velocities, and the enthalpy assembly and solve with
- * the temperature and Mach updates -- all on the context's stream, with no
- * host round trip between the stages.  The state of ocsl_flow_state is read
- * AND WRITTEN in place (pressure, velocity, density_c, temperature, enthalpy,
- * pressure_corr, pressure_grad, mdot, density, qy); its boundary arrays
- * bc_type, bc_area_vector are read.  Other boundary kinds or eq->viscous give
- * OCSL_BAD_ARGUMENT.  ocsl_set_faces must have been called.
+ * (cflow_solver.cpp:229-476) -- boundary conditions, the pressure gradient,
+ * the explicit viscous stress (viscous flows), the three momentum assemblies
+ * and solves, face mass fluxes, the pressure-correction assembly and solve,
+ * the corrections of pressure, mass fluxes, densities and velocities, and the
+ * enthalpy assembly and solve with the temperature and Mach updates -- all on
+ * the context's stream, with no host round trip between the stages.  Every
+ * boundary kind of ocsl_bc_type, inviscid or viscous, transient or steady
+ * (eq->transient, eq->implicit_underrelaxation).  The state of
+ * ocsl_flow_state is read AND WRITTEN in place: cells (pressure, velocity,
+ * density_c, temperature, enthalpy, pressure_corr, pressure_grad), interior
+ * faces (mdot, density, qy, stress for viscous flows) and boundary faces
+ * (bc_mdot, bc_density, bc_qy, bc_enthalpy, bc_supersonic, and on pressure
+ * outlets bc_temperature, bc_velocity).  ocsl_set_faces must have been
+ * called.
  * ---------------------------------------------------------------------- */
 typedef struct {
     /* interior-face metrics (CFVM_face), [3][n_faces] for vectors */
@@ -342,6 +345,8 @@ typedef struct {
     /* boundary-face metrics (CFVM_BC_face), [3][n_bc] for vectors */
     const double* bc_distance;
     const double* bc_unit;
+    const double* bc_alpha;
+    const double* bc_out_pressure; /* CFlow_BC_face::Out_Pressure (outlets)     */
     /* per-iteration fields the iteration writes (DEVICE pointers) */
     double* bc_pressure;           /* CFlow_BC_face::Pressure (n_bc)             */
     double* pressure_corr_grad;    /* [3][n]                                     */

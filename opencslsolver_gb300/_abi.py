@@ -101,7 +101,8 @@ def flow_state(arrays: dict, ptr) -> FlowState:
 # ocsl_flow_iteration / ocsl_flow_report (include/ocsl.h)
 FLOW_ITERATION_ARRAYS = (
     "face_area_vector", "face_alpha", "face_distance", "face_unit", "bc_distance", "bc_unit",
-    "bc_pressure", "pressure_corr_grad", "ap", "ap_vec", "mach", "total_mdot")
+    "bc_alpha", "bc_out_pressure", "bc_pressure", "pressure_corr_grad", "ap", "ap_vec", "mach",
+    "total_mdot")
 FLOW_ITERATION_CONSTANTS = ("cp", "Tref", "H_formation", "relax_p", "relax_u")
 
 

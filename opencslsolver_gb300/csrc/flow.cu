@@ -1,24 +1,21 @@
 // The rest of the SIMPLE inner iteration on the device
 // (CFlow_solver::iterate, cflow_solver.cpp:229-476, and the routines of
 // cflow_solver_supply.cpp it calls), around the face-loop assembly and the
-// linear solves: boundary pressures, Green-Gauss pressure and
-// pressure-correction gradients, face mass fluxes and their correction, the
-// field updates after each solve, and the end-of-step copy
-// (update_timestep, :503-512).
+// linear solves: boundary conditions, Green-Gauss pressure and
+// pressure-correction gradients, the explicit viscous stress, face and
+// boundary mass fluxes and their correction, the field updates after each
+// solve, and the end-of-step copy (update_timestep, :503-512).
 //
 // Every kernel is owner-computes, like the assembly: a per-cell gradient is
 // one thread walking the cell's faces in ascending face order and then its
 // boundary faces (the incidence lists of ocsl_set_faces), so each component
 // is the running sum the reference's serial face loops produce, without
-// atomics; per-face and per-cell updates are one thread each.  Rounding
-// follows the reference as compiled (-ffast-math: contractions, a / 3 as
-// a * (1/3), p / R / T as p / (R T), the two mass-flux corrections
-// reassociated), and the CPU oracle (oracle/ocsl_oracle_flow.c) makes the
-// same choices, so results are bit-identical to it.
-//
-// Boundary kinds: walls, symmetry and empty faces (the shock tube's); the
-// host refuses states with inlets or outlets.  Inviscid flows only (the
-// explicit viscous stress is not formed here).
+// atomics; per-face, per-boundary-face and per-cell updates are one thread
+// each.  Rounding follows the reference as compiled (-ffast-math:
+// contractions, a / 3 as a * (1/3), p / R / T as p / (R T), the two
+// mass-flux corrections reassociated), and the CPU oracle
+// (oracle/ocsl_oracle_flow.c) makes the same choices, so results are
+// bit-identical to it.
 #include <cfloat>
 
 #include "ocsl_internal.cuh"
@@ -51,31 +48,97 @@ __device__ __forceinline__ double dot3(double a0, double a1, double a2, double b
     return fma(a2, b2, r);
 }
 
-__device__ __forceinline__ double drho_dp(double R, double gamma, double T)  // cfluid_properties.cpp:79-86
+__device__ __forceinline__ double dot3(const double* a, size_t sa, size_t ka, const double* b,
+                                       size_t sb, size_t kb)
 {
-    double r = R * T;
-    r = r * gamma;
+    return dot3(a[ka], a[sa + ka], a[2 * sa + ka], b[kb], b[sb + kb], b[2 * sb + kb]);
+}
+
+// |u|^2 in the order the compiled mag() sums it
+__device__ __forceinline__ double usq(double u0, double u1, double u2)
+{
+    return fma(u2, u2, fma(u0, u0, u1 * u1));
+}
+
+// cfluid_properties.cpp:46-51 (p / R / T under -ffast-math), :79-86, :89-96,
+// :98-106, :123-128
+__device__ __forceinline__ double density(const FlowDev& f, double p, double T)
+{
+    return p / (f.R * T);
+}
+
+__device__ __forceinline__ double drho_dp(const FlowDev& f, double T)
+{
+    double r = f.R * T;
+    r = r * f.gamma;
     return 1.0 / r;
 }
 
-// Wall faces take the cell pressure extrapolated along the cell-to-face
-// vector with the current gradient (cflow_solver.cpp:221-226).
-__global__ void bc_pressure_kernel(int n, int nb, FlowDev f)
+__device__ __forceinline__ double sound(const FlowDev& f, double T)
+{
+    return sqrt(f.R * T * f.gamma);
+}
+
+__device__ __forceinline__ double enthalpy(const FlowDev& f, double T, double u0, double u1,
+                                           double u2)
+{
+    return fma(usq(u0, u1, u2), 0.5, fma(T - f.Tref, f.cp, f.H_formation));
+}
+
+__device__ __forceinline__ double viscosity(const FlowDev& f, double T)
+{
+    return f.suth0 * (T * sqrt(T)) / (T + f.suth1);
+}
+
+// CFlow_solver::set_boundary_conditions (cflow_solver.cpp:195-227).  Outlets
+// read their density from the boundary pressure of the previous iteration and
+// then mark themselves supersonic on both branches, as the reference does.
+__global__ void set_bc_kernel(int n, int nb, FlowDev f)
 {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nb) return;
-    if (f.bc_type[g] != OCSL_BC_WALL) return;
     const int c = f.bc_left[g];
-    const double* gp = f.pressure_grad;
-    const double d = dot3(gp[c], gp[n + c], gp[2 * n + c], f.bc_unit[g], f.bc_unit[nb + g],
-                          f.bc_unit[2 * nb + g]);
-    f.bc_pressure[g] = fma(d, f.bc_distance[g], f.pressure[c]);
+    const size_t N = n, B = nb;
+    switch (f.bc_type[g]) {
+    case OCSL_BC_VELOCITY_INLET: {
+        const double v0 = f.bc_velocity[g], v1 = f.bc_velocity[B + g], v2 = f.bc_velocity[2 * B + g];
+        f.bc_pressure[g] = f.pressure[c];
+        const double rho = density(f, f.pressure[c], f.bc_temperature[g]);
+        f.bc_density[g] = rho;
+        f.bc_mdot[g] = rho * dot3(v0, v1, v2, f.bc_area_vector[g], f.bc_area_vector[B + g],
+                                  f.bc_area_vector[2 * B + g]);
+        f.bc_enthalpy[g] = enthalpy(f, f.bc_temperature[g], v0, v1, v2);
+        break;
+    }
+    case OCSL_BC_PRESSURE_OUTLET: {
+        const double u0 = f.velocity[c], u1 = f.velocity[N + c], u2 = f.velocity[2 * N + c];
+        const double T = f.temperature[c];
+        f.bc_temperature[g] = T;
+        f.bc_velocity[g] = u0;
+        f.bc_velocity[B + g] = u1;
+        f.bc_velocity[2 * B + g] = u2;
+        f.bc_density[g] = density(f, f.bc_pressure[g], T);
+        f.bc_enthalpy[g] = enthalpy(f, T, u0, u1, u2);
+        const double speed = f.bc_mdot[g] / (f.density_c[c] * f.bc_area[g]);
+        f.bc_supersonic[g] = 1;
+        f.bc_pressure[g] = speed >= sound(f, T) ? f.pressure[c] : f.bc_out_pressure[g];
+        break;
+    }
+    case OCSL_BC_WALL: {
+        const double d = dot3(f.pressure_grad, N, c, f.bc_unit, B, g);
+        f.bc_pressure[g] = fma(d, f.bc_distance[g], f.pressure[c]);
+        break;
+    }
+    default: break;  // supersonic inlets, symmetry, empty faces: nothing
+    }
 }
 
-// Green-Gauss gradient of the pressure (cflow_solver_supply.cpp:132-177,
-// face value weighted by the cells' ap) or of the pressure correction
-// (:179-220, face average), for the boundary kinds accepted here: the cell's
-// own value on every boundary face.
+// Green-Gauss gradient of the pressure (cflow_solver_supply.cpp:132-177, face
+// value weighted by the cells' ap) or of the pressure correction (:179-220,
+// face average).  Boundary faces add the cell's own value, except that
+// outlets and supersonic inlets add their boundary pressure to the pressure
+// gradient, and add nothing to the correction's unless the outlet is
+// supersonic (supersonic inlets never).
 template <bool CORR>
 __global__ void grad_kernel(int n, int nf, int nb, FlowDev f, DevFaces F)
 {
@@ -96,21 +159,61 @@ __global__ void grad_kernel(int n, int nf, int nb, FlowDev f, DevFaces F)
         }
         const double s = (ent & 1) ? -fp : fp;  // the right cell subtracts
         g0 = fma(s, f.area_vector[k], g0);
-        g1 = fma(s, f.area_vector[nf + k], g1);
-        g2 = fma(s, f.area_vector[2 * nf + k], g2);
+        g1 = fma(s, f.area_vector[(size_t)nf + k], g1);
+        g2 = fma(s, f.area_vector[2 * (size_t)nf + k], g2);
     }
     for (int e = F.bc_ptr[c]; e < F.bc_ptr[c + 1]; ++e) {
         const int k = F.bc_ent[e];
-        const double pc = v[c];
-        g0 = fma(pc, f.bc_area_vector[k], g0);
-        g1 = fma(pc, f.bc_area_vector[nb + k], g1);
-        g2 = fma(pc, f.bc_area_vector[2 * nb + k], g2);
+        const int kind = f.bc_type[k];
+        double fv = v[c];
+        if (kind == OCSL_BC_PRESSURE_OUTLET || kind == OCSL_BC_SUPERSONIC_INLET) {
+            if (!CORR) fv = f.bc_pressure[k];
+            else if (kind == OCSL_BC_SUPERSONIC_INLET || !f.bc_supersonic[k]) continue;
+        }
+        g0 = fma(fv, f.bc_area_vector[k], g0);
+        g1 = fma(fv, f.bc_area_vector[(size_t)nb + k], g1);
+        g2 = fma(fv, f.bc_area_vector[2 * (size_t)nb + k], g2);
     }
     const double inv = 1.0 / f.volume[c];
     double* out = CORR ? f.pressure_corr_grad : f.pressure_grad;
     out[c] = inv * g0;
-    out[n + c] = inv * g1;
-    out[2 * n + c] = inv * g2;
+    out[(size_t)n + c] = inv * g1;
+    out[2 * (size_t)n + c] = inv * g2;
+}
+
+// The explicit part of the viscous stress (cflow_solver_cell_face_loops.cpp:
+// 25-35, tensor.h:194-225): mu(T_f) (grad u^T - 2/3 div u I) A, the gradients
+// taken along the cell-to-cell direction; T_f is the face-loop translation
+// unit's face average.
+__global__ void stress_kernel(int n, int nf, FlowDev f)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nf) return;
+    const int L = f.left[k], R = f.right[k];
+    const size_t N = n, NF = nf;
+    double dv[3], un[3], A[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        dv[d] = f.velocity[d * N + R] - f.velocity[d * N + L];
+        un[d] = f.unit[d * NF + k];
+        A[d] = f.area_vector[d * NF + k];
+    }
+    const double dist = f.distance[k];
+    double div = dv[0] * un[0] / dist;
+    div = div + dv[1] * un[1] / dist;
+    div = div + dv[2] * un[2] / dist;
+    const double geo = f.geo_aver[k];
+    const double m = viscosity(f, fma(1.0 - geo, f.temperature[R], geo * f.temperature[L]));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double t[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[j] = dv[j] * un[i] / dist;  // transpose(grad u)
+        t[i] = fma(-(2.0 / 3.0), div, t[i]);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[j] = m * t[j];
+        f.stress[i * NF + k] = dot3(t[0], t[1], t[2], A[0], A[1], A[2]);
+    }
 }
 
 // After momentum component d's solve (cflow_solver.cpp:292-301) and its cell
@@ -159,6 +262,37 @@ __global__ void face_mdot_kernel(int n, int nf, FlowDev f, int blended)
     f.mdot[k] = m;
 }
 
+// Boundary mass fluxes (cflow_solver_supply.cpp:51-93).
+__global__ void bc_mdot_kernel(int n, int nb, FlowDev f)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nb) return;
+    const int c = f.bc_left[g];
+    const int kind = f.bc_type[g];
+    const size_t N = n, B = nb;
+    if (kind == OCSL_BC_VELOCITY_INLET) {
+        f.bc_mdot[g] = density(f, f.pressure[c], f.bc_temperature[g]) *
+                       dot3(f.bc_velocity, B, g, f.bc_area_vector, B, g);
+    } else if (kind == OCSL_BC_SUPERSONIC_INLET) {
+        f.bc_qy[g] = f.volume[c] / f.ap[c] * dot3(f.bc_alpha, B, g, f.bc_area_vector, B, g);
+    } else if (kind == OCSL_BC_PRESSURE_OUTLET) {
+        const double ua = dot3(f.velocity, N, c, f.bc_area_vector, B, g);
+        if (f.bc_supersonic[g]) {
+            f.bc_mdot[g] = density(f, f.pressure[c], f.temperature[c]) * ua;
+            f.bc_qy[g] = 1.0;
+        } else {
+            const double qy = f.volume[c] / f.ap[c] * dot3(f.bc_alpha, B, g, f.bc_area_vector, B, g);
+            const double dist = f.bc_distance[g];
+            const double t = f.bc_pressure[g] - f.pressure[c] -
+                             0.5 * dot3(f.pressure_grad[c], f.pressure_grad[N + c],
+                                        f.pressure_grad[2 * N + c], dist * f.bc_unit[g],
+                                        dist * f.bc_unit[B + g], dist * f.bc_unit[2 * B + g]);
+            f.bc_qy[g] = qy;
+            f.bc_mdot[g] = fma(-qy, t, ua) * f.bc_density[g];
+        }
+    }
+}
+
 // p' = relax_p x, p += p' (cflow_solver.cpp:352-358).
 __global__ void pcorr_kernel(int n, const double* x, FlowDev f)
 {
@@ -169,8 +303,18 @@ __global__ void pcorr_kernel(int n, const double* x, FlowDev f)
     f.pressure[c] = f.pressure[c] + pc;
 }
 
+// Boundary pressures that follow the corrected cell pressure (cflow_solver.cpp:361-372).
+__global__ void bc_pcorr_kernel(int nb, FlowDev f)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nb) return;
+    const int kind = f.bc_type[g];
+    if (kind == OCSL_BC_VELOCITY_INLET || (kind == OCSL_BC_PRESSURE_OUTLET && f.bc_supersonic[g]))
+        f.bc_pressure[g] = f.pressure[f.bc_left[g]];
+}
+
 // Mass-flux correction with the compressible term (cflow_solver_supply.cpp:95-123).
-__global__ void correct_mdot_kernel(int nf, FlowDev f, int blended, double R_specific, double gamma)
+__global__ void correct_mdot_kernel(int nf, FlowDev f, int blended)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nf) return;
@@ -182,16 +326,16 @@ __global__ void correct_mdot_kernel(int nf, FlowDev f, int blended, double R_spe
     const double rho = f.face_density[k];
     // the reference's two `Mdot +=`, reassociated: the Qy term goes in first
     const double t = fma(f.qy[k] * rho, f.pressure_corr[L] - f.pressure_corr[R], m);
-    f.mdot[k] = fma(m / rho * drho_dp(R_specific, gamma, tf), pcf, t);
+    f.mdot[k] = fma(m / rho * drho_dp(f, tf), pcf, t);
 }
 
 // Densities from the corrected pressure (cflow_solver.cpp:386-391) and the
 // velocity correction u -= relax_u vol grad(p') / ap_vec (:422-426, tensor.h:136-146).
-__global__ void correct_cells_kernel(int n, FlowDev f, double R_specific)
+__global__ void correct_cells_kernel(int n, FlowDev f)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    f.density_c[c] = f.pressure[c] / (R_specific * f.temperature[c]);  // p / R / T
+    f.density_c[c] = density(f, f.pressure[c], f.temperature[c]);
     const double s = f.relax_u * f.volume[c];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -202,25 +346,40 @@ __global__ void correct_cells_kernel(int n, FlowDev f, double R_specific)
     }
 }
 
+// Boundary faces after the correction: the subsonic outlets' mass flux
+// (cflow_solver_supply.cpp:113-123, with the density before its update) and
+// the boundary densities (cflow_solver.cpp:393-410).
+__global__ void correct_bc_kernel(int nb, FlowDev f)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nb) return;
+    const int c = f.bc_left[g];
+    const int kind = f.bc_type[g];
+    if (kind == OCSL_BC_PRESSURE_OUTLET && !f.bc_supersonic[g])
+        f.bc_mdot[g] = fma(f.bc_qy[g] * f.bc_density[g], f.pressure_corr[c], f.bc_mdot[g]);
+    if (kind == OCSL_BC_VELOCITY_INLET)
+        f.bc_density[g] = density(f, f.pressure[c], f.bc_temperature[g]);
+    else if (kind == OCSL_BC_PRESSURE_OUTLET)
+        f.bc_density[g] =
+            density(f, f.bc_supersonic[g] ? f.pressure[c] : f.bc_pressure[g], f.temperature[c]);
+}
+
 // After the enthalpy solve (cflow_solver.cpp:463-474, cfluid_properties.cpp:
-// 88-120): residual term |h - x|, h = x, T from h and |u|, Mach number.
-__global__ void enthalpy_update_kernel(int n, const double* x, FlowDev f, double* res,
-                                       double R_specific, double gamma)
+// 88-120): residual term |h - x|, h = x, T from h and |u| clamped to
+// [200, 6000], Mach = |u| / sqrt(R T gamma).
+__global__ void enthalpy_update_kernel(int n, const double* x, FlowDev f, double* res)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     res[c] = fabs(f.enthalpy[c] - x[c]);
     const double h = x[c];
     f.enthalpy[c] = h;
-    const double u0 = f.velocity[c], u1 = f.velocity[(size_t)n + c],
-                 u2 = f.velocity[2 * (size_t)n + c];
-    // |u|^2 in the order the compiled mag() sums it; |u| |u| folds to it
-    const double s = fma(u2, u2, fma(u0, u0, u1 * u1));
-    double T = f.Tref + fma(-s, 0.5, h - f.H_formation) / f.cp;
+    const double s = usq(f.velocity[c], f.velocity[(size_t)n + c], f.velocity[2 * (size_t)n + c]);
+    double T = f.Tref + fma(-s, 0.5, h - f.H_formation) / f.cp;  // |u| |u| folds to |u|^2
     if (T <= 200.0) T = 200.0;
     if (T >= 6000.0) T = 6000.0;
     f.temperature[c] = T;
-    f.mach[c] = sqrt(s) / sqrt(R_specific * T * gamma);
+    f.mach[c] = sqrt(s) / sound(f, T);
 }
 
 // update_timestep (cflow_solver.cpp:505-512).
@@ -241,9 +400,9 @@ inline int blocks(int count) { return (count + kThreads - 1) / kThreads; }
 
 }  // namespace
 
-void launch_flow_bc_pressure(cudaStream_t st, int n, int nb, const FlowDev& f)
+void launch_flow_set_bc(cudaStream_t st, int n, int nb, const FlowDev& f)
 {
-    if (nb > 0) bc_pressure_kernel<<<blocks(nb), kThreads, 0, st>>>(n, nb, f);
+    if (nb > 0) set_bc_kernel<<<blocks(nb), kThreads, 0, st>>>(n, nb, f);
 }
 
 void launch_flow_grad(cudaStream_t st, bool corr, int n, int nf, int nb, const FlowDev& f,
@@ -256,35 +415,40 @@ void launch_flow_grad(cudaStream_t st, bool corr, int n, int nf, int nb, const F
         grad_kernel<false><<<blocks(n), kThreads, 0, st>>>(n, nf, nb, f, F);
 }
 
+void launch_flow_stress(cudaStream_t st, int n, int nf, const FlowDev& f)
+{
+    if (nf > 0) stress_kernel<<<blocks(nf), kThreads, 0, st>>>(n, nf, f);
+}
+
 void launch_flow_velocity_update(cudaStream_t st, int n, int d, const double* x, const FlowDev& f,
                                  double* res)
 {
     if (n > 0) velocity_update_kernel<<<blocks(n), kThreads, 0, st>>>(n, d, x, f, res);
 }
 
-void launch_flow_face_mdot(cudaStream_t st, int n, int nf, const FlowDev& f, int blended)
+void launch_flow_face_mdot(cudaStream_t st, int n, int nf, int nb, const FlowDev& f, int blended)
 {
     if (nf > 0) face_mdot_kernel<<<blocks(nf), kThreads, 0, st>>>(n, nf, f, blended);
+    if (nb > 0) bc_mdot_kernel<<<blocks(nb), kThreads, 0, st>>>(n, nb, f);
 }
 
-void launch_flow_pcorr(cudaStream_t st, int n, const double* x, const FlowDev& f)
+void launch_flow_pcorr(cudaStream_t st, int n, int nb, const double* x, const FlowDev& f)
 {
     if (n > 0) pcorr_kernel<<<blocks(n), kThreads, 0, st>>>(n, x, f);
+    if (nb > 0) bc_pcorr_kernel<<<blocks(nb), kThreads, 0, st>>>(nb, f);
 }
 
-void launch_flow_correct(cudaStream_t st, int n, int nf, const FlowDev& f, int blended,
-                         double R_specific, double gamma)
+void launch_flow_correct(cudaStream_t st, int n, int nf, int nb, const FlowDev& f, int blended)
 {
-    if (nf > 0)
-        correct_mdot_kernel<<<blocks(nf), kThreads, 0, st>>>(nf, f, blended, R_specific, gamma);
-    if (n > 0) correct_cells_kernel<<<blocks(n), kThreads, 0, st>>>(n, f, R_specific);
+    if (nf > 0) correct_mdot_kernel<<<blocks(nf), kThreads, 0, st>>>(nf, f, blended);
+    if (n > 0) correct_cells_kernel<<<blocks(n), kThreads, 0, st>>>(n, f);
+    if (nb > 0) correct_bc_kernel<<<blocks(nb), kThreads, 0, st>>>(nb, f);
 }
 
 void launch_flow_enthalpy_update(cudaStream_t st, int n, const double* x, const FlowDev& f,
-                                 double* res, double R_specific, double gamma)
+                                 double* res)
 {
-    if (n > 0)
-        enthalpy_update_kernel<<<blocks(n), kThreads, 0, st>>>(n, x, f, res, R_specific, gamma);
+    if (n > 0) enthalpy_update_kernel<<<blocks(n), kThreads, 0, st>>>(n, x, f, res);
 }
 
 void launch_flow_end_step(cudaStream_t st, int n, const FlowDev& f)

@@ -336,29 +336,42 @@ struct FlowDev {
     double* mdot;
     double* face_density;
     double* qy;
+    double* stress;              // [3][nf], viscous flows
     // boundary faces
     const int* bc_type;
     const int* bc_left;
+    const double* bc_area;
     const double* bc_area_vector;  // [3][nb]
     const double* bc_unit;         // [3][nb]
+    const double* bc_alpha;        // [3][nb]
     const double* bc_distance;
+    const double* bc_out_pressure;
     double* bc_pressure;
+    double* bc_mdot;
+    double* bc_density;
+    double* bc_qy;
+    double* bc_enthalpy;
+    double* bc_temperature;
+    double* bc_velocity;           // [3][nb]
+    int* bc_supersonic;
     // constants
     double relax_p, relax_u, cp, Tref, H_formation;
+    double R, gamma, suth0, suth1;
 };
-void launch_flow_bc_pressure(cudaStream_t st, int n, int nb, const FlowDev& f);
+// The stages of one inner iteration (flow.cu); each launch is skipped when
+// its loop is empty.
+void launch_flow_set_bc(cudaStream_t st, int n, int nb, const FlowDev& f);
 void launch_flow_grad(cudaStream_t st, bool corr, int n, int nf, int nb, const FlowDev& f,
                       const DevFaces& F);
+void launch_flow_stress(cudaStream_t st, int n, int nf, const FlowDev& f);
 void launch_flow_velocity_update(cudaStream_t st, int n, int d, const double* x, const FlowDev& f,
                                  double* res);
-void launch_flow_face_mdot(cudaStream_t st, int n, int nf, const FlowDev& f, int blended);
-void launch_flow_pcorr(cudaStream_t st, int n, const double* x, const FlowDev& f);
-void launch_flow_correct(cudaStream_t st, int n, int nf, const FlowDev& f, int blended,
-                         double R_specific, double gamma);
+void launch_flow_face_mdot(cudaStream_t st, int n, int nf, int nb, const FlowDev& f, int blended);
+void launch_flow_pcorr(cudaStream_t st, int n, int nb, const double* x, const FlowDev& f);
+void launch_flow_correct(cudaStream_t st, int n, int nf, int nb, const FlowDev& f, int blended);
 void launch_flow_enthalpy_update(cudaStream_t st, int n, const double* x, const FlowDev& f,
-                                 double* res, double R_specific, double gamma);
+                                 double* res);
 void launch_flow_end_step(cudaStream_t st, int n, const FlowDev& f);
-// *out = sc->sum[0] (on the stream, no host round trip)
 void launch_take_sum(cudaStream_t st, const Scalars* sc, double* out);
 
 // adjoint.cu

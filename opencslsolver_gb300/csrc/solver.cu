@@ -2336,7 +2336,6 @@ static int flow_view(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state*
     int rc = check_assembly(c, q, s);
     if (rc) return rc;
     if (!it) return fail(c, OCSL_BAD_ARGUMENT, "null iteration arguments");
-    if (q->viscous) return fail(c, OCSL_BAD_ARGUMENT, "the device iteration is for inviscid flows");
     const bool nf = c->F.nf > 0, nb = c->F.nb > 0;
     for (int e : {OCSL_EQ_MOMENTUM, OCSL_EQ_PRESSURE, OCSL_EQ_ENTHALPY}) {
         ocsl_assembly qe = *q;
@@ -2350,26 +2349,30 @@ static int flow_view(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state*
         bool want;
     };
     const Need need[] = {
-        {s->density, "density", nf}, {s->qy, "qy", nf}, {s->bc_area_vector, "bc_area_vector", nb},
+        {s->density, "density", nf}, {s->qy, "qy", nf}, {s->stress, "stress", nf && q->viscous},
         {s->temperature, "temperature", true}, {s->pressure, "pressure", true},
         {s->pressure_last, "pressure_last", true},
+        {s->bc_area, "bc_area", nb}, {s->bc_area_vector, "bc_area_vector", nb},
+        {s->bc_mdot, "bc_mdot", nb}, {s->bc_density, "bc_density", nb}, {s->bc_qy, "bc_qy", nb},
+        {s->bc_enthalpy, "bc_enthalpy", nb}, {s->bc_temperature, "bc_temperature", nb},
+        {s->bc_velocity, "bc_velocity", nb}, {s->bc_supersonic, "bc_supersonic", nb},
         {it->face_area_vector, "face_area_vector", nf}, {it->face_alpha, "face_alpha", nf},
         {it->face_distance, "face_distance", nf}, {it->face_unit, "face_unit", nf},
         {it->bc_distance, "bc_distance", nb}, {it->bc_unit, "bc_unit", nb},
+        {it->bc_alpha, "bc_alpha", nb}, {it->bc_out_pressure, "bc_out_pressure", nb},
         {it->bc_pressure, "bc_pressure", nb}, {it->pressure_corr_grad, "pressure_corr_grad", true},
         {it->ap, "ap", true}, {it->ap_vec, "ap_vec", true}, {it->mach, "mach", true},
         {it->total_mdot, "total_mdot", true}};
     for (const Need& x : need)
         if (x.want && !x.p) return fail(c, OCSL_BAD_ARGUMENT, std::string(x.name) + " is NULL");
-    // boundary kinds: walls, symmetry and empty faces only (checked once per array)
+    // boundary kinds within ocsl_bc_type (checked once per array)
     if (nb && c->flow_bc_checked != s->bc_type) {
         std::vector<int32_t> kind(c->F.nb);
         CK(cudaMemcpy(kind.data(), s->bc_type, sizeof(int32_t) * kind.size(),
                       cudaMemcpyDeviceToHost));
         for (int32_t k : kind)
-            if (k != OCSL_BC_WALL && k != OCSL_BC_SYMMETRY && k != OCSL_BC_EMPTY)
-                return fail(c, OCSL_BAD_ARGUMENT,
-                            "the device iteration supports wall, symmetry and empty boundaries");
+            if (k < OCSL_BC_EMPTY || k > OCSL_BC_PRESSURE_OUTLET)
+                return fail(c, OCSL_BAD_ARGUMENT, "a boundary kind outside ocsl_bc_type");
         c->flow_bc_checked = s->bc_type;
     }
     auto w = [](const double* p) { return const_cast<double*>(p); };
@@ -2399,17 +2402,32 @@ static int flow_view(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flow_state*
     f.mdot = w(s->mdot);
     f.face_density = w(s->density);
     f.qy = w(s->qy);
+    f.stress = w(s->stress);
     f.bc_type = s->bc_type;
     f.bc_left = c->F.bc_left;
+    f.bc_area = s->bc_area;
     f.bc_area_vector = s->bc_area_vector;
     f.bc_unit = it->bc_unit;
+    f.bc_alpha = it->bc_alpha;
     f.bc_distance = it->bc_distance;
+    f.bc_out_pressure = it->bc_out_pressure;
     f.bc_pressure = it->bc_pressure;
+    f.bc_mdot = w(s->bc_mdot);
+    f.bc_density = w(s->bc_density);
+    f.bc_qy = w(s->bc_qy);
+    f.bc_enthalpy = w(s->bc_enthalpy);
+    f.bc_temperature = w(s->bc_temperature);
+    f.bc_velocity = w(s->bc_velocity);
+    f.bc_supersonic = const_cast<int*>(s->bc_supersonic);
     f.relax_p = it->relax_p;
     f.relax_u = it->relax_u;
     f.cp = it->cp;
     f.Tref = it->Tref;
     f.H_formation = it->H_formation;
+    f.R = q->R_specific;
+    f.gamma = q->gamma;
+    f.suth0 = q->sutherland[0];
+    f.suth1 = q->sutherland[1];
     return OCSL_OK;
 }
 
@@ -2433,9 +2451,10 @@ static void enqueue_flow(ocsl_ctx* c, cudaStream_t st, const ocsl_assembly* q,
     };
     ocsl_assembly qe = *q;
     // boundary conditions and the pressure gradient (:234-241)
-    launch_flow_bc_pressure(st, n, nb, f);
+    launch_flow_set_bc(st, n, nb, f);
     launch_flow_grad(st, false, n, nf, nb, f, c->F);
     CK(cudaMemsetAsync(f.ap, 0, sizeof(double) * n, st));  // :244-247
+    if (q->viscous) launch_flow_stress(st, n, nf, f);      // :250-255
     // momentum components (:257-302)
     for (int d = 0; d < 3; ++d) {
         qe.equation = OCSL_EQ_MOMENTUM;
@@ -2447,21 +2466,21 @@ static void enqueue_flow(ocsl_ctx* c, cudaStream_t st, const ocsl_assembly* q,
         residual(c->d_ftmp, d);
     }
     // face mass fluxes (:305-309), pressure correction (:316-358)
-    launch_flow_face_mdot(st, n, nf, f, q->blended);
+    launch_flow_face_mdot(st, n, nf, nb, f, q->blended);  // and the boundary faces', :312-315
     qe.equation = OCSL_EQ_PRESSURE;
     qe.dimension = 0;
     launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, it->total_mdot);
     residual(c->d_fb, 3);  // Pressure_global_residual = ABSsum(b), :346
     solve(3, methods[1]);
-    launch_flow_pcorr(st, n, c->d_fx, f);
+    launch_flow_pcorr(st, n, nb, c->d_fx, f);  // and the boundary pressures, :361-372
     // corrections (:375-426)
     launch_flow_grad(st, true, n, nf, nb, f, c->F);
-    launch_flow_correct(st, n, nf, f, q->blended, q->R_specific, q->gamma);
+    launch_flow_correct(st, n, nf, nb, f, q->blended);
     // enthalpy (:428-474)
     qe.equation = OCSL_EQ_ENTHALPY;
     launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, nullptr);
     solve(4, methods[2]);
-    launch_flow_enthalpy_update(st, n, c->d_fx, f, c->d_ftmp, q->R_specific, q->gamma);
+    launch_flow_enthalpy_update(st, n, c->d_fx, f, c->d_ftmp);
     residual(c->d_ftmp, 4);
 }
 

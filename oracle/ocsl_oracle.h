@@ -115,8 +115,15 @@ void orc_bc_value_grad(size_t n, const uint64_t* rp, int64_t nb, const int32_t* 
  * replaces solve e's result by given_x[e]; sys_* (may be NULL) receive the
  * five assembled systems (5 x nnz, 5 x n) before each solve.  Returns 0, or -1
  * for an unsupported method. */
-void orc_flow_bc_pressure(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
-                          const ocsl_flow_iteration* it);
+void orc_flow_set_bc(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_assembly* q,
+                     const ocsl_flow_state* st, const ocsl_flow_iteration* it);
+void orc_flow_stress(size_t n, int64_t nf, const int32_t* left, const int32_t* right,
+                     const ocsl_assembly* q, const ocsl_flow_state* st,
+                     const ocsl_flow_iteration* it);
+void orc_flow_bc_mdot(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_assembly* q,
+                      const ocsl_flow_state* st, const ocsl_flow_iteration* it);
+void orc_flow_bc_pcorr(int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
+                       const ocsl_flow_iteration* it);
 void orc_flow_grad(int corr, size_t n, int64_t nf, const int32_t* left, const int32_t* right,
                    int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
                    const ocsl_flow_iteration* it);
@@ -127,8 +134,8 @@ void orc_flow_face_mdot(size_t n, int64_t nf, const int32_t* left, const int32_t
 void orc_flow_pcorr(size_t n, const double* x, const ocsl_flow_state* st,
                     const ocsl_flow_iteration* it);
 void orc_flow_correct(size_t n, int64_t nf, const int32_t* left, const int32_t* right,
-                      const ocsl_assembly* q, const ocsl_flow_state* st,
-                      const ocsl_flow_iteration* it);
+                      int64_t nb, const int32_t* bc_left, const ocsl_assembly* q,
+                      const ocsl_flow_state* st, const ocsl_flow_iteration* it);
 void orc_flow_enthalpy_update(size_t n, const double* x, const ocsl_assembly* q,
                               const ocsl_flow_state* st, const ocsl_flow_iteration* it,
                               double* res);

@@ -1,8 +1,8 @@
 /* TEST INFRASTRUCTURE ONLY -- oracle restatement of the SIMPLE inner
  * iteration around the assembly and the solves: CFlow_solver::iterate
  * (cflow_solver.cpp:229-476), the routines of cflow_solver_supply.cpp it
- * calls, and update_timestep (:503-512), for an inviscid flow with wall,
- * symmetry and empty boundary faces.  Loops run in the reference's
+ * calls, and update_timestep (:503-512), for every boundary kind, inviscid
+ * or viscous, transient or steady.  Loops run in the reference's
  * single-thread order (faces ascending, boundary faces ascending, cells
  * ascending), so every gradient component is the running sum the reference
  * forms.
@@ -17,8 +17,11 @@
  * recorded solutions -- a given x per solve.
  *
  * Pinned against states the reference itself wrote before every solve and
- * after whole inner iterations of the 1000-cell shock tube
- * (tests/golden/flow_shocktube.npz, recorded by oracle/ref_flow.cpp). */
+ * after whole inner iterations of the 1000-cell shock tube and the 200-cell
+ * viscous channel and steady cases (tests/golden/flow_*.npz, recorded by
+ * oracle/ref_flow.cpp).  The 1D cases carry no transverse velocity, so the
+ * summation order inside |u|^2 and the rounding of the viscous stress (about
+ * 1e-10 of the momentum terms there) are not discriminated by them. */
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -52,23 +55,117 @@ static double dot3(const double a[3], const double b[3]) /* tensor.h:128-134 */
 
 #define W(p) ((double*)(uintptr_t)(p))
 
-/* Wall faces: p_face = p_cell + dot(grad p, unit) * distance (cflow_solver.cpp:221-226). */
-void orc_flow_bc_pressure(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
-                          const ocsl_flow_iteration* it)
+static double density(const ocsl_assembly* q, double p, double T) /* cfluid_properties.cpp:46-51 */
+{
+    return p / (q->R_specific * T); /* p / R / T under -ffast-math */
+}
+
+static double sound(const ocsl_assembly* q, double T) /* cfluid_properties.cpp:89-96 */
+{
+    return sqrt(q->R_specific * T * q->gamma);
+}
+
+static double usq(const double u[3]) /* |u|^2 in the order the compiled mag() sums it */
+{
+    return fma(u[2], u[2], fma(u[0], u[0], u[1] * u[1]));
+}
+
+static double enthalpy(const ocsl_flow_iteration* it, double T, const double u[3])
+{ /* cfluid_properties.cpp:98-106: Hf + (T - Tref) cp + |u| |u| / 2 */
+    return fma(usq(u), 0.5, fma(T - it->Tref, it->cp, it->H_formation));
+}
+
+static double mu(const ocsl_assembly* q, double T) /* cfluid_properties.cpp:123-128 */
+{
+    return q->sutherland[0] * (T * sqrt(T)) / (T + q->sutherland[1]);
+}
+
+static void vec3(const double* a, size_t stride, size_t k, double out[3])
+{
+    out[0] = a[k];
+    out[1] = a[stride + k];
+    out[2] = a[2 * stride + k];
+}
+
+/* CFlow_solver::set_boundary_conditions (cflow_solver.cpp:195-227), per
+ * boundary face.  Outlets read their density from the boundary pressure of
+ * the previous iteration and then mark themselves supersonic on both
+ * branches, as the reference does. */
+void orc_flow_set_bc(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_assembly* q,
+                     const ocsl_flow_state* st, const ocsl_flow_iteration* it)
 {
     for (int64_t g = 0; g < nb; ++g) {
-        if (st->bc_type[g] != OCSL_BC_WALL) continue;
         const int32_t c = bc_left[g];
-        const double gp[3] = {st->pressure_grad[c], st->pressure_grad[n + c],
-                              st->pressure_grad[2 * n + c]};
-        const double u[3] = {it->bc_unit[g], it->bc_unit[nb + g], it->bc_unit[2 * nb + g]};
-        it->bc_pressure[g] = fma(dot3(gp, u), it->bc_distance[g], st->pressure[c]);
+        double A[3], V[3], u[3];
+        vec3(st->bc_area_vector, (size_t)nb, (size_t)g, A);
+        switch (st->bc_type[g]) {
+        case OCSL_BC_VELOCITY_INLET:
+            vec3(st->bc_velocity, (size_t)nb, (size_t)g, V);
+            it->bc_pressure[g] = st->pressure[c];
+            W(st->bc_density)[g] = density(q, st->pressure[c], st->bc_temperature[g]);
+            W(st->bc_mdot)[g] = st->bc_density[g] * dot3(V, A);
+            W(st->bc_enthalpy)[g] = enthalpy(it, st->bc_temperature[g], V);
+            break;
+        case OCSL_BC_PRESSURE_OUTLET: {
+            vec3(st->velocity, n, (size_t)c, u);
+            W(st->bc_temperature)[g] = st->temperature[c];
+            for (int d = 0; d < 3; ++d) W(st->bc_velocity)[d * nb + g] = u[d];
+            W(st->bc_density)[g] = density(q, it->bc_pressure[g], st->temperature[c]);
+            W(st->bc_enthalpy)[g] = enthalpy(it, st->temperature[c], u);
+            const double speed = st->bc_mdot[g] / (st->density_c[c] * st->bc_area[g]);
+            ((int32_t*)(uintptr_t)st->bc_supersonic)[g] = 1;
+            it->bc_pressure[g] = speed >= sound(q, st->temperature[c]) ? st->pressure[c]
+                                                                       : it->bc_out_pressure[g];
+            break;
+        }
+        case OCSL_BC_WALL: {
+            double gp[3], un[3];
+            vec3(st->pressure_grad, n, (size_t)c, gp);
+            vec3(it->bc_unit, (size_t)nb, (size_t)g, un);
+            it->bc_pressure[g] = fma(dot3(gp, un), it->bc_distance[g], st->pressure[c]);
+            break;
+        }
+        default: break; /* supersonic inlets, symmetry, empty faces: nothing */
+        }
+    }
+}
+
+/* The explicit part of the viscous stress on the interior faces
+ * (cflow_solver_cell_face_loops.cpp:25-35, tensor.h:194-225): mu(T_f) times
+ * (grad u^T - 2/3 div u I) applied to the area vector, with the gradients
+ * taken along the cell-to-cell direction. */
+void orc_flow_stress(size_t n, int64_t nf, const int32_t* left, const int32_t* right,
+                     const ocsl_assembly* q, const ocsl_flow_state* st,
+                     const ocsl_flow_iteration* it)
+{
+    for (int64_t k = 0; k < nf; ++k) {
+        const int32_t L = left[k], R = right[k];
+        double dv[3], un[3], A[3];
+        for (int d = 0; d < 3; ++d) dv[d] = st->velocity[d * n + R] - st->velocity[d * n + L];
+        vec3(it->face_unit, (size_t)nf, (size_t)k, un);
+        vec3(it->face_area_vector, (size_t)nf, (size_t)k, A);
+        const double dist = it->face_distance[k];
+        double div = dv[0] * un[0] / dist;
+        div = div + dv[1] * un[1] / dist;
+        div = div + dv[2] * un[2] / dist;
+        const double geo = st->geo_aver[k];
+        const double m = mu(q, fma(1.0 - geo, st->temperature[R], geo * st->temperature[L]));
+        for (int i = 0; i < 3; ++i) {
+            double t[3];
+            for (int j = 0; j < 3; ++j) t[j] = dv[j] * un[i] / dist; /* transpose(grad u) */
+            t[i] = fma(-(2.0 / 3.0), div, t[i]);
+            for (int j = 0; j < 3; ++j) t[j] = m * t[j];
+            W(st->stress)[i * nf + k] = dot3(t, A);
+        }
     }
 }
 
 /* Green-Gauss gradients: the pressure with the ap-weighted face value
  * (cflow_solver_supply.cpp:132-177) or the pressure correction with the face
- * average (:179-220); wall / symmetry / empty faces add the cell's own value. */
+ * average (:179-220).  Boundary faces add the cell's own value, except that
+ * outlets and supersonic inlets add their boundary pressure to the pressure
+ * gradient, and add nothing to the correction's unless the outlet is
+ * supersonic (supersonic inlets never). */
 void orc_flow_grad(int corr, size_t n, int64_t nf, const int32_t* left, const int32_t* right,
                    int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
                    const ocsl_flow_iteration* it)
@@ -93,7 +190,13 @@ void orc_flow_grad(int corr, size_t n, int64_t nf, const int32_t* left, const in
     }
     for (int64_t q = 0; q < nb; ++q) {
         const int32_t c = bc_left[q];
-        for (int d = 0; d < 3; ++d) g[d * n + c] = fma(v[c], st->bc_area_vector[d * nb + q], g[d * n + c]);
+        const int kind = st->bc_type[q];
+        double fv = v[c];
+        if (kind == OCSL_BC_PRESSURE_OUTLET || kind == OCSL_BC_SUPERSONIC_INLET) {
+            if (!corr) fv = it->bc_pressure[q];
+            else if (kind == OCSL_BC_SUPERSONIC_INLET || !st->bc_supersonic[q]) continue;
+        }
+        for (int d = 0; d < 3; ++d) g[d * n + c] = fma(fv, st->bc_area_vector[d * nb + q], g[d * n + c]);
     }
     for (size_t c = 0; c < n; ++c) {
         const double inv = 1.0 / st->volume[c];
@@ -144,6 +247,40 @@ void orc_flow_face_mdot(size_t n, int64_t nf, const int32_t* left, const int32_t
     }
 }
 
+/* Boundary mass fluxes (cflow_solver_supply.cpp:51-93). */
+void orc_flow_bc_mdot(size_t n, int64_t nb, const int32_t* bc_left, const ocsl_assembly* q,
+                      const ocsl_flow_state* st, const ocsl_flow_iteration* it)
+{
+    for (int64_t g = 0; g < nb; ++g) {
+        const int32_t c = bc_left[g];
+        const int kind = st->bc_type[g];
+        double A[3], al[3], u[3];
+        vec3(st->bc_area_vector, (size_t)nb, (size_t)g, A);
+        vec3(it->bc_alpha, (size_t)nb, (size_t)g, al);
+        vec3(st->velocity, n, (size_t)c, u);
+        if (kind == OCSL_BC_VELOCITY_INLET) {
+            double V[3];
+            vec3(st->bc_velocity, (size_t)nb, (size_t)g, V);
+            W(st->bc_mdot)[g] = density(q, st->pressure[c], st->bc_temperature[g]) * dot3(V, A);
+        } else if (kind == OCSL_BC_SUPERSONIC_INLET) {
+            W(st->bc_qy)[g] = st->volume[c] / it->ap[c] * dot3(al, A);
+        } else if (kind == OCSL_BC_PRESSURE_OUTLET) {
+            if (st->bc_supersonic[g]) {
+                W(st->bc_mdot)[g] = density(q, st->pressure[c], st->temperature[c]) * dot3(u, A);
+                W(st->bc_qy)[g] = 1.0;
+            } else {
+                const double qy = st->volume[c] / it->ap[c] * dot3(al, A);
+                double gp[3], dv[3];
+                vec3(st->pressure_grad, n, (size_t)c, gp);
+                for (int d = 0; d < 3; ++d) dv[d] = it->bc_distance[g] * it->bc_unit[d * nb + g];
+                const double t = it->bc_pressure[g] - st->pressure[c] - 0.5 * dot3(gp, dv);
+                W(st->bc_qy)[g] = qy;
+                W(st->bc_mdot)[g] = fma(-qy, t, dot3(u, A)) * st->bc_density[g];
+            }
+        }
+    }
+}
+
 /* p' = relax_p x, p += p' (cflow_solver.cpp:352-358). */
 void orc_flow_pcorr(size_t n, const double* x, const ocsl_flow_state* st,
                     const ocsl_flow_iteration* it)
@@ -155,12 +292,25 @@ void orc_flow_pcorr(size_t n, const double* x, const ocsl_flow_state* st,
     }
 }
 
+/* Boundary pressures that follow the corrected cell pressure (cflow_solver.cpp:361-372). */
+void orc_flow_bc_pcorr(int64_t nb, const int32_t* bc_left, const ocsl_flow_state* st,
+                       const ocsl_flow_iteration* it)
+{
+    for (int64_t g = 0; g < nb; ++g) {
+        const int kind = st->bc_type[g];
+        if (kind == OCSL_BC_VELOCITY_INLET ||
+            (kind == OCSL_BC_PRESSURE_OUTLET && st->bc_supersonic[g]))
+            it->bc_pressure[g] = st->pressure[bc_left[g]];
+    }
+}
+
 /* Mass-flux correction (cflow_solver_supply.cpp:95-123), densities from the
- * corrected pressure (cflow_solver.cpp:386-391, cfluid_properties.cpp:46-51)
- * and the velocity correction (:422-426, tensor.h:136-146). */
+ * corrected pressure, cells and boundary faces (cflow_solver.cpp:386-410,
+ * cfluid_properties.cpp:46-51) and the velocity correction (:422-426,
+ * tensor.h:136-146). */
 void orc_flow_correct(size_t n, int64_t nf, const int32_t* left, const int32_t* right,
-                      const ocsl_assembly* q, const ocsl_flow_state* st,
-                      const ocsl_flow_iteration* it)
+                      int64_t nb, const int32_t* bc_left, const ocsl_assembly* q,
+                      const ocsl_flow_state* st, const ocsl_flow_iteration* it)
 {
     for (int64_t k = 0; k < nf; ++k) {
         const int32_t L = left[k], R = right[k];
@@ -177,9 +327,12 @@ void orc_flow_correct(size_t n, int64_t nf, const int32_t* left, const int32_t* 
         const double t = fma(st->qy[k] * rho, st->pressure_corr[L] - st->pressure_corr[R], m);
         W(st->mdot)[k] = fma(m / rho * dp, pcf, t);
     }
+    for (int64_t g = 0; g < nb; ++g) /* cflow_solver_supply.cpp:113-123 */
+        if (st->bc_type[g] == OCSL_BC_PRESSURE_OUTLET && !st->bc_supersonic[g])
+            W(st->bc_mdot)[g] = fma(st->bc_qy[g] * st->bc_density[g],
+                                    st->pressure_corr[bc_left[g]], st->bc_mdot[g]);
     for (size_t c = 0; c < n; ++c) {
-        /* p / R / T, which -ffast-math evaluates as p / (R T) */
-        W(st->density_c)[c] = st->pressure[c] / (q->R_specific * st->temperature[c]);
+        W(st->density_c)[c] = density(q, st->pressure[c], st->temperature[c]);
         const double s = it->relax_u * st->volume[c];
         for (int d = 0; d < 3; ++d) {
             double a = it->ap_vec[d * n + c];
@@ -187,6 +340,14 @@ void orc_flow_correct(size_t n, int64_t nf, const int32_t* left, const int32_t* 
             const double r = it->pressure_corr_grad[d * n + c] / a;
             W(st->velocity)[d * n + c] = fma(-s, r, st->velocity[d * n + c]);
         }
+    }
+    for (int64_t g = 0; g < nb; ++g) { /* cflow_solver.cpp:393-410 */
+        const int32_t c = bc_left[g];
+        if (st->bc_type[g] == OCSL_BC_VELOCITY_INLET)
+            W(st->bc_density)[g] = density(q, st->pressure[c], st->bc_temperature[g]);
+        else if (st->bc_type[g] == OCSL_BC_PRESSURE_OUTLET)
+            W(st->bc_density)[g] = density(q, st->bc_supersonic[g] ? st->pressure[c] : it->bc_pressure[g],
+                                           st->temperature[c]);
     }
 }
 
@@ -201,14 +362,14 @@ void orc_flow_enthalpy_update(size_t n, const double* x, const ocsl_assembly* q,
         res[c] = fabs(st->enthalpy[c] - x[c]);
         const double h = x[c];
         W(st->enthalpy)[c] = h;
-        const double u0 = st->velocity[c], u1 = st->velocity[n + c], u2 = st->velocity[2 * n + c];
-        /* |u|^2 in the order the compiled mag() sums it; |u| |u| folds to it */
-        const double s = fma(u2, u2, fma(u0, u0, u1 * u1));
+        double u[3];
+        vec3(st->velocity, n, c, u);
+        const double s = usq(u); /* |u| |u| folds to |u|^2 */
         double T = it->Tref + fma(-s, 0.5, h - it->H_formation) / it->cp;
         if (T <= 200.0) T = 200.0;
         if (T >= 6000.0) T = 6000.0;
         W(st->temperature)[c] = T;
-        it->mach[c] = sqrt(s) / sqrt(q->R_specific * T * q->gamma);
+        it->mach[c] = sqrt(s) / sound(q, T);
     }
 }
 
@@ -271,9 +432,10 @@ int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t 
             rc = -1;                                                                       \
     } while (0)
 
-    orc_flow_bc_pressure(n, nb, bc_left, st, it);               /* :234-237 */
+    orc_flow_set_bc(n, nb, bc_left, q, st, it);                 /* :234-237 */
     orc_flow_grad(0, n, nf, left, right, nb, bc_left, st, it);  /* :240 */
     memset(it->ap, 0, n * sizeof(double));                      /* :244-247 */
+    if (q->viscous) orc_flow_stress(n, nf, left, right, q, st, it); /* :250-255 */
     for (int d = 0; d < 3; ++d, ++slot) {                       /* :257-302 */
         qe.equation = OCSL_EQ_MOMENTUM;
         qe.dimension = d;
@@ -284,6 +446,7 @@ int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t 
         residual[d] = orc_sum(n, res, 1);
     }
     orc_flow_face_mdot(n, nf, left, right, q->blended, st, it); /* :305-309 */
+    orc_flow_bc_mdot(n, nb, bc_left, q, st, it);                /* :312-315 */
     qe.equation = OCSL_EQ_PRESSURE;                             /* :316-346 */
     qe.dimension = 0;
     orc_assemble(n, rp, col, nf, left, right, nb, bc_left, &qe, st, val, b, x, NULL,
@@ -292,8 +455,9 @@ int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t 
     SOLVE();
     ++slot;
     orc_flow_pcorr(n, x, st, it);                               /* :352-358 */
+    orc_flow_bc_pcorr(nb, bc_left, st, it);                     /* :361-372 */
     orc_flow_grad(1, n, nf, left, right, nb, bc_left, st, it);  /* :375 */
-    orc_flow_correct(n, nf, left, right, q, st, it);            /* :379-426 */
+    orc_flow_correct(n, nf, left, right, nb, bc_left, q, st, it); /* :379-426 */
     qe.equation = OCSL_EQ_ENTHALPY;                             /* :428-474 */
     orc_assemble(n, rp, col, nf, left, right, nb, bc_left, &qe, st, val, b, x, NULL, NULL);
     SOLVE();

@@ -21,6 +21,7 @@
 //                     temperatures at both ends, adiabatic sides
 // File format: repeated [u32 name length][name][u8 kind 'd'|'i'|'u'][u64 count][data].
 #include "croot.h"
+#include "flow_configs.h"
 
 #include <cstdint>
 #include <cstdio>
@@ -190,19 +191,6 @@ void record_heat(CMatrix_solver* s)
     w.d("x0", s->x_vector.value);
 }
 
-void base_1d(Cconfiguration& c, int cells)
-{
-    c.openmp_number_of_threads = 1;
-    c.eproblem_type = enums::Eproblem_type::Fluid_flow;
-    c.ematrix_solver_type = enums::Ematrix_solver_type::ILU_BICSTAB;
-    c.emesh_source = enums::Emesh_source::generate_1D;
-    c.geo_parameters_1D[0] = 1.0;
-    c.geo_parameters_1D[1] = 0.01;
-    c.geo_parameters_1D[2] = 0.01;
-    c.geo_parameters_1D[3] = cells;
-    c.set_BC_number(3);
-}
-
 }  // namespace
 
 extern "C" void __wrap__ZN14CMatrix_solver5solveEv(CMatrix_solver* self)
@@ -252,38 +240,7 @@ int main(int argc, char** argv)
         c.max_inner_iteration = 3;
     } else if (kase == "channel" || kase == "steady") {
         const bool steady = kase == "steady";
-        base_1d(c, 200);
-        c.eflow_type_visc = enums::Eflow_type_visc::Viscous;
-        c.econv_flux_type = steady ? enums::Econv_flux_type::Blended_central
-                                   : enums::Econv_flux_type::First_order_upwind;
-        c.etimestepping_type = steady ? enums::Etimestepping_type::Steady
-                                      : enums::Etimestepping_type::Transient;
-        c.global_delta_t = 1.0e-5;
-        c.implicit_underrelax = 0.5;
-        c.implicit_underrelax_max = 0.8;
-        c.underrelax_ramp_iteration = 10;
-        const double u = steady ? 700.0 : 20.0;
-        ic.einitial_condition_type = enums::Einitial_condition_type::Uniform;
-        ic.Pressure = 1.0e5;
-        ic.Temperature = 300.0;
-        ic.Velocity.val[0] = u;
-        ic.Velocity.val[1] = 0.0;
-        ic.Velocity.val[2] = 0.0;
-        auto& in = c.boundary_conditions[0];
-        in.eflow_BC_type = steady ? enums::Eflow_BC_type::supersonic_velocity_inlet
-                                  : enums::Eflow_BC_type::velocity_inlet;
-        in.Velocity.val[0] = u;
-        in.Velocity.val[1] = 0.0;
-        in.Velocity.val[2] = 0.0;
-        in.Temperature = 300.0;
-        in.Pressure = 1.0e5;
-        c.boundary_conditions[1].eflow_BC_type = enums::Eflow_BC_type::wall;
-        c.boundary_conditions[1].ewall_BC_type =
-            steady ? enums::Ewall_BC_type::slip : enums::Ewall_BC_type::no_slip;
-        c.boundary_conditions[2].eflow_BC_type = enums::Eflow_BC_type::pressure_outlet;
-        c.boundary_conditions[2].Pressure = 1.0e5;
-        c.max_iteration = steady ? 4 : 2;
-        c.max_inner_iteration = steady ? 1 : 3;
+        make_viscous_config(c, steady, steady ? 4 : 2, steady ? 1 : 3);
     } else if (kase == "heat") {
         base_1d(c, 100);
         c.eproblem_type = enums::Eproblem_type::Heat_conduction;

@@ -1,10 +1,11 @@
-// Test infrastructure only: runs the UNMODIFIED reference SIMPLE loop on the
-// 1000-cell 1D shock tube (the config of shocktube_config.h) one inner
-// iteration at a time -- CFlow_solver::iterate (cflow_solver.cpp:229-476)
+// Test infrastructure only: runs the UNMODIFIED reference SIMPLE loop one
+// inner iteration at a time -- CFlow_solver::iterate (cflow_solver.cpp:229-476)
 // and update_timestep (:503-519), the calls Croot::start_solver makes
-// (croot.cpp:119-252) -- and writes the whole flow state at chosen points, so
-// that the device SIMPLE iteration and its oracle restatement can be checked
-// against the reference's own arithmetic.
+// (croot.cpp:119-252) -- on the 1000-cell 1D shock tube (shocktube_config.h)
+// or the 200-cell viscous channel / steady cases (flow_configs.h), and writes
+// the whole flow state at chosen points, so that the device SIMPLE iteration
+// and its oracle restatement can be checked against the reference's own
+// arithmetic.
 //
 // Linked by oracle/Makefile with -Wl,--wrap=_ZN14CMatrix_solver5solveEv: the
 // wrapper picks the linear solver per equation (the reference has one global
@@ -12,7 +13,8 @@
 // writes the flow state and the assembled system right before each of the
 // five solves.
 //
-// Usage: ref_flow <out_dir> <bicg|cg> <steps> <inner> <record spec...>
+// Usage: ref_flow <out_dir> <shocktube|channel|steady> <bicg|cg> <steps> <inner>
+//                 <record spec...>
 //   bicg: every equation through ILU_BICGSTAB_solve; cg: the three momentum
 //   equations through CG_solve, p' and enthalpy through ILU_BICGSTAB_solve.
 //   A record spec "s:i" records inner iteration i of step s: the state before
@@ -21,6 +23,7 @@
 // final.bin (the state after the last step).
 // File format: repeated [u32 name length][name][u8 kind 'd'|'i'|'u'][u64 count][data].
 #include "croot.h"
+#include "flow_configs.h"
 #include "shocktube_config.h"
 
 #include <omp.h>
@@ -143,6 +146,37 @@ void write_state(Writer& w)
     w.d("residuals", {fl.Momentum_global_residual.val[0], fl.Momentum_global_residual.val[1],
                       fl.Momentum_global_residual.val[2], fl.Pressure_global_residual,
                       fl.Enthalpy_global_residual});
+    w.d("implicit_underrelaxation", {fl.implicit_underrelaxation});
+}
+
+// CFlow_solver::iterate for the configuration's three switches (croot.cpp:139-213).
+template <enums::Etimestepping_type T, enums::Eflow_type_visc V>
+void iterate_flux()
+{
+    auto& fl = *root.Flow_solver;
+    if (root.configuration->econv_flux_type == enums::Econv_flux_type::Blended_central)
+        fl.iterate<T, V, enums::Econv_flux_type::Blended_central>(root.FVM, root.Matrix_solver,
+                                                                  root.Fluid_properties);
+    else
+        fl.iterate<T, V, enums::Econv_flux_type::First_order_upwind>(root.FVM, root.Matrix_solver,
+                                                                     root.Fluid_properties);
+}
+
+template <enums::Etimestepping_type T>
+void iterate_visc()
+{
+    if (root.configuration->eflow_type_visc == enums::Eflow_type_visc::Viscous)
+        iterate_flux<T, enums::Eflow_type_visc::Viscous>();
+    else
+        iterate_flux<T, enums::Eflow_type_visc::Inviscid>();
+}
+
+void iterate_once()
+{
+    if (root.configuration->etimestepping_type == enums::Etimestepping_type::Transient)
+        iterate_visc<enums::Etimestepping_type::Transient>();
+    else
+        iterate_visc<enums::Etimestepping_type::Steady>();
 }
 
 void write_setup()
@@ -151,6 +185,12 @@ void write_setup()
     const auto& fl = *root.Flow_solver;
     const auto& fp = *root.Fluid_properties;
     Writer w(g_out + "/setup.bin");
+    const auto& cfg = *root.configuration;
+    w.i("switches", {cfg.eflow_type_visc == enums::Eflow_type_visc::Viscous ? 1 : 0,
+                     cfg.econv_flux_type == enums::Econv_flux_type::Blended_central ? 1 : 0,
+                     cfg.etimestepping_type == enums::Etimestepping_type::Transient ? 1 : 0});
+    w.d("relax_ramp", {cfg.implicit_underrelax, cfg.implicit_underrelax_max,
+                       (double)cfg.underrelax_ramp_iteration});
     w.d("fluid", {fp.R_specific, fp.gamma, fp.Sutherland_coefs[0], fp.Sutherland_coefs[1],
                   fp.Prandlt_number, fl.implicit_underrelaxation, fp.cp, fp.Tref,
                   fp.H_formation, fl.explicit_underrelaxation_P, fl.explicit_underrelaxation_u});
@@ -204,19 +244,28 @@ extern "C" void __wrap__ZN14CMatrix_solver5solveEv(CMatrix_solver* self)
 
 int main(int argc, char** argv)
 {
-    if (argc < 5) {
-        std::fprintf(stderr, "usage: ref_flow <out_dir> <bicg|cg> <steps> <inner> [s:i ...]\n");
+    if (argc < 6) {
+        std::fprintf(stderr, "usage: ref_flow <out_dir> <shocktube|channel|steady> <bicg|cg> "
+                             "<steps> <inner> [s:i ...]\n");
         return 2;
     }
     g_out = argv[1];
-    g_cg = std::strcmp(argv[2], "cg") == 0;
-    const int steps = std::atoi(argv[3]), inner = std::atoi(argv[4]);
-    for (int k = 5; k < argc; ++k) {
+    const std::string kase = argv[2];
+    g_cg = std::strcmp(argv[3], "cg") == 0;
+    const int steps = std::atoi(argv[4]), inner = std::atoi(argv[5]);
+    for (int k = 6; k < argc; ++k) {
         int s = 0, i = 0;
         if (std::sscanf(argv[k], "%d:%d", &s, &i) == 2) g_record.insert({s, i});
     }
     Cconfiguration config;
-    make_shocktube_config(config, 1, steps, inner);
+    if (kase == "shocktube") {
+        make_shocktube_config(config, 1, steps, inner);
+    } else if (kase == "channel" || kase == "steady") {
+        make_viscous_config(config, kase == "steady", steps, inner);
+    } else {
+        std::fprintf(stderr, "unknown case %s\n", kase.c_str());
+        return 2;
+    }
     root.configuration = std::make_shared<Cconfiguration>(config);
     omp_set_dynamic(0);
     omp_set_num_threads(1);
@@ -228,9 +277,7 @@ int main(int argc, char** argv)
         for (int i = 0; i < inner; ++i) {
             root.i_iteration = s;
             root.i_inner_iter = i;
-            fl.iterate<enums::Etimestepping_type::Transient, enums::Eflow_type_visc::Inviscid,
-                       enums::Econv_flux_type::Blended_central>(root.FVM, root.Matrix_solver,
-                                                                root.Fluid_properties);
+            iterate_once();
             if (g_record.count({s, i})) {
                 char name[512];
                 std::snprintf(name, sizeof name, "%s/post_%d_%d.bin", g_out.c_str(), s, i);

@@ -1,7 +1,9 @@
-"""Flow cases for the SIMPLE-iteration tests: the reference's recorded shock
-tube states (tests/golden/flow_shocktube.npz, written by
-tests/golden/make_golden.py from oracle/ref_flow.cpp's dumps) turned into the
-library's ocsl_flow_state / ocsl_flow_iteration layout."""
+"""Flow cases for the SIMPLE-iteration tests: the reference's recorded states
+of the shock tube and the viscous channel and steady cases
+(tests/golden/flow_<case>.npz, written by tests/golden/make_golden.py from
+oracle/ref_flow.cpp's dumps) turned into the library's ocsl_flow_state /
+ocsl_flow_iteration layout, and the reference's own driver logic around the
+iteration (update_timestep and its under-relaxation ramp)."""
 import os
 
 import numpy as np
@@ -28,29 +30,35 @@ STATE_FROM = {
 ARRAYS_FROM = {
     "face_area_vector": "face_area_vector", "face_alpha": "face_alpha",
     "face_distance": "face_distance", "face_unit": "face_unit", "bc_distance": "bc_distance",
-    "bc_unit": "bc_unit", "bc_pressure": "bc_pressure",
+    "bc_unit": "bc_unit", "bc_alpha": "bc_alpha", "bc_out_pressure": "bc_out_pressure",
+    "bc_pressure": "bc_pressure",
     "pressure_corr_grad": "cell_pressure_corr_grad", "ap": "cell_ap", "ap_vec": "cell_ap_vec",
     "mach": "cell_mach", "total_mdot": "cell_total_mdot",
 }
 # geometry: taken from the setup record, never changed by the iteration
 SETUP_ONLY = {"geo_aver", "ksi_A", "bc_area", "bc_area_vector", "bc_perp_dist", "bc_ksi_A",
               "volume", "face_area_vector", "face_alpha", "face_distance", "face_unit",
-              "bc_distance", "bc_unit"}
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "flow_shocktube.npz")
-# recorded inner iterations (step_iteration) of the fixture
-ITERATIONS = ("0_0", "0_1", "57_2")
-STEPS, INNER = 200, 5
+              "bc_distance", "bc_unit", "bc_alpha"}
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ("shocktube", "channel", "steady")
+# recorded inner iterations (step_iteration) of each fixture
+ITERATIONS = {"shocktube": ("0_0", "0_1", "57_2"), "channel": ("0_0", "0_1", "40_1"),
+              "steady": ("0_0", "1_0", "10_0")}
 
 # the fields one inner iteration writes (compared after it)
 WRITTEN_STATE = ("velocity", "density_c", "pressure", "pressure_grad", "pressure_corr",
-                 "temperature", "enthalpy", "mdot", "density", "qy")
+                 "temperature", "enthalpy", "mdot", "density", "qy", "stress", "bc_mdot",
+                 "bc_density", "bc_qy", "bc_enthalpy", "bc_supersonic", "bc_temperature",
+                 "bc_velocity")
 WRITTEN_ARRAYS = ("bc_pressure", "pressure_corr_grad", "ap", "ap_vec", "mach", "total_mdot")
 
 
 def make_case(setup: dict, rec: dict) -> dict:
-    """A flow case: the mesh and constants of ``setup`` with the state of
-    ``rec`` (a state record), every array a fresh contiguous copy."""
+    """A flow case: the mesh, switches and constants of ``setup`` with the
+    state of ``rec`` (a state record), every array a fresh contiguous copy."""
     fl = setup["fluid"]
+    visc, blended, transient = (int(v) for v in setup["switches"])
+    relax = float(rec["implicit_underrelaxation"][0])
     state, arrays = {}, {}
     for k, name in STATE_FROM.items():
         src = setup if k in SETUP_ONLY else rec
@@ -62,9 +70,10 @@ def make_case(setup: dict, rec: dict) -> dict:
     return {
         "row_ptr": setup["row_ptr"], "column_index": setup["column_index"],
         "left": setup["face_left"], "right": setup["face_right"], "bc_left": setup["bc_left"],
-        "eq": {"viscous": 0, "blended": 1, "transient": 1, "R_specific": fl[0], "gamma": fl[1],
-               "sutherland": (fl[2], fl[3]), "prandtl": fl[4],
-               "implicit_underrelaxation": fl[5]},
+        "eq": {"viscous": visc, "blended": blended, "transient": transient,
+               "R_specific": fl[0], "gamma": fl[1], "sutherland": (fl[2], fl[3]),
+               "prandtl": fl[4], "implicit_underrelaxation": relax},
+        "ramp": tuple(float(v) for v in setup["relax_ramp"]),
         "constants": {"cp": fl[6], "Tref": fl[7], "H_formation": fl[8], "relax_p": fl[9],
                       "relax_u": fl[10]},
         "state": state, "arrays": arrays,
@@ -84,12 +93,26 @@ def recorded(setup: dict, rec: dict) -> dict:
     return written(c)
 
 
-class Golden:
-    """tests/golden/flow_shocktube.npz, by record."""
+def end_step(case: dict, end_step_fn) -> None:
+    """The rest of CFlow_solver::update_timestep (cflow_solver.cpp:503-519)
+    after ``end_step_fn`` copied the fields to their *_last: the steady
+    under-relaxation ramp, with the reference's own arithmetic."""
+    end_step_fn(case)
+    eq = case["eq"]
+    init, top, steps = case["ramp"]
+    if not eq["transient"] and eq["implicit_underrelaxation"] < top:
+        eq["implicit_underrelaxation"] += (top - init) / steps
 
-    def __init__(self, path: str = GOLDEN):
-        z = np.load(path)
+
+class Golden:
+    """tests/golden/flow_<case>.npz, by record."""
+
+    def __init__(self, case: str = "shocktube"):
+        z = np.load(os.path.join(GOLDEN_DIR, f"flow_{case}.npz"))
+        self.name = case
         self._z = {k: z[k] for k in z.files}
+        self.steps, self.inner = (int(v) for v in self._z["run"])
+        self.iterations = ITERATIONS[case]
 
     def record(self, prefix: str) -> dict:
         p = prefix + "__"
@@ -101,6 +124,15 @@ class Golden:
 
     def start(self, tag: str) -> dict:
         return self.setup if tag == "0_0" else self.record(f"start_{tag}")
+
+    def start_case(self, tag: str, end_step_fn) -> dict:
+        """The case right before inner iteration ``tag``, with the
+        under-relaxation the reference used in it."""
+        c = self.case(self.start(tag))
+        if tag != "0_0" and int(self._z[f"endstep_{tag}"]):
+            end_step_fn(c)
+        c["eq"]["implicit_underrelaxation"] = float(self._z[f"relax_{tag}"][0])
+        return c
 
     def systems(self, tag: str) -> dict:
         return {k: self._z[f"{k}_{tag}"] for k in ("value", "b", "x0", "x")}
@@ -115,8 +147,9 @@ def relerr(got, want) -> float:
 
 
 def field_errors(got: dict, want: dict) -> dict:
-    """Max |got - want| / max |want| per field."""
-    return {k: relerr(got[k], want[k]) for k in want}
+    """Max |got - want| / max |want| per field (the supersonic flags exactly)."""
+    return {k: (float(not np.array_equal(got[k], want[k])) if k == "bc_supersonic"
+                else relerr(got[k], want[k])) for k in want}
 
 
 class DeviceCase:
@@ -143,7 +176,7 @@ class DeviceCase:
                                        self.case["constants"], methods, **opts)
 
     def end_step(self, ctx) -> None:
-        ctx.flow_end_step_device(self.state)
+        end_step(self.case, lambda c: ctx.flow_end_step_device(self.state))
 
     def written(self) -> dict:
         out = {k: self.state[k].cpu().numpy() for k in WRITTEN_STATE}

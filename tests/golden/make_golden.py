@@ -22,17 +22,19 @@ then writes:
 * small_systems.npz -- seeded small systems in the reference layout with the
   reference's gemv, ILU_decompose, ILU_forsub/backsub, CG_solve and
   ILU_BICGSTAB_solve outputs;
-* flow_shocktube.npz -- the reference's SIMPLE loop on the same shock tube,
-  recorded by oracle/ref_flow.cpp one inner iteration at a time: the setup
-  (mesh metrics, fluid constants, initial state; keys setup__*), for the inner
-  iterations 0:0, 0:1 and 57:2 (step:iteration) of the run with every
-  equation through ILU_BICGSTAB_solve the state before the iteration
-  (start_<tag>__*, 0:0 starts from the setup), the five assembled systems and
-  the reference's solutions (value_<tag>, b_<tag>, x0_<tag>, x_<tag>) and the
-  state after it (post_<tag>__*), and the final state after 200 steps x 5
-  inner iterations with every equation through ILU_BICGSTAB_solve
-  (final_bicg__*) and with the momentum equations through CG_solve
-  (final_cg__*);
+* flow_<case>.npz -- the reference's SIMPLE loop, recorded by
+  oracle/ref_flow.cpp one inner iteration at a time, on the shock tube
+  (200 steps x 5 inner iterations), the 200-cell viscous channel (100 x 3)
+  and the 200-cell viscous steady case (60 x 1) of FLOW_CASES: the setup
+  (mesh metrics, fluid constants, switches, initial state; keys setup__*);
+  for three recorded inner iterations of the run with every equation through
+  ILU_BICGSTAB_solve, the state before the iteration (start_<tag>__*, with
+  endstep_<tag> when the step's update_timestep comes first; the first
+  starts from the setup), the five assembled systems and the reference's
+  solutions (value_<tag>, b_<tag>, x0_<tag>, x_<tag>), the under-relaxation
+  in force (relax_<tag>) and the state after it (post_<tag>__*); the final
+  state of that run (final_bicg__*) and, for the shock tube, of the run with
+  the momentum equations through CG_solve (final_cg__*);
 * assembly_<case>.npz -- the inputs (cell / face state) and outputs (matrix
   values, b, x0, ap_vec, total_mdot) of the reference's face-loop assembly,
   recorded by oracle/ref_assembly.cpp right before the 5 solve calls of one
@@ -203,35 +205,57 @@ def make_assembly(out_dir):
         np.savez_compressed(os.path.join(out_dir, f"assembly_{case}.npz"), **arrays)
 
 
-# (start record, recorded iteration) of the flow fixture; "setup" = initial state
-FLOW_ITERATIONS = [("setup", "0_0"), ("post_0_0", "0_1"), ("post_57_1", "57_2")]
+# The flow fixtures: run length, recorded inner iterations (tag "s_i" =
+# step s, inner iteration i) with the record they start from ("setup" = the
+# initial state; a start from the previous step's last inner iteration needs
+# that step's update_timestep applied first), and whether the run with CG for
+# the momentum equations is recorded too.
+FLOW_CASES = {
+    "shocktube": {"steps": 200, "inner": 5, "cg": True,
+                  "iterations": [("setup", "0_0"), ("post_0_0", "0_1"), ("post_57_1", "57_2")]},
+    "channel": {"steps": 100, "inner": 3, "cg": False,
+                "iterations": [("setup", "0_0"), ("post_0_0", "0_1"), ("post_40_0", "40_1")]},
+    "steady": {"steps": 60, "inner": 1, "cg": False,
+               "iterations": [("setup", "0_0"), ("post_0_0", "1_0"), ("post_9_0", "10_0")]},
+}
 
 
-def make_flow(path):
+def make_flow(out_dir, case):
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_flow")
-    arrays = {}
+    spec = FLOW_CASES[case]
+    steps, inner = str(spec["steps"]), str(spec["inner"])
+    arrays = {"run": np.array([spec["steps"], spec["inner"]])}
+    starts = [st for st, _ in spec["iterations"] if st != "setup"]
+    tags = [tag for _, tag in spec["iterations"]]
+    want = sorted({t.replace("_", ":") for t in tags} |
+                  {st[len("post_"):].replace("_", ":") for st in starts})
     with tempfile.TemporaryDirectory() as d:
-        subprocess.run([exe, d, "bicg", "200", "5", "0:0", "0:1", "57:1", "57:2"], cwd=d,
-                       check=True, stdout=subprocess.DEVNULL)
+        subprocess.run([exe, d, case, "bicg", steps, inner] + want, cwd=d, check=True,
+                       stdout=subprocess.DEVNULL)
         rec = lambda name: read_named_arrays(os.path.join(d, name + ".bin"))  # noqa: E731
         for k, v in rec("setup").items():
             arrays[f"setup__{k}"] = v
-        for start, tag in FLOW_ITERATIONS:
+        for start, tag in spec["iterations"]:
             if start != "setup":
                 for k, v in rec(start).items():
                     arrays[f"start_{tag}__{k}"] = v
+                s0, i0 = (int(x) for x in tag.split("_"))
+                arrays[f"endstep_{tag}"] = np.array(int(i0 == 0 and s0 > 0))
             for k, v in rec(f"post_{tag}").items():
                 arrays[f"post_{tag}__{k}"] = v
             pre = [rec(f"pre_{tag}_{e}") for e in range(5)]
             for key in ("value", "b", "x0", "x"):
                 arrays[f"{key}_{tag}"] = np.stack([p[key] for p in pre])
+            arrays[f"relax_{tag}"] = pre[0]["implicit_underrelaxation"]
         for k, v in rec("final").items():
             arrays[f"final_bicg__{k}"] = v
-    with tempfile.TemporaryDirectory() as d:
-        subprocess.run([exe, d, "cg", "200", "5"], cwd=d, check=True, stdout=subprocess.DEVNULL)
-        for k, v in read_named_arrays(os.path.join(d, "final.bin")).items():
-            arrays[f"final_cg__{k}"] = v
-    np.savez_compressed(path, **arrays)
+    if spec["cg"]:
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.run([exe, d, case, "cg", steps, inner], cwd=d, check=True,
+                           stdout=subprocess.DEVNULL)
+            for k, v in read_named_arrays(os.path.join(d, "final.bin")).items():
+                arrays[f"final_cg__{k}"] = v
+    np.savez_compressed(os.path.join(out_dir, f"flow_{case}.npz"), **arrays)
 
 
 def main():
@@ -253,7 +277,8 @@ def main():
     if want("assembly"):
         make_assembly(HERE)
     if want("flow"):
-        make_flow(os.path.join(HERE, "flow_shocktube.npz"))
+        for case in FLOW_CASES:
+            make_flow(HERE, case)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
