@@ -18,6 +18,12 @@ during the timed region, and the reference algorithm's CPU rate on the host
 cores (the oracle's OpenMP port of ILU_BICGSTAB_solve; the reference itself
 cannot reach 1e-10, so a reference "solve" is its own fixed 3-iteration call).
 
+Also on rank 0 (`simple_iteration`): the reference's own CPU-runnable case end
+to end -- the 1000-cell shock tube's 200 steps x 5 SIMPLE inner iterations as
+device iterations (one CUDA graph each), their time per inner iteration, the
+final fields against the reference's recorded ones, and the oracle's C
+restatement of the same iteration timed on one host core.
+
 `--impl reference` times only that CPU implementation (rank 0).  Multi-GPU:
 independent replicas, one per rank, no collective on the data path.
 """
@@ -219,6 +225,68 @@ def run_reference(args):
     return 0
 
 
+def simple_iteration(torch, dev, cpu_inner=50):
+    """The reference's own CPU-runnable case end to end: the 1000-cell shock
+    tube (200 steps x 5 inner iterations, momentum through CG_solve, p' and
+    enthalpy through ILU_BICGSTAB_solve) as ocsl_flow_iterate_device calls,
+    one CUDA graph per inner iteration, from the reference's recorded initial
+    state; the final fields against the reference's recorded ones; and the
+    oracle's C restatement of the same iteration on one host core for a
+    bounded number of inner iterations."""
+    import opencslsolver_gb300 as ocsl
+    from oracle import oracle as orc
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import flow_cases as FC
+
+    g = FC.Golden("shocktube")
+    methods = (ocsl.CG_REF, ocsl.BICGSTAB_REF, ocsl.BICGSTAB_REF)
+    ctx = ocsl.Context(dev.index)
+    try:
+        case = FC.DeviceCase(torch, g.case())
+        case.bind(ctx)
+        stream = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(g.steps):
+            for _ in range(g.inner):
+                rep = case.iterate(ctx, methods)
+                assert rep["status"] == [0] * 5, rep
+            case.end_step(ctx)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        iters = g.steps * g.inner
+        errs = FC.field_errors(case.written(), FC.recorded(g.setup, g.record("final_cg")))
+    finally:
+        ctx.close()
+    # the oracle's restatement on one host core, a bounded sample from the start
+    cpu_case = g.case()
+    orc.Oracle().set_threads(1)
+    t0 = time.perf_counter()
+    for k in range(cpu_inner):
+        orc.flow_iterate(cpu_case, methods)
+        if k % g.inner == g.inner - 1:
+            FC.end_step(cpu_case, orc.flow_end_step)
+    cpu_ms = 1000.0 * (time.perf_counter() - t0) / cpu_inner
+    return {
+        "workload": "1D shock tube, 1000 cells, 200 steps x 5 inner iterations, momentum "
+                    "CG_solve, p' and enthalpy ILU_BICGSTAB_solve (reference-faithful)",
+        "gpu_ms_per_inner_iteration": 1000.0 * wall / iters,
+        "gpu_event_ms_per_inner_iteration": e0.elapsed_time(e1) / iters,
+        "cpu_port_ms_per_inner_iteration": cpu_ms,
+        "cpu_port": f"oracle C restatement of the same iteration, 1 core, first {cpu_inner} "
+                    "inner iterations",
+        "max_rel_err_vs_reference": {"state": max(errs[k] for k in
+                                                  ("velocity", "pressure", "temperature",
+                                                   "density_c", "enthalpy")),
+                                     "all_fields": max(errs.values())},
+        "graph": "one CUDA graph per inner iteration (captured on the second call)",
+    }
+
+
 def run_ours(args):
     import torch
 
@@ -365,6 +433,9 @@ def run_ours(args):
     # the same launch sequence, without graph replay)
     gpu_launches = sum(v["launches"] for v in per_cat.values())
 
+    # ---- the reference's CPU-runnable case (1000-cell shock tube) end to end
+    simple = simple_iteration(torch, dev) if rank == 0 else None
+
     # ---- CPU baseline: reference algorithm, bounded sample, rank 0
     cpu = None
     if rank == 0:
@@ -408,6 +479,7 @@ def run_ours(args):
                         "autotune": round(t_tune, 3)},
             "sweep_kernel": dict(ctx.sweep_info(), autotuned_pair_us=round(tune["sweep_us"], 1),
                                  autotuned_pair_us_f64=round(tune64["sweep_us"], 1)),
+            "simple_iteration": simple,
         }
         print(json.dumps(line))
     ctx.close()
