@@ -577,3 +577,73 @@ def batch_systems(count: int = 64, *, seed: int = BASE_SEED + 40, min_cells: int
         rhs = np.random.default_rng(seed + 100 * k + 60).uniform(-1.0, 1.0, size=(3, m.n))
         out.append(BatchSystem(m, rhs, "momentum"))
     return out
+
+
+def write_su2_box(path: str, nx: int, ny: int, nz: int, *, lengths=(1.0, 0.2, 0.1),
+                  jitter: float = 0.1, seed: int = BASE_SEED + 70, cells: str = "hex") -> dict:
+    """Write a seeded nx*ny*nz box mesh in SU2 ASCII (the format the reference
+    reads, cgeometry_supply.h:201-433): interior nodes jittered by +-jitter
+    of the spacing, hexahedra (type 12) or each hex split into 6 Kuhn tetrahedra
+    (type 10), three markers in this order -- "inlet" (x = 0), "walls" (the four
+    sides), "outlet" (x = lengths[0]) -- as quads (type 9) or triangles (type 5).
+    Returns the counts."""
+    rng = np.random.default_rng(seed)
+    P = _jittered_nodes(nx, ny, nz, rng, jitter) * np.asarray(lengths, float)
+    nid = np.arange((nx + 1) * (ny + 1) * (nz + 1)).reshape(nx + 1, ny + 1, nz + 1)
+    X = P.reshape(-1, 3)
+    h = np.arange(nx * ny * nz)
+    hi, hj, hk = h % nx, (h // nx) % ny, h // (nx * ny)
+    corner = np.empty((h.size, 8), np.int64)  # lexicographic corners: bit 0 x, 1 y, 2 z
+    for cid in range(8):
+        corner[:, cid] = nid[hi + (cid & 1), hj + ((cid >> 1) & 1), hk + ((cid >> 2) & 1)]
+    if cells == "hex":
+        vtk = corner[:, [0, 1, 3, 2, 4, 5, 7, 6]]  # SU2 / VTK hexahedron order
+        elems = [(12, row) for row in vtk]
+    elif cells == "tet":
+        elems = [(10, row) for row in corner[:, _kuhn_tets()].reshape(-1, 4)]
+    else:
+        raise ValueError(cells)
+
+    def quads(fixed_axis, value):
+        out = []
+        dims = [nx, ny, nz]
+        a, b = [ax for ax in range(3) if ax != fixed_axis]
+        for u in range(dims[a]):
+            for v in range(dims[b]):
+                idx = [0, 0, 0]
+                idx[fixed_axis] = value
+                c = []
+                for du, dv in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                    idx[a], idx[b] = u + du, v + dv
+                    c.append(nid[tuple(idx)])
+                out.append(c)
+        return out
+
+    markers = {"inlet": quads(0, 0),
+               "walls": quads(1, 0) + quads(1, ny) + quads(2, 0) + quads(2, nz),
+               "outlet": quads(0, nx)}
+    with open(path, "w") as f:
+        f.write("NDIME= 3\n")
+        f.write(f"NELEM= {len(elems)}\n")
+        for k, (t, row) in enumerate(elems):
+            f.write(f"{t} " + " ".join(str(int(v)) for v in row) + f" {k}\n")
+        f.write(f"NPOIN= {X.shape[0]}\n")
+        for k, p in enumerate(X):
+            f.write(f"{p[0]:.17g} {p[1]:.17g} {p[2]:.17g} {k}\n")
+        f.write(f"NMARK= {len(markers)}\n")
+        for name, faces in markers.items():
+            f.write(f"MARKER_TAG= {name}\n")
+            if cells == "hex":
+                f.write(f"MARKER_ELEMS= {len(faces)}\n")
+                for q in faces:
+                    f.write("9 " + " ".join(str(int(v)) for v in q) + "\n")
+            else:  # the two triangles the Kuhn split puts on each boundary quad
+                tris = []
+                for q in faces:
+                    a, b, c, d = q
+                    lo = min(q)  # the split diagonal runs through the lowest node id
+                    tris += [(a, b, c), (a, c, d)] if lo in (a, c) else [(a, b, d), (b, c, d)]
+                f.write(f"MARKER_ELEMS= {len(tris)}\n")
+                for t3 in tris:
+                    f.write("5 " + " ".join(str(int(v)) for v in t3) + "\n")
+    return {"cells": len(elems), "nodes": X.shape[0]}

@@ -64,3 +64,44 @@ inline void make_viscous_config(Cconfiguration& c, bool steady, int steps, int i
     c.max_iteration = steps;
     c.max_inner_iteration = inner;
 }
+
+// box3d:   a mesh read from an SU2 file (markers: inlet, walls, outlet, in this
+//          order), viscous, blended, transient (dt 2e-6 s): velocity inlet
+//          (20, 3, 2) m/s at 300 K, no-slip walls, pressure outlet (1e5 Pa);
+//          uniform start (20, 0, 0) m/s, 300 K, 1e5 Pa.
+inline void make_box3d_config(Cconfiguration& c, const std::string& mesh, int steps, int inner)
+{
+    auto& ic = *c.inital_condition;
+    c.openmp_number_of_threads = 1;
+    c.eproblem_type = enums::Eproblem_type::Fluid_flow;
+    c.ematrix_solver_type = enums::Ematrix_solver_type::ILU_BICSTAB;
+    c.emesh_source = enums::Emesh_source::from_file;
+    c.mesh_filename = mesh;
+    c.set_BC_number(3);
+    c.eflow_type_visc = enums::Eflow_type_visc::Viscous;
+    c.econv_flux_type = enums::Econv_flux_type::Blended_central;
+    c.etimestepping_type = enums::Etimestepping_type::Transient;
+    c.global_delta_t = 2.0e-6;
+    c.implicit_underrelax = 0.5;
+    c.implicit_underrelax_max = 0.8;
+    c.underrelax_ramp_iteration = 10;
+    ic.einitial_condition_type = enums::Einitial_condition_type::Uniform;
+    ic.Pressure = 1.0e5;
+    ic.Temperature = 300.0;
+    ic.Velocity.val[0] = 20.0;
+    ic.Velocity.val[1] = 0.0;
+    ic.Velocity.val[2] = 0.0;
+    auto& in = c.boundary_conditions[0];
+    in.eflow_BC_type = enums::Eflow_BC_type::velocity_inlet;
+    in.Velocity.val[0] = 20.0;
+    in.Velocity.val[1] = 3.0;
+    in.Velocity.val[2] = 2.0;
+    in.Temperature = 300.0;
+    in.Pressure = 1.0e5;
+    c.boundary_conditions[1].eflow_BC_type = enums::Eflow_BC_type::wall;
+    c.boundary_conditions[1].ewall_BC_type = enums::Ewall_BC_type::no_slip;
+    c.boundary_conditions[2].eflow_BC_type = enums::Eflow_BC_type::pressure_outlet;
+    c.boundary_conditions[2].Pressure = 1.0e5;
+    c.max_iteration = steps;
+    c.max_inner_iteration = inner;
+}

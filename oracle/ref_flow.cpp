@@ -1,8 +1,9 @@
 // Test infrastructure only: runs the UNMODIFIED reference SIMPLE loop one
 // inner iteration at a time -- CFlow_solver::iterate (cflow_solver.cpp:229-476)
 // and update_timestep (:503-519), the calls Croot::start_solver makes
-// (croot.cpp:119-252) -- on the 1000-cell 1D shock tube (shocktube_config.h)
-// or the 200-cell viscous channel / steady cases (flow_configs.h), and writes
+// (croot.cpp:119-252) -- on the 1000-cell 1D shock tube (shocktube_config.h),
+// the 200-cell viscous channel / steady cases or a 3D viscous channel on a mesh
+// read from an SU2 file (flow_configs.h), and writes
 // the whole flow state at chosen points, so that the device SIMPLE iteration
 // and its oracle restatement can be checked against the reference's own
 // arithmetic.
@@ -13,8 +14,8 @@
 // writes the flow state and the assembled system right before each of the
 // five solves.
 //
-// Usage: ref_flow <out_dir> <shocktube|channel|steady> <bicg|cg> <steps> <inner>
-//                 <record spec...>
+// Usage: ref_flow <out_dir> <shocktube|channel|steady|box3d=<mesh.su2>> <bicg|cg> <steps>
+//                 <inner> <record spec...>
 //   bicg: every equation through ILU_BICGSTAB_solve; cg: the three momentum
 //   equations through CG_solve, p' and enthalpy through ILU_BICGSTAB_solve.
 //   A record spec "s:i" records inner iteration i of step s: the state before
@@ -262,6 +263,8 @@ int main(int argc, char** argv)
         make_shocktube_config(config, 1, steps, inner);
     } else if (kase == "channel" || kase == "steady") {
         make_viscous_config(config, kase == "steady", steps, inner);
+    } else if (kase.rfind("box3d=", 0) == 0) {
+        make_box3d_config(config, kase.substr(6), steps, inner);
     } else {
         std::fprintf(stderr, "unknown case %s\n", kase.c_str());
         return 2;

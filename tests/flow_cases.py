@@ -1,5 +1,6 @@
 """Flow cases for the SIMPLE-iteration tests: the reference's recorded states
-of the shock tube and the viscous channel and steady cases
+of the shock tube, the viscous channel and steady cases and a 3D viscous
+channel on an SU2 hex mesh
 (tests/golden/flow_<case>.npz, written by tests/golden/make_golden.py from
 oracle/ref_flow.cpp's dumps) turned into the library's ocsl_flow_state /
 ocsl_flow_iteration layout, and the reference's own driver logic around the
@@ -40,10 +41,10 @@ SETUP_ONLY = {"geo_aver", "ksi_A", "bc_area", "bc_area_vector", "bc_perp_dist", 
               "volume", "face_area_vector", "face_alpha", "face_distance", "face_unit",
               "bc_distance", "bc_unit", "bc_alpha"}
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("shocktube", "channel", "steady")
+CASES = ("shocktube", "channel", "steady", "box3d")
 # recorded inner iterations (step_iteration) of each fixture
 ITERATIONS = {"shocktube": ("0_0", "0_1", "57_2"), "channel": ("0_0", "0_1", "40_1"),
-              "steady": ("0_0", "1_0", "10_0")}
+              "steady": ("0_0", "1_0", "10_0"), "box3d": ("0_0", "0_1", "20_1")}
 
 # the fields one inner iteration writes (compared after it)
 WRITTEN_STATE = ("velocity", "density_c", "pressure", "pressure_grad", "pressure_corr",

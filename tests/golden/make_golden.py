@@ -24,8 +24,9 @@ then writes:
   ILU_BICGSTAB_solve outputs;
 * flow_<case>.npz -- the reference's SIMPLE loop, recorded by
   oracle/ref_flow.cpp one inner iteration at a time, on the shock tube
-  (200 steps x 5 inner iterations), the 200-cell viscous channel (100 x 3)
-  and the 200-cell viscous steady case (60 x 1) of FLOW_CASES: the setup
+  (200 steps x 5 inner iterations), the 200-cell viscous channel (100 x 3),
+  the 200-cell viscous steady case (60 x 1) and a 3D viscous channel on a
+  240-cell jittered hex mesh read from an SU2 file (40 x 3) of FLOW_CASES: the setup
   (mesh metrics, fluid constants, switches, initial state; keys setup__*);
   for three recorded inner iterations of the run with every equation through
   ILU_BICGSTAB_solve, the state before the iteration (start_<tag>__*, with
@@ -217,7 +218,12 @@ FLOW_CASES = {
                 "iterations": [("setup", "0_0"), ("post_0_0", "0_1"), ("post_40_0", "40_1")]},
     "steady": {"steps": 60, "inner": 1, "cg": False,
                "iterations": [("setup", "0_0"), ("post_0_0", "1_0"), ("post_9_0", "10_0")]},
+    # 3D viscous channel on a 10 x 6 x 4 jittered hex mesh the reference reads
+    # from an SU2 file (workloads.write_su2_box with BOX3D_MESH)
+    "box3d": {"steps": 40, "inner": 3, "cg": False,
+              "iterations": [("setup", "0_0"), ("post_0_0", "0_1"), ("post_20_0", "20_1")]},
 }
+BOX3D_MESH = {"nx": 10, "ny": 6, "nz": 4, "lengths": (1.0, 0.2, 0.1), "jitter": 0.1}
 
 
 def make_flow(out_dir, case):
@@ -230,7 +236,14 @@ def make_flow(out_dir, case):
     want = sorted({t.replace("_", ":") for t in tags} |
                   {st[len("post_"):].replace("_", ":") for st in starts})
     with tempfile.TemporaryDirectory() as d:
-        subprocess.run([exe, d, case, "bicg", steps, inner] + want, cwd=d, check=True,
+        arg = case
+        if case == "box3d":
+            mesh = os.path.join(d, "box3d.su2")
+            m = dict(BOX3D_MESH)
+            W.write_su2_box(mesh, m.pop("nx"), m.pop("ny"), m.pop("nz"), **m)
+            arg = f"box3d={mesh}"
+            arrays["mesh"] = np.array([BOX3D_MESH["nx"], BOX3D_MESH["ny"], BOX3D_MESH["nz"]])
+        subprocess.run([exe, d, arg, "bicg", steps, inner] + want, cwd=d, check=True,
                        stdout=subprocess.DEVNULL)
         rec = lambda name: read_named_arrays(os.path.join(d, name + ".bin"))  # noqa: E731
         for k, v in rec("setup").items():

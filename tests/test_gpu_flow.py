@@ -1,8 +1,9 @@
 """The SIMPLE inner iteration on the device (ocsl_flow_iterate_device) on the
 reference's recorded runs (tests/golden/flow_<case>.npz): the 1000-cell
-inviscid shock tube and the 200-cell viscous channel (velocity inlet,
-no-slip walls, pressure outlet) and steady (supersonic inlet, slip walls,
-outlet, implicit under-relaxation ramp) cases.
+inviscid shock tube, the 200-cell viscous channel (velocity inlet, no-slip
+walls, pressure outlet) and steady (supersonic inlet, slip walls, outlet,
+implicit under-relaxation ramp) cases, and a 3D viscous channel on a
+240-cell jittered hex mesh read by the reference from an SU2 file.
 
 * Bit-exact to the oracle restatement, inner iteration by inner iteration
   (every field the iteration writes, the residual sums and the solves'
@@ -64,7 +65,8 @@ def _same(got: dict, want: dict, where):
 
 @pytest.mark.parametrize("case,mode", [("shocktube", "bicg"), ("shocktube", "cg"),
                                        ("shocktube", "tol"), ("channel", "bicg"),
-                                       ("channel", "tol"), ("steady", "bicg"), ("steady", "tol")])
+                                       ("channel", "tol"), ("steady", "bicg"), ("steady", "tol"),
+                                       ("box3d", "bicg"), ("box3d", "cg"), ("box3d", "tol")])
 def test_iteration_bit_exact_vs_oracle(ctx, torch_cuda, case, mode):
     g = golden(case)
     c = g.case()
@@ -88,7 +90,8 @@ def test_iteration_bit_exact_vs_oracle(ctx, torch_cuda, case, mode):
 @pytest.mark.parametrize("case,mode", [("shocktube", "bicg"), ("shocktube", "cg"),
                                        ("shocktube", "tol"), ("shocktube", "ir32"),
                                        ("channel", "bicg"), ("channel", "tol"),
-                                       ("steady", "bicg"), ("steady", "ir32")])
+                                       ("steady", "bicg"), ("steady", "ir32"),
+                                       ("box3d", "bicg"), ("box3d", "tol")])
 def test_recorded_run_vs_reference(ctx, torch_cuda, case, mode):
     g = golden(case)
     dev = FC.DeviceCase(torch_cuda, g.case())

@@ -3,7 +3,9 @@ reference's own recorded runs (tests/golden/flow_<case>.npz): the 1000-cell
 inviscid shock tube (walls, empty sides), the 200-cell viscous channel
 (velocity inlet, no-slip walls, pressure outlet; transient, upwind) and the
 200-cell viscous steady case (supersonic inlet, slip walls, pressure outlet;
-implicit under-relaxation ramp, blended).
+implicit under-relaxation ramp, blended) and a 3D viscous channel on a
+240-cell jittered hex mesh the reference read from an SU2 file (velocity
+inlet with transverse components, no-slip walls, outlet; blended).
 
 * Stages: each recorded inner iteration is replayed from the reference's
   state before it, with the reference's own solutions in place of the five
@@ -64,7 +66,8 @@ def test_oracle_iteration_stages_match_reference(oracle, case, tag):
 
 
 @pytest.mark.parametrize("case,mode", [("shocktube", "bicg"), ("shocktube", "cg"),
-                                       ("channel", "bicg"), ("steady", "bicg")])
+                                       ("channel", "bicg"), ("steady", "bicg"),
+                                       ("box3d", "bicg")])
 def test_oracle_trajectory_matches_reference(oracle, case, mode):
     g = golden(case)
     c = g.case()
