@@ -384,6 +384,51 @@ int ocsl_flow_iterate_device(ocsl_ctx* ctx, const ocsl_assembly* eq,
  * velocity, density, pressure and enthalpy are copied to their *_last fields. */
 int ocsl_flow_end_step_device(ocsl_ctx* ctx, const ocsl_flow_state* state);
 
+/* ------------------------------------------------------------------------
+ * Mesh input: an SU2 ASCII mesh (tetrahedra, hexahedra, wedges; triangle and
+ * quadrilateral boundary markers), read and turned into the finite-volume
+ * arrays the reference builds in Read_SU2_mesh (cgeometry_supply.h:201-433),
+ * Cgeometry (cgeometry.cpp) and CFVM::create_FVM_from_geometry
+ * (cfvm.cpp:100-175), with the reference's face and boundary-face numbering,
+ * in O(cells + faces) on the host (the reference's connectivity search is
+ * quadratic around every node).  Vectors are [3][count].  The arrays feed
+ * ocsl_build_pattern / ocsl_set_faces and the state structs above; they stay
+ * owned by the mesh object.
+ * ---------------------------------------------------------------------- */
+typedef struct ocsl_mesh ocsl_mesh;
+typedef struct {
+    int64_t n_cells, n_faces, n_bc;
+    int32_t n_markers;
+    /* interior faces (CFVM_face) */
+    const int32_t* face_left;
+    const int32_t* face_right;
+    const double* face_geo_aver;
+    const double* face_ksi_A;        /* diffusion_ksi_A                         */
+    const double* face_area_vector;
+    const double* face_alpha;
+    const double* face_distance;     /* cell_center_distance                    */
+    const double* face_unit;         /* cell_center_unit_vector                 */
+    /* boundary faces (CFVM_BC_face), marker by marker in file order */
+    const int32_t* bc_left;
+    const int32_t* bc_marker;        /* marker index (the configuration's BC)   */
+    const double* bc_area;
+    const double* bc_area_vector;
+    const double* bc_alpha;
+    const double* bc_distance;
+    const double* bc_unit;
+    const double* bc_perp_dist;
+    const double* bc_ksi_A;
+    /* cells (CFVM_cell, Cgeo_cell) */
+    const double* cell_volume;
+    const double* cell_center;
+} ocsl_mesh_arrays;
+/* OCSL_BAD_ARGUMENT with the reason in err (may be NULL) on a file the reader
+ * cannot take. */
+int ocsl_mesh_read_su2(const char* path, ocsl_mesh** mesh, char* err, size_t err_len);
+int ocsl_mesh_view(const ocsl_mesh* mesh, ocsl_mesh_arrays* arrays);
+const char* ocsl_mesh_marker_name(const ocsl_mesh* mesh, int marker);
+int ocsl_mesh_destroy(ocsl_mesh* mesh);
+
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured CTA kernel, 3 the structured

@@ -18,6 +18,7 @@ library and fails loudly (``LibraryMissing`` / ``OcslError``) without it.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -27,7 +28,8 @@ from ._abi import (BICGSTAB_REF, CG_REF, ILU_BICGSTAB, ILU_BICGSTAB_IR32, METHOD
 
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
-__all__ = ["Context", "Batch", "CMatrix_solver", "build_pattern", "check_pattern", "LibraryMissing", "OcslError",
+__all__ = ["Context", "Batch", "CMatrix_solver", "build_pattern", "check_pattern", "read_su2",
+           "LibraryMissing", "OcslError",
            "CG_REF", "BICGSTAB_REF", "PCG", "ILU_BICGSTAB", "ILU_BICGSTAB_IR32", "METHODS",
            "PHANTOM"]
 
@@ -554,3 +556,29 @@ class CMatrix_solver:
     def solve(self, method=None, **opts):
         """cmatrix_solver.cpp:764-780, with the method chosen per call."""
         return self._run(_method(method if method is not None else self.method), **opts)
+
+
+def read_su2(path: str) -> dict:
+    """Read an SU2 ASCII mesh into the finite-volume arrays of ocsl_mesh_arrays
+    (numpy copies, vectors [3][count]) plus "markers" (names, in file order),
+    with the reference's face numbering (ocsl_mesh_read_su2)."""
+    L = _abi.lib()
+    h = C.c_void_p()
+    err = C.create_string_buffer(512)
+    st = L.ocsl_mesh_read_su2(os.fsencode(path), C.byref(h), err, 512)
+    if st != 0:
+        raise OcslError(st, f"read_su2: {err.value.decode()}")
+    try:
+        v = _abi.MeshArrays()
+        L.ocsl_mesh_view(h, C.byref(v))
+        out = {"n_cells": v.n_cells, "n_faces": v.n_faces, "n_bc": v.n_bc}
+        for name, kind, comps, count in _abi.MESH_ARRAYS:
+            size = comps * int(getattr(v, count))
+            ptr = getattr(v, name)
+            dt = np.int32 if kind == "i" else np.float64
+            out[name] = np.ctypeslib.as_array(ptr, shape=(size,)).astype(dt, copy=True) \
+                if size else np.zeros(0, dt)
+        out["markers"] = [L.ocsl_mesh_marker_name(h, k).decode() for k in range(v.n_markers)]
+        return out
+    finally:
+        L.ocsl_mesh_destroy(h)

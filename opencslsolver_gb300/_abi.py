@@ -132,6 +132,26 @@ def flow_iteration(arrays: dict, constants: dict, ptr) -> FlowIteration:
     return it
 
 
+# ocsl_mesh_arrays (include/ocsl.h), in declaration order
+MESH_ARRAYS = (
+    ("face_left", "i", 1, "n_faces"), ("face_right", "i", 1, "n_faces"),
+    ("face_geo_aver", "d", 1, "n_faces"), ("face_ksi_A", "d", 1, "n_faces"),
+    ("face_area_vector", "d", 3, "n_faces"), ("face_alpha", "d", 3, "n_faces"),
+    ("face_distance", "d", 1, "n_faces"), ("face_unit", "d", 3, "n_faces"),
+    ("bc_left", "i", 1, "n_bc"), ("bc_marker", "i", 1, "n_bc"), ("bc_area", "d", 1, "n_bc"),
+    ("bc_area_vector", "d", 3, "n_bc"), ("bc_alpha", "d", 3, "n_bc"),
+    ("bc_distance", "d", 1, "n_bc"), ("bc_unit", "d", 3, "n_bc"),
+    ("bc_perp_dist", "d", 1, "n_bc"), ("bc_ksi_A", "d", 1, "n_bc"),
+    ("cell_volume", "d", 1, "n_cells"), ("cell_center", "d", 3, "n_cells"))
+
+
+class MeshArrays(C.Structure):
+    _fields_ = ([("n_cells", C.c_int64), ("n_faces", C.c_int64), ("n_bc", C.c_int64),
+                 ("n_markers", C.c_int32)] +
+                [(name, C.POINTER(C.c_int32) if kind == "i" else C.POINTER(C.c_double))
+                 for name, kind, _, _ in MESH_ARRAYS])
+
+
 _CTX = C.c_void_p
 _PROTOS = {
     "ocsl_default_opts": (None, [C.POINTER(Opts)]),
@@ -184,6 +204,10 @@ _PROTOS = {
                                            C.POINTER(FlowIteration), C.POINTER(C.c_int),
                                            C.POINTER(Opts), C.POINTER(FlowReport)]),
     "ocsl_flow_end_step_device": (C.c_int, [_CTX, C.POINTER(FlowState)]),
+    "ocsl_mesh_read_su2": (C.c_int, [C.c_char_p, C.POINTER(_P), C.c_char_p, _SZ]),
+    "ocsl_mesh_view": (C.c_int, [_P, C.POINTER(MeshArrays)]),
+    "ocsl_mesh_marker_name": (C.c_char_p, [_P, C.c_int]),
+    "ocsl_mesh_destroy": (C.c_int, [_P]),
     "ocsl_set_sweep_kernel": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_int]),
     "ocsl_sweep_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),

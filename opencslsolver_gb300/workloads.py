@@ -583,10 +583,11 @@ def write_su2_box(path: str, nx: int, ny: int, nz: int, *, lengths=(1.0, 0.2, 0.
                   jitter: float = 0.1, seed: int = BASE_SEED + 70, cells: str = "hex") -> dict:
     """Write a seeded nx*ny*nz box mesh in SU2 ASCII (the format the reference
     reads, cgeometry_supply.h:201-433): interior nodes jittered by +-jitter
-    of the spacing, hexahedra (type 12) or each hex split into 6 Kuhn tetrahedra
-    (type 10), three markers in this order -- "inlet" (x = 0), "walls" (the four
-    sides), "outlet" (x = lengths[0]) -- as quads (type 9) or triangles (type 5).
-    Returns the counts."""
+    of the spacing; hexahedra (type 12), each hex split into 6 Kuhn tetrahedra
+    (type 10), or each hex split into 2 wedges (type 13) along its (x, y)
+    diagonal; three markers in this order -- "inlet" (x = 0), "walls" (the four
+    sides), "outlet" (x = lengths[0]) -- as quads (type 9) and, where the
+    cells split a box face, triangles (type 5).  Returns the counts."""
     rng = np.random.default_rng(seed)
     P = _jittered_nodes(nx, ny, nz, rng, jitter) * np.asarray(lengths, float)
     nid = np.arange((nx + 1) * (ny + 1) * (nz + 1)).reshape(nx + 1, ny + 1, nz + 1)
@@ -601,6 +602,11 @@ def write_su2_box(path: str, nx: int, ny: int, nz: int, *, lengths=(1.0, 0.2, 0.
         elems = [(12, row) for row in vtk]
     elif cells == "tet":
         elems = [(10, row) for row in corner[:, _kuhn_tets()].reshape(-1, 4)]
+    elif cells == "wedge":  # prisms (c0, c1, c3 | c4, c5, c7) and (c0, c3, c2 | c4, c7, c6)
+        elems = []
+        for row in corner:
+            elems.append((13, row[[0, 1, 3, 4, 5, 7]]))
+            elems.append((13, row[[0, 3, 2, 4, 7, 6]]))
     else:
         raise ValueError(cells)
 
@@ -616,7 +622,7 @@ def write_su2_box(path: str, nx: int, ny: int, nz: int, *, lengths=(1.0, 0.2, 0.
                 for du, dv in ((0, 0), (1, 0), (1, 1), (0, 1)):
                     idx[a], idx[b] = u + du, v + dv
                     c.append(nid[tuple(idx)])
-                out.append(c)
+                out.append((c, fixed_axis))
         return out
 
     markers = {"inlet": quads(0, 0),
@@ -633,17 +639,17 @@ def write_su2_box(path: str, nx: int, ny: int, nz: int, *, lengths=(1.0, 0.2, 0.
         f.write(f"NMARK= {len(markers)}\n")
         for name, faces in markers.items():
             f.write(f"MARKER_TAG= {name}\n")
-            if cells == "hex":
-                f.write(f"MARKER_ELEMS= {len(faces)}\n")
-                for q in faces:
-                    f.write("9 " + " ".join(str(int(v)) for v in q) + "\n")
-            else:  # the two triangles the Kuhn split puts on each boundary quad
-                tris = []
-                for q in faces:
-                    a, b, c, d = q
-                    lo = min(q)  # the split diagonal runs through the lowest node id
-                    tris += [(a, b, c), (a, c, d)] if lo in (a, c) else [(a, b, d), (b, c, d)]
-                f.write(f"MARKER_ELEMS= {len(tris)}\n")
-                for t3 in tris:
-                    f.write("5 " + " ".join(str(int(v)) for v in t3) + "\n")
+            # a split cell face is two triangles along the diagonal from its lowest
+            # to its highest corner (the Kuhn split; the wedges' z faces)
+            elements = []
+            for q, axis in faces:
+                a, b, c, d = q
+                split = cells == "tet" or (cells == "wedge" and axis == 2)
+                if split:
+                    elements += [(5, (a, b, c)), (5, (a, c, d))]
+                else:
+                    elements.append((9, q))
+            f.write(f"MARKER_ELEMS= {len(elements)}\n")
+            for t, nodes in elements:
+                f.write(f"{t} " + " ".join(str(int(v)) for v in nodes) + "\n")
     return {"cells": len(elems), "nodes": X.shape[0]}

@@ -36,6 +36,10 @@ then writes:
   in force (relax_<tag>) and the state after it (post_<tag>__*); the final
   state of that run (final_bicg__*) and, for the shock tube, of the run with
   the momentum equations through CG_solve (final_cg__*);
+* mesh_<cells>.npz -- the reference's finite-volume arrays (face numbering,
+  metrics, cell volumes) and matrix pattern for a 5 x 4 x 3 jittered box of
+  hexahedra, tetrahedra or wedges that it read from the SU2 file
+  workloads.write_su2_box writes;
 * assembly_<case>.npz -- the inputs (cell / face state) and outputs (matrix
   values, b, x0, ap_vec, total_mdot) of the reference's face-loop assembly,
   recorded by oracle/ref_assembly.cpp right before the 5 solve calls of one
@@ -271,10 +275,32 @@ def make_flow(out_dir, case):
     np.savez_compressed(os.path.join(out_dir, f"flow_{case}.npz"), **arrays)
 
 
+MESH_KEYS_FVM = ("face_left", "face_right", "face_geo_aver", "face_ksi_A", "face_area_vector",
+                 "face_alpha", "face_distance", "face_unit", "bc_left", "bc_area",
+                 "bc_area_vector", "bc_alpha", "bc_distance", "bc_unit", "bc_perp_dist",
+                 "bc_ksi_A", "cell_volume", "row_ptr", "column_index")
+
+
+def make_meshes(out_dir):
+    """mesh_<cells>.npz: the reference's finite-volume arrays and matrix
+    pattern for a 5 x 4 x 3 jittered box of hexahedra, Kuhn tetrahedra or
+    wedges read from the SU2 file workloads.write_su2_box writes."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_flow")
+    for cells in ("hex", "tet", "wedge"):
+        with tempfile.TemporaryDirectory() as d:
+            mesh = os.path.join(d, "m.su2")
+            W.write_su2_box(mesh, 5, 4, 3, cells=cells)
+            subprocess.run([exe, d, f"box3d={mesh}", "bicg", "1", "1"], cwd=d, check=True,
+                           stdout=subprocess.DEVNULL)
+            setup = read_named_arrays(os.path.join(d, "setup.bin"))
+        np.savez_compressed(os.path.join(out_dir, f"mesh_{cells}.npz"),
+                            **{k: setup[k] for k in MESH_KEYS_FVM})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=orc.REF_DIR)
-    ap.add_argument("--only", choices=["kat", "shocktube", "small", "assembly", "flow"],
+    ap.add_argument("--only", choices=["kat", "shocktube", "small", "assembly", "flow", "mesh"],
                     help="write one fixture (default: all)")
     a = ap.parse_args()
     orc.build(a.reference)
@@ -292,6 +318,8 @@ def main():
     if want("flow"):
         for case in FLOW_CASES:
             make_flow(HERE, case)
+    if want("mesh"):
+        make_meshes(HERE)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -187,3 +187,33 @@ def test_graph_replay_matches_direct_launches(ctx, torch_cuda):
             assert r0["iterations"] == list(want["iterations"])
     finally:
         ctx2.close()
+
+
+def test_su2_mesh_to_device_iteration(ctx, torch_cuda, tmp_path):
+    """The whole chain from the mesh file: the SU2 file the reference read,
+    turned into finite-volume arrays and the matrix pattern by the library's
+    own reader, drives the recorded 3D run on the device; the final state
+    meets the reference's within 1e-11 (the reader's metrics differ from the
+    reference's -ffast-math ones by ~1e-14)."""
+    from opencslsolver_gb300 import workloads as W
+
+    g = golden("box3d")
+    path = str(tmp_path / "box3d.su2")
+    W.write_su2_box(path, 10, 6, 4)
+    m = ocsl.read_su2(path)
+    rp, col = ocsl.build_pattern(m["n_cells"], m["face_left"], m["face_right"], m["bc_left"])
+    setup = dict(g.setup, row_ptr=rp, column_index=col)
+    for k in ("face_left", "face_right", "bc_left", "face_geo_aver", "face_ksi_A",
+              "face_area_vector", "face_alpha", "face_distance", "face_unit", "bc_area",
+              "bc_area_vector", "bc_alpha", "bc_distance", "bc_unit", "bc_perp_dist", "bc_ksi_A"):
+        setup[k] = m[k]
+    setup["cell_volume"] = m["cell_volume"]
+    dev = FC.DeviceCase(torch_cuda, FC.make_case(setup, g.setup))
+    dev.bind(ctx)
+    for _ in range(g.steps):
+        for _ in range(g.inner):
+            assert dev.iterate(ctx, METHODS["bicg"])["status"] == [0] * 5
+        dev.end_step(ctx)
+    errs = FC.field_errors(dev.written(), FC.recorded(g.setup, g.record("final_bicg")))
+    assert max(errs[k] for k in STATE) <= 1e-11, errs
+    assert max(errs.values()) <= 1e-8, errs
