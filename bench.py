@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--flow-size", type=int, default=128,
+                    help="N of the N^3 SIMPLE-iteration case (0: skip it)")
+    ap.add_argument("--flow-inner", type=int, default=5)
     return ap.parse_args()
 
 
@@ -287,6 +290,49 @@ def simple_iteration(torch, dev, cpu_inner=50):
     }
 
 
+def simple_iteration_at_scale(size, inner, cpu_inner=1):
+    """The same iteration at scale: an N^3 hex box from an SU2 file through the
+    library's reader, pattern builder and initial state (flow_bench), device
+    iterations with each solver choice, and the oracle's C restatement with the
+    reference's solvers on every host core for ``cpu_inner`` iterations."""
+    from opencslsolver_gb300 import flow as F
+    from opencslsolver_gb300 import flow_bench as FB
+    from oracle import oracle as orc
+
+    case, info = FB.box_case(size)
+    info["gpu"] = FB.time_gpu(case, inner)
+    cores = os.cpu_count() or 1
+    orc.Oracle().set_threads(cores)
+    cpu_case = F.initial_state({k: v for k, v in _mesh_of(case).items()}, **FB.CONFIG)
+    t0 = time.perf_counter()
+    for _ in range(cpu_inner):
+        orc.flow_iterate(cpu_case, FB.methods()["reference_solvers"])
+    cpu_ms = 1000.0 * (time.perf_counter() - t0) / cpu_inner
+    info["cpu_port"] = {"ms_per_inner_iteration": round(cpu_ms, 1), "cores": cores,
+                        "sample": f"{cpu_inner} inner iteration(s) of the oracle's C "
+                                  "restatement, reference's solvers (face loops on one thread, "
+                                  "solves on every core)"}
+    info["speedup_reference_solvers"] = round(
+        cpu_ms / info["gpu"]["reference_solvers"]["ms_per_inner_iteration"], 1)
+    return info
+
+
+def _mesh_of(case):
+    """The mesh arrays an initial_state case was built from."""
+    st, ar = case["state"], case["arrays"]
+    return {"n_cells": st["volume"].size, "n_faces": case["left"].size,
+            "n_bc": case["bc_left"].size, "face_left": case["left"], "face_right": case["right"],
+            "bc_left": case["bc_left"], "bc_marker": case["bc_marker"],
+            "face_geo_aver": st["geo_aver"], "face_ksi_A": st["ksi_A"],
+            "face_area_vector": ar["face_area_vector"], "face_alpha": ar["face_alpha"],
+            "face_distance": ar["face_distance"], "face_unit": ar["face_unit"],
+            "bc_area": st["bc_area"], "bc_area_vector": st["bc_area_vector"],
+            "bc_alpha": ar["bc_alpha"], "bc_distance": ar["bc_distance"], "bc_unit": ar["bc_unit"],
+            "bc_perp_dist": st["bc_perp_dist"], "bc_ksi_A": st["bc_ksi_A"],
+            "cell_volume": st["volume"], "row_ptr": case["row_ptr"],
+            "column_index": case["column_index"]}
+
+
 def run_ours(args):
     import torch
 
@@ -435,6 +481,8 @@ def run_ours(args):
 
     # ---- the reference's CPU-runnable case (1000-cell shock tube) end to end
     simple = simple_iteration(torch, dev) if rank == 0 else None
+    if rank == 0 and args.flow_size > 0:
+        simple["at_scale"] = simple_iteration_at_scale(args.flow_size, args.flow_inner)
 
     # ---- CPU baseline: reference algorithm, bounded sample, rank 0
     cpu = None

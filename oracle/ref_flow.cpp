@@ -204,6 +204,9 @@ void write_setup()
     w.d("face_distance", col(fvm.faces, [](const Vf& f) { return f.cell_center_distance; }));
     w.d("face_unit", col3(fvm.faces, [](const Vf& f) { return f.cell_center_unit_vector; }));
     w.i("bc_left", coli(fvm.BC_faces, [](const Vb& f) { return f.left_cell_index; }));
+    w.i("bc_marker", coli(fvm.BC_faces, [](const Vb& f) {
+            return root.geometry->faces[f.global_face_index].boundary_marker;
+        }));
     w.d("bc_area", col(fvm.BC_faces, [](const Vb& f) { return f.area; }));
     w.d("bc_area_vector", col3(fvm.BC_faces, [](const Vb& f) { return f.area_vector; }));
     w.d("bc_alpha", col3(fvm.BC_faces, [](const Vb& f) { return f.alpha; }));

@@ -183,3 +183,44 @@ class DeviceCase:
         out = {k: self.state[k].cpu().numpy() for k in WRITTEN_STATE}
         out.update({k: self.arrays[k].cpu().numpy() for k in WRITTEN_ARRAYS})
         return out
+
+
+# The configurations oracle/ref_flow.cpp runs (shocktube_config.h, flow_configs.h),
+# as opencslsolver_gb300.flow.initial_state arguments.
+CONFIGS = {
+    "shocktube": dict(initial={"pressure": 1e5, "temperature": 348.4, "velocity": (0, 0, 0),
+                               "pressure2": 1e4, "temperature2": 278.7},
+                      boundaries=[{"kind": "wall", "wall": "slip"}, {"kind": "empty"},
+                                  {"kind": "wall", "wall": "slip"}],
+                      viscous=False, blended=True, transient=True, dt=1e-6),
+    "channel": dict(initial={"pressure": 1e5, "temperature": 300.0, "velocity": (20, 0, 0)},
+                    boundaries=[{"kind": "velocity_inlet", "velocity": (20, 0, 0),
+                                 "temperature": 300.0, "pressure": 1e5},
+                                {"kind": "wall", "wall": "no_slip"},
+                                {"kind": "pressure_outlet", "pressure": 1e5}],
+                    viscous=True, blended=False, transient=True, dt=1e-5),
+    "steady": dict(initial={"pressure": 1e5, "temperature": 300.0, "velocity": (700, 0, 0)},
+                   boundaries=[{"kind": "supersonic_inlet", "velocity": (700, 0, 0),
+                                "temperature": 300.0, "pressure": 1e5},
+                               {"kind": "wall", "wall": "slip"},
+                               {"kind": "pressure_outlet", "pressure": 1e5}],
+                   viscous=True, blended=True, transient=False, dt=1e-5),
+    "box3d": dict(initial={"pressure": 1e5, "temperature": 300.0, "velocity": (20, 0, 0)},
+                  boundaries=[{"kind": "velocity_inlet", "velocity": (20, 3, 2),
+                               "temperature": 300.0, "pressure": 1e5},
+                              {"kind": "wall", "wall": "no_slip"},
+                              {"kind": "pressure_outlet", "pressure": 1e5}],
+                  viscous=True, blended=True, transient=True, dt=2e-6),
+}
+
+
+def mesh_from_setup(setup: dict) -> dict:
+    """The recorded finite-volume arrays in the form of read_su2's output."""
+    keys = ("face_left", "face_right", "face_geo_aver", "face_ksi_A", "face_area_vector",
+            "face_alpha", "face_distance", "face_unit", "bc_left", "bc_marker", "bc_area",
+            "bc_area_vector", "bc_alpha", "bc_distance", "bc_unit", "bc_perp_dist", "bc_ksi_A",
+            "cell_volume", "row_ptr", "column_index")
+    m = {k: setup[k] for k in keys}
+    m.update(n_cells=setup["cell_volume"].size, n_faces=setup["face_left"].size,
+             n_bc=setup["bc_left"].size)
+    return m
