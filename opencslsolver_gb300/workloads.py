@@ -601,7 +601,13 @@ def write_su2_box(path: str, nx: int, ny: int, nz: int, *, lengths=(1.0, 0.2, 0.
         vtk = corner[:, [0, 1, 3, 2, 4, 5, 7, 6]]  # SU2 / VTK hexahedron order
         elems = [(12, row) for row in vtk]
     elif cells == "tet":
-        elems = [(10, row) for row in corner[:, _kuhn_tets()].reshape(-1, 4)]
+        tets = corner[:, _kuhn_tets()].reshape(-1, 4)
+        # positive orientation ((p1 - p0) . ((p2 - p0) x (p3 - p0)) > 0), the one
+        # whose faces' normals the reader computes pointing out of the cell
+        p0, p1, p2, p3 = (X[tets[:, k]] for k in range(4))
+        neg = np.einsum("ij,ij->i", p1 - p0, np.cross(p2 - p0, p3 - p0)) < 0
+        tets[neg] = tets[neg][:, [0, 1, 3, 2]]
+        elems = [(10, row) for row in tets]
     elif cells == "wedge":  # prisms (c0, c1, c3 | c4, c5, c7) and (c0, c3, c2 | c4, c7, c6)
         elems = []
         for row in corner:
