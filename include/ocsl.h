@@ -524,6 +524,42 @@ const char* ocsl_noalloc_last_error(void);
 #define OCSL_FAULT_SKIP_FIRST_TILE 1
 int ocsl_inject_fault(ocsl_ctx* ctx, int kind);
 
+/* Row ordering of the tolerance-mode solves (OCSL_PCG, OCSL_ILU_BICGSTAB,
+ * OCSL_ILU_BICGSTAB_IR32; no reference counterpart: the reference factors
+ * and sweeps in natural order, cmatrix_solver.cpp:682-762).
+ *   OCSL_ORDER_NATURAL (default): the system as given.
+ *   OCSL_ORDER_MULTICOLOUR: the rows are coloured greedily in natural order
+ *     (each row the smallest colour none of its lower neighbours has: the
+ *     red-black parity colouring of a box stencil) and renumbered colour by
+ *     colour, ascending within a colour; the solve runs on P A P^T, P b,
+ *     P x0 and scatters x back.  Every triangular sweep then has one level
+ *     per colour, so its rows are independent within a level, at the price
+ *     of a weaker ILU(0) (more Krylov iterations); Jacobi PCG is unchanged
+ *     up to the summation order.  The permuted pattern is built by the
+ *     first solve after the pattern is set (OCSL_BAD_PATTERN when two
+ *     neighbouring rows could share a colour: a pattern that is not
+ *     structurally symmetric).  The reference-faithful methods ignore the
+ *     setting; ocsl_solve_multi_device solves its right-hand sides one after
+ *     another (no column batching), each through the permuted system.
+ * The sweep-kernel settings (ocsl_set_sweep_kernel and the structured
+ * geometry) apply to the natural order only: the permuted pattern is swept by
+ * the level-scheduled kernel. */
+#define OCSL_ORDER_NATURAL 0
+#define OCSL_ORDER_MULTICOLOUR 1
+int ocsl_set_ordering(ocsl_ctx* ctx, int ordering);
+/* The ordering in use, and the colour count and sweep levels (forward,
+ * backward) of the permuted pattern: zeros while it is not built. */
+int ocsl_ordering_info(const ocsl_ctx* ctx, int* ordering, int* colours, int32_t* levels);
+/* perm[new row] = original row of the multicolour ordering (n entries,
+ * host memory); builds the permuted pattern if needed. */
+int ocsl_ordering_permutation(ocsl_ctx* ctx, int32_t* perm, size_t n);
+/* Host-only (no device needed): the multicolour ordering of a pattern, as
+ * ocsl_set_ordering builds it -- perm[n] (perm[new row] = original row) and
+ * the colour count; OCSL_BAD_PATTERN with the reason in err (may be NULL) for
+ * a pattern ocsl_set_pattern rejects or one that cannot be coloured. */
+int ocsl_colour_pattern(size_t n, const size_t* row_ptr, const size_t* column_index,
+                        int32_t* perm, int32_t* colours, char* err, size_t err_len);
+
 /* Tolerance-mode solves replay each batch of Krylov iterations after the
  * first from a CUDA graph captured on the context's stream (not on the legacy
  * default stream, not while profiling).  enable = 0 launches every kernel

@@ -28,7 +28,8 @@ from ._abi import (BICGSTAB_REF, CG_REF, ILU_BICGSTAB, ILU_BICGSTAB_IR32, METHOD
 
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
-__all__ = ["Context", "Batch", "CMatrix_solver", "build_pattern", "check_pattern", "read_su2",
+__all__ = ["Context", "Batch", "CMatrix_solver", "build_pattern", "check_pattern", "colour_pattern",
+           "read_su2",
            "LibraryMissing", "OcslError",
            "CG_REF", "BICGSTAB_REF", "PCG", "ILU_BICGSTAB", "ILU_BICGSTAB_IR32", "METHODS",
            "PHANTOM"]
@@ -78,6 +79,20 @@ def check_pattern(row_ptr, column_index):
                                        C.byref(fw), C.byref(bw), box, buf, 512)
     return st, {"nnz_real": nr.value, "fw_levels": fw.value, "bw_levels": bw.value,
                 "box": tuple(box), "error": buf.value.decode()}
+
+
+def colour_pattern(row_ptr, column_index):
+    """Host-only multicolour ordering (ocsl_colour_pattern): ``(status,
+    perm, colours, error)`` with perm[new row] = original row (int32)."""
+    rp, col = _u64(row_ptr), _u64(column_index)
+    n = rp.size - 1
+    perm = np.zeros(max(n, 0), dtype=np.int32)
+    k = C.c_int32(0)
+    buf = C.create_string_buffer(512)
+    st = _abi.lib().ocsl_colour_pattern(n, _ptr(rp), _ptr(col),
+                                        perm.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(k),
+                                        buf, 512)
+    return st, perm, k.value, buf.value.decode()
 
 
 class Context:
@@ -353,6 +368,32 @@ class Context:
         """Solve the right-hand sides of solve_multi_device with the FP32-inner
         solver in lockstep groups of up to four (default on)."""
         self._check(self._L.ocsl_set_col_batching(self._h, int(bool(enable))), "set_col_batching")
+
+    def set_ordering(self, ordering):
+        """Row ordering of the tolerance-mode solves: "natural" (default) or
+        "multicolour" (greedy colouring, colour-major renumbering; the solve
+        runs on P A P^T and scatters x back)."""
+        codes = {"natural": _abi.ORDER_NATURAL, "multicolour": _abi.ORDER_MULTICOLOUR}
+        code = codes.get(ordering, ordering)
+        self._check(self._L.ocsl_set_ordering(self._h, int(code)), "set_ordering")
+
+    def ordering_info(self):
+        """{"ordering", "colours", "levels": (forward, backward)} of the
+        permuted pattern (zeros until a solve or ordering_permutation built it)."""
+        o, k = C.c_int(), C.c_int()
+        lv = (C.c_int32 * 2)()
+        self._check(self._L.ocsl_ordering_info(self._h, C.byref(o), C.byref(k), lv),
+                    "ordering_info")
+        return {"ordering": "multicolour" if o.value == _abi.ORDER_MULTICOLOUR else "natural",
+                "colours": k.value, "levels": (lv[0], lv[1])}
+
+    def ordering_permutation(self):
+        """perm[new row] = original row of the multicolour ordering (int32 numpy)."""
+        n = self.pattern_info()["n"]
+        perm = np.zeros(n, dtype=np.int32)
+        self._check(self._L.ocsl_ordering_permutation(
+            self._h, perm.ctypes.data_as(C.POINTER(C.c_int32)), n), "ordering_permutation")
+        return perm
 
     # -- kernel timing (ocsl_profile_*)
     def profile(self, enable: bool = True):

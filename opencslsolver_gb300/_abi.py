@@ -220,6 +220,12 @@ _PROTOS = {
     "ocsl_set_graphs": (C.c_int, [_CTX, C.c_int]),
     "ocsl_inject_fault": (C.c_int, [_CTX, C.c_int]),
     "ocsl_set_col_batching": (C.c_int, [_CTX, C.c_int]),
+    "ocsl_set_ordering": (C.c_int, [_CTX, C.c_int]),
+    "ocsl_ordering_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int32)]),
+    "ocsl_ordering_permutation": (C.c_int, [_CTX, C.POINTER(C.c_int32), _SZ]),
+    "ocsl_colour_pattern": (C.c_int, [_SZ, _P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                      C.c_char_p, _SZ]),
     "ocsl_autotune_device": (C.c_int, [_CTX, C.c_int, C.c_void_p, C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "ocsl_profile_enable": (C.c_int, [_CTX, C.c_int]),
@@ -227,6 +233,7 @@ _PROTOS = {
     "ocsl_profile_category_name": (C.c_char_p, [C.c_int]),
 }
 PROFILE_CATEGORIES = 10
+ORDER_NATURAL, ORDER_MULTICOLOUR = 0, 1
 
 _lib = None
 

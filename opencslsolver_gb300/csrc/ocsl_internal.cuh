@@ -374,9 +374,11 @@ void launch_flow_enthalpy_update(cudaStream_t st, int n, const double* x, const 
 void launch_flow_end_step(cudaStream_t st, int n, const FlowDev& f);
 void launch_take_sum(cudaStream_t st, const Scalars* sc, double* out);
 
-// adjoint.cu
+// adjoint.cu: out[k] = val[perm[k]] (gather) and out[perm[k]] = in[k] (scatter)
 void launch_gather_values(cudaStream_t st, long long nnz, const int* perm, const double* val,
                           double* out);
+void launch_scatter_values(cudaStream_t st, long long n, const int* perm, const double* in,
+                           double* out);
 void launch_pattern_outer(cudaStream_t st, const DevPattern& P, double alpha, const double* u,
                           const double* v, double* out);
 

@@ -287,4 +287,69 @@ bool build_pattern_from_faces(size_t n, long long nf, const int32_t* left, const
     return true;
 }
 
+bool colour_pattern(int n, const std::vector<int>& rp, const std::vector<int>& col,
+                    ColouredPattern& cp, std::string& err)
+{
+    cp = ColouredPattern();
+    std::vector<int> colour(n, -1);
+    std::vector<int> seen;  // seen[c] == i: colour c is taken by a neighbour of row i
+    int nc = 0;
+    for (int i = 0; i < n; ++i) {
+        for (int q = rp[i]; q < rp[i + 1]; ++q) {
+            const int j = col[q];
+            if (j >= 0 && j != i && colour[j] >= 0) {
+                if ((int)seen.size() <= colour[j]) seen.resize(colour[j] + 1, -1);
+                seen[colour[j]] = i;
+            }
+        }
+        int c = 0;
+        while (c < (int)seen.size() && seen[c] == i) ++c;
+        colour[i] = c;
+        nc = std::max(nc, c + 1);
+    }
+    // a neighbour with the same colour means the pattern is not symmetric
+    for (int i = 0; i < n; ++i)
+        for (int q = rp[i]; q < rp[i + 1]; ++q)
+            if (col[q] >= 0 && col[q] != i && colour[col[q]] == colour[i])
+                return fail(err, "rows %lld and %lld: the pattern is not structurally symmetric",
+                            i, col[q]);
+    cp.colours = nc;
+    std::vector<int> start(nc + 1, 0), inv(n);
+    for (int i = 0; i < n; ++i) ++start[colour[i] + 1];
+    for (int c = 0; c < nc; ++c) start[c + 1] += start[c];
+    cp.perm.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const int k = start[colour[i]]++;
+        cp.perm[k] = i;
+        inv[i] = k;
+    }
+    cp.rp.assign(n + 1, 0);
+    cp.col.reserve(col.size());
+    cp.slot.reserve(col.size());
+    std::vector<std::pair<int, int>> row;  // (new column, old slot)
+    std::vector<int> phantoms;
+    for (int k = 0; k < n; ++k) {
+        const int i = cp.perm[k];
+        row.clear();
+        phantoms.clear();
+        for (int q = rp[i]; q < rp[i + 1]; ++q) {
+            if (col[q] < 0)
+                phantoms.push_back(q);
+            else
+                row.push_back({inv[col[q]], q});
+        }
+        std::sort(row.begin(), row.end());
+        for (const auto& e : row) {
+            cp.col.push_back((size_t)e.first);
+            cp.slot.push_back(e.second);
+        }
+        for (int q : phantoms) {  // phantom columns stay after the real ones
+            cp.col.push_back(kPhantom);
+            cp.slot.push_back(q);
+        }
+        cp.rp[k + 1] = cp.col.size();
+    }
+    return true;
+}
+
 }  // namespace ocsl

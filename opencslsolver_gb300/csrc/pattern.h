@@ -61,4 +61,20 @@ bool build_pattern_from_faces(size_t n, long long nf, const int32_t* left, const
                               long long nb, const int32_t* bc_left, std::vector<size_t>& row_ptr,
                               std::vector<size_t>& column_index, std::string& err);
 
+// A multicolour ordering of a structurally symmetric pattern: rows coloured
+// greedily in natural order (the smallest colour none of the row's
+// already-coloured neighbours has; the parity colouring of a box stencil),
+// then numbered colour by colour, ascending within a colour.  In the
+// permuted pattern a row's lower entries are rows of lower colours only, so
+// a triangular sweep has one level per colour.  perm[new] = old row;
+// rp / col: the permuted pattern in the reference's layout (phantom column
+// SIZE_MAX kept last); slot[new slot] = the original slot of the entry.
+struct ColouredPattern {
+    int colours = 0;
+    std::vector<int> perm, slot;
+    std::vector<size_t> rp, col;
+};
+bool colour_pattern(int n, const std::vector<int>& rp, const std::vector<int>& col,
+                    ColouredPattern& cp, std::string& err);
+
 }  // namespace ocsl

@@ -246,6 +246,16 @@ struct ocsl_ctx {
     int* d_tperm = nullptr;
     long long nnzT = 0;
 
+    // multicolour ordering of the tolerance-mode solves (ocsl_set_ordering):
+    // a child context holding the permuted pattern P A P^T, the permutation
+    // (perm[new row] = original row) and the map from its CSR slots to this
+    // pattern's slots (built by the first solve that needs them)
+    int ordering = OCSL_ORDER_NATURAL;
+    ocsl_ctx* cctx = nullptr;
+    int* d_cperm = nullptr;
+    int* d_cslot = nullptr;
+    int colours = 0;
+
     // kernel timing (ocsl_profile_*)
     bool prof_on = false;
     std::vector<cudaEvent_t> prof_ev;  // pairs
@@ -281,6 +291,10 @@ void ocsl_ctx::free_pattern()
     if (d_tperm) cudaFree(d_tperm);
     d_tperm = nullptr;
     nnzT = 0;
+    if (cctx) ocsl_destroy(cctx);
+    cctx = nullptr;
+    for (int** pp : {&d_cperm, &d_cslot}) { if (*pp) cudaFree(*pp); *pp = nullptr; }
+    colours = 0;
     for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
     F = DevFaces{};
     has_faces = false;
@@ -1290,8 +1304,97 @@ int check_ready(ocsl_ctx* c)
     return OCSL_OK;
 }
 
+// Builds the multicolour-permuted pattern (colour_pattern) and its child
+// context; the permutation and the slot map go to the device.
+int ensure_coloured(ocsl_ctx* c)
+{
+    if (c->cctx) return OCSL_OK;
+    const int n = c->P.n, nnz = c->P.nnz;
+    std::vector<int> rp(n + 1), col(nnz);
+    CK(cudaMemcpy(rp.data(), c->P.rp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    if (nnz) CK(cudaMemcpy(col.data(), c->P.col, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    ColouredPattern cp;
+    std::string err;
+    if (!colour_pattern(n, rp, col, cp, err)) return fail(c, OCSL_BAD_PATTERN, err);
+    ocsl_ctx* t = nullptr;
+    int rc = ocsl_create(&t, c->device);
+    if (rc != OCSL_OK) return fail(c, rc, "ordering context: " + g_create_error);
+    t->graphs_on = c->graphs_on;
+    rc = ocsl_set_pattern(t, (size_t)n, cp.rp.data(), cp.col.data());
+    if (rc != OCSL_OK) {
+        const std::string msg = t->last_error;
+        ocsl_destroy(t);
+        return fail(c, rc, "multicolour pattern: " + msg);
+    }
+    try {
+        c->d_cperm = upload(cp.perm);
+        c->d_cslot = upload(cp.slot);
+    } catch (...) {
+        ocsl_destroy(t);
+        for (int** pp : {&c->d_cperm, &c->d_cslot}) { if (*pp) cudaFree(*pp); *pp = nullptr; }
+        throw;
+    }
+    c->colours = cp.colours;
+    c->cctx = t;
+    return OCSL_OK;
+}
+
 int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b, double* x,
-                      const ocsl_opts* opts, ocsl_result* out, bool reuse_factor = false)
+                      const ocsl_opts* opts, ocsl_result* out, bool reuse_factor = false);
+
+// A tolerance-mode solve through the multicolour ordering: the values, b and
+// x0 gathered into the child context's buffers, the solve there, x scattered
+// back; solve_ms covers the gathers and the scatter.
+int solve_coloured(ocsl_ctx* c, int method, const double* A, const double* b, double* x,
+                   const ocsl_opts* opts, ocsl_result* out, bool reuse_factor)
+{
+    ocsl_result r;
+    std::memset(&r, 0, sizeof r);
+    ocsl_ctx* t = nullptr;
+    try {
+        const int rc = ensure_coloured(c);
+        if (rc != OCSL_OK) {
+            r.status = rc;
+            if (out) *out = r;
+            return rc;
+        }
+        t = c->cctx;
+        t->stream = c->stream;
+        t->prof_on = c->prof_on;
+        CK(cudaEventRecord(c->ev_start, c->stream));
+        launch_gather_values(c->stream, t->P.nnz, c->d_cslot, A, t->d_A);
+        launch_gather_values(c->stream, t->P.n, c->d_cperm, b, t->d_b);
+        launch_gather_values(c->stream, t->P.n, c->d_cperm, x, t->d_x);
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        r.status = from_cuda(c, e);
+        if (out) *out = r;
+        return r.status;
+    }
+    int status = solve_device_impl(t, method, t->d_A, t->d_b, t->d_x, opts, &r, reuse_factor);
+    if (status != OCSL_OK) c->last_error = t->last_error;
+    if (status == OCSL_CUDA_ERROR) {
+        if (out) *out = r;
+        return status;
+    }
+    try {
+        launch_scatter_values(c->stream, t->P.n, c->d_cperm, t->d_x, x);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(c->ev_stop, c->stream));
+        CK(cudaEventSynchronize(c->ev_stop));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev_start, c->ev_stop));
+        r.solve_ms = ms;
+    } catch (const CudaError& e) {
+        status = from_cuda(c, e);
+        r.status = status;
+    }
+    if (out) *out = r;
+    return status;
+}
+
+int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b, double* x,
+                      const ocsl_opts* opts, ocsl_result* out, bool reuse_factor)
 {
     const ocsl_opts o = resolve(opts);
     ocsl_result r;
@@ -1305,6 +1408,8 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
     if (!A || !b || !x) return fail(c, OCSL_BAD_ARGUMENT, "null value, b or x pointer");
     if (!aligned8(A) || !aligned8(b) || !aligned8(x))
         return fail(c, OCSL_BAD_ARGUMENT, "device pointers must be 8-byte aligned");
+    if (c->ordering == OCSL_ORDER_MULTICOLOUR && method >= OCSL_PCG)
+        return solve_coloured(c, method, A, b, x, opts, out, reuse_factor);
     Solve s{c, c->stream, c->P, c->P.n};
     s.reuse = reuse_factor;
     if (!reuse_factor) c->fac_M = nullptr;
@@ -1646,6 +1751,21 @@ int ocsl_check_pattern(size_t n, const size_t* rp, const size_t* col, int64_t* n
     return OCSL_OK;
 }
 
+int ocsl_colour_pattern(size_t n, const size_t* rp, const size_t* col, int32_t* perm,
+                        int32_t* colours, char* err, size_t err_len)
+{
+    HostPattern hp;
+    ColouredPattern cp;
+    std::string msg;
+    const bool ok = analyse_pattern(n, rp, col, hp, msg) &&
+                    colour_pattern(hp.n, hp.rp, hp.col, cp, msg);
+    if (err && err_len) std::snprintf(err, err_len, "%s", ok ? "" : msg.c_str());
+    if (!ok) return OCSL_BAD_PATTERN;
+    if (perm && n) std::memcpy(perm, cp.perm.data(), n * sizeof(int32_t));
+    if (colours) *colours = cp.colours;
+    return OCSL_OK;
+}
+
 int ocsl_build_pattern(size_t n, int64_t n_faces, const int32_t* left, const int32_t* right,
                        int64_t n_bc, const int32_t* bc_left, size_t* row_ptr,
                        size_t* column_index, size_t* nnz)
@@ -1743,7 +1863,8 @@ int ocsl_solve_multi_device(ocsl_ctx* c, int method, const double* A, int nrhs, 
     if (nrhs < 1) return fail(c, OCSL_BAD_ARGUMENT, "nrhs must be >= 1");
     if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, OCSL_CUDA_ERROR, "cudaSetDevice");
     const size_t n = (size_t)c->P.n;
-    if (method == OCSL_ILU_BICGSTAB_IR32 && nrhs > 1 && n > 0 && c->col_batching) {
+    if (method == OCSL_ILU_BICGSTAB_IR32 && nrhs > 1 && n > 0 && c->col_batching &&
+        c->ordering == OCSL_ORDER_NATURAL) {
         // groups of up to kMaxCols columns in lockstep; the factor is built once
         int first = OCSL_OK;
         for (int r0 = 0; r0 < nrhs; r0 += kMaxCols) {
@@ -2201,6 +2322,45 @@ int ocsl_set_graphs(ocsl_ctx* c, int enable)
     c->graphs_on = enable != 0;
     if (!c->graphs_on) c->drop_graph();
     if (c->tctx) ocsl_set_graphs(c->tctx, enable);
+    if (c->cctx) ocsl_set_graphs(c->cctx, enable);
+    return OCSL_OK;
+}
+
+int ocsl_set_ordering(ocsl_ctx* c, int ordering)
+{
+    if (!c || (ordering != OCSL_ORDER_NATURAL && ordering != OCSL_ORDER_MULTICOLOUR))
+        return OCSL_BAD_ARGUMENT;
+    c->ordering = ordering;
+    return OCSL_OK;
+}
+
+int ocsl_ordering_info(const ocsl_ctx* c, int* ordering, int* colours, int32_t* levels)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    if (ordering) *ordering = c->ordering;
+    if (colours) *colours = c->cctx ? c->colours : 0;
+    if (levels) {
+        levels[0] = c->cctx ? c->cctx->hp.fw_levels : 0;
+        levels[1] = c->cctx ? c->cctx->hp.bw_levels : 0;
+    }
+    return OCSL_OK;
+}
+
+int ocsl_ordering_permutation(ocsl_ctx* c, int32_t* perm, size_t n)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (n != (size_t)c->P.n || (n > 0 && !perm))
+        return fail(c, OCSL_BAD_ARGUMENT, "perm must hold n entries");
+    if (n == 0) return OCSL_OK;
+    try {
+        CK(cudaSetDevice(c->device));
+        rc = ensure_coloured(c);
+        if (rc) return rc;
+        CK(cudaMemcpy(perm, c->d_cperm, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
     return OCSL_OK;
 }
 
@@ -2216,6 +2376,7 @@ int ocsl_profile_enable(ocsl_ctx* c, int enable)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
     c->prof_on = enable != 0;
+    if (c->cctx) c->cctx->prof_on = c->prof_on;
     return OCSL_OK;
 }
 
@@ -2242,6 +2403,16 @@ int ocsl_profile_read(ocsl_ctx* c, double* ms, int64_t* launches)
     }
     c->prof_used = 0;
     c->prof_cat.clear();
+    if (c->cctx) {  // the kernels of solves through the multicolour ordering
+        double cms[PC_COUNT];
+        int64_t cl[PC_COUNT];
+        const int rc = ocsl_profile_read(c->cctx, cms, cl);
+        if (rc != OCSL_OK) return fail(c, rc, c->cctx->last_error);
+        for (int k = 0; k < PC_COUNT; ++k) {
+            if (ms) ms[k] += cms[k];
+            if (launches) launches[k] += cl[k];
+        }
+    }
     return OCSL_OK;
 }
 
