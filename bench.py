@@ -17,6 +17,10 @@ roofline of the dominant kernel from CUDA events recorded around every launch
 during the timed region, and the reference algorithm's CPU rate on the host
 cores (the oracle's OpenMP port of ILU_BICGSTAB_solve; the reference itself
 cannot reach 1e-10, so a reference "solve" is its own fixed 3-iteration call).
+`multicolour_ordering`: the same solves through ocsl_set_ordering's
+multicolour ordering (red-black on this machine; one sweep level per colour, a
+different ILU(0) factor than the reference's, so never the headline), and
+natural against multicolour on the tet 64^3 x 6 p' system.
 
 Also on rank 0 (`simple_iteration`): the reference's own CPU-runnable case end
 to end -- the 1000-cell shock tube's 200 steps x 5 SIMPLE inner iterations as
@@ -60,6 +64,8 @@ def parse():
     ap.add_argument("--flow-size", type=int, default=128,
                     help="N of the N^3 SIMPLE-iteration case (0: skip it)")
     ap.add_argument("--flow-inner", type=int, default=5)
+    ap.add_argument("--tet-size", type=int, default=64,
+                    help="N of the N^3 x 6 tet system of the ordering comparison (0: skip it)")
     return ap.parse_args()
 
 
@@ -333,6 +339,49 @@ def _mesh_of(case):
             "column_index": case["column_index"]}
 
 
+def ordering_comparison(torch, dev, stream, size, warmup, steps, tol):
+    """Natural against multicolour ordering on the size^3 x 6 tet p' system
+    (Peclet <= 50): ms per solve (CUDA events) for the FP32-inner and the
+    FP64 ILU-BiCGSTAB to tol, iterations and true relative residuals."""
+    import opencslsolver_gb300 as ocsl
+    from opencslsolver_gb300 import workloads as W
+
+    t = W.tet_pprime(size, peclet=50.0)
+    ctx = ocsl.Context(dev.index)
+    ctx.set_pattern(t.row_ptr, t.column_index)
+    ctx.set_stream(stream.cuda_stream)
+    A = torch.from_numpy(t.value).to(dev)
+    B = torch.from_numpy(t.b).to(dev)
+    X = torch.zeros(t.n, dtype=torch.float64, device=dev)
+    out = {"workload": f"tet {size}^3 x 6 jittered p' system ({t.n} cells), ILU-BiCGSTAB to "
+                       f"{tol:g}, x0=0"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    try:
+        for ordering in ("natural", "multicolour"):
+            ctx.set_ordering(ordering)
+            for name, method in (("ir32", ocsl.ILU_BICGSTAB_IR32), ("fp64", ocsl.ILU_BICGSTAB)):
+                for k in range(warmup + steps):
+                    if k == warmup:
+                        torch.cuda.synchronize(dev)
+                        e0.record(stream)
+                    X.zero_()
+                    r = ctx.solve_device(method, A, B, X, tol=tol)
+                    if r["status"] != 0:
+                        raise RuntimeError(f"tet solve failed: {r}")
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                out[f"{ordering}_{name}"] = {"ms_per_solve": round(e0.elapsed_time(e1) / steps, 3),
+                                             "iterations": r["iterations"],
+                                             "relres": r["residual"]}
+        out["colours"] = ctx.ordering_info()["colours"]
+        out["natural_sweep_levels"] = ctx.pattern_info()["fw_levels"]
+        out["speedup_ir32"] = round(out["natural_ir32"]["ms_per_solve"] /
+                                    out["multicolour_ir32"]["ms_per_solve"], 2)
+    finally:
+        ctx.close()
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -420,6 +469,22 @@ def run_ours(args):
     _, _, prof_64 = timed(ocsl.ILU_BICGSTAB, max(3, args.steps // 2), profile=True)
     # ---- reference-faithful solve() (ILU + 3 fixed iterations)
     ms_ref, _, _ = timed(ocsl.BICGSTAB_REF, max(3, args.steps // 2))
+    # ---- the multicolour ordering: an option beside the headline (its ILU(0)
+    # factor is that of the permuted system, not the reference's natural one)
+    ctx.set_ordering("multicolour")
+    ms_mc_ir, its_mc_ir, _ = timed(ocsl.ILU_BICGSTAB_IR32, args.steps)
+    ms_mc_64, its_mc_64, _ = timed(ocsl.ILU_BICGSTAB, max(3, args.steps // 2))
+    mc_info = ctx.ordering_info()
+    ctx.set_ordering("natural")
+    multicolour = {"ir32_solves_per_s": world * 1000.0 / ms_mc_ir,
+                   "fp64_solves_per_s": world * 1000.0 / ms_mc_64,
+                   "iterations": {"ir32_inner": its_mc_ir[-1][0], "ir32_outer": its_mc_ir[-1][1],
+                                  "fp64": its_mc_64[-1][0]},
+                   "relres": {"ir32": its_mc_ir[-1][2], "fp64": its_mc_64[-1][2]},
+                   "colours": mc_info["colours"], "sweep_levels": mc_info["levels"]}
+    if args.tet_size > 0 and rank == 0:
+        multicolour["tet"] = ordering_comparison(torch, dev, stream, args.tet_size, args.warmup,
+                                                 max(3, args.steps // 2), args.tol)
 
     # ---- e2e: ocsl_solve with pinned host buffers (H2D of A, b, x0; D2H of x)
     hA = torch.from_numpy(s.value).pin_memory().numpy()
@@ -527,6 +592,7 @@ def run_ours(args):
                         "autotune": round(t_tune, 3)},
             "sweep_kernel": dict(ctx.sweep_info(), autotuned_pair_us=round(tune["sweep_us"], 1),
                                  autotuned_pair_us_f64=round(tune64["sweep_us"], 1)),
+            "multicolour_ordering": multicolour,
             "simple_iteration": simple,
         }
         print(json.dumps(line))
