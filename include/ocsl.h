@@ -466,7 +466,9 @@ int ocsl_sweep_geometry(const ocsl_ctx* ctx, int fp32, int* tiles, int* cluster)
 /* The sweep kernel in use (1 level-scheduled, 2 structured CTA kernel, 3
  * structured warp-pipelined, 4 the one-warp serial sweep that automatic mode
  * gives tiny systems whose schedule is at least a quarter as deep as they are
- * long, such as 1D meshes: n * sizeof(double) <= 40 KB), the detected box
+ * long, such as 1D meshes: n * sizeof(double) <= 40 KB, 5 one launch per
+ * level, for schedules of at most 16 levels that are each a contiguous row
+ * range, such as multicolour-ordered patterns), the detected box
  * dims (nx, ny, nz; zeros when not a box) and the structured tile (TA, TB)
  * of the FP64 sweeps (ocsl_sweep_geometry: either precision). */
 int ocsl_sweep_info(const ocsl_ctx* ctx, int* kind, int* dims, int* tiles);

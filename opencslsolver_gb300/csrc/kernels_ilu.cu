@@ -20,6 +20,7 @@
 // Each row's sum runs over its CSR entries in storage order with fma from 0,
 // exactly as the reference's sequential loop, so the schedule does not
 // change a single bit of the result.
+#include <algorithm>
 #include <cfloat>
 
 #include "ocsl_internal.cuh"
@@ -188,6 +189,143 @@ __global__ void __launch_bounds__(kThreads) bw_sweep_kernel(SweepParams<T> p)
         publish(p.out + i, xi);
     }
     sweep_epilogue(p.S);
+}
+
+// Sweeps over schedules whose levels are contiguous row ranges (multicolour
+// orderings: a row's lower neighbours all lie in lower colours, its upper
+// ones in higher colours).  One launch per level, one thread per row: every
+// dependency lies in a level an earlier launch finished, so plain read-only
+// loads serve, nothing is prefilled and nothing waits.  Rows of up to 8
+// triangle entries load all entries, then all neighbour values, before the
+// fma chain (CSR order from 0, as above), keeping a row's loads in flight
+// together.
+//
+// KIND 0: forward, y_i = rhs_i - sum_{j<i} M_ij y_j.
+// KIND 2: backward, x_i = (y_i - sum_{j>i} M_ij x_j) / M_ii (DIV) or * dinv_i.
+// KIND 1: both for a level whose rows have no upper entries (the last colour):
+//         x_i = y_i / M_ii or * dinv_i, y_i not stored.
+// Rows below rhs_end take y from rhs: level 0 of the forward sweep has no
+// lower entries, so its y equals rhs bit for bit (rhs - 0.0) and the
+// preconditioner skips that level's copy.
+template <typename T>
+struct RangeParams {
+    const int* rp;
+    const int* col;
+    const int* diag;
+    const T* M;
+    const T* dinv;
+    const T* rhs;
+    T* y;
+    T* x;
+    int r0, r1, rhs_end;
+    const int* done;
+};
+
+template <typename T>
+__device__ __forceinline__ T y_of(const RangeParams<T>& p, int j)
+{
+    return j < p.rhs_end ? __ldg(p.rhs + j) : __ldg(p.y + j);
+}
+
+template <typename T>
+__device__ __forceinline__ T lower_sum(const RangeParams<T>& p, int b, int d)
+{
+    T sum = T(0);
+    if (d - b <= 8) {
+        int c[8];
+        T v[8], yv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            c[k] = b + k < d ? __ldg(p.col + b + k) : 0;
+            v[k] = b + k < d ? __ldg(p.M + b + k) : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) yv[k] = b + k < d ? y_of(p, c[k]) : T(0);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (b + k < d) sum = fma_t(v[k], yv[k], sum);
+    } else {
+        for (int q = b; q < d; ++q) sum = fma_t(__ldg(p.M + q), y_of(p, __ldg(p.col + q)), sum);
+    }
+    return sum;
+}
+
+template <typename T>
+__device__ __forceinline__ T upper_sum(const RangeParams<T>& p, int d, int e)
+{
+    T sum = T(0);
+    const int b = d + 1;
+    if (e - b <= 8) {
+        int c[8];
+        T v[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            c[k] = b + k < e ? __ldg(p.col + b + k) : -1;
+            v[k] = b + k < e ? __ldg(p.M + b + k) : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) xv[k] = c[k] >= 0 ? __ldg(p.x + c[k]) : T(0);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (c[k] >= 0) sum = fma_t(v[k], xv[k], sum);  // phantoms skipped
+    } else {
+        for (int q = b; q < e; ++q) {
+            const int j = __ldg(p.col + q);
+            if (j >= 0) sum = fma_t(__ldg(p.M + q), __ldg(p.x + j), sum);
+        }
+    }
+    return sum;
+}
+
+template <typename T, int KIND, bool DIV>
+__global__ void __launch_bounds__(kThreads) range_sweep_kernel(RangeParams<T> p)
+{
+    if (p.done && *p.done) return;
+    const int i = p.r0 + (int)(blockIdx.x * kThreads + threadIdx.x);
+    if (i >= p.r1) return;
+    const int d = __ldg(p.diag + i);
+    if constexpr (KIND == 2) {
+        const T num = y_of(p, i) - upper_sum(p, d, __ldg(p.rp + i + 1));
+        p.x[i] = DIV ? num / __ldg(p.M + d) : num * __ldg(p.dinv + i);
+    } else {
+        const T yi = __ldg(p.rhs + i) - lower_sum(p, __ldg(p.rp + i), d);
+        if constexpr (KIND == 0)
+            p.y[i] = yi;
+        else
+            p.x[i] = DIV ? yi / __ldg(p.M + d) : yi * __ldg(p.dinv + i);
+    }
+}
+
+template <typename T, int KIND>
+void range_launch(cudaStream_t st, RangeParams<T> p, int r0, int r1, bool div)
+{
+    if (r1 <= r0) return;
+    p.r0 = r0;
+    p.r1 = r1;
+    const int grid = (r1 - r0 + kThreads - 1) / kThreads;
+    if (div)
+        range_sweep_kernel<T, KIND, true><<<grid, kThreads, 0, st>>>(p);
+    else
+        range_sweep_kernel<T, KIND, false><<<grid, kThreads, 0, st>>>(p);
+}
+
+template <typename T>
+RangeParams<T> make_range(const DevPattern& P, const T* M, const T* dinv, const T* rhs, T* y,
+                          T* x, const int* done)
+{
+    RangeParams<T> p;
+    p.rp = P.rp;
+    p.col = P.col;
+    p.diag = P.diag;
+    p.M = M;
+    p.dinv = dinv;
+    p.rhs = rhs;
+    p.y = y;
+    p.x = x;
+    p.r0 = p.r1 = 0;
+    p.rhs_end = 0;
+    p.done = done;
+    return p;
 }
 
 // Tiny systems with a deep schedule (the 1D shock tube's chain: one row per
@@ -465,6 +603,37 @@ void launch_fw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 }
 
 template <typename T>
+void launch_range_sweep(cudaStream_t st, const DevPattern& P, bool forward, const T* M,
+                        const T* dinv, const T* rhs, T* out, int divmode, const int* done)
+{
+    const int nr = forward ? P.fw_nrange : P.bw_nrange;
+    const int* rg = forward ? P.fw_range : P.bw_range;
+    // forward: y = out, rhs the input; backward: y = the input, x = out
+    const auto p = forward ? make_range<T>(P, M, dinv, rhs, out, nullptr, done)
+                           : make_range<T>(P, M, dinv, nullptr, const_cast<T*>(rhs), out, done);
+    for (int l = 0; l < nr; ++l) {
+        if (forward)
+            range_launch<T, 0>(st, p, rg[2 * l], rg[2 * l + 1], false);
+        else
+            range_launch<T, 2>(st, p, rg[2 * l], rg[2 * l + 1], divmode == 0);
+    }
+}
+
+template <typename T>
+void launch_coloured_precond(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
+                             const T* rhs, T* tmp, T* out, int divmode, const int* done)
+{
+    const int C = P.fw_nrange;  // colours; fw_range holds them in ascending order
+    if (C == 0) return;
+    auto p = make_range<T>(P, M, dinv, rhs, tmp, out, done);
+    p.rhs_end = P.fw_range[1];  // colour 0: y = rhs
+    const bool div = divmode == 0;
+    for (int c = 1; c < C - 1; ++c) range_launch<T, 0>(st, p, P.fw_range[2 * c], P.fw_range[2 * c + 1], false);
+    range_launch<T, 1>(st, p, P.fw_range[2 * (C - 1)], P.fw_range[2 * C - 1], div);
+    for (int c = C - 2; c >= 0; --c) range_launch<T, 2>(st, p, P.fw_range[2 * c], P.fw_range[2 * c + 1], div);
+}
+
+template <typename T>
 void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
                      const T* rhs, T* out, int divmode, const SweepSync& S, const int* done)
 {
@@ -555,6 +724,16 @@ template void launch_bw_sweep<double>(cudaStream_t, const DevPattern&, const dou
                                       const SweepSync&, const int*);
 template void launch_bw_sweep<float>(cudaStream_t, const DevPattern&, const float*, const float*,
                                      const float*, float*, int, const SweepSync&, const int*);
+template void launch_range_sweep<double>(cudaStream_t, const DevPattern&, bool, const double*,
+                                         const double*, const double*, double*, int, const int*);
+template void launch_range_sweep<float>(cudaStream_t, const DevPattern&, bool, const float*,
+                                        const float*, const float*, float*, int, const int*);
+template void launch_coloured_precond<double>(cudaStream_t, const DevPattern&, const double*,
+                                              const double*, const double*, double*, double*, int,
+                                              const int*);
+template void launch_coloured_precond<float>(cudaStream_t, const DevPattern&, const float*,
+                                             const float*, const float*, float*, float*, int,
+                                             const int*);
 template void launch_serial_sweep<double>(cudaStream_t, const DevPattern&, bool, const double*,
                                           const double*, const double*, double*, int,
                                           const int*);

@@ -308,10 +308,44 @@ struct SpmvParams {
     Cols cols;
 };
 
+// One row's sum in CSR storage order with fma from 0.0, phantom columns
+// skipped.  Rows of up to 8 entries load every entry, then every x, before
+// the chain, so a thread has all of its row's loads in flight at once.
+template <typename T>
+__device__ __forceinline__ T csr_row_sum(const int* __restrict__ col, const T* __restrict__ val,
+                                         const T* __restrict__ x, int b, int e)
+{
+    T dum = T(0);
+    if (e - b <= 8) {
+        int c[8];
+        T v[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            c[k] = b + k < e ? __ldg(col + b + k) : -1;
+            v[k] = b + k < e ? __ldg(val + b + k) : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) xv[k] = c[k] >= 0 ? __ldg(x + c[k]) : T(0);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (c[k] >= 0) dum = fma_t(v[k], xv[k], dum);
+    } else {
+        for (int q = b; q < e; ++q) {
+            const int c = __ldg(col + q);
+            if (c >= 0) dum = fma_t(__ldg(val + q), __ldg(x + c), dum);
+        }
+    }
+    return dum;
+}
+
 // y = A x (MODE 0), y = z - A x (MODE 1), y = fma(a, A x, z) (MODE 2);
-// cmatrix_solver.cpp:338-453.  Each 256-row slab of the tile is staged
-// into shared memory with coalesced loads; each thread then sums its row in
-// CSR storage order with fma from 0.0 (:346-350), skipping phantom columns.
+// cmatrix_solver.cpp:338-453.  Thread t of tile k owns rows k * 2048 + j * 256
+// + t (j = 0..7) and sums each in CSR storage order with fma from 0.0
+// (:346-350), skipping phantom columns.  Entries are loaded directly: a
+// warp's 32 consecutive rows cover one contiguous stretch of the CSR arrays,
+// so the loads coalesce in L1, and two rows are kept in flight.  (Staging
+// each 256-row slab through shared memory first measured 1.4x slower on the
+// tet and multicolour-ordered systems: two barriers per slab, one wave.)
 template <typename T, int MODE, int DOTS>
 __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
 {
@@ -319,8 +353,6 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
     Scalars* const sc = at(p.sc, ct.col);
     if (sc && sc->done) return;
     constexpr int ND = DotCount<DOTS>::value;
-    __shared__ T s_val[kSpmvCap];
-    __shared__ int s_col[kSpmvCap];
     __shared__ double s_red[kMaxDots * 8];
     __shared__ int s_last;
     const int tile = ct.tile;
@@ -332,35 +364,11 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
     const T* const wv = at(p.w, ct.off);
     DotAcc<T> acc[ND > 0 ? ND : 1];
 
-#pragma unroll 1
+#pragma unroll 2
     for (int j = 0; j < kRowsPerThread; ++j) {
-        const int r0 = tile * kTile + j * kThreads;
-        if (r0 >= n) break;  // uniform over the CTA
-        const int r1 = min(r0 + kThreads, n);
-        const int q0 = __ldg(p.rp + r0), q1 = __ldg(p.rp + r1);
-        const bool staged = (q1 - q0) <= kSpmvCap;
-        if (staged) {
-            for (int q = q0 + (int)threadIdx.x; q < q1; q += kThreads) {
-                s_val[q - q0] = __ldg(p.val + q);
-                s_col[q - q0] = __ldg(p.col + q);
-            }
-        }
-        __syncthreads();
-        const int row = r0 + (int)threadIdx.x;
+        const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
         if (row < n) {
-            const int b = __ldg(p.rp + row), e = __ldg(p.rp + row + 1);
-            T dum = T(0);
-            if (staged) {
-                for (int q = b - q0; q < e - q0; ++q) {
-                    const int c = s_col[q];
-                    if (c >= 0) dum = fma_t(s_val[q], __ldg(xv + c), dum);
-                }
-            } else {
-                for (int q = b; q < e; ++q) {
-                    const int c = __ldg(p.col + q);
-                    if (c >= 0) dum = fma_t(__ldg(p.val + q), __ldg(xv + c), dum);
-                }
-            }
+            const T dum = csr_row_sum(p.col, p.val, xv, __ldg(p.rp + row), __ldg(p.rp + row + 1));
             T y, zv = T(0);
             if constexpr (MODE == 0) {
                 y = dum;
@@ -379,7 +387,6 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
             if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(wv + row), y);
             (void)k;
         }
-        __syncthreads();
     }
     if constexpr (ND > 0) {
         double v[ND];

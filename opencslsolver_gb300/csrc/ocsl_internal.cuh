@@ -20,13 +20,13 @@
 #include <stdint.h>
 
 #include "../../include/ocsl.h"
+#include "pattern.h"
 
 namespace ocsl {
 
 constexpr int kThreads = 256;          // threads per CTA of every tile kernel
 constexpr int kRowsPerThread = 8;      // rows / elements per thread per tile
 constexpr int kTile = kThreads * kRowsPerThread;  // 2048 rows per tile
-constexpr int kSpmvCap = 2560;         // staged nnz per 256-row slab
 constexpr int kMaxDots = 3;
 constexpr int kMaxCols = 4;            // right-hand sides of one column-batched launch
 
@@ -112,6 +112,14 @@ struct DevPattern {
     const int* bw_order;
     const int* bw_chunk;
     int bw_nchunks;
+    // levels that are contiguous row ranges (HostPattern::fw_range / bw_range):
+    // count (0 = not applicable) and (first row, end row) per level
+    int fw_nrange, bw_nrange;
+    int fw_range[2 * kRangeMaxLevels], bw_range[2 * kRangeMaxLevels];
+    // the ranges are the colours of a multicolour ordering (fw ascending, bw
+    // descending): a row's lower entries lie in lower colours, its upper ones
+    // in higher colours, so the last colour's rows have no upper entries
+    bool coloured;
 };
 
 // Face-to-cell incidence of the mesh (ocsl_set_faces), for the assembly.
@@ -212,6 +220,17 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 // bytes of shared memory (at most kSerialMaxBytes, which leaves the kernel's
 // row staging room under the 48 KB a launch may take without opting in).
 constexpr int kSerialMaxBytes = 40 * 1024;
+// One sweep over a pattern whose levels are contiguous row ranges: one launch
+// per level, rows of a level independent, plain loads (no waits, no prefill).
+template <typename T>
+void launch_range_sweep(cudaStream_t st, const DevPattern& P, bool forward, const T* M,
+                        const T* dinv, const T* rhs, T* out, int divmode, const int* done);
+// Both sweeps of the ILU preconditioner, out = U^-1 L^-1 rhs, on a
+// colour-ordered pattern (DevPattern::coloured: fw_range holds the colours in
+// ascending order): 2 colours - 2 launches, tmp holds y of the middle colours.
+template <typename T>
+void launch_coloured_precond(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
+                             const T* rhs, T* tmp, T* out, int divmode, const int* done);
 template <typename T>
 void launch_serial_sweep(cudaStream_t st, const DevPattern& P, bool forward, const T* M,
                          const T* dinv, const T* rhs, T* out, int divmode, const int* done);

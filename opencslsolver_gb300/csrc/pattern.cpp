@@ -32,7 +32,7 @@ bool fail(std::string& err, const char* fmt, long long a, long long b = 0)
 }
 
 void schedule(int n, const std::vector<int>& level, int nlevels, std::vector<int>& order,
-              std::vector<int>& chunk, int chunk_rows)
+              std::vector<int>& chunk, std::vector<int>& range, int chunk_rows)
 {
     std::vector<int> count(nlevels + 1, 0);
     for (int i = 0; i < n; ++i) ++count[level[i] + 1];
@@ -45,6 +45,19 @@ void schedule(int n, const std::vector<int>& level, int nlevels, std::vector<int
         for (int b = count[l]; b < count[l + 1]; b += chunk_rows) chunk.push_back(b);
     }
     chunk.push_back(n);
+    // levels that are contiguous row ranges (rows ascend within a level, so
+    // the first and last row tell)
+    range.clear();
+    if (nlevels > kRangeMaxLevels) return;
+    for (int l = 0; l < nlevels; ++l) {
+        const int a = count[l], b = count[l + 1];
+        if (b > a && order[b - 1] - order[a] != b - 1 - a) {
+            range.clear();
+            return;
+        }
+        range.push_back(b > a ? order[a] : 0);
+        range.push_back(b > a ? order[b - 1] + 1 : 0);
+    }
 }
 
 }  // namespace
@@ -179,7 +192,7 @@ bool analyse_pattern(size_t n_in, const size_t* rp, const size_t* col, HostPatte
         nl = std::max(nl, l + 1);
     }
     hp.fw_levels = nl;
-    schedule(n, level, nl, hp.fw_order, hp.fw_chunk, kChunkRows);
+    schedule(n, level, nl, hp.fw_order, hp.fw_chunk, hp.fw_range, kChunkRows);
     nl = 0;
     for (int i = n - 1; i >= 0; --i) {
         int l = 0;
@@ -189,7 +202,7 @@ bool analyse_pattern(size_t n_in, const size_t* rp, const size_t* col, HostPatte
         nl = std::max(nl, l + 1);
     }
     hp.bw_levels = nl;
-    schedule(n, level, nl, hp.bw_order, hp.bw_chunk, kChunkRows);
+    schedule(n, level, nl, hp.bw_order, hp.bw_chunk, hp.bw_range, kChunkRows);
     hp.box = detect_box(n, hp.rp, hp.col);
     return true;
 }
@@ -317,6 +330,7 @@ bool colour_pattern(int n, const std::vector<int>& rp, const std::vector<int>& c
     std::vector<int> start(nc + 1, 0), inv(n);
     for (int i = 0; i < n; ++i) ++start[colour[i] + 1];
     for (int c = 0; c < nc; ++c) start[c + 1] += start[c];
+    cp.start = start;
     cp.perm.resize(n);
     for (int i = 0; i < n; ++i) {
         const int k = start[colour[i]]++;

@@ -9,6 +9,9 @@
 namespace ocsl {
 
 constexpr int kChunkRows = 256;  // rows per chunk of a sweep level (one CTA)
+// Schedules of at most this many levels, each a contiguous ascending row
+// range (multicolour orderings), are swept one launch per level.
+constexpr int kRangeMaxLevels = 16;
 
 // A pattern that is exactly the 7-point stencil of an nx * ny * nz box in
 // natural order (row = i + nx * (j + ny * k)), with optional phantom columns
@@ -28,6 +31,9 @@ struct HostPattern {
     std::vector<int> rp, col, diag;
     std::vector<int> pair_ptr, pair_k, pair_slot;
     std::vector<int> fw_order, fw_chunk, bw_order, bw_chunk;
+    // (first row, end row) of each level in schedule order when every level is
+    // a contiguous row range and there are at most kRangeMaxLevels; else empty
+    std::vector<int> fw_range, bw_range;
 };
 
 // Recognise the 7-point box stencil (see BoxShape); O(nnz).
@@ -71,6 +77,7 @@ bool build_pattern_from_faces(size_t n, long long nf, const int32_t* left, const
 // SIZE_MAX kept last); slot[new slot] = the original slot of the entry.
 struct ColouredPattern {
     int colours = 0;
+    std::vector<int> start;  // [colours + 1]: colour c holds new rows [start[c], start[c+1])
     std::vector<int> perm, slot;
     std::vector<size_t> rp, col;
 };

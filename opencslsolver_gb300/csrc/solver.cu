@@ -665,11 +665,17 @@ struct Solve {
     template <typename TT>
     void fw(const TT* M, const TT* rhs, TT* out, int k, bool prefilled = false)
     {
-        if (use_serial<TT>()) {
+        if (use_serial<TT>() || use_range()) {
             ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
-            for (int q = 0; q < cols.n; ++q)
-                launch_serial_sweep<TT>(st, P, true, M, nullptr, rhs + q * cols.ld,
-                                        out + q * cols.ld, 0, k >= 0 ? done(k + q) : nullptr);
+            for (int q = 0; q < cols.n; ++q) {
+                const int* dn = k >= 0 ? done(k + q) : nullptr;
+                if (!use_serial<TT>())
+                    launch_range_sweep<TT>(st, P, true, M, nullptr, rhs + q * cols.ld,
+                                           out + q * cols.ld, 0, dn);
+                else
+                    launch_serial_sweep<TT>(st, P, true, M, nullptr, rhs + q * cols.ld,
+                                            out + q * cols.ld, 0, dn);
+            }
             return;
         }
         const bool wave = use_box() && soa<TT>() && use_wave<TT>();
@@ -688,6 +694,29 @@ struct Solve {
                 launch_fw_sweep<TT>(st, P, M, rhs + q * cols.ld, out + q * cols.ld,
                                     c->next_sync(), k >= 0 ? done(k + q) : nullptr);
     }
+    // out = U^-1 L^-1 rhs through tmp (dead afterwards): one fused pass per
+    // colour on a colour-ordered pattern, else the two sweeps
+    template <typename TT>
+    void precond(const TT* M, const TT* dinv, const TT* rhs, TT* tmp, TT* out, int divmode, int k,
+                 bool prefilled)
+    {
+        if (P.coloured && use_range() && !use_serial<TT>()) {
+            ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
+            for (int q = 0; q < cols.n; ++q)
+                launch_coloured_precond<TT>(st, P, M, dinv, rhs + q * cols.ld, tmp + q * cols.ld,
+                                            out + q * cols.ld, divmode,
+                                            k >= 0 ? done(k + q) : nullptr);
+            return;
+        }
+        fw<TT>(M, rhs, tmp, k, prefilled);
+        bw<TT>(M, dinv, tmp, out, divmode, k, prefilled);
+    }
+    // the sweeps write every row without a prefilled output
+    template <typename TT>
+    bool sweeps_need_fill() const
+    {
+        return !use_serial<TT>() && !use_range() && !(use_box() && use_wave<TT>());
+    }
     // The box geometry, narrowed while a CTA's staging for cols.n columns
     // exceeds the shared-memory limit.
     template <typename TT>
@@ -703,6 +732,13 @@ struct Solve {
         return g;
     }
     bool use_box() const { return P.box_ok && c->sweep_kernel != 1; }
+    // one launch per level: few levels, each a contiguous row range (not a
+    // box; a pending fault injection exercises the waits of the other kernels)
+    bool use_range() const
+    {
+        return P.fw_nrange > 0 && P.bw_nrange > 0 && !P.box_ok && c->sweep_kernel <= 1 &&
+               !c->fault_skip_pending;
+    }
     // the one-warp serial sweep (automatic mode, tiny deep patterns; a
     // pending fault injection exercises the waits of the other kernels)
     template <typename TT>
@@ -821,11 +857,17 @@ struct Solve {
     void bw(const TT* M, const TT* dinv, const TT* rhs, TT* out, int divmode, int k,
             bool prefilled = false)
     {
-        if (use_serial<TT>()) {
+        if (use_serial<TT>() || use_range()) {
             ProfScope ps(c, st, is_f64<TT>() ? PC_BW64 : PC_BW32);
-            for (int q = 0; q < cols.n; ++q)
-                launch_serial_sweep<TT>(st, P, false, M, dinv, rhs + q * cols.ld,
-                                        out + q * cols.ld, divmode, k >= 0 ? done(k + q) : nullptr);
+            for (int q = 0; q < cols.n; ++q) {
+                const int* dn = k >= 0 ? done(k + q) : nullptr;
+                if (!use_serial<TT>())
+                    launch_range_sweep<TT>(st, P, false, M, dinv, rhs + q * cols.ld,
+                                           out + q * cols.ld, divmode, dn);
+                else
+                    launch_serial_sweep<TT>(st, P, false, M, dinv, rhs + q * cols.ld,
+                                            out + q * cols.ld, divmode, dn);
+            }
             return;
         }
         const bool wave = use_box() && soa<TT>() && use_wave<TT>();
@@ -1042,16 +1084,14 @@ void bicgstab_iteration(Solve& s, const TT* A, const TT* M, const TT* dinv, TT* 
     // single column: the vector kernels before each sweep pair fill the
     // pair's outputs (tmp is dead after each backward sweep, s^ after the x
     // update, p^ after the p update), so no fill launches inside the loop
-    const bool fuse = s.cols.n == 1 && !(s.use_box() && s.template use_wave<TT>());
+    const bool fuse = s.cols.n == 1 && s.template sweeps_need_fill<TT>();
     const bool pre = fuse && s.tb_prefilled;
     TT* f0 = fuse ? tmp : nullptr;
-    s.fw<TT>(M, p, tmp, k, pre);
-    s.bw<TT>(M, dinv, tmp, ph, 1, k, pre);
+    s.precond<TT>(M, dinv, p, tmp, ph, 1, k, pre);
     s.spmv<TT>(A, ph, vv, 0, nullptr, nullptr, rh, DOT_WY, k, EP_TB_SIGMA);
     s.vec<TT>(V_TB_S, {ss, vv, r, nullptr, nullptr, nullptr, f0, fuse ? sh : nullptr}, k,
               EP_TB_S);
-    s.fw<TT>(M, ss, tmp, k, fuse);
-    s.bw<TT>(M, dinv, tmp, sh, 1, k, fuse);
+    s.precond<TT>(M, dinv, ss, tmp, sh, 1, k, fuse);
     s.spmv<TT>(A, sh, t, 0, nullptr, nullptr, ss, DOT_YY | DOT_WY, k, EP_TB_OMEGA);
     s.vec<TT>(V_TB_XR, {x, ph, sh, r, t, ss, rh}, k, EP_TB_RUPD);
     s.vec<TT>(V_TB_P, {p, vv, r, nullptr, nullptr, nullptr, f0, fuse ? ph : nullptr}, k,
@@ -1325,6 +1365,21 @@ int ensure_coloured(ocsl_ctx* c)
         const std::string msg = t->last_error;
         ocsl_destroy(t);
         return fail(c, rc, "multicolour pattern: " + msg);
+    }
+    // Two colours (red-black): sweep colour by colour, one launch per colour
+    // (ascending forward, descending backward), and the fused preconditioner
+    // in two launches.  With more colours the per-launch cost outweighs the
+    // waits: on the tet 64^3 x 6 system (4 colours) six fused launches took
+    // 88 us per FP64 preconditioner against 71 us for the two single-launch
+    // level-scheduled sweeps, which the child then keeps.
+    DevPattern& Q = t->P;
+    Q.coloured = cp.colours <= 2;
+    Q.fw_nrange = Q.bw_nrange = Q.coloured ? cp.colours : 0;
+    for (int k = 0; Q.coloured && k < cp.colours; ++k) {
+        Q.fw_range[2 * k] = cp.start[k];
+        Q.fw_range[2 * k + 1] = cp.start[k + 1];
+        Q.bw_range[2 * k] = cp.start[cp.colours - 1 - k];
+        Q.bw_range[2 * k + 1] = cp.start[cp.colours - k];
     }
     try {
         c->d_cperm = upload(cp.perm);
@@ -1700,6 +1755,10 @@ int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
         P.bw_chunk = c->d_pat[9];
         P.bw_nchunks = (int)hp.bw_chunk.size() - 1;
         P.box_ok = hp.box.ok && c->sweep_kernel != 1;
+        P.fw_nrange = (int)hp.fw_range.size() / 2;
+        P.bw_nrange = (int)hp.bw_range.size() / 2;
+        std::copy(hp.fw_range.begin(), hp.fw_range.end(), P.fw_range);
+        std::copy(hp.bw_range.begin(), hp.bw_range.end(), P.bw_range);
         c->hp.box = hp.box;
         c->rebuild_box_geoms();
         // the one-warp sweep: the solution fits its shared memory and the
@@ -2298,6 +2357,8 @@ int ocsl_sweep_info(const ocsl_ctx* c, int* kind, int* dims, int* tiles)
     if (!c->has_pattern) return OCSL_NO_PATTERN;
     if (kind)
         *kind = c->sweep_kernel == 0 && c->serial_ok[0] ? 4
+                : c->P.fw_nrange > 0 && c->P.bw_nrange > 0 && !c->P.box_ok && c->sweep_kernel <= 1
+                    ? 5
                 : !c->P.box_ok ? 1
                 : (c->sweep_kernel != 2 && c->wave_fits[0] &&
                    (c->sweep_kernel == 3 || c->wave_on[0])) ? 3 : 2;

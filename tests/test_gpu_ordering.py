@@ -135,3 +135,26 @@ def test_multicolour_profile_and_pattern_change(ctx):
     x = np.zeros(t.n)
     assert ctx.solve(ocsl.ILU_BICGSTAB, t.value, t.b, x)["status"] == 0
     assert ctx.ordering_info()["colours"] > 2
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_range_sweeps_on_permuted_pattern_bit_exact(ctx, oracle, torch_cuda, k):
+    """A multicolour-ordered pattern handed to ocsl_set_pattern directly: its
+    level schedule is a few contiguous row ranges, swept one launch per
+    level (sweep kind 5); forward and backward sweeps equal the oracle's."""
+    torch = torch_cuda
+    s = systems()[k]
+    perm, colours = OC.colour_order(s.row_ptr, s.column_index)
+    rp, col, val, b = OC.permuted_system(s, perm)
+    ctx.set_pattern(rp, col)
+    if k < 2:  # red-black: two levels each way
+        assert ctx.sweep_info()["kind"] == 5
+    Mh = oracle.ilu(rp, col, val)
+    M = torch.from_numpy(Mh).cuda()
+    B = torch.from_numpy(b).cuda()
+    Y, X = torch.empty_like(B), torch.empty_like(B)
+    ctx.forsub_device(M, B, Y)
+    y = oracle.forsub(rp, col, Mh, b)
+    assert np.array_equal(Y.cpu().numpy(), y)
+    ctx.backsub_device(M, Y, X)
+    assert np.array_equal(X.cpu().numpy(), oracle.backsub(rp, col, Mh, y))
