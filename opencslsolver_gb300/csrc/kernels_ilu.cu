@@ -195,10 +195,9 @@ __global__ void __launch_bounds__(kThreads) bw_sweep_kernel(SweepParams<T> p)
 // orderings: a row's lower neighbours all lie in lower colours, its upper
 // ones in higher colours).  One launch per level, one thread per row: every
 // dependency lies in a level an earlier launch finished, so plain read-only
-// loads serve, nothing is prefilled and nothing waits.  Rows of up to 8
-// triangle entries load all entries, then all neighbour values, before the
-// fma chain (CSR order from 0, as above), keeping a row's loads in flight
-// together.
+// loads serve, nothing is prefilled and nothing waits.  A row's first
+// triangle entries (preload_width below) are loaded together, then their
+// neighbour values, then the fma chain runs (CSR order from 0, as above).
 //
 // KIND 0: forward, y_i = rhs_i - sum_{j<i} M_ij y_j.
 // KIND 2: backward, x_i = (y_i - sum_{j>i} M_ij x_j) / M_ii (DIV) or * dinv_i.
@@ -227,58 +226,64 @@ __device__ __forceinline__ T y_of(const RangeParams<T>& p, int j)
     return j < p.rhs_end ? __ldg(p.rhs + j) : __ldg(p.y + j);
 }
 
+// Triangle entries preloaded per row: 4 (a 7-point row has at most 3 per
+// triangle, a tetrahedral cell 4 face neighbours), so the kernel stays at 32
+// registers, 8 CTAs per SM, without spills; longer rows continue the same
+// chain in a loop.
+template <typename T>
+__host__ __device__ constexpr int preload_width()
+{
+    return 4;
+}
+
 template <typename T>
 __device__ __forceinline__ T lower_sum(const RangeParams<T>& p, int b, int d)
 {
-    T sum = T(0);
-    if (d - b <= 8) {
-        int c[8];
-        T v[8], yv[8];
+    constexpr int K = preload_width<T>();
+    int c[K];
+    T v[K], yv[K];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            c[k] = b + k < d ? __ldg(p.col + b + k) : 0;
-            v[k] = b + k < d ? __ldg(p.M + b + k) : T(0);
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) yv[k] = b + k < d ? y_of(p, c[k]) : T(0);
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (b + k < d) sum = fma_t(v[k], yv[k], sum);
-    } else {
-        for (int q = b; q < d; ++q) sum = fma_t(__ldg(p.M + q), y_of(p, __ldg(p.col + q)), sum);
+    for (int k = 0; k < K; ++k) {
+        c[k] = b + k < d ? __ldg(p.col + b + k) : 0;
+        v[k] = b + k < d ? __ldg(p.M + b + k) : T(0);
     }
+#pragma unroll
+    for (int k = 0; k < K; ++k) yv[k] = b + k < d ? y_of(p, c[k]) : T(0);
+    T sum = T(0);
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (b + k < d) sum = fma_t(v[k], yv[k], sum);
+    for (int q = b + K; q < d; ++q) sum = fma_t(__ldg(p.M + q), y_of(p, __ldg(p.col + q)), sum);
     return sum;
 }
 
 template <typename T>
 __device__ __forceinline__ T upper_sum(const RangeParams<T>& p, int d, int e)
 {
-    T sum = T(0);
+    constexpr int K = preload_width<T>();
     const int b = d + 1;
-    if (e - b <= 8) {
-        int c[8];
-        T v[8], xv[8];
+    int c[K];
+    T v[K], xv[K];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            c[k] = b + k < e ? __ldg(p.col + b + k) : -1;
-            v[k] = b + k < e ? __ldg(p.M + b + k) : T(0);
-        }
+    for (int k = 0; k < K; ++k) {
+        c[k] = b + k < e ? __ldg(p.col + b + k) : -1;
+        v[k] = b + k < e ? __ldg(p.M + b + k) : T(0);
+    }
 #pragma unroll
-        for (int k = 0; k < 8; ++k) xv[k] = c[k] >= 0 ? __ldg(p.x + c[k]) : T(0);
+    for (int k = 0; k < K; ++k) xv[k] = c[k] >= 0 ? __ldg(p.x + c[k]) : T(0);
+    T sum = T(0);
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (c[k] >= 0) sum = fma_t(v[k], xv[k], sum);  // phantoms skipped
-    } else {
-        for (int q = b; q < e; ++q) {
-            const int j = __ldg(p.col + q);
-            if (j >= 0) sum = fma_t(__ldg(p.M + q), __ldg(p.x + j), sum);
-        }
+    for (int k = 0; k < K; ++k)
+        if (c[k] >= 0) sum = fma_t(v[k], xv[k], sum);  // phantoms skipped
+    for (int q = b + K; q < e; ++q) {
+        const int j = __ldg(p.col + q);
+        if (j >= 0) sum = fma_t(__ldg(p.M + q), __ldg(p.x + j), sum);
     }
     return sum;
 }
 
 template <typename T, int KIND, bool DIV>
-__global__ void __launch_bounds__(kThreads) range_sweep_kernel(RangeParams<T> p)
+__global__ void __launch_bounds__(kThreads, 8) range_sweep_kernel(RangeParams<T> p)
 {
     if (p.done && *p.done) return;
     const int i = p.r0 + (int)(blockIdx.x * kThreads + threadIdx.x);

@@ -308,51 +308,27 @@ struct SpmvParams {
     Cols cols;
 };
 
-// One row's sum in CSR storage order with fma from 0.0, phantom columns
-// skipped.  Rows of up to 8 entries load every entry, then every x, before
-// the chain, so a thread has all of its row's loads in flight at once.
-template <typename T>
-__device__ __forceinline__ T csr_row_sum(const int* __restrict__ col, const T* __restrict__ val,
-                                         const T* __restrict__ x, int b, int e)
-{
-    T dum = T(0);
-    if (e - b <= 8) {
-        int c[8];
-        T v[8], xv[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            c[k] = b + k < e ? __ldg(col + b + k) : -1;
-            v[k] = b + k < e ? __ldg(val + b + k) : T(0);
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) xv[k] = c[k] >= 0 ? __ldg(x + c[k]) : T(0);
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (c[k] >= 0) dum = fma_t(v[k], xv[k], dum);
-    } else {
-        for (int q = b; q < e; ++q) {
-            const int c = __ldg(col + q);
-            if (c >= 0) dum = fma_t(__ldg(val + q), __ldg(x + c), dum);
-        }
-    }
-    return dum;
-}
-
 // y = A x (MODE 0), y = z - A x (MODE 1), y = fma(a, A x, z) (MODE 2);
 // cmatrix_solver.cpp:338-453.  Thread t of tile k owns rows k * 2048 + j * 256
 // + t (j = 0..7) and sums each in CSR storage order with fma from 0.0
 // (:346-350), skipping phantom columns.  Entries are loaded directly: a
 // warp's 32 consecutive rows cover one contiguous stretch of the CSR arrays,
-// so the loads coalesce in L1, and two rows are kept in flight.  (Staging
-// each 256-row slab through shared memory first measured 1.4x slower on the
-// tet and multicolour-ordered systems: two barriers per slab, one wave.)
+// so the loads coalesce in L1.  A row's first 8 entries are loaded together
+// (predicated loads), then their x values, then the chain runs; entries past
+// the 8th continue the same chain after.  One row at a time keeps the kernel
+// at 32-40 registers and the SMs full of warps, which measured faster than
+// more rows in flight per thread (2 rows: 1.26x, 4 rows: 1.5x slower at 64-205
+// registers) and than staging each 256-row slab through shared memory first
+// (1.4x slower: two barriers per slab).
 template <typename T, int MODE, int DOTS>
 __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
 {
+    constexpr int G = 1;
     const ColTile ct = col_tile(p.cols);
     Scalars* const sc = at(p.sc, ct.col);
     if (sc && sc->done) return;
     constexpr int ND = DotCount<DOTS>::value;
+    constexpr int K = 8;
     __shared__ double s_red[kMaxDots * 8];
     __shared__ int s_last;
     const int tile = ct.tile;
@@ -364,35 +340,65 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
     const T* const wv = at(p.w, ct.off);
     DotAcc<T> acc[ND > 0 ? ND : 1];
 
-#pragma unroll 2
-    for (int j = 0; j < kRowsPerThread; ++j) {
-        const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
-        if (row < n) {
-            const T dum = csr_row_sum(p.col, p.val, xv, __ldg(p.rp + row), __ldg(p.rp + row + 1));
+#pragma unroll 1
+    for (int j0 = 0; j0 < kRowsPerThread; j0 += G) {
+        int row[G], b[G], e[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            row[g] = tile * kTile + (j0 + g) * kThreads + (int)threadIdx.x;
+            const bool in = row[g] < n;
+            b[g] = in ? __ldg(p.rp + row[g]) : 0;
+            e[g] = in ? __ldg(p.rp + row[g] + 1) : 0;
+        }
+        int c[G][K];
+        T v[G][K], xk[G][K];
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const bool in = b[g] + k < e[g];
+                c[g][k] = in ? __ldg(p.col + b[g] + k) : -1;
+                v[g][k] = in ? __ldg(p.val + b[g] + k) : T(0);
+            }
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+#pragma unroll
+            for (int k = 0; k < K; ++k) xk[g][k] = c[g][k] >= 0 ? __ldg(xv + c[g][k]) : T(0);
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            if (row[g] >= n) continue;
+            T dum = T(0);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (c[g][k] >= 0) dum = fma_t(v[g][k], xk[g][k], dum);
+            for (int q = b[g] + K; q < e[g]; ++q) {  // rows longer than K entries
+                const int cq = __ldg(p.col + q);
+                if (cq >= 0) dum = fma_t(__ldg(p.val + q), __ldg(xv + cq), dum);
+            }
             T y, zv = T(0);
             if constexpr (MODE == 0) {
                 y = dum;
             } else if constexpr (MODE == 1) {
-                zv = __ldg(zvec + row);
+                zv = __ldg(zvec + row[g]);
                 y = zv - dum;
             } else {
-                zv = __ldg(zvec + row);
+                zv = __ldg(zvec + row[g]);
                 y = fma_t(p.a, dum, zv);
             }
-            yv[row] = y;
-            if (MODE == 1 && ycp) ycp[row] = y;
+            yv[row[g]] = y;
+            if (MODE == 1 && ycp) ycp[row[g]] = y;
             int k = 0;
             if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
             if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
-            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(wv + row), y);
+            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(wv + row[g]), y);
             (void)k;
         }
     }
     if constexpr (ND > 0) {
-        double v[ND];
+        double vals[ND];
 #pragma unroll
-        for (int k = 0; k < ND; ++k) v[k] = acc[k].value();
-        finish_reduction<ND>(v, tile, ct.ntiles, ct.col, p.R, sc, p.epi, p.it, p.maxit, s_red,
+        for (int k = 0; k < ND; ++k) vals[k] = acc[k].value();
+        finish_reduction<ND>(vals, tile, ct.ntiles, ct.col, p.R, sc, p.epi, p.it, p.maxit, s_red,
                              &s_last);
     }
 }

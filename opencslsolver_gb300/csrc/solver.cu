@@ -1366,14 +1366,12 @@ int ensure_coloured(ocsl_ctx* c)
         ocsl_destroy(t);
         return fail(c, rc, "multicolour pattern: " + msg);
     }
-    // Two colours (red-black): sweep colour by colour, one launch per colour
-    // (ascending forward, descending backward), and the fused preconditioner
-    // in two launches.  With more colours the per-launch cost outweighs the
-    // waits: on the tet 64^3 x 6 system (4 colours) six fused launches took
-    // 88 us per FP64 preconditioner against 71 us for the two single-launch
-    // level-scheduled sweeps, which the child then keeps.
+    // Sweep colour by colour: one launch per colour (ascending forward,
+    // descending backward), and the fused preconditioner (2C - 2 launches for
+    // C colours).  With at most kRangeMaxLevels colours; beyond, the child
+    // keeps the single-launch level-scheduled sweeps.
     DevPattern& Q = t->P;
-    Q.coloured = cp.colours <= 2;
+    Q.coloured = cp.colours <= kRangeMaxLevels;
     Q.fw_nrange = Q.bw_nrange = Q.coloured ? cp.colours : 0;
     for (int k = 0; Q.coloured && k < cp.colours; ++k) {
         Q.fw_range[2 * k] = cp.start[k];
