@@ -29,15 +29,27 @@ constexpr double kAlpha = 0.7;  // solvers_common.h:29
 
 enum Target { T_LL, T_LR, T_RR, T_RL, T_BL, T_BR, T_ML, T_MR };
 
-struct Ops {
-    int n = 0;
-    int tgt[12];
-    double v[12];
-    __device__ void add(int t, double x)
+// The running sums of one cell's row while it walks a face: a face
+// contribution with target t lands in the diagonal, this face's off-diagonal
+// slot, b or total_mdot when t names the cell's side of the face, else
+// nowhere -- in call order, so every sum is the reference's sequence of
+// additions.  (Targets are constants at every call site once inlined.)
+struct Sink {
+    bool left;
+    double a, b, tm, off;
+    __device__ __forceinline__ void add(int t, double x)
     {
-        tgt[n] = t;
-        v[n] = x;
-        ++n;
+        if (left) {
+            if (t == T_LL) a += x;
+            else if (t == T_LR) off += x;
+            else if (t == T_BL) b += x;
+            else if (t == T_ML) tm += x;
+        } else {
+            if (t == T_RR) a += x;
+            else if (t == T_RL) off += x;
+            else if (t == T_BR) b += x;
+            else if (t == T_MR) tm += x;
+        }
     }
 };
 
@@ -66,7 +78,7 @@ __device__ __forceinline__ double face_interp(int blended, double geo, double m,
 }
 
 // solvers_common.h:96-135
-__device__ __forceinline__ void convective(Ops& o, int blended, double geo, double m, double l,
+__device__ __forceinline__ void convective(Sink& o, int blended, double geo, double m, double l,
                                            double r)
 {
     if (m >= 0.0) {
@@ -89,7 +101,7 @@ __device__ __forceinline__ void convective(Ops& o, int blended, double geo, doub
 }
 
 // solvers_common.h:42-53
-__device__ __forceinline__ void diffusive(Ops& o, double D)
+__device__ __forceinline__ void diffusive(Sink& o, double D)
 {
     o.add(T_LL, D);
     o.add(T_LR, -D);
@@ -97,9 +109,12 @@ __device__ __forceinline__ void diffusive(Ops& o, double D)
     o.add(T_RL, -D);
 }
 
-// One interior face's contributions, in the reference's call order.
-__device__ void face_ops(const ocsl_assembly& q, const ocsl_flow_state& st, int n, int nf, int f,
-                         int L, int R, Ops& o)
+// One interior face's contributions, in the reference's call order.  mu_f
+// and pdum_f: the face's viscosity and pressure coefficient computed once per
+// face by the iteration (null: evaluated here, the same expressions).
+__device__ __forceinline__ void face_ops(const ocsl_assembly& q, const ocsl_flow_state& st, int n,
+                                         int nf, int f, int L, int R, const double* mu_f,
+                                         const double* pdum_f, Sink& o)
 {
     if (q.equation == OCSL_EQ_HEAT) {  // cheat_solver.cpp:32-37 (reads no flow state)
         diffusive(o, q.thermal_diffusivity * st.ksi_A[f]);
@@ -110,8 +125,7 @@ __device__ void face_ops(const ocsl_assembly& q, const ocsl_flow_state& st, int 
         const double* u = st.velocity + (size_t)q.dimension * n;
         convective(o, q.blended, g, m, u[L], u[R]);
         if (q.viscous) {
-            const double Tf = face_avg(g, st.temperature[L], st.temperature[R]);
-            double D = mu(q, Tf);
+            double D = mu_f ? mu_f[f] : mu(q, face_avg(g, st.temperature[L], st.temperature[R]));
             D = D * st.ksi_A[f];
             diffusive(o, D);
             const double sp = st.stress[(size_t)q.dimension * nf + f];
@@ -123,16 +137,20 @@ __device__ void face_ops(const ocsl_assembly& q, const ocsl_flow_state& st, int 
         o.add(T_BR, m);
         o.add(T_ML, m);
         o.add(T_MR, -m);
-        const double Tf = face_interp(q.blended, g, m, st.temperature[L], st.temperature[R]);
-        double dum = drho_dp(q, Tf);
-        dum = dum / st.density[f];
-        dum *= m;
+        double dum;
+        if (pdum_f) {
+            dum = pdum_f[f];
+        } else {
+            const double Tf = face_interp(q.blended, g, m, st.temperature[L], st.temperature[R]);
+            dum = drho_dp(q, Tf);
+            dum = dum / st.density[f];
+            dum *= m;
+        }
         convective(o, q.blended, g, dum, st.pressure_corr[L], st.pressure_corr[R]);
         diffusive(o, st.qy[f] * st.density[f]);
     } else {  // :334-345
         convective(o, q.blended, g, m, st.enthalpy[L], st.enthalpy[R]);
-        const double Tf = face_avg(g, st.temperature[L], st.temperature[R]);
-        double D = mu(q, Tf);
+        double D = mu_f ? mu_f[f] : mu(q, face_avg(g, st.temperature[L], st.temperature[R]));
         D = D / q.prandtl * st.ksi_A[f];
         diffusive(o, D);
     }
@@ -229,7 +247,8 @@ __device__ void bc_apply(const ocsl_assembly& q, const ocsl_flow_state& st, int 
 
 __global__ void __launch_bounds__(kThreads)
 assemble_kernel(DevPattern P, DevFaces F, ocsl_assembly q, ocsl_flow_state st, double* value,
-                double* bvec, double* x0, double* ap, double* total_mdot)
+                double* bvec, double* x0, double* ap, double* total_mdot, const double* face_mu,
+                const double* face_pdum)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = P.n;
@@ -237,30 +256,23 @@ assemble_kernel(DevPattern P, DevFaces F, ocsl_assembly q, ocsl_flow_state st, d
     const int r0 = P.rp[i], r1 = P.rp[i + 1];
     for (int k = r0; k < r1; ++k) value[k] = 0.0;  // clear (phantoms stay 0)
     Acc c;
+    Sink o;
+    o.a = 0.0;
+    o.b = 0.0;
+    o.tm = 0.0;
     // interior faces, ascending
     for (int e = F.cell_ptr[i]; e < F.cell_ptr[i + 1]; ++e) {
         const int ent = F.cell_ent[e];
         const int f = ent >> 1;
-        const bool is_left = (ent & 1) == 0;
         const int k = F.cell_slot[e];
-        Ops o;
-        face_ops(q, st, n, F.nf, f, F.left[f], F.right[f], o);
-        for (int t = 0; t < o.n; ++t) {
-            const int tg = o.tgt[t];
-            const double v = o.v[t];
-            if (is_left) {
-                if (tg == T_LL) c.a += v;
-                else if (tg == T_LR) value[k] += v;
-                else if (tg == T_BL) c.b += v;
-                else if (tg == T_ML) c.tm += v;
-            } else {
-                if (tg == T_RR) c.a += v;
-                else if (tg == T_RL) value[k] += v;
-                else if (tg == T_BR) c.b += v;
-                else if (tg == T_MR) c.tm += v;
-            }
-        }
+        o.left = (ent & 1) == 0;
+        o.off = value[k];  // continues this slot's sum (0 unless an earlier face shares it)
+        face_ops(q, st, n, F.nf, f, F.left[f], F.right[f], face_mu, face_pdum, o);
+        value[k] = o.off;
     }
+    c.a = o.a;
+    c.b = o.b;
+    c.tm = o.tm;
     // boundary faces, ascending
     for (int e = F.bc_ptr[i]; e < F.bc_ptr[i + 1]; ++e) bc_apply(q, st, n, F.nb, F.bc_ent[e], i, c);
     // cell terms (:143-172 momentum, :273-296 pressure, :413-436 enthalpy)
@@ -349,11 +361,12 @@ bc_value_grad_kernel(DevFaces F, ocsl_assembly q, ocsl_flow_state st, const doub
 
 void launch_assemble(cudaStream_t st, const DevPattern& P, const DevFaces& F,
                      const ocsl_assembly& q, const ocsl_flow_state& s, double* value, double* b,
-                     double* x0, double* ap, double* total_mdot)
+                     double* x0, double* ap, double* total_mdot, const double* face_mu,
+                     const double* face_pdum)
 {
     if (P.n == 0) return;
-    assemble_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(P, F, q, s, value, b, x0,
-                                                                        ap, total_mdot);
+    assemble_kernel<<<(P.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+        P, F, q, s, value, b, x0, ap, total_mdot, face_mu, face_pdum);
 }
 
 void launch_bc_value_grad(cudaStream_t st, const DevFaces& F, const ocsl_assembly& q,

@@ -18,6 +18,7 @@
 // bit-identical to it.
 #include <cfloat>
 
+#include "division.cuh"
 #include "ocsl_internal.cuh"
 
 namespace ocsl {
@@ -88,6 +89,22 @@ __device__ __forceinline__ double enthalpy(const FlowDev& f, double T, double u0
 __device__ __forceinline__ double viscosity(const FlowDev& f, double T)
 {
     return f.suth0 * (T * sqrt(T)) / (T + f.suth1);
+}
+
+// The face-loop translation unit's forms (cflow_solver_cell_face_loops.cpp
+// as compiled: the other product of a*b + c*d is the contracted one there),
+// for the per-face values the assembly reads (assembly.cu uses the same).
+__device__ __forceinline__ double loop_face_avg(double geo, double l, double r)
+{
+    return fma(1.0 - geo, r, geo * l);
+}
+
+__device__ __forceinline__ double loop_face_interp(int blended, double geo, double m, double l,
+                                                   double r)
+{
+    if (m >= 0.0) return blended ? fma(kAlpha, loop_face_avg(geo, l, r), l * (1.0 - kAlpha)) : l;
+    if (m < 0.0) return blended ? fma(kAlpha, loop_face_avg(geo, l, r), r * (1.0 - kAlpha)) : r;
+    return 0.0;
 }
 
 // CFlow_solver::set_boundary_conditions (cflow_solver.cpp:195-227).  Outlets
@@ -184,12 +201,19 @@ __global__ void grad_kernel(int n, int nf, int nb, FlowDev f, DevFaces F)
 // The explicit part of the viscous stress (cflow_solver_cell_face_loops.cpp:
 // 25-35, tensor.h:194-225): mu(T_f) (grad u^T - 2/3 div u I) A, the gradients
 // taken along the cell-to-cell direction; T_f is the face-loop translation
-// unit's face average.
+// unit's face average.  mu(T_f) is kept per face (face_mu) for the momentum
+// and enthalpy assemblies of the iteration, which evaluate the same
+// expression on the same temperatures; without viscosity only face_mu.
+template <bool VISCOUS>
 __global__ void stress_kernel(int n, int nf, FlowDev f)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nf) return;
     const int L = f.left[k], R = f.right[k];
+    const double geo = f.geo_aver[k];
+    const double m = viscosity(f, loop_face_avg(geo, f.temperature[L], f.temperature[R]));
+    f.face_mu[k] = m;
+    if constexpr (!VISCOUS) return;
     const size_t N = n, NF = nf;
     double dv[3], un[3], A[3];
 #pragma unroll
@@ -198,17 +222,16 @@ __global__ void stress_kernel(int n, int nf, FlowDev f)
         un[d] = f.unit[d * NF + k];
         A[d] = f.area_vector[d * NF + k];
     }
-    const double dist = f.distance[k];
-    double div = dv[0] * un[0] / dist;
-    div = div + dv[1] * un[1] / dist;
-    div = div + dv[2] * un[2] / dist;
-    const double geo = f.geo_aver[k];
-    const double m = viscosity(f, fma(1.0 - geo, f.temperature[R], geo * f.temperature[L]));
+    // twelve quotients over one distance: one IEEE division (division.cuh)
+    const Recip dist = recip(f.distance[k]);
+    double div = divide(dv[0] * un[0], dist);
+    div = div + divide(dv[1] * un[1], dist);
+    div = div + divide(dv[2] * un[2], dist);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         double t[3];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) t[j] = dv[j] * un[i] / dist;  // transpose(grad u)
+        for (int j = 0; j < 3; ++j) t[j] = divide(dv[j] * un[i], dist);  // transpose(grad u)
         t[i] = fma(-(2.0 / 3.0), div, t[i]);
 #pragma unroll
         for (int j = 0; j < 3; ++j) t[j] = m * t[j];
@@ -260,6 +283,13 @@ __global__ void face_mdot_kernel(int n, int nf, FlowDev f, int blended)
     f.qy[k] = qy;
     f.face_density[k] = rho;
     f.mdot[k] = m;
+    // the pressure equation's convective coefficient of this face
+    // (cflow_solver_cell_face_loops.cpp:186-191), once per face
+    const double tf = loop_face_interp(blended, geo, m, f.temperature[L], f.temperature[R]);
+    double dum = drho_dp(f, tf);
+    dum = dum / rho;
+    dum *= m;
+    f.face_pdum[k] = dum;
 }
 
 // Boundary mass fluxes (cflow_solver_supply.cpp:51-93).
@@ -415,9 +445,13 @@ void launch_flow_grad(cudaStream_t st, bool corr, int n, int nf, int nb, const F
         grad_kernel<false><<<blocks(n), kThreads, 0, st>>>(n, nf, nb, f, F);
 }
 
-void launch_flow_stress(cudaStream_t st, int n, int nf, const FlowDev& f)
+void launch_flow_stress(cudaStream_t st, int n, int nf, const FlowDev& f, bool viscous)
 {
-    if (nf > 0) stress_kernel<<<blocks(nf), kThreads, 0, st>>>(n, nf, f);
+    if (nf == 0) return;
+    if (viscous)
+        stress_kernel<true><<<blocks(nf), kThreads, 0, st>>>(n, nf, f);
+    else
+        stress_kernel<false><<<blocks(nf), kThreads, 0, st>>>(n, nf, f);
 }
 
 void launch_flow_velocity_update(cudaStream_t st, int n, int d, const double* x, const FlowDev& f,

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cfloat>
 
+#include "division.cuh"
 #include "ocsl_internal.cuh"
 
 namespace ocsl {
@@ -359,18 +360,9 @@ constexpr int kSerialK = 4;
 // infinities, NaN, values near over- or underflow) take the IEEE division.
 // Four dependent FP64 operations instead of a division, which costs about
 // nine times one of them on this GPU.
-__device__ __forceinline__ bool markstein_range(double v)
-{
-    const int e = (__double2hiint(v) >> 20) & 0x7ff;  // biased exponent
-    return e >= 1023 - 500 && e <= 1023 + 500;
-}
-
 __device__ __forceinline__ double div_rcp(double a, double b, double y, double ylo, bool b_ok)
 {
-    if (!b_ok || !markstein_range(a)) return a / b;
-    const double q = fma(a, y, a * ylo);
-    const double r = fma(-b, q, a);
-    return fma(r, y, q);
+    return divide(a, Recip{b, y, ylo, b_ok});  // division.cuh
 }
 
 __device__ __forceinline__ float div_rcp(float a, float b, float, float, bool) { return a / b; }

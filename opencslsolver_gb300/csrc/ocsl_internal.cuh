@@ -317,9 +317,12 @@ void launch_factor_outputs(cudaStream_t st, const DevPattern& P, const double* M
                            int* pivot_err = nullptr);
 
 // assembly.cu
+// face_mu / face_pdum (FlowDev): per-face values computed once per iteration
+// (bit-identical to evaluating them per face side); null: evaluated here.
 void launch_assemble(cudaStream_t st, const DevPattern& P, const DevFaces& F,
                      const ocsl_assembly& q, const ocsl_flow_state& s, double* value, double* b,
-                     double* x0, double* ap, double* total_mdot);
+                     double* x0, double* ap, double* total_mdot, const double* face_mu = nullptr,
+                     const double* face_pdum = nullptr);
 void launch_bc_value_grad(cudaStream_t st, const DevFaces& F, const ocsl_assembly& q,
                           const ocsl_flow_state& s, const double* lambda, double* grad);
 
@@ -356,6 +359,11 @@ struct FlowDev {
     double* face_density;
     double* qy;
     double* stress;              // [3][nf], viscous flows
+    // per-face values the iteration's assemblies share (library buffers [nf]):
+    // mu(T_f) of the face-loop translation unit (momentum and enthalpy) and
+    // the pressure equation's convective coefficient drho/dp(T_f) / rho_f * m
+    double* face_mu;
+    double* face_pdum;
     // boundary faces
     const int* bc_type;
     const int* bc_left;
@@ -382,7 +390,8 @@ struct FlowDev {
 void launch_flow_set_bc(cudaStream_t st, int n, int nb, const FlowDev& f);
 void launch_flow_grad(cudaStream_t st, bool corr, int n, int nf, int nb, const FlowDev& f,
                       const DevFaces& F);
-void launch_flow_stress(cudaStream_t st, int n, int nf, const FlowDev& f);
+// stress (viscous) and face_mu; face_mu alone when !viscous
+void launch_flow_stress(cudaStream_t st, int n, int nf, const FlowDev& f, bool viscous);
 void launch_flow_velocity_update(cudaStream_t st, int n, int d, const double* x, const FlowDev& f,
                                  double* res);
 void launch_flow_face_mdot(cudaStream_t st, int n, int nf, int nb, const FlowDev& f, int blended);

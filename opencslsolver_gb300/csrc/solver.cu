@@ -216,6 +216,8 @@ struct ocsl_ctx {
     double* d_fb = nullptr;
     double* d_fx = nullptr;
     double* d_ftmp = nullptr;
+    double* d_fmu = nullptr;    // [nf] FlowDev::face_mu
+    double* d_fpdum = nullptr;  // [nf] FlowDev::face_pdum
     FlowOut* d_fout = nullptr;
     FlowOut* h_fout = nullptr;
     const void* flow_bc_checked = nullptr;
@@ -298,7 +300,7 @@ void ocsl_ctx::free_pattern()
     for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
     F = DevFaces{};
     has_faces = false;
-    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp};
+    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp, &d_fmu, &d_fpdum};
     for (auto pp : dflow) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     flow_bc_checked = nullptr;
     for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
@@ -2499,6 +2501,8 @@ int ocsl_set_faces(ocsl_ctx* c, int64_t n_faces, const int32_t* left, const int3
             return fail(c, OCSL_BAD_ARGUMENT, err);
         CK(cudaStreamSynchronize(c->stream));
         for (auto& p : c->d_faces) { if (p) cudaFree(p); p = nullptr; }
+        for (double** pp : {&c->d_fmu, &c->d_fpdum}) { if (*pp) cudaFree(*pp); *pp = nullptr; }
+        c->drop_flow_graph();  // its launches read the old face tables and buffers
         c->has_faces = false;
         c->flow_bc_checked = nullptr;
         const std::vector<int> l(left, left + n_faces), r(right, right + n_faces),
@@ -2684,13 +2688,15 @@ static void enqueue_flow(ocsl_ctx* c, cudaStream_t st, const ocsl_assembly* q,
     launch_flow_set_bc(st, n, nb, f);
     launch_flow_grad(st, false, n, nf, nb, f, c->F);
     CK(cudaMemsetAsync(f.ap, 0, sizeof(double) * n, st));  // :244-247
-    if (q->viscous) launch_flow_stress(st, n, nf, f);      // :250-255
+    // :250-255; and mu(T_f) per face for the momentum and enthalpy assemblies
+    // (the temperature changes only in the enthalpy update at the end)
+    launch_flow_stress(st, n, nf, f, q->viscous != 0);
     // momentum components (:257-302)
     for (int d = 0; d < 3; ++d) {
         qe.equation = OCSL_EQ_MOMENTUM;
         qe.dimension = d;
         launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx,
-                        f.ap_vec + (size_t)d * n, it->total_mdot);
+                        f.ap_vec + (size_t)d * n, it->total_mdot, f.face_mu);
         solve(d, methods[0]);
         launch_flow_velocity_update(st, n, d, c->d_fx, f, c->d_ftmp);
         residual(c->d_ftmp, d);
@@ -2699,7 +2705,8 @@ static void enqueue_flow(ocsl_ctx* c, cudaStream_t st, const ocsl_assembly* q,
     launch_flow_face_mdot(st, n, nf, nb, f, q->blended);  // and the boundary faces', :312-315
     qe.equation = OCSL_EQ_PRESSURE;
     qe.dimension = 0;
-    launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, it->total_mdot);
+    launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, it->total_mdot,
+                    nullptr, f.face_pdum);
     residual(c->d_fb, 3);  // Pressure_global_residual = ABSsum(b), :346
     solve(3, methods[1]);
     launch_flow_pcorr(st, n, nb, c->d_fx, f);  // and the boundary pressures, :361-372
@@ -2708,7 +2715,8 @@ static void enqueue_flow(ocsl_ctx* c, cudaStream_t st, const ocsl_assembly* q,
     launch_flow_correct(st, n, nf, nb, f, q->blended);
     // enthalpy (:428-474)
     qe.equation = OCSL_EQ_ENTHALPY;
-    launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, nullptr);
+    launch_assemble(st, c->P, c->F, qe, *s, c->d_fval, c->d_fb, c->d_fx, nullptr, nullptr,
+                    f.face_mu);
     solve(4, methods[2]);
     launch_flow_enthalpy_update(st, n, c->d_fx, f, c->d_ftmp);
     residual(c->d_ftmp, 4);
@@ -2860,6 +2868,12 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
             c->d_fx = dalloc<double>((size_t)n);
             c->d_ftmp = dalloc<double>((size_t)n);
         }
+        if (!c->d_fmu && c->F.nf > 0) {
+            c->d_fmu = dalloc<double>((size_t)c->F.nf);
+            c->d_fpdum = dalloc<double>((size_t)c->F.nf);
+        }
+        f.face_mu = c->d_fmu;
+        f.face_pdum = c->d_fpdum;
         if (!c->d_fout) {
             c->d_fout = dalloc<ocsl_ctx::FlowOut>(1);
             CK(cudaMallocHost(&c->h_fout, sizeof *c->h_fout));
