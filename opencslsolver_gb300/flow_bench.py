@@ -10,7 +10,8 @@ state of CFlow_solver::initialize (``flow.initial_state``: a 3D viscous channel,
 velocity inlet (20, 3, 2) m/s at 300 K, no-slip walls, pressure outlet, 1e5 Pa,
 transient dt 2e-6 s, blended convection), then ``--inner`` device inner
 iterations with each solver choice, the reference's (one CUDA graph per
-iteration), the FP64 tolerance mode and the FP32-inner / FP64-refined mode.
+iteration), the FP64 tolerance mode and the FP32-inner / FP64-refined mode,
+the last two also through the multicolour ordering (ocsl_set_ordering).
 Prints one JSON object (``bench.py`` times the CPU restatement beside it).
 """
 from __future__ import annotations
@@ -68,6 +69,10 @@ def methods():
             "fp32_refined": (ocsl.ILU_BICGSTAB_IR32,) * 3}
 
 
+# solver choices run a second time through the multicolour ordering
+MULTICOLOUR = ("fp64_tolerance", "fp32_refined")
+
+
 def time_gpu(case: dict, inner: int, device: int = 0) -> dict:
     """ms per inner iteration for every solver choice (two untimed calls
     first: allocation, then the graph capture of the reference's solvers)."""
@@ -81,8 +86,11 @@ def time_gpu(case: dict, inner: int, device: int = 0) -> dict:
 
     ctx = ocsl.Context(device)
     out = {}
+    runs = [(name, m, "natural") for name, m in methods().items()]
+    runs += [(name + "_multicolour", methods()[name], "multicolour") for name in MULTICOLOUR]
     try:
-        for name, m in methods().items():
+        for name, m, ordering in runs:
+            ctx.set_ordering(ordering)
             run = F.FlowRun(ctx, copy.deepcopy(case))
             run.iterate(m)
             run.iterate(m)
