@@ -73,9 +73,10 @@ def methods():
 MULTICOLOUR = ("fp64_tolerance", "fp32_refined")
 
 
-def time_gpu(case: dict, inner: int, device: int = 0) -> dict:
+def time_gpu(case: dict, inner: int, device: int = 0, only=None) -> dict:
     """ms per inner iteration for every solver choice (two untimed calls
-    first: allocation, then the graph capture of the reference's solvers)."""
+    first: allocation, then the graph capture of the reference's solvers);
+    `only`: the one choice to run (a key of the result)."""
     import copy
 
     import numpy as np
@@ -88,6 +89,10 @@ def time_gpu(case: dict, inner: int, device: int = 0) -> dict:
     out = {}
     runs = [(name, m, "natural") for name, m in methods().items()]
     runs += [(name + "_multicolour", methods()[name], "multicolour") for name in MULTICOLOUR]
+    if only is not None:
+        runs = [r for r in runs if r[0] == only]
+        if not runs:
+            raise ValueError(f"unknown solver choice {only!r}")
     try:
         for name, m, ordering in runs:
             ctx.set_ordering(ordering)
@@ -116,9 +121,11 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--inner", type=int, default=10)
+    ap.add_argument("--only", default=None,
+                    help="run one solver choice (e.g. fp32_refined_multicolour)")
     a = ap.parse_args(argv)
     case, info = box_case(a.size)
-    info["gpu"] = time_gpu(case, a.inner)
+    info["gpu"] = time_gpu(case, a.inner, only=a.only)
     print(json.dumps(info))
     return 0
 
