@@ -26,6 +26,8 @@ def main(argv=None):
     ap.add_argument("--cluster", type=int, nargs=2, default=(1, 1),
                     help="structured sweep tiles per thread-block cluster")
     ap.add_argument("--inner-tol", type=float, default=None, help="IR32 inner tolerance")
+    ap.add_argument("--ordering", default="natural", choices=["natural", "multicolour"],
+                    help="row ordering of the tolerance-mode solves")
     ap.add_argument("--profile", action="store_true",
                     help="print CUDA-event time per launch by kernel category (last solve)")
     a = ap.parse_args(argv)
@@ -45,6 +47,7 @@ def main(argv=None):
     ctx.set_pattern(s.row_ptr, s.column_index)
     ctx.set_sweep_kernel(a.sweep_kernel, *a.tiles)
     ctx.set_sweep_cluster(*a.cluster)
+    ctx.set_ordering(a.ordering)
     A = torch.from_numpy(s.value).cuda()
     B = torch.from_numpy(s.b).cuda()
     X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
