@@ -222,16 +222,22 @@ __global__ void stress_kernel(int n, int nf, FlowDev f)
         un[d] = f.unit[d * NF + k];
         A[d] = f.area_vector[d * NF + k];
     }
-    // twelve quotients over one distance: one IEEE division (division.cuh)
+    // the nine quotients (dv_j un_i) / dist over one distance: one IEEE
+    // division (division.cuh); div u sums the three with i = j
     const Recip dist = recip(f.distance[k]);
-    double div = divide(dv[0] * un[0], dist);
-    div = div + divide(dv[1] * un[1], dist);
-    div = div + divide(dv[2] * un[2], dist);
+    double g[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) g[i][j] = divide(dv[j] * un[i], dist);  // transpose(grad u)
+    double div = g[0][0];
+    div = div + g[1][1];
+    div = div + g[2][2];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         double t[3];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) t[j] = divide(dv[j] * un[i], dist);  // transpose(grad u)
+        for (int j = 0; j < 3; ++j) t[j] = g[i][j];
         t[i] = fma(-(2.0 / 3.0), div, t[i]);
 #pragma unroll
         for (int j = 0; j < 3; ++j) t[j] = m * t[j];
@@ -249,7 +255,11 @@ __global__ void velocity_update_kernel(int n, int d, const double* x, FlowDev f,
     double* u = f.velocity + (size_t)d * n;
     res[c] = fabs(u[c] - x[c]);
     u[c] = x[c];
-    f.ap[c] = fma(f.ap_vec[(size_t)d * n + c], 1.0 / 3.0, f.ap[c]);  // a / 3 as a * (1/3)
+    const double ap = fma(f.ap_vec[(size_t)d * n + c], 1.0 / 3.0, f.ap[c]);  // a / 3 as a * (1/3)
+    f.ap[c] = ap;
+    // ap is final after the last component: vol / ap once per cell for the
+    // face and boundary mass fluxes (each face side divided again before)
+    if (d == 2) f.vol_ap[c] = f.volume[c] / ap;
 }
 
 // Face mass flux with the pressure-gradient (Rhie-Chow-like) correction
@@ -260,7 +270,7 @@ __global__ void face_mdot_kernel(int n, int nf, FlowDev f, int blended)
     if (k >= nf) return;
     const int L = f.left[k], R = f.right[k];
     const size_t n1 = n, n2 = 2 * (size_t)n, f1 = nf, f2 = 2 * (size_t)nf;
-    const double qy = (f.volume[L] / f.ap[L] + f.volume[R] / f.ap[R]) *
+    const double qy = (f.vol_ap[L] + f.vol_ap[R]) *
                       dot3(f.alpha[k], f.alpha[f1 + k], f.alpha[f2 + k], f.area_vector[k],
                            f.area_vector[f1 + k], f.area_vector[f2 + k]);
     const double geo = f.geo_aver[k];
@@ -304,14 +314,14 @@ __global__ void bc_mdot_kernel(int n, int nb, FlowDev f)
         f.bc_mdot[g] = density(f, f.pressure[c], f.bc_temperature[g]) *
                        dot3(f.bc_velocity, B, g, f.bc_area_vector, B, g);
     } else if (kind == OCSL_BC_SUPERSONIC_INLET) {
-        f.bc_qy[g] = f.volume[c] / f.ap[c] * dot3(f.bc_alpha, B, g, f.bc_area_vector, B, g);
+        f.bc_qy[g] = f.vol_ap[c] * dot3(f.bc_alpha, B, g, f.bc_area_vector, B, g);
     } else if (kind == OCSL_BC_PRESSURE_OUTLET) {
         const double ua = dot3(f.velocity, N, c, f.bc_area_vector, B, g);
         if (f.bc_supersonic[g]) {
             f.bc_mdot[g] = density(f, f.pressure[c], f.temperature[c]) * ua;
             f.bc_qy[g] = 1.0;
         } else {
-            const double qy = f.volume[c] / f.ap[c] * dot3(f.bc_alpha, B, g, f.bc_area_vector, B, g);
+            const double qy = f.vol_ap[c] * dot3(f.bc_alpha, B, g, f.bc_area_vector, B, g);
             const double dist = f.bc_distance[g];
             const double t = f.bc_pressure[g] - f.pressure[c] -
                              0.5 * dot3(f.pressure_grad[c], f.pressure_grad[N + c],

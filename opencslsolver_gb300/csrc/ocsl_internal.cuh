@@ -364,6 +364,7 @@ struct FlowDev {
     // the pressure equation's convective coefficient drho/dp(T_f) / rho_f * m
     double* face_mu;
     double* face_pdum;
+    double* vol_ap;  // [n] volume / ap after the momentum components (library buffer)
     // boundary faces
     const int* bc_type;
     const int* bc_left;

@@ -218,6 +218,7 @@ struct ocsl_ctx {
     double* d_ftmp = nullptr;
     double* d_fmu = nullptr;    // [nf] FlowDev::face_mu
     double* d_fpdum = nullptr;  // [nf] FlowDev::face_pdum
+    double* d_fvolap = nullptr;  // [n] FlowDev::vol_ap
     FlowOut* d_fout = nullptr;
     FlowOut* h_fout = nullptr;
     const void* flow_bc_checked = nullptr;
@@ -300,7 +301,7 @@ void ocsl_ctx::free_pattern()
     for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
     F = DevFaces{};
     has_faces = false;
-    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp, &d_fmu, &d_fpdum};
+    double** dflow[] = {&d_fval, &d_fb, &d_fx, &d_ftmp, &d_fmu, &d_fpdum, &d_fvolap};
     for (auto pp : dflow) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     flow_bc_checked = nullptr;
     for (auto& p : d_pat) { if (p) cudaFree(p); p = nullptr; }
@@ -2867,6 +2868,7 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
             c->d_fb = dalloc<double>((size_t)n);
             c->d_fx = dalloc<double>((size_t)n);
             c->d_ftmp = dalloc<double>((size_t)n);
+            c->d_fvolap = dalloc<double>((size_t)n);
         }
         if (!c->d_fmu && c->F.nf > 0) {
             c->d_fmu = dalloc<double>((size_t)c->F.nf);
@@ -2874,6 +2876,7 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
         }
         f.face_mu = c->d_fmu;
         f.face_pdum = c->d_fpdum;
+        f.vol_ap = c->d_fvolap;
         if (!c->d_fout) {
             c->d_fout = dalloc<ocsl_ctx::FlowOut>(1);
             CK(cudaMallocHost(&c->h_fout, sizeof *c->h_fout));

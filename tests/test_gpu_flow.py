@@ -20,8 +20,9 @@ implicit under-relaxation ramp) cases, and a 3D viscous channel on a
   one, the state within 5e-9 of the reference run that uses
   ILU_BICGSTAB_solve everywhere (measured 1.1e-9 on the shock tube: the
   reference's own solves stop after a fixed count; p' and its gradient,
-  nearly zero in a settled flow, are reported, not bounded); the same bound
-  with those solves run through the multicolour ordering.
+  nearly zero in a settled flow, are reported, not bounded); with those
+  solves run through the multicolour ordering (another ILU(0) factor, the
+  same residual), within 1e-7 (measured 2.3e-8 on the shock tube).
 * Input the iteration cannot take is refused before anything is written.
 """
 import time
@@ -123,8 +124,12 @@ def test_recorded_run_vs_reference(ctx, torch_cuda, case, mode):
         assert max(errs.values()) <= 1e-8, errs
     else:
         # converged solves against fixed-count ones: the state; the derived
-        # fields of a nearly settled p' carry no meaningful relative error
-        assert state <= 5e-9, errs
+        # fields of a nearly settled p' carry no meaningful relative error.
+        # Through the multicolour ordering the solves reach the same 1e-10
+        # residual with another factor, so their solutions differ from the
+        # natural-order ones within the conditioning of each equation
+        # (measured 2.3e-8 in the shock tube's enthalpy over 1000 iterations)
+        assert state <= (1e-7 if mode.endswith("_mc") else 5e-9), errs
 
 
 def test_rejects_unsupported_input(ctx, torch_cuda):
