@@ -550,8 +550,13 @@ int ocsl_inject_fault(ocsl_ctx* ctx, int kind);
 #define OCSL_ORDER_MULTICOLOUR 1
 int ocsl_set_ordering(ocsl_ctx* ctx, int ordering);
 /* The ordering in use, and the colour count and sweep levels (forward,
- * backward) of the permuted pattern: zeros while it is not built. */
-int ocsl_ordering_info(const ocsl_ctx* ctx, int* ordering, int* colours, int32_t* levels);
+ * backward) of the permuted pattern: zeros while it is not built.  *stencil
+ * is 1 when the permuted pattern is the red-black ordering of a 7-point box
+ * with an even x extent: SpMV and preconditioner then read stencil records
+ * (neighbour rows computed, no column indices), bit-identical to the CSR
+ * kernels. */
+int ocsl_ordering_info(const ocsl_ctx* ctx, int* ordering, int* colours, int32_t* levels,
+                       int* stencil);
 /* perm[new row] = original row of the multicolour ordering (n entries,
  * host memory); builds the permuted pattern if needed. */
 int ocsl_ordering_permutation(ocsl_ctx* ctx, int32_t* perm, size_t n);

@@ -378,14 +378,15 @@ class Context:
         self._check(self._L.ocsl_set_ordering(self._h, int(code)), "set_ordering")
 
     def ordering_info(self):
-        """{"ordering", "colours", "levels": (forward, backward)} of the
-        permuted pattern (zeros until a solve or ordering_permutation built it)."""
-        o, k = C.c_int(), C.c_int()
+        """{"ordering", "colours", "levels": (forward, backward), "stencil"}
+        of the permuted pattern (zeros until a solve or ordering_permutation
+        built it); stencil: red-black box records in use."""
+        o, k, st = C.c_int(), C.c_int(), C.c_int()
         lv = (C.c_int32 * 2)()
-        self._check(self._L.ocsl_ordering_info(self._h, C.byref(o), C.byref(k), lv),
-                    "ordering_info")
+        self._check(self._L.ocsl_ordering_info(self._h, C.byref(o), C.byref(k), lv,
+                                               C.byref(st)), "ordering_info")
         return {"ordering": "multicolour" if o.value == _abi.ORDER_MULTICOLOUR else "natural",
-                "colours": k.value, "levels": (lv[0], lv[1])}
+                "colours": k.value, "levels": (lv[0], lv[1]), "stencil": bool(st.value)}
 
     def ordering_permutation(self):
         """perm[new row] = original row of the multicolour ordering (int32 numpy)."""

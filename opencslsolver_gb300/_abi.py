@@ -222,7 +222,7 @@ _PROTOS = {
     "ocsl_set_col_batching": (C.c_int, [_CTX, C.c_int]),
     "ocsl_set_ordering": (C.c_int, [_CTX, C.c_int]),
     "ocsl_ordering_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                     C.POINTER(C.c_int32)]),
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int)]),
     "ocsl_ordering_permutation": (C.c_int, [_CTX, C.POINTER(C.c_int32), _SZ]),
     "ocsl_colour_pattern": (C.c_int, [_SZ, _P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                       C.c_char_p, _SZ]),

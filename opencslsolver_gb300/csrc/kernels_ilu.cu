@@ -22,6 +22,7 @@
 // change a single bit of the result.
 #include <algorithm>
 #include <cfloat>
+#include <type_traits>
 
 #include "division.cuh"
 #include "ocsl_internal.cuh"
@@ -334,6 +335,50 @@ RangeParams<T> make_range(const DevPattern& P, const T* M, const T* dinv, const 
     return p;
 }
 
+// The preconditioner on a red-black box's records (RbGeom), arithmetic of
+// range_sweep_kernel: colour 1 (KIND 1: y = rhs - sum over z-, y-, x-, x+,
+// y+, z+ of M y with y = rhs on colour 0, then x = y / M_ii or y dinv),
+// colour 0 (KIND 2: x = (rhs - sum over the same neighbours of M x) / M_ii or
+// dinv); neighbour rows computed, not read.
+template <typename T, int KIND, bool DIV>
+__global__ void __launch_bounds__(kThreads, 8) rb_precond_kernel(RbGeom g, const T* rec,
+                                                                 const T* dinv, const T* rhs,
+                                                                 T* out, const int* done)
+{
+    if (done && *done) return;
+    using V = typename std::conditional<sizeof(T) == 8, double4, float4>::type;
+    const int t = (KIND == 1 ? g.n0 : 0) + (int)(blockIdx.x * kThreads + threadIdx.x);
+    if (t >= (KIND == 1 ? g.n : g.n0)) return;
+    const RbRow q = rb_row_info(g, t);
+    const V* lo = reinterpret_cast<const V*>(rec);
+    const V l = lo[t], h = lo[g.n + t];
+    const T v[6] = {l.x, l.y, l.z, l.w, h.x, h.y};
+    const T* src = KIND == 1 ? rhs : out;  // colour 0's y is rhs; colour 1's x is out
+    T xn[6];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) xn[s] = q.has[s] ? __ldg(src + q.nb[s]) : T(0);
+    T sum = T(0);
+#pragma unroll
+    for (int s = 0; s < 6; ++s)
+        if (q.has[s]) sum = fma_t(v[s], xn[s], sum);
+    const T num = __ldg(rhs + t) - sum;
+    out[t] = DIV ? num / h.z : num * __ldg(dinv + t);
+}
+
+// CSR values -> red-black stencil records through the slot map.
+template <typename TO>
+__global__ void __launch_bounds__(kThreads) rb_records_kernel(int n, const int* rp,
+                                                              const signed char* slot,
+                                                              const double* M, TO* rec)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    for (int q = __ldg(rp + t); q < __ldg(rp + t + 1); ++q) {
+        const int s = slot[q];
+        if (s >= 0) rec[((size_t)(s >> 2) * n + t) * 4 + (s & 3)] = (TO)M[q];
+    }
+}
+
 // Tiny systems with a deep schedule (the 1D shock tube's chain: one row per
 // level): a single warp walks the rows in natural order (reverse order for
 // the backward sweep), a topological order of either triangle, so there is
@@ -617,6 +662,33 @@ void launch_range_sweep(cudaStream_t st, const DevPattern& P, bool forward, cons
 }
 
 template <typename T>
+void launch_rb_precond(cudaStream_t st, const RbGeom& g, const T* rec, const T* dinv,
+                       const T* rhs, T* out, int divmode, const int* done)
+{
+    const int n1 = g.n - g.n0;
+    const bool div = divmode == 0;
+    if (n1 > 0) {
+        const int grid = (n1 + kThreads - 1) / kThreads;
+        if (div) rb_precond_kernel<T, 1, true><<<grid, kThreads, 0, st>>>(g, rec, dinv, rhs, out, done);
+        else rb_precond_kernel<T, 1, false><<<grid, kThreads, 0, st>>>(g, rec, dinv, rhs, out, done);
+    }
+    if (g.n0 > 0) {
+        const int grid = (g.n0 + kThreads - 1) / kThreads;
+        if (div) rb_precond_kernel<T, 2, true><<<grid, kThreads, 0, st>>>(g, rec, dinv, rhs, out, done);
+        else rb_precond_kernel<T, 2, false><<<grid, kThreads, 0, st>>>(g, rec, dinv, rhs, out, done);
+    }
+}
+
+template <typename TO>
+void launch_rb_records(cudaStream_t st, const RbGeom& g, const int* rp, const signed char* slot,
+                       const double* M, TO* rec)
+{
+    if (g.n > 0)
+        rb_records_kernel<TO><<<(g.n + kThreads - 1) / kThreads, kThreads, 0, st>>>(g.n, rp, slot,
+                                                                                  M, rec);
+}
+
+template <typename T>
 void launch_coloured_precond(cudaStream_t st, const DevPattern& P, const T* M, const T* dinv,
                              const T* rhs, T* tmp, T* out, int divmode, const int* done)
 {
@@ -725,6 +797,14 @@ template void launch_range_sweep<double>(cudaStream_t, const DevPattern&, bool, 
                                          const double*, const double*, double*, int, const int*);
 template void launch_range_sweep<float>(cudaStream_t, const DevPattern&, bool, const float*,
                                         const float*, const float*, float*, int, const int*);
+template void launch_rb_precond<double>(cudaStream_t, const RbGeom&, const double*,
+                                        const double*, const double*, double*, int, const int*);
+template void launch_rb_precond<float>(cudaStream_t, const RbGeom&, const float*, const float*,
+                                       const float*, float*, int, const int*);
+template void launch_rb_records<double>(cudaStream_t, const RbGeom&, const int*,
+                                        const signed char*, const double*, double*);
+template void launch_rb_records<float>(cudaStream_t, const RbGeom&, const int*,
+                                       const signed char*, const double*, float*);
 template void launch_coloured_precond<double>(cudaStream_t, const DevPattern&, const double*,
                                               const double*, const double*, double*, double*, int,
                                               const int*);

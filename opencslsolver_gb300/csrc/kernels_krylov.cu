@@ -512,6 +512,84 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
     }
 }
 
+// spmv_kernel on the red-black stencil records (RbGeom): the neighbours'
+// rows computed, not read; each row's chain in its CSR order (colour 0: the
+// diagonal, then z-, y-, x-, x+, y+, z+; colour 1: the neighbours, then the
+// diagonal), absent neighbours skipped -- bit-identical to spmv_kernel on
+// the permuted CSR, without column indices or row pointers.
+template <typename T>
+struct RbSpmvParams {
+    RbGeom g;
+    const T* rec;  // [2][n][4]
+    const T* x;
+    T* y;
+    const T* z;
+    T* y_copy;
+    const T* w;
+    T a;
+    ReduceState R;
+    Scalars* sc;
+    int epi, it, maxit;
+};
+
+template <typename T, int MODE, int DOTS>
+__global__ void __launch_bounds__(kThreads) rb_spmv_kernel(RbSpmvParams<T> p)
+{
+    Scalars* const sc = p.sc;
+    if (sc && sc->done) return;
+    constexpr int ND = DotCount<DOTS>::value;
+    using V = typename Rec4<T>::V;
+    __shared__ double s_red[kMaxDots * 8];
+    __shared__ int s_last;
+    const int tile = blockIdx.x;
+    const int n = p.g.n;
+    const V* lo = reinterpret_cast<const V*>(p.rec);
+    const V* hi = lo + n;
+    DotAcc<T> acc[ND > 0 ? ND : 1];
+#pragma unroll 1
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
+        if (row >= n) continue;
+        const RbRow q = rb_row_info(p.g, row);
+        const V l = lo[row], h = hi[row];
+        const T v[6] = {l.x, l.y, l.z, l.w, h.x, h.y};
+        T xn[6];
+#pragma unroll
+        for (int s = 0; s < 6; ++s) xn[s] = q.has[s] ? __ldg(p.x + q.nb[s]) : T(0);
+        const T xc = __ldg(p.x + row);
+        T dum = T(0);
+        if (q.c == 0) dum = fma_t(h.z, xc, dum);
+#pragma unroll
+        for (int s = 0; s < 6; ++s)
+            if (q.has[s]) dum = fma_t(v[s], xn[s], dum);
+        if (q.c == 1) dum = fma_t(h.z, xc, dum);
+        T y, zv = T(0);
+        if constexpr (MODE == 0) {
+            y = dum;
+        } else if constexpr (MODE == 1) {
+            zv = __ldg(p.z + row);
+            y = zv - dum;
+        } else {
+            zv = __ldg(p.z + row);
+            y = fma_t(p.a, dum, zv);
+        }
+        p.y[row] = y;
+        if (MODE == 1 && p.y_copy) p.y_copy[row] = y;
+        int k = 0;
+        if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
+        if constexpr ((DOTS & DOT_ZZ) != 0) acc[k++].add(zv, zv);
+        if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(p.w + row), y);
+        (void)k;
+    }
+    if constexpr (ND > 0) {
+        double vals[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) vals[k] = acc[k].value();
+        finish_reduction<ND>(vals, tile, (int)gridDim.x, 0, p.R, sc, p.epi, p.it, p.maxit, s_red,
+                             &s_last);
+    }
+}
+
 template <int OP>
 struct OpDots {
     static constexpr int value =
@@ -833,6 +911,52 @@ void launch_box_spmv(cudaStream_t st, int n, const int* dims, const T* rec, cons
     }
 }
 
+template <typename T, int MODE, int DOTS>
+void rb_spmv_dispatch(cudaStream_t st, const RbSpmvParams<T>& p)
+{
+    const int nt = ntiles_of(p.g.n);
+    if (nt > 0) rb_spmv_kernel<T, MODE, DOTS><<<nt, kThreads, 0, st>>>(p);
+}
+
+template <typename T, int MODE>
+void rb_spmv_dots(cudaStream_t st, const RbSpmvParams<T>& p, int dots)
+{
+    switch (dots) {
+    case 0: rb_spmv_dispatch<T, MODE, 0>(st, p); break;
+    case DOT_YY: rb_spmv_dispatch<T, MODE, DOT_YY>(st, p); break;
+    case DOT_YY | DOT_ZZ: rb_spmv_dispatch<T, MODE, DOT_YY | DOT_ZZ>(st, p); break;
+    case DOT_WY: rb_spmv_dispatch<T, MODE, DOT_WY>(st, p); break;
+    case DOT_YY | DOT_WY: rb_spmv_dispatch<T, MODE, DOT_YY | DOT_WY>(st, p); break;
+    default: break;
+    }
+}
+
+template <typename T>
+void launch_rb_spmv(cudaStream_t st, const RbGeom& g, const T* rec, const T* x, T* y, int mode,
+                    double a_const, const T* z, T* y_copy, const T* w, int dots,
+                    const ReduceState& R, Scalars* sc, int epi, int it, int maxit)
+{
+    RbSpmvParams<T> p;
+    p.g = g;
+    p.rec = rec;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.y_copy = y_copy;
+    p.w = w;
+    p.a = (T)a_const;
+    p.R = R;
+    p.sc = sc;
+    p.epi = epi;
+    p.it = it;
+    p.maxit = maxit;
+    switch (mode) {
+    case 0: rb_spmv_dots<T, 0>(st, p, dots); break;
+    case 1: rb_spmv_dots<T, 1>(st, p, dots); break;
+    default: rb_spmv_dots<T, 2>(st, p, dots); break;
+    }
+}
+
 template <typename T>
 void launch_vec(cudaStream_t st, int op, int n, const VecPtrs& ptrs, const ReduceState& R,
                 Scalars* sc, const Scalars* sc_outer, int epi, int it, int maxit,
@@ -889,6 +1013,12 @@ template void launch_spmv<float>(cudaStream_t, const DevPattern&, const float*, 
                                  float*, int, const double*, double, const float*, float*,
                                  const float*, int, const ReduceState&, Scalars*, int, int, int,
                                  const Cols&);
+template void launch_rb_spmv<double>(cudaStream_t, const RbGeom&, const double*, const double*,
+                                     double*, int, double, const double*, double*, const double*,
+                                     int, const ReduceState&, Scalars*, int, int, int);
+template void launch_rb_spmv<float>(cudaStream_t, const RbGeom&, const float*, const float*,
+                                    float*, int, double, const float*, float*, const float*, int,
+                                    const ReduceState&, Scalars*, int, int, int);
 template void launch_box_spmv<double>(cudaStream_t, int, const int*, const double*,
                                       const double*, double*, int, double, const double*,
                                       double*, const double*, int, const ReduceState&, Scalars*,

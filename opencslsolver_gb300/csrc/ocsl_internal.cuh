@@ -220,6 +220,92 @@ void launch_bw_sweep(cudaStream_t st, const DevPattern& P, const T* M, const T* 
 // bytes of shared memory (at most kSerialMaxBytes, which leaves the kernel's
 // row staging room under the 48 KB a launch may take without opting in).
 constexpr int kSerialMaxBytes = 40 * 1024;
+// A natural-order nx x ny x nz 7-point box with even nx in its red-black
+// (multicolour) ordering: colour 0 = cells with i + j + k even, numbered
+// first, each colour in natural order.  Since nx is even, every pair of cells
+// (2m, 2m + 1) of an x-line holds one of each colour, so natural cell p has
+// rank p / 2 in its colour: row t (colour c = t >= n0, rank r = t - c n0) is
+// cell p = 2r + b with j = (r / hx) % ny, k = r / (hx ny), b = (c + j + k) & 1,
+// i = 2 (r % hx) + b, hx = nx / 2.  Its neighbours lie in the other colour at
+// ranks r - 1 + b (x-), r + b (x+), r -+ hx (y-+), r -+ hx ny (z-+), and its CSR
+// row holds them in the order z-, y-, x-, x+, y+, z+ with the diagonal last
+// (colour 1: every neighbour has a smaller index) or first (colour 0).
+// Stencil records [2][n][4]: (z-, y-, x-, x+) and (y+, z+, diagonal, unused).
+struct RbGeom {
+    int n, n0, nx, ny, nz, hx;
+    // per row: bits 0-5 which neighbours exist, bit 6 the parity b (saves
+    // the kernels four integer divisions a row; built and checked on the host)
+    const unsigned char* info;
+};
+struct RbRow {
+    int c;        // colour
+    int nb[6];    // neighbour rows z-, y-, x-, x+, y+, z+ (valid where has)
+    bool has[6];
+};
+// The row's neighbours from its info byte.
+__device__ __forceinline__ RbRow rb_row_info(const RbGeom& g, int t)
+{
+    RbRow o;
+    o.c = t >= g.n0 ? 1 : 0;
+    const int r = t - o.c * g.n0;
+    const unsigned f = __ldg(g.info + t);
+    const int b = (int)(f >> 6) & 1;
+    const int ob = (1 - o.c) * g.n0;
+    const int sz = g.hx * g.ny;
+    const int off[6] = {-sz, -g.hx, b - 1, b, g.hx, sz};
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        o.has[s] = (f >> s) & 1u;
+        o.nb[s] = o.has[s] ? ob + r + off[s] : t;
+    }
+    return o;
+}
+__host__ __device__ __forceinline__ RbRow rb_row(const RbGeom& g, int t)
+{
+    RbRow o;
+    o.c = t >= g.n0 ? 1 : 0;
+    const int r = t - o.c * g.n0;
+    const int rx = r % g.hx, rjk = r / g.hx;
+    const int j = rjk % g.ny, k = rjk / g.ny;
+    const int b = (o.c + j + k) & 1;
+    const int i = 2 * rx + b;
+    const int ob = (1 - o.c) * g.n0;  // the other colour's first row
+    const int sz = g.hx * g.ny;
+    o.has[0] = k > 0;
+    o.has[1] = j > 0;
+    o.has[2] = i > 0;
+    o.has[3] = i < g.nx - 1;
+    o.has[4] = j < g.ny - 1;
+    o.has[5] = k < g.nz - 1;
+    o.nb[0] = ob + r - sz;
+    o.nb[1] = ob + r - g.hx;
+    o.nb[2] = ob + r - 1 + b;
+    o.nb[3] = ob + r + b;
+    o.nb[4] = ob + r + g.hx;
+    o.nb[5] = ob + r + sz;
+#pragma unroll
+    for (int s = 0; s < 6; ++s)
+        if (!o.has[s]) o.nb[s] = t;  // never read; an address inside the vector
+    return o;
+}
+// CSR (FP64) -> red-black stencil records in TO, through the host-built
+// slot of every entry (0-5 neighbours, 6 diagonal, -1 phantom).
+template <typename TO>
+void launch_rb_records(cudaStream_t st, const RbGeom& g, const int* rp, const signed char* slot,
+                       const double* M, TO* rec);
+// y = A x and its fused dots / epilogues on the records (spmv_kernel's
+// contract, bit-identical to it on the same matrix).
+template <typename T>
+void launch_rb_spmv(cudaStream_t st, const RbGeom& g, const T* rec, const T* x, T* y, int mode,
+                    double a_const, const T* z, T* y_copy, const T* w, int dots,
+                    const ReduceState& R, Scalars* sc, int epi, int it, int maxit);
+// out = U^-1 L^-1 rhs on the factor's records: colour 1 (forward then
+// backward: no upper entries), then colour 0 (backward; its y is rhs) --
+// launch_coloured_precond's arithmetic, two launches, no column indices.
+template <typename T>
+void launch_rb_precond(cudaStream_t st, const RbGeom& g, const T* rec, const T* dinv,
+                       const T* rhs, T* out, int divmode, const int* done);
+
 // One sweep over a pattern whose levels are contiguous row ranges: one launch
 // per level, rows of a level independent, plain loads (no waits, no prefill).
 template <typename T>

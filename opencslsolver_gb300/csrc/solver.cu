@@ -202,6 +202,12 @@ struct ocsl_ctx {
 
     // the pattern qualifies for the one-warp serial sweep ([0] FP64, [1] FP32)
     bool serial_ok[2] = {false, false};
+    // the pattern is the red-black ordering of an even-nx box (a multicolour
+    // child): SpMV and preconditioner on stencil records (d_recA*, d_soa*)
+    // built through the slot of every CSR entry
+    bool rb_ok = false;
+    RbGeom rb{};
+    signed char* d_rbslot = nullptr;
 
     // SIMPLE iteration on the device (ocsl_flow_iterate_device): the system
     // of the equation being solved, a residual work vector, the per-call
@@ -296,6 +302,9 @@ void ocsl_ctx::free_pattern()
     nnzT = 0;
     if (cctx) ocsl_destroy(cctx);
     cctx = nullptr;
+    if (d_rbslot) cudaFree(d_rbslot);
+    d_rbslot = nullptr;
+    rb_ok = false;
     for (int** pp : {&d_cperm, &d_cslot}) { if (*pp) cudaFree(*pp); *pp = nullptr; }
     colours = 0;
     for (auto& p : d_faces) { if (p) cudaFree(p); p = nullptr; }
@@ -591,7 +600,10 @@ struct Solve {
         } else {
             if (recA32 && val == c->d_A32) rec = recA32;
         }
-        if (rec)
+        if (rec && c->rb_ok)
+            launch_rb_spmv<TT>(st, c->rb, rec, x, y, mode, 0.0, z, ycopy, w, dots, c->R,
+                               k >= 0 ? sc(k) : nullptr, epi, it, maxit);
+        else if (rec)
             launch_box_spmv<TT>(st, P.n, c->hp.box.dim, rec, x, y, mode, 0.0, z, ycopy, w, dots,
                                 c->R, k >= 0 ? sc(k) : nullptr, epi, it, maxit, cols);
         else
@@ -605,6 +617,24 @@ struct Solve {
         matA64 = A;
         recA64 = nullptr;
         recA32 = nullptr;
+        if (c->rb_ok && cols.n == 1) {  // red-black records (single right-hand side)
+            // the FP32-inner solver's few FP64 residuals read the CSR: building
+            // FP64 records for them would cost more than it saves
+            if (want32) want64 = false;
+            if (want64 && !c->d_recA64) c->d_recA64 = dalloc<double>(8 * (size_t)P.n);
+            if (want32 && !c->d_recA32) c->d_recA32 = dalloc<float>(8 * (size_t)P.n);
+            const bool have = reuse && c->fac_M;
+            ProfScope ps(c, st, PC_ILU);
+            if (want64) {
+                if (!have) launch_rb_records<double>(st, c->rb, P.rp, c->d_rbslot, A, c->d_recA64);
+                recA64 = c->d_recA64;
+            }
+            if (want32) {
+                if (!have) launch_rb_records<float>(st, c->rb, P.rp, c->d_rbslot, A, c->d_recA32);
+                recA32 = c->d_recA32;
+            }
+            return;
+        }
         if (!c->hp.box.ok) return;
         if (want64 && !c->d_recA64) c->d_recA64 = dalloc<double>(8 * (size_t)P.n);
         if (want32 && !c->d_recA32) c->d_recA32 = dalloc<float>(8 * (size_t)P.n);
@@ -703,6 +733,12 @@ struct Solve {
     void precond(const TT* M, const TT* dinv, const TT* rhs, TT* tmp, TT* out, int divmode, int k,
                  bool prefilled)
     {
+        if (c->rb_ok && cols.n == 1 && soa<TT>() && use_range()) {
+            ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
+            launch_rb_precond<TT>(st, c->rb, soa<TT>(), dinv, rhs, out, divmode,
+                                  k >= 0 ? done(k) : nullptr);
+            return;
+        }
         if (P.coloured && use_range() && !use_serial<TT>()) {
             ProfScope ps(c, st, is_f64<TT>() ? PC_FW64 : PC_FW32);
             for (int q = 0; q < cols.n; ++q)
@@ -793,6 +829,20 @@ struct Solve {
     {
         soa64 = nullptr;
         soa32 = nullptr;
+        if (c->rb_ok && cols.n == 1) {  // red-black records of the factor (its diagonal kept)
+            if (want64 && !c->d_soa64) c->d_soa64 = dalloc<double>(8 * (size_t)P.n);
+            if (want32 && !c->d_soa32) c->d_soa32 = dalloc<float>(8 * (size_t)P.n);
+            ProfScope ps(c, st, PC_ILU);
+            if (want64) {
+                launch_rb_records<double>(st, c->rb, P.rp, c->d_rbslot, M, c->d_soa64);
+                soa64 = c->d_soa64;
+            }
+            if (want32) {
+                launch_rb_records<float>(st, c->rb, P.rp, c->d_rbslot, M, c->d_soa32);
+                soa32 = c->d_soa32;
+            }
+            return;
+        }
         if (!use_box()) return;
         if (use_serial<double>()) want64 = false;  // the serial sweep reads the CSR factor
         if (use_serial<float>()) want32 = false;
@@ -1382,9 +1432,56 @@ int ensure_coloured(ocsl_ctx* c)
         Q.bw_range[2 * k] = cp.start[cp.colours - 1 - k];
         Q.bw_range[2 * k + 1] = cp.start[cp.colours - k];
     }
+    // red-black ordering of an even-nx box: stencil records instead of the
+    // CSR, if every row of the permuted pattern is what RbGeom says it is
+    std::vector<signed char> rbslot;
+    std::vector<unsigned char> rbinfo;
+    if (c->hp.box.ok && cp.colours == 2 && c->hp.box.dim[0] % 2 == 0 && n % 2 == 0 &&
+        cp.start[1] == n / 2) {
+        RbGeom g{n, n / 2, c->hp.box.dim[0], c->hp.box.dim[1], c->hp.box.dim[2],
+                 c->hp.box.dim[0] / 2, nullptr};
+        rbslot.assign((size_t)cp.col.size(), (signed char)-1);
+        rbinfo.assign((size_t)n, 0);
+        bool ok = true;
+        for (int t = 0; t < n && ok; ++t) {
+            const RbRow q = rb_row(g, t);
+            // the natural cell of row t
+            const int r = t - q.c * g.n0, rjk = r / g.hx;
+            const int b = (q.c + rjk % g.ny + rjk / g.ny) & 1;
+            ok = cp.perm[t] == 2 * r + b;
+            unsigned char f = (unsigned char)(b << 6);
+            for (int s = 0; s < 6; ++s)
+                if (q.has[s]) f |= (unsigned char)(1u << s);
+            rbinfo[t] = f;
+            // entries in the order the kernels sum them, then phantoms
+            int want[7], m = 0;
+            if (q.c == 0) want[m++] = 6;
+            for (int s = 0; s < 6; ++s)
+                if (q.has[s]) want[m++] = s;
+            if (q.c == 1) want[m++] = 6;
+            int e = 0;
+            for (size_t k = cp.rp[t]; k < cp.rp[t + 1] && ok; ++k) {
+                if (cp.col[k] == ~size_t(0)) continue;  // phantom
+                ok = e < m && (size_t)(want[e] == 6 ? t : q.nb[want[e]]) == cp.col[k];
+                if (ok) rbslot[k] = (signed char)want[e++];
+            }
+            ok = ok && e == m;
+        }
+        if (ok) {
+            t->rb = g;
+            t->rb_ok = true;
+        }
+    }
     try {
         c->d_cperm = upload(cp.perm);
         c->d_cslot = upload(cp.slot);
+        if (t->rb_ok) {
+            CK(cudaMalloc(&t->d_rbslot, rbslot.size() + rbinfo.size()));
+            CK(cudaMemcpy(t->d_rbslot, rbslot.data(), rbslot.size(), cudaMemcpyHostToDevice));
+            unsigned char* info = reinterpret_cast<unsigned char*>(t->d_rbslot) + rbslot.size();
+            CK(cudaMemcpy(info, rbinfo.data(), rbinfo.size(), cudaMemcpyHostToDevice));
+            t->rb.info = info;
+        }
     } catch (...) {
         ocsl_destroy(t);
         for (int** pp : {&c->d_cperm, &c->d_cslot}) { if (*pp) cudaFree(*pp); *pp = nullptr; }
@@ -2396,11 +2493,13 @@ int ocsl_set_ordering(ocsl_ctx* c, int ordering)
     return OCSL_OK;
 }
 
-int ocsl_ordering_info(const ocsl_ctx* c, int* ordering, int* colours, int32_t* levels)
+int ocsl_ordering_info(const ocsl_ctx* c, int* ordering, int* colours, int32_t* levels,
+                       int* stencil)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
     if (ordering) *ordering = c->ordering;
     if (colours) *colours = c->cctx ? c->colours : 0;
+    if (stencil) *stencil = c->cctx && c->cctx->rb_ok ? 1 : 0;
     if (levels) {
         levels[0] = c->cctx ? c->cctx->hp.fw_levels : 0;
         levels[1] = c->cctx ? c->cctx->hp.bw_levels : 0;

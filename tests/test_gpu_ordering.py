@@ -20,8 +20,10 @@ pytestmark = pytest.mark.gpu
 
 
 def systems():
+    """Red-black boxes with even nx (stencil records), a box with odd nx
+    (red-black through the CSR kernels) and a 4-colour tet mesh."""
     return [W.hex_pprime(16, peclet=10.0), W.hex_pprime(12, 10, 9, peclet=0.0),
-            W.tet_pprime(5, peclet=50.0)]
+            W.tet_pprime(5, peclet=50.0), W.hex_pprime(9, 8, 7, peclet=10.0)]
 
 
 def oracle_permuted(oracle, fn, s, x0, **kw):
@@ -33,11 +35,12 @@ def oracle_permuted(oracle, fn, s, x0, **kw):
     return x, rc, it
 
 
-@pytest.mark.parametrize("k", range(3))
+@pytest.mark.parametrize("k", range(4))
 def test_permutation_and_levels(ctx, k):
     s = systems()[k]
     ctx.set_pattern(s.row_ptr, s.column_index)
-    assert ctx.ordering_info() == {"ordering": "natural", "colours": 0, "levels": (0, 0)}
+    assert ctx.ordering_info() == {"ordering": "natural", "colours": 0, "levels": (0, 0),
+                                   "stencil": False}
     ctx.set_ordering("multicolour")
     perm = ctx.ordering_permutation()
     want, colours = OC.colour_order(s.row_ptr, s.column_index)
@@ -45,11 +48,13 @@ def test_permutation_and_levels(ctx, k):
     info = ctx.ordering_info()
     assert info["ordering"] == "multicolour" and info["colours"] == colours
     assert info["levels"] == (colours, colours)
-    if k < 2:
-        assert colours == 2
+    if k < 2:  # even-nx boxes: red-black stencil records
+        assert colours == 2 and info["stencil"]
+    else:
+        assert not info["stencil"]
 
 
-@pytest.mark.parametrize("k", range(3))
+@pytest.mark.parametrize("k", range(4))
 def test_multicolour_bicgstab_bit_exact(ctx, oracle, k):
     s = systems()[k]
     ctx.set_pattern(s.row_ptr, s.column_index)
@@ -75,7 +80,7 @@ def test_multicolour_pcg_bit_exact(ctx, oracle):
     assert np.array_equal(x, xo) and r["iterations"] == it
 
 
-@pytest.mark.parametrize("k", range(3))
+@pytest.mark.parametrize("k", range(4))
 def test_multicolour_ir32_reaches_tolerance(ctx, oracle, k):
     s = systems()[k]
     ctx.set_pattern(s.row_ptr, s.column_index)
