@@ -473,6 +473,7 @@ def run_ours(args):
     # factor is that of the permuted system, not the reference's natural one)
     ctx.set_ordering("multicolour")
     ms_mc_ir, its_mc_ir, _ = timed(ocsl.ILU_BICGSTAB_IR32, args.steps)
+    _, _, prof_mc = timed(ocsl.ILU_BICGSTAB_IR32, max(3, args.steps // 2), profile=True)
     ms_mc_64, its_mc_64, _ = timed(ocsl.ILU_BICGSTAB, max(3, args.steps // 2))
     mc_info = ctx.ordering_info()
     ctx.set_ordering("natural")
@@ -481,7 +482,12 @@ def run_ours(args):
                    "iterations": {"ir32_inner": its_mc_ir[-1][0], "ir32_outer": its_mc_ir[-1][1],
                                   "fp64": its_mc_64[-1][0]},
                    "relres": {"ir32": its_mc_ir[-1][2], "fp64": its_mc_64[-1][2]},
-                   "colours": mc_info["colours"], "sweep_levels": mc_info["levels"]}
+                   "colours": mc_info["colours"], "sweep_levels": mc_info["levels"],
+                   "stencil_records": mc_info["stencil"],
+                   # per-launch CUDA-event times of the FP32-refined solves
+                   # (the red-black preconditioner is accounted to fw_sweep)
+                   "kernel_us_per_launch": {k: round(1000.0 * v[0] / v[1], 2)
+                                            for k, v in prof_mc.items() if v[1]}}
     if args.tet_size > 0 and rank == 0:
         multicolour["tet"] = ordering_comparison(torch, dev, stream, args.tet_size, args.warmup,
                                                  max(3, args.steps // 2), args.tol)

@@ -542,7 +542,8 @@ int ocsl_inject_fault(ocsl_ctx* ctx, int kind);
  *     neighbouring rows could share a colour: a pattern that is not
  *     structurally symmetric).  The reference-faithful methods ignore the
  *     setting; ocsl_solve_multi_device solves its right-hand sides one after
- *     another (no column batching), each through the permuted system.
+ *     another (no column batching), each through the permuted system; the
+ *     transposed solves (ocsl_solve_transpose*) follow the setting too.
  * The sweep-kernel settings (ocsl_set_sweep_kernel and the structured
  * geometry) apply to the natural order only: the permuted pattern is swept by
  * the level-scheduled kernel. */

@@ -1638,6 +1638,7 @@ int ensure_transpose(ocsl_ctx* c)
     int rc = ocsl_create(&t, c->device);
     if (rc != OCSL_OK) return fail(c, rc, "adjoint context: " + g_create_error);
     ocsl_set_sweep_kernel(t, c->sweep_kernel, 0, 0);
+    t->ordering = c->ordering;
     std::memcpy(t->box_tile, c->box_tile, sizeof(c->box_tile));
     std::memcpy(t->box_cluster, c->box_cluster, sizeof(c->box_cluster));
     t->graphs_on = c->graphs_on;
@@ -2490,6 +2491,7 @@ int ocsl_set_ordering(ocsl_ctx* c, int ordering)
     if (!c || (ordering != OCSL_ORDER_NATURAL && ordering != OCSL_ORDER_MULTICOLOUR))
         return OCSL_BAD_ARGUMENT;
     c->ordering = ordering;
+    if (c->tctx) ocsl_set_ordering(c->tctx, ordering);  // transposed solves follow
     return OCSL_OK;
 }
 
