@@ -146,6 +146,19 @@ int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t 
                      const ocsl_flow_iteration* it, const int* methods, const ocsl_opts* opts,
                      const double* const* given_x, double* sys_value, double* sys_b,
                      double* sys_x0, double* residual, int* iterations);
+/* The same iteration with every solve handed to `solve` instead (slot 0-2
+ * momentum x/y/z, 3 pressure correction, 4 enthalpy; method = methods[] of
+ * that equation): x holds x0 on entry and the solution on return, nonzero
+ * return = failure.  Lets a host program put an external solver -- the C++
+ * drop-in over the GPU library -- under the oracle's SIMPLE loop. */
+typedef int (*orc_solve_fn)(void* user, int slot, int method, size_t n, const double* val,
+                            const double* b, double* x);
+int orc_flow_iterate_with(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
+                          const int32_t* left, const int32_t* right, int64_t nb,
+                          const int32_t* bc_left, const ocsl_assembly* q,
+                          const ocsl_flow_state* st, const ocsl_flow_iteration* it,
+                          const int* methods, orc_solve_fn solve, void* user,
+                          double* residual);
 
 /* Exact relative residual ||b - A x||_2 / ||b||_2 in long double. */
 double orc_true_relres(size_t n, const uint64_t* rp, const uint64_t* col, const double* val,

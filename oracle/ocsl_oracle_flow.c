@@ -406,12 +406,14 @@ static int run_solve(size_t n, const uint64_t* rp, const uint64_t* col, int meth
     }
 }
 
-int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
-                     const int32_t* left, const int32_t* right, int64_t nb,
-                     const int32_t* bc_left, const ocsl_assembly* q, const ocsl_flow_state* st,
-                     const ocsl_flow_iteration* it, const int* methods, const ocsl_opts* opts,
-                     const double* const* given_x, double* sys_value, double* sys_b,
-                     double* sys_x0, double* residual, int* iterations)
+static int flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
+                        const int32_t* left, const int32_t* right, int64_t nb,
+                        const int32_t* bc_left, const ocsl_assembly* q,
+                        const ocsl_flow_state* st, const ocsl_flow_iteration* it,
+                        const int* methods, const ocsl_opts* opts,
+                        const double* const* given_x, orc_solve_fn ext, void* user,
+                        double* sys_value, double* sys_b, double* sys_x0, double* residual,
+                        int* iterations)
 {
     const size_t nnz = rp[n];
     double* val = (double*)malloc((nnz ? nnz : 1) * sizeof(double));
@@ -427,8 +429,11 @@ int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t 
         if (sys_value) memcpy(sys_value + (size_t)slot * nnz, val, nnz * sizeof(double));  \
         if (sys_b) memcpy(sys_b + (size_t)slot * n, b, n * sizeof(double));                \
         if (sys_x0) memcpy(sys_x0 + (size_t)slot * n, x, n * sizeof(double));              \
-        if (run_solve(n, rp, col, eq_method[slot], opts, val, b, x,                        \
-                      given_x ? given_x[slot] : NULL, &iterations[slot]))                  \
+        if (ext) {                                                                         \
+            iterations[slot] = 0;                                                          \
+            if (ext(user, slot, eq_method[slot], n, val, b, x)) rc = -1;                   \
+        } else if (run_solve(n, rp, col, eq_method[slot], opts, val, b, x,                 \
+                             given_x ? given_x[slot] : NULL, &iterations[slot]))           \
             rc = -1;                                                                       \
     } while (0)
 
@@ -469,4 +474,28 @@ int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t 
     free(x);
     free(res);
     return rc;
+}
+
+int orc_flow_iterate(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
+                     const int32_t* left, const int32_t* right, int64_t nb,
+                     const int32_t* bc_left, const ocsl_assembly* q, const ocsl_flow_state* st,
+                     const ocsl_flow_iteration* it, const int* methods, const ocsl_opts* opts,
+                     const double* const* given_x, double* sys_value, double* sys_b,
+                     double* sys_x0, double* residual, int* iterations)
+{
+    return flow_iterate(n, rp, col, nf, left, right, nb, bc_left, q, st, it, methods, opts,
+                        given_x, NULL, NULL, sys_value, sys_b, sys_x0, residual, iterations);
+}
+
+int orc_flow_iterate_with(size_t n, const uint64_t* rp, const uint64_t* col, int64_t nf,
+                          const int32_t* left, const int32_t* right, int64_t nb,
+                          const int32_t* bc_left, const ocsl_assembly* q,
+                          const ocsl_flow_state* st, const ocsl_flow_iteration* it,
+                          const int* methods, orc_solve_fn solve, void* user,
+                          double* residual)
+{
+    int iterations[5];
+    if (!solve) return -1;
+    return flow_iterate(n, rp, col, nf, left, right, nb, bc_left, q, st, it, methods, NULL,
+                        NULL, solve, user, NULL, NULL, NULL, residual, iterations);
 }

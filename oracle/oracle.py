@@ -92,6 +92,8 @@ _ORACLE_PROTOS = {
     "orc_bc_value_grad": (None, [_SZ, _P, C.c_int64, _P, _P, _P, _P, _P]),
     "orc_flow_iterate": (C.c_int, _CSR + [C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, _P, _P,
                                           _P, _P, _P, _P, _P, _P]),
+    "orc_flow_iterate_with": (C.c_int, _CSR + [C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P,
+                                               _P, _P, _P, _P]),
     "orc_flow_end_step": (None, [_SZ, _P]),
 }
 _REF_CSR = [_SZ, _SZ, _P, _P]
@@ -361,6 +363,30 @@ def flow_iterate(case: dict, methods, given_x=None, capture=False, tol=1e-10, ma
     if capture:
         out.update(value=sv, b=sb, x0=sx)
     return out
+
+
+def flow_iterate_with(case: dict, methods, solve_fn) -> np.ndarray:
+    """One SIMPLE inner iteration of the oracle on ``case`` with every solve
+    handed to ``solve_fn``, a C function pointer of the orc_solve_fn type (an
+    external solver under the oracle's host-side stages).  Returns the five
+    residuals."""
+    lib = Oracle()._l
+    rp = np.ascontiguousarray(case["row_ptr"], np.uint64)
+    col = np.ascontiguousarray(case["column_index"], np.uint64)
+    left = np.ascontiguousarray(case["left"], np.int32)
+    right = np.ascontiguousarray(case["right"], np.int32)
+    bc_left = np.ascontiguousarray(case["bc_left"], np.int32)
+    q = _assembly_struct(case["eq"])
+    st, it = _flow_structs(case)
+    m = (C.c_int * 3)(*[int(v) for v in methods])
+    res = np.zeros(5)
+    rc = lib.orc_flow_iterate_with(rp.size - 1, _ptr(rp), _ptr(col), left.size, _ptr(left),
+                                   _ptr(right), bc_left.size, _ptr(bc_left), C.addressof(q),
+                                   C.addressof(st), C.addressof(it), m,
+                                   C.cast(solve_fn, _P), None, _ptr(res))
+    if rc:
+        raise RuntimeError("the external solver refused a solve")
+    return res
 
 
 def flow_end_step(case: dict) -> None:

@@ -130,3 +130,130 @@ def test_dropin_replays_shocktube_calls_on_gpu(lib_built, torch_cuda, oracle, go
     tx, _, _ = read_out(tmp_path / "tol.out", rp.size - 1, len(pcalls))
     for i, (_, val, b, _) in enumerate(pcalls):
         assert oracle.true_relres(rp, col, val, b, tx[i]) <= 1e-11
+
+
+# ---------------------------------------------------------------------------
+# The shock tube's whole SIMPLE loop with every solve through the drop-in.
+# The host-side stages of CFlow_solver::iterate (boundary conditions,
+# gradients, assembly, mass fluxes, corrections, field updates) are the
+# oracle's restatement (oracle/ocsl_oracle_flow.c), standing in for the
+# reference's own flow solver, which cannot be built where the GPU is; each of
+# the five solves of an inner iteration goes through CMatrix_solver::solve()
+# of one solver object (tests/shim_host/simple_host.cpp) into the C++ drop-in
+# and libocsl_gb300.so, with the dispatch of the 1000-cell case: momentum CG,
+# pressure correction and enthalpy ILU-BiCGSTAB, 200 steps x 5 inner
+# iterations, pattern uploaded once.
+
+CG_METHODS = (0, 1, 1)  # OCSL_CG_REF for momentum, OCSL_BICGSTAB_REF for p' and enthalpy
+
+
+def build_simple_host(out_dir):
+    lib_dir = os.path.dirname(_abi.LIB_PATH)
+    so = os.path.join(str(out_dir), "libsimple_host.so")
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", "-fPIC", "-shared", "-I", HOST,
+           "-I", os.path.join(ROOT, "include"), SHIM, os.path.join(HOST, "simple_host.cpp"),
+           *WRAP, "-L", lib_dir, "-locsl_gb300", f"-Wl,-rpath,{lib_dir}", "-o", so]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return so
+
+
+def _simple_loop(solve_with, steps=None):
+    """Runs the shock tube from its recorded set-up; ``solve_with`` None uses
+    the oracle's own reference-faithful solves, else a path to the built
+    simple_host library.  Returns the written fields and the loop's time."""
+    import ctypes
+    import sys
+    import time
+
+    sys.path.insert(0, HERE_TESTS)
+    import flow_cases as FC
+    from oracle import oracle as orc
+
+    g = FC.Golden("shocktube")
+    c = g.case()
+    fn = lib = None
+    if solve_with:
+        lib = ctypes.CDLL(solve_with)
+        lib.simple_host_set_pattern.argtypes = [ctypes.c_size_t, ctypes.c_void_p,
+                                                ctypes.c_void_p]
+        lib.simple_host_elapsed_us.restype = ctypes.c_ulonglong
+        rp = np.ascontiguousarray(c["row_ptr"], np.uint64)
+        col = np.ascontiguousarray(c["column_index"], np.uint64)
+        lib.simple_host_set_pattern(rp.size - 1, rp.ctypes.data, col.ctypes.data)
+        fn = lib.simple_host_solve
+    t0 = time.perf_counter()
+    for _ in range(steps or g.steps):
+        for _ in range(g.inner):
+            if fn is not None:
+                orc.flow_iterate_with(c, CG_METHODS, fn)
+            else:
+                orc.flow_iterate(c, CG_METHODS)
+        FC.end_step(c, orc.flow_end_step)
+    wall = time.perf_counter() - t0
+    out = {k: np.array(v) for k, v in FC.written(c).items()}
+    out["_wall_s"] = np.array(wall)
+    out["_solve_us"] = np.array(lib.simple_host_elapsed_us() if lib else 0)
+    out["_inner"] = np.array((steps or g.steps) * g.inner)
+    return out
+
+
+HERE_TESTS = os.path.join(ROOT, "tests")
+
+
+def test_simple_host_builds_and_refuses_without_gpu(lib_built, tmp_path):
+    import sys
+
+    import torch
+
+    so = build_simple_host(tmp_path)
+    if torch.cuda.is_available():
+        pytest.skip("host has a GPU (covered by the GPU test)")
+    p = subprocess.run([sys.executable, os.path.abspath(__file__), "simple-loop", so,
+                        str(tmp_path / "out.npz")], capture_output=True, text=True, timeout=300,
+                       cwd=ROOT, env=dict(os.environ,
+                                          PYTHONPATH=os.pathsep.join([ROOT, HERE_TESTS])))
+    assert p.returncode == 1
+    assert "ocsl: ocsl_create failed" in p.stderr
+
+
+@pytest.mark.gpu
+def test_dropin_runs_shocktube_simple_loop_on_gpu(lib_built, torch_cuda, oracle, tmp_path):
+    import sys
+
+    import flow_cases as FC
+
+    so = build_simple_host(tmp_path)
+    out = tmp_path / "gpu_loop.npz"
+    # a child process: the drop-in ends its program on a library failure, as
+    # the reference ends on its own errors
+    p = subprocess.run([sys.executable, os.path.abspath(__file__), "simple-loop", so, str(out)],
+                       capture_output=True, text=True, timeout=900, cwd=ROOT,
+                       env=dict(os.environ, PYTHONPATH=os.pathsep.join([ROOT, HERE_TESTS])))
+    assert p.returncode == 0, p.stderr[-2000:]
+    got = dict(np.load(out))
+    wall, solve_us, inner = (float(got.pop(k)) for k in ("_wall_s", "_solve_us", "_inner"))
+    # the same loop with the oracle's own solves: identical bits, since every
+    # drop-in solve equals the oracle's reference-faithful solve bit for bit
+    want = _simple_loop(None)
+    for k in ("_wall_s", "_solve_us", "_inner"):
+        want.pop(k)
+    for k in want:
+        assert np.array_equal(got[k], want[k]), (k, FC.relerr(got[k], want[k]))
+    # and the reference's own run (its final state with momentum through CG)
+    g = FC.Golden("shocktube")
+    errs = FC.field_errors(got, FC.recorded(g.setup, g.record("final_cg")))
+    state = max(errs[k] for k in ("velocity", "pressure", "temperature", "density_c",
+                                  "enthalpy", "mdot", "density"))
+    print(f"shock tube through the C++ drop-in: {inner:.0f} inner iterations, "
+          f"{wall * 1e3 / inner:.2f} ms each ({solve_us / 1e3 / inner:.2f} ms in solve()); "
+          f"vs the reference's run: state {state:.2e}, all fields {max(errs.values()):.2e}")
+    assert state <= 1e-11, errs
+    assert max(errs.values()) <= 1e-8, errs
+
+
+if __name__ == "__main__":
+    import sys
+
+    if len(sys.argv) == 4 and sys.argv[1] == "simple-loop":
+        res = _simple_loop(sys.argv[2])
+        np.savez(sys.argv[3], **res)
