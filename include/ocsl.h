@@ -429,6 +429,41 @@ int ocsl_mesh_view(const ocsl_mesh* mesh, ocsl_mesh_arrays* arrays);
 const char* ocsl_mesh_marker_name(const ocsl_mesh* mesh, int marker);
 int ocsl_mesh_destroy(ocsl_mesh* mesh);
 
+/* ------------------------------------------------------------------------
+ * VTK output of a solution on a mesh read by ocsl_mesh_read_su2: the two
+ * legacy-ASCII files of Cpost_processing::write_VTK_file and
+ * write_boundary_VTK_file (cpost_processing.cpp:26-187, 238-401; written by
+ * Croot::start_solver at the end of a run and every VTK_file_frequency steps,
+ * croot.cpp:226-240) with the same sections, names, node orders and number
+ * format -- byte-identical to the reference's files for the same state at
+ * the default 6 significant digits (its std::ostream default); digits up to
+ * 17 give a round-trip exact file.  Field pointers may be DEVICE memory (the
+ * ocsl_flow_state arrays the device SIMPLE iteration writes, streamed to the
+ * host in chunks while the previous chunk is formatted) or host memory
+ * (no GPU needed then).  Vectors are [3][count].  Either path may be NULL to
+ * skip that file.  OCSL_BAD_ARGUMENT with the reason in err on a missing field
+ * or an unwritable file.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    int heat;        /* 1: heat conduction (Temperature only), 0: fluid flow            */
+    int digits;      /* significant digits, 0 = 6 (the reference's), at most 17         */
+    /* cells (n_cells; vectors [3][n_cells]) */
+    const double* density;        /* flow: CFlow_cell::Density                           */
+    const double* pressure;       /* flow                                                */
+    const double* temperature;    /* flow and heat                                       */
+    const double* mach;           /* flow                                                */
+    const double* velocity;       /* flow                                                */
+    const double* pressure_grad;  /* flow                                                */
+    /* boundary faces (n_bc), in the mesh's boundary-face order */
+    const double* bc_temperature; /* heat: CHeat_BC_face::Temperature                     */
+    const int32_t* bc_type;       /* flow: ocsl_bc_type, for the wall stress             */
+    const int32_t* bc_wall;       /* flow: ocsl_wall_type                                */
+    int viscous;                  /* flow: Eflow_type_visc::Viscous (wall stress != 0)   */
+    double sutherland[2];         /* flow: viscosity C1 T^1.5 / (T + C2)                 */
+} ocsl_vtk_fields;
+int ocsl_vtk_write(const ocsl_mesh* mesh, const ocsl_vtk_fields* fields, const char* cells_path,
+                   const char* boundary_path, char* err, size_t err_len);
+
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured CTA kernel, 3 the structured

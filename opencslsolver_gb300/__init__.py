@@ -29,7 +29,7 @@ from ._abi import (BICGSTAB_REF, CG_REF, ILU_BICGSTAB, ILU_BICGSTAB_IR32, METHOD
 PHANTOM = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 __all__ = ["Context", "Batch", "CMatrix_solver", "build_pattern", "check_pattern", "colour_pattern",
-           "read_su2",
+           "read_su2", "Mesh",
            "LibraryMissing", "OcslError",
            "CG_REF", "BICGSTAB_REF", "PCG", "ILU_BICGSTAB", "ILU_BICGSTAB_IR32", "METHODS",
            "PHANTOM"]
@@ -624,3 +624,73 @@ def read_su2(path: str) -> dict:
         return out
     finally:
         L.ocsl_mesh_destroy(h)
+
+
+class Mesh:
+    """An SU2 mesh held by the library (ocsl_mesh_read_su2) for VTK output of a
+    solution on it (ocsl_vtk_write), as Cpost_processing writes it."""
+
+    def __init__(self, path: str):
+        self._L = _abi.lib()
+        self._h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        st = self._L.ocsl_mesh_read_su2(os.fsencode(path), C.byref(self._h), err, 512)
+        if st != 0:
+            raise OcslError(st, f"read_su2: {err.value.decode()}")
+        v = _abi.MeshArrays()
+        self._L.ocsl_mesh_view(self._h, C.byref(v))
+        self.n_cells, self.n_faces, self.n_bc = int(v.n_cells), int(v.n_faces), int(v.n_bc)
+
+    def close(self) -> None:
+        if self._h:
+            self._L.ocsl_mesh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _field(a, keep: list, dtype):
+        """Pointer to a field: a CUDA tensor stays on the device (the writer
+        streams it), anything else is made a contiguous host array."""
+        if a is None:
+            return None
+        if hasattr(a, "is_cuda") and a.is_cuda:
+            keep.append(a)
+            return a.data_ptr()
+        h = np.ascontiguousarray(a.cpu().numpy() if hasattr(a, "cpu") else a, dtype)
+        keep.append(h)
+        return h.ctypes.data
+
+    def write_vtk(self, cells_path=None, boundary_path=None, *, heat=False, digits=0,
+                  density=None, pressure=None, temperature=None, mach=None, velocity=None,
+                  pressure_grad=None, bc_temperature=None, bc_type=None, bc_wall=None,
+                  viscous=False, sutherland=(0.0, 0.0)) -> None:
+        """Write solution.vtk / solution_BC.vtk of the reference's
+        post-processing (either path may be None).  Fields are numpy arrays or
+        CUDA tensors; vectors [3][count] (flattened or shaped (3, count))."""
+        keep: list = []
+        f = _abi.VtkFields()
+        f.heat, f.digits, f.viscous = int(bool(heat)), int(digits), int(bool(viscous))
+        for name, a in (("density", density), ("pressure", pressure),
+                        ("temperature", temperature), ("mach", mach), ("velocity", velocity),
+                        ("pressure_grad", pressure_grad), ("bc_temperature", bc_temperature)):
+            setattr(f, name, self._field(a, keep, np.float64))
+        f.bc_type = self._field(bc_type, keep, np.int32)
+        f.bc_wall = self._field(bc_wall, keep, np.int32)
+        f.sutherland[0], f.sutherland[1] = float(sutherland[0]), float(sutherland[1])
+        err = C.create_string_buffer(512)
+        enc = (lambda p: None if p is None else os.fsencode(str(p)))  # noqa: E731
+        st = self._L.ocsl_vtk_write(self._h, C.byref(f), enc(cells_path), enc(boundary_path),
+                                    err, 512)
+        if st != 0:
+            raise OcslError(st, f"write_vtk: {err.value.decode()}")

@@ -145,6 +145,15 @@ MESH_ARRAYS = (
     ("cell_volume", "d", 1, "n_cells"), ("cell_center", "d", 3, "n_cells"))
 
 
+class VtkFields(C.Structure):
+    """ocsl_vtk_fields (include/ocsl.h)."""
+    _fields_ = [("heat", C.c_int), ("digits", C.c_int), ("density", C.c_void_p),
+                ("pressure", C.c_void_p), ("temperature", C.c_void_p), ("mach", C.c_void_p),
+                ("velocity", C.c_void_p), ("pressure_grad", C.c_void_p),
+                ("bc_temperature", C.c_void_p), ("bc_type", C.c_void_p), ("bc_wall", C.c_void_p),
+                ("viscous", C.c_int), ("sutherland", C.c_double * 2)]
+
+
 class MeshArrays(C.Structure):
     _fields_ = ([("n_cells", C.c_int64), ("n_faces", C.c_int64), ("n_bc", C.c_int64),
                  ("n_markers", C.c_int32)] +
@@ -208,6 +217,8 @@ _PROTOS = {
     "ocsl_mesh_view": (C.c_int, [_P, C.POINTER(MeshArrays)]),
     "ocsl_mesh_marker_name": (C.c_char_p, [_P, C.c_int]),
     "ocsl_mesh_destroy": (C.c_int, [_P]),
+    "ocsl_vtk_write": (C.c_int, [_P, C.POINTER(VtkFields), C.c_char_p, C.c_char_p, C.c_char_p,
+                                 _SZ]),
     "ocsl_set_sweep_kernel": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_int]),
     "ocsl_sweep_info": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),

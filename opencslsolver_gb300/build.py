@@ -22,7 +22,7 @@ LIB = os.path.join(OUT_DIR, "libocsl_gb300.so")
 
 SOURCES = ["kernels_krylov.cu", "kernels_ilu.cu", "kernels_box.cu", "kernels_wave.cu", "solver.cu",
            "pattern.cpp",
-           "noalloc.cu", "adjoint.cu", "assembly.cu", "flow.cu", "batch.cpp", "mesh.cpp"]
+           "noalloc.cu", "adjoint.cu", "assembly.cu", "flow.cu", "batch.cpp", "mesh.cpp", "vtk.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

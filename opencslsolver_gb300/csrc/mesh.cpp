@@ -30,15 +30,7 @@
 #include <vector>
 
 #include "../../include/ocsl.h"
-
-struct ocsl_mesh {
-    int64_t n_cells = 0, n_faces = 0, n_bc = 0;
-    std::vector<std::string> markers;
-    std::vector<int32_t> face_left, face_right, bc_left, bc_marker;
-    std::vector<double> face_geo_aver, face_ksi_A, face_area_vector, face_alpha, face_distance,
-        face_unit, bc_area, bc_area_vector, bc_alpha, bc_distance, bc_unit, bc_perp_dist,
-        bc_ksi_A, cell_volume, cell_center;
-};
+#include "mesh.h"
 
 namespace {
 
@@ -374,6 +366,21 @@ int ocsl_mesh_read_su2(const char* path, ocsl_mesh** out, char* err, size_t err_
         m->face_ksi_A[k] = dot(alpha, A);
         m->face_geo_aver[k] = mag(cc[p.R] - fc) / dist;
     }
+    m->nodes.resize(3 * X.size());
+    for (size_t i = 0; i < X.size(); ++i) {
+        m->nodes[3 * i] = X[i].x;
+        m->nodes[3 * i + 1] = X[i].y;
+        m->nodes[3 * i + 2] = X[i].z;
+    }
+    m->cell_kind.resize(n);
+    m->cell_nodes.assign(8 * n, -1);
+    for (int64_t i = 0; i < n; ++i) {
+        m->cell_kind[i] = (int8_t)cells[i].kind;
+        for (int k = 0; k < cells[i].nnodes(); ++k) m->cell_nodes[8 * i + k] = cells[i].node[k];
+    }
+    m->bc_nodes.resize(4 * nb);
+    m->bc_normal.resize(3 * nb);
+    m->bc_center.resize(3 * nb);
     m->bc_left.resize(nb);
     m->bc_area.resize(nb);
     m->bc_distance.resize(nb);
@@ -390,6 +397,9 @@ int ocsl_mesh_read_su2(const char* path, ocsl_mesh** out, char* err, size_t err_
         V3 normal, fc;
         face_geometry(X, nd, area, normal, fc);
         const V3 A = area * normal;
+        std::memcpy(&m->bc_nodes[4 * g], nd, sizeof nd);
+        put3(m->bc_normal, nb, g, normal);
+        put3(m->bc_center, nb, g, fc);
         const V3 d = fc - cc[c];
         const double dist = mag(fc - cc[c]);
         const V3 alpha = (1.0 / dot(A, d)) * A;

@@ -20,8 +20,9 @@
 //   equations through CG_solve, p' and enthalpy through ILU_BICGSTAB_solve.
 //   A record spec "s:i" records inner iteration i of step s: the state before
 //   each solve (pre_s_i_e.bin, e = 0..4) and after the iteration (post_s_i.bin).
-// Also written: setup.bin (mesh metrics, fluid constants, initial state) and
-// final.bin (the state after the last step).
+// Also written: setup.bin (mesh metrics, fluid constants, initial state),
+// final.bin (the state after the last step) and the reference's VTK files of
+// that state, solution.vtk and solution_BC.vtk (Cpost_processing).
 // File format: repeated [u32 name length][name][u8 kind 'd'|'i'|'u'][u64 count][data].
 #include "croot.h"
 #include "flow_configs.h"
@@ -293,7 +294,13 @@ int main(int argc, char** argv)
         }
         fl.update_timestep();
     }
-    Writer w(g_out + "/final.bin");
-    write_state(w);
+    {
+        Writer w(g_out + "/final.bin");
+        write_state(w);
+    }
+    // the reference's own VTK output of the final state (croot.cpp:239-240)
+    root.post_processing = std::make_shared<Cpost_processing>();
+    root.post_processing->write_VTK_file(g_out + "/solution.vtk");
+    root.post_processing->write_boundary_VTK_file(g_out + "/solution_BC.vtk");
     return 0;
 }

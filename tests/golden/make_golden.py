@@ -40,6 +40,10 @@ then writes:
   metrics, cell volumes) and matrix pattern for a 5 x 4 x 3 jittered box of
   hexahedra, tetrahedra or wedges that it read from the SU2 file
   workloads.write_su2_box writes;
+* vtk_<cells>.npz -- the reference's own VTK output (solution.vtk and
+  solution_BC.vtk, as bytes) after a short run of the 3D viscous channel on a
+  jittered box of hexahedra, tetrahedra or wedges read from an SU2 file, with
+  the final state and fluid constants it was written from;
 * assembly_<case>.npz -- the inputs (cell / face state) and outputs (matrix
   values, b, x0, ap_vec, total_mdot) of the reference's face-loop assembly,
   recorded by oracle/ref_assembly.cpp right before the 5 solve calls of one
@@ -297,10 +301,50 @@ def make_meshes(out_dir):
                             **{k: setup[k] for k in MESH_KEYS_FVM})
 
 
+# The VTK fixtures: the reference's own solution.vtk / solution_BC.vtk
+# (Cpost_processing::write_VTK_file / write_boundary_VTK_file) after a short
+# run of the 3D viscous channel on a jittered box of hexahedra (the box3d flow
+# case), tetrahedra or wedges, with the final state they were written from.
+VTK_CASES = {
+    "hex": {"mesh": BOX3D_MESH, "cells": "hex", "steps": 40, "inner": 3},
+    "tet": {"mesh": {"nx": 5, "ny": 4, "nz": 3, "lengths": (1.0, 0.2, 0.1), "jitter": 0.1},
+            "cells": "tet", "steps": 3, "inner": 2},
+    "wedge": {"mesh": {"nx": 5, "ny": 4, "nz": 3, "lengths": (1.0, 0.2, 0.1), "jitter": 0.1},
+              "cells": "wedge", "steps": 3, "inner": 2},
+}
+
+
+def make_vtk(out_dir):
+    """vtk_<cells>.npz: the reference's VTK files (bytes) and the state and
+    setup they were written from."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_flow")
+    for name, spec in VTK_CASES.items():
+        with tempfile.TemporaryDirectory() as d:
+            mesh = os.path.join(d, "m.su2")
+            m = dict(spec["mesh"])
+            W.write_su2_box(mesh, m.pop("nx"), m.pop("ny"), m.pop("nz"), cells=spec["cells"], **m)
+            subprocess.run([exe, d, f"box3d={mesh}", "bicg", str(spec["steps"]),
+                            str(spec["inner"])], cwd=d, check=True, stdout=subprocess.DEVNULL)
+            arrays = {f"final__{k}": v
+                      for k, v in read_named_arrays(os.path.join(d, "final.bin")).items()}
+            setup = read_named_arrays(os.path.join(d, "setup.bin"))
+            arrays.update({f"setup__{k}": setup[k] for k in ("switches", "fluid")})
+            for key, f in (("cells_vtk", "solution.vtk"), ("bc_vtk", "solution_BC.vtk")):
+                with open(os.path.join(d, f), "rb") as fh:
+                    arrays[key] = np.frombuffer(fh.read(), np.uint8)
+        mesh_args = spec["mesh"]
+        arrays["mesh_dims"] = np.array([mesh_args[k] for k in ("nx", "ny", "nz")])
+        arrays["mesh_lengths"] = np.array(mesh_args["lengths"], float)
+        arrays["mesh_jitter"] = np.array(float(mesh_args["jitter"]))
+        arrays["mesh_cells"] = np.array(spec["cells"])
+        np.savez_compressed(os.path.join(out_dir, f"vtk_{name}.npz"), **arrays)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=orc.REF_DIR)
-    ap.add_argument("--only", choices=["kat", "shocktube", "small", "assembly", "flow", "mesh"],
+    ap.add_argument("--only", choices=["kat", "shocktube", "small", "assembly", "flow", "mesh",
+                                       "vtk"],
                     help="write one fixture (default: all)")
     a = ap.parse_args()
     orc.build(a.reference)
@@ -320,6 +364,8 @@ def main():
             make_flow(HERE, case)
     if want("mesh"):
         make_meshes(HERE)
+    if want("vtk"):
+        make_vtk(HERE)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
