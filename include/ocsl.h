@@ -613,7 +613,11 @@ int ocsl_set_graphs(ocsl_ctx* ctx, int enable);
  * sides in lockstep, up to four per pass: every SpMV, vector and sweep launch
  * serves all of them, and each keeps its own scalars, inner tolerance and
  * stopping test, so every column's result is bit-identical to solving it
- * alone with the same factor.  enable = 0 solves them one after another. */
+ * alone with the same factor.  enable = 0 solves them one after another;
+ * enable = 2 runs the lockstep with an SpMM-style SpMV on box patterns (one
+ * CTA per row tile reads each stencil record once for all columns, same
+ * bits; measured no faster than the default one CTA per tile and column,
+ * whose repeated record reads L2 serves). */
 int ocsl_set_col_batching(ocsl_ctx* ctx, int enable);
 
 /* Kernel timing.  While enabled, every kernel the context launches is

@@ -364,10 +364,14 @@ class Context:
         kind 0 cancels a pending injection."""
         self._check(self._L.ocsl_inject_fault(self._h, int(kind)), "inject_fault")
 
-    def set_col_batching(self, enable: bool = True):
+    def set_col_batching(self, enable=True):
         """Solve the right-hand sides of solve_multi_device with the FP32-inner
-        solver in lockstep groups of up to four (default on)."""
-        self._check(self._L.ocsl_set_col_batching(self._h, int(bool(enable))), "set_col_batching")
+        solver in lockstep groups of up to four (default on).  2: lockstep with
+        the SpMM-style box SpMV (each stencil record read once for all
+        columns)."""
+        mode = enable if isinstance(enable, int) and not isinstance(enable, bool) \
+            else int(bool(enable))
+        self._check(self._L.ocsl_set_col_batching(self._h, mode), "set_col_batching")
 
     def set_ordering(self, ordering):
         """Row ordering of the tolerance-mode solves: "natural" (default) or

@@ -512,6 +512,88 @@ __global__ void __launch_bounds__(kThreads) box_spmv_kernel(BoxSpmvParams<T> p)
     }
 }
 
+// box_spmv_kernel for NC right-hand sides sharing the matrix (the lockstep
+// columns of ocsl_solve_multi_device), SpMM-style: one CTA per tile loads
+// each row's stencil record once and applies it to every live column, instead
+// of one CTA per (tile, column) each fetching the records again.  Column q's
+// vectors sit q * ld elements after column 0's, its scalars at sc + q, its
+// partial sums and counter in its own slot; a column whose solve is done
+// when the launch starts is skipped whole, as its own launch would return.
+// Each column's arithmetic, stores and tile partials are exactly those of
+// box_spmv_kernel, so results are bit-identical.
+template <typename T, int MODE, int DOTS, int NC>
+__global__ void __launch_bounds__(kThreads) box_spmm_kernel(BoxSpmvParams<T> p)
+{
+    constexpr int ND = DotCount<DOTS>::value;
+    using V = typename Rec4<T>::V;
+    __shared__ double s_red[kMaxDots * 8];
+    __shared__ int s_last;
+    bool live[NC];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+        live[q] = !(p.sc && p.sc[q].done);
+        any = any || live[q];
+    }
+    if (!any) return;
+    const int tile = (int)blockIdx.x;
+    const int ntiles = (int)gridDim.x;
+    const int n = p.n;
+    const V* lo = reinterpret_cast<const V*>(p.rec);
+    const V* hi = lo + n;
+    DotAcc<T> acc[NC][ND > 0 ? ND : 1];
+#pragma unroll 2
+    for (int j = 0; j < kRowsPerThread; ++j) {
+        const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
+        if (row >= n) continue;
+        const V l = lo[row], h = hi[row];
+        const int izm = max(row - p.sz, 0), iym = max(row - p.sy, 0), ixm = max(row - 1, 0);
+        const int ixp = min(row + 1, n - 1), iyp = min(row + p.sy, n - 1);
+        const int izp = min(row + p.sz, n - 1);
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            if (!live[q]) continue;
+            const size_t off = (size_t)q * (size_t)p.cols.ld;
+            const T* x = p.x + off;
+            T dum = fma_t(l.x, __ldg(x + izm), T(0));
+            dum = fma_t(l.y, __ldg(x + iym), dum);
+            dum = fma_t(l.z, __ldg(x + ixm), dum);
+            dum = fma_t(h.w, __ldg(x + row), dum);
+            dum = fma_t(h.x, __ldg(x + ixp), dum);
+            dum = fma_t(h.y, __ldg(x + iyp), dum);
+            dum = fma_t(h.z, __ldg(x + izp), dum);
+            T y, zv = T(0);
+            if constexpr (MODE == 0) {
+                y = dum;
+            } else if constexpr (MODE == 1) {
+                zv = __ldg(p.z + off + row);
+                y = zv - dum;
+            } else {
+                zv = __ldg(p.z + off + row);
+                y = fma_t(p.a, dum, zv);
+            }
+            p.y[off + row] = y;
+            if (MODE == 1 && p.y_copy) p.y_copy[off + row] = y;
+            int k = 0;
+            if constexpr ((DOTS & DOT_YY) != 0) acc[q][k++].add(y, y);
+            if constexpr ((DOTS & DOT_ZZ) != 0) acc[q][k++].add(zv, zv);
+            if constexpr ((DOTS & DOT_WY) != 0) acc[q][k++].add(__ldg(p.w + off + row), y);
+            (void)k;
+        }
+    }
+    if constexpr (ND > 0) {
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            if (!live[q]) continue;  // uniform over the CTA
+            double v[ND];
+#pragma unroll
+            for (int k = 0; k < ND; ++k) v[k] = acc[q][k].value();
+            finish_reduction<ND>(v, tile, ntiles, q, p.R, p.sc ? p.sc + q : nullptr, p.epi, p.it,
+                                 p.maxit, s_red, &s_last);
+        }
+    }
+}
+
 // spmv_kernel on the red-black stencil records (RbGeom): the neighbours'
 // rows computed, not read; each row's chain in its CSR order (colour 0: the
 // diagonal, then z-, y-, x-, x+, y+, z+; colour 1: the neighbours, then the
@@ -825,6 +907,14 @@ void box_spmv_dispatch(cudaStream_t st, const BoxSpmvParams<T>& p)
 {
     const int nt = ntiles_of(p.n);
     if (nt == 0) return;
+    if (p.cols.spmm && p.cols.n > 1) {
+        switch (p.cols.n) {
+        case 2: box_spmm_kernel<T, MODE, DOTS, 2><<<nt, kThreads, 0, st>>>(p); return;
+        case 3: box_spmm_kernel<T, MODE, DOTS, 3><<<nt, kThreads, 0, st>>>(p); return;
+        case 4: box_spmm_kernel<T, MODE, DOTS, 4><<<nt, kThreads, 0, st>>>(p); return;
+        default: break;
+        }
+    }
     box_spmv_kernel<T, MODE, DOTS><<<nt * p.cols.n, kThreads, 0, st>>>(p);
 }
 

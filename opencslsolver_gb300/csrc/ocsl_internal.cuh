@@ -78,6 +78,7 @@ struct Cols {
     int n = 1;
     long long ld = 0;
     unsigned shared = 0;
+    int spmm = 0;  // box SpMV: one CTA per tile serves every column (box_spmm_kernel)
 };
 
 // Geometry of the structured sweep (7-point box patterns): canonical dims

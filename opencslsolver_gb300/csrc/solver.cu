@@ -190,7 +190,7 @@ struct ocsl_ctx {
     bool graphs_on = true;
     int graph_kind = 0;
     // several right-hand sides of the FP32-inner solver in lockstep (else one by one)
-    bool col_batching = true;
+    int col_batching = 1;  // 0 one after another, 1 lockstep, 2 lockstep with the SpMM box SpMV
     const void* graph_ptr[6] = {};
 
     // factor of the last solve (buffer and SoA copies), for solves that reuse it
@@ -1305,7 +1305,7 @@ std::vector<TolResult> run_bicgstab_ir32_cols(Solve& s, const double* A, const d
     double* R64 = c->v64c;
     float** f = c->v32c;
     const int n = s.n;
-    s.cols = Cols{nc, (long long)n, 0u};
+    s.cols = Cols{nc, (long long)n, 0u, c->col_batching == 2 ? 1 : 0};
     s.outer_k = kScOuterCols;
     const int KO = kScOuterCols, KI = kScInnerCols;
     std::vector<TolResult> res(nc);
@@ -2530,8 +2530,9 @@ int ocsl_ordering_permutation(ocsl_ctx* c, int32_t* perm, size_t n)
 int ocsl_set_col_batching(ocsl_ctx* c, int enable)
 {
     if (!c) return OCSL_BAD_ARGUMENT;
+    if (enable < 0 || enable > 2) return OCSL_BAD_ARGUMENT;
     c->drop_graph();
-    c->col_batching = enable != 0;
+    c->col_batching = enable;
     return OCSL_OK;
 }
 

@@ -71,6 +71,42 @@ def test_lockstep_columns_equal_one_by_one(ctx, oracle, torch_cuda, kind, nrhs):
         assert rr <= 1e-10, (q, rr)
 
 
+def test_spmm_spmv_equals_per_column_spmv(ctx, torch_cuda):
+    """The lockstep solve's SpMM-style box SpMV (one CTA per tile, every
+    column) against one SpMV CTA per (tile, column): the same bits; the time
+    of both at 128^3 x 3 right-hand sides is printed."""
+    torch = torch_cuda
+    for dims, timed in (((19, 13, 11), False), ((128, 128, 128), True)):
+        s = W.hex_pprime(*dims, peclet=10.0)
+        ctx.set_pattern(s.row_ptr, s.column_index)
+        rng = np.random.default_rng(11)
+        B = torch.from_numpy(rng.uniform(-1, 1, (3, s.n))).cuda()
+        A = torch.from_numpy(s.value).cuda()
+        out = {}
+        for mode in (2, 1):
+            ctx.set_col_batching(mode)
+            X = torch.zeros_like(B)
+            res = ctx.solve_multi_device(ocsl.ILU_BICGSTAB_IR32, A, B, X, tol=1e-10)
+            ms = None
+            if timed:
+                t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                X2 = torch.zeros_like(B)
+                torch.cuda.synchronize()
+                t0.record()
+                ctx.solve_multi_device(ocsl.ILU_BICGSTAB_IR32, A, B, X2, tol=1e-10)
+                t1.record()
+                torch.cuda.synchronize()
+                ms = t0.elapsed_time(t1)
+                assert torch.equal(X2, X)
+            out[mode] = (X, [r["iterations"] for r in res], ms)
+        ctx.set_col_batching(True)
+        assert torch.equal(out[1][0], out[2][0])
+        assert out[1][1] == out[2][1]
+        if timed:
+            print(f"128^3 x 3 rhs FP32-refined lockstep: SpMM SpMV {out[2][2]:.2f} ms, "
+                  f"per-column SpMV {out[1][2]:.2f} ms (iterations {out[1][1]})")
+
+
 def test_lockstep_uneven_columns(ctx, torch_cuda):
     """Columns that finish at different points: b = 0 (x = 0 at once), a tiny
     and a large right-hand side, a column with a NaN (its own status only)."""
