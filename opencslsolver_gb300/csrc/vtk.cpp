@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -59,9 +60,44 @@ struct LineFormat {
     int width;  // numbers per line
 };
 
+// std::to_chars with a precision formats exactly as printf's "%.*g" does
+// (C locale), several times faster than snprintf.
 int put_number(char* out, double v, int digits)
 {
-    return std::snprintf(out, 32, "%.*g", digits, v);
+    const auto r = std::to_chars(out, out + 32, v, std::chars_format::general, digits);
+    return (int)(r.ptr - out);
+}
+
+int put_int(char* out, long long v)
+{
+    const auto r = std::to_chars(out, out + 24, v);
+    return (int)(r.ptr - out);
+}
+
+// Lines [0, count) of integers: line i = ints(i, out) written into out
+// (returns the characters written, at most max_line), in parallel slices.
+template <typename F>
+void format_int_lines(size_t count, size_t max_line, F ints, std::string& text, unsigned threads)
+{
+    const unsigned t = (unsigned)std::max<size_t>(1, std::min<size_t>(threads, count / 4096 + 1));
+    std::vector<std::vector<char>> parts(t);
+    std::vector<size_t> used(t, 0);
+    auto work = [&](unsigned k) {
+        const size_t lo = count * k / t, hi = count * (k + 1) / t;
+        std::vector<char>& buf = parts[k];
+        buf.resize((hi - lo) * max_line + 1);
+        char* p = buf.data();
+        for (size_t i = lo; i < hi; ++i) p += ints(i, p);
+        used[k] = (size_t)(p - buf.data());
+    };
+    if (t == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (unsigned k = 0; k < t; ++k) pool.emplace_back(work, k);
+        for (auto& th : pool) th.join();
+    }
+    for (unsigned k = 0; k < t; ++k) text.append(parts[k].data(), used[k]);
 }
 
 // Formats lines [0, count) whose numbers are cols[c][i] into `text`, in
@@ -261,32 +297,36 @@ void write_cells(const ocsl_mesh& m, const ocsl_vtk_fields& f, const char* path,
     static const int kTet[4] = {0, 1, 2, 3}, kWedge[6] = {0, 2, 1, 3, 5, 4},
                      kHex[8] = {0, 1, 3, 2, 4, 5, 7, 6};
     std::string s;
-    s.reserve(std::min<size_t>(n, kChunk) * 72);
-    for (size_t i = 0; i < n; ++i) {
-        const int kind = m.cell_kind[i];
-        const int* order = kind == 10 ? kTet : kind == 13 ? kWedge : kHex;
-        const int cnt = kind == 10 ? 4 : kind == 13 ? 6 : 8;
-        s += std::to_string(cnt);
-        for (int k = 0; k < cnt; ++k) {
-            s += ' ';
-            s += std::to_string(m.cell_nodes[8 * i + order[k]]);
-        }
-        s += '\n';
-        if (s.size() > (size_t(8) << 20)) {
-            w.text(s);
-            s.clear();
-        }
+    for (size_t lo = 0; lo < n; lo += kChunk) {
+        const size_t len = std::min(kChunk, n - lo);
+        format_int_lines(len, 9 * 12, [&](size_t i, char* p) {
+            const size_t c = lo + i;
+            const int kind = m.cell_kind[c];
+            const int* order = kind == 10 ? kTet : kind == 13 ? kWedge : kHex;
+            const int cnt = kind == 10 ? 4 : kind == 13 ? 6 : 8;
+            char* q = p + put_int(p, cnt);
+            for (int k = 0; k < cnt; ++k) {
+                *q++ = ' ';
+                q += put_int(q, m.cell_nodes[8 * c + order[k]]);
+            }
+            *q++ = '\n';
+            return (int)(q - p);
+        }, s, w.threads());
+        w.text(s);
+        s.clear();
     }
-    s += "CELL_TYPES " + std::to_string(n) + "\n";
-    for (size_t i = 0; i < n; ++i) {
-        s += std::to_string((int)m.cell_kind[i]);
-        s += '\n';
-        if (s.size() > (size_t(8) << 20)) {
-            w.text(s);
-            s.clear();
-        }
+    s = "CELL_TYPES " + std::to_string(n) + "\n";
+    for (size_t lo = 0; lo < n; lo += kChunk) {
+        const size_t len = std::min(kChunk, n - lo);
+        format_int_lines(len, 4, [&](size_t i, char* p) {
+            char* q = p + put_int(p, m.cell_kind[lo + i]);
+            *q++ = '\n';
+            return (int)(q - p);
+        }, s, w.threads());
+        w.text(s);
+        s.clear();
     }
-    s += "CELL_DATA " + std::to_string(n) + "\n";
+    s = "CELL_DATA " + std::to_string(n) + "\n";
     w.text(s);
     // write_VTK_data (cpost_processing.cpp:26-127)
     scalar(w, "Volume[m3]", m.cell_volume.data(), n);

@@ -12,6 +12,9 @@ transient dt 2e-6 s, blended convection), then ``--inner`` device inner
 iterations with each solver choice, the reference's (one CUDA graph per
 iteration), the FP64 tolerance mode and the FP32-inner / FP64-refined mode,
 the last two also through the multicolour ordering (ocsl_set_ordering).
+With ``--vtk`` the state after the first choice's iterations is written from
+device memory as the reference's solution.vtk / solution_BC.vtk
+(``Mesh.write_vtk``, ocsl_vtk_write), timed.
 Prints one JSON object (``bench.py`` times the CPU restatement beside it).
 """
 from __future__ import annotations
@@ -30,16 +33,18 @@ CONFIG = dict(initial={"pressure": 1e5, "temperature": 300.0, "velocity": (20, 0
               viscous=True, blended=True, transient=True, dt=2e-6)
 
 
-def box_case(size: int):
+def box_case(size: int, keep_dir: str | None = None):
     """The N^3 box case: SU2 file -> read_su2 -> build_pattern ->
-    initial_state.  Returns (case, set-up facts)."""
+    initial_state.  Returns (case, set-up facts); the SU2 file stays in
+    keep_dir (as box.su2) when given."""
     import opencslsolver_gb300 as ocsl
     from opencslsolver_gb300 import flow as F
     from opencslsolver_gb300 import workloads as W
 
     info = {"workload": f"{size}^3 jittered hex box from SU2, 3D viscous channel (velocity "
                         "inlet, no-slip walls, pressure outlet), transient"}
-    with tempfile.TemporaryDirectory() as d:
+    with tempfile.TemporaryDirectory() as tmp:
+        d = keep_dir or tmp
         path = os.path.join(d, "box.su2")
         t0 = time.perf_counter()
         W.write_su2_box(path, size, size, size, lengths=(1.0, 1.0, 1.0))
@@ -73,10 +78,37 @@ def methods():
 MULTICOLOUR = ("fp64_tolerance", "fp32_refined")
 
 
-def time_gpu(case: dict, inner: int, device: int = 0, only=None) -> dict:
+def write_vtk(run, su2_path: str, out_dir: str) -> dict:
+    """The run's device state as the reference's two VTK files; seconds
+    (mesh read, write) and file sizes."""
+    import torch
+
+    import opencslsolver_gb300 as ocsl
+
+    st, ar, eq = run.state, run.arrays, run.case["eq"]
+    t0 = time.perf_counter()
+    mesh = ocsl.Mesh(su2_path)
+    t1 = time.perf_counter()
+    cells, bc = os.path.join(out_dir, "solution.vtk"), os.path.join(out_dir, "solution_BC.vtk")
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    mesh.write_vtk(cells, bc, density=st["density_c"], pressure=st["pressure"],
+                   temperature=st["temperature"], mach=ar["mach"], velocity=st["velocity"],
+                   pressure_grad=st["pressure_grad"], bc_type=st["bc_type"],
+                   bc_wall=st["bc_wall"], viscous=bool(eq["viscous"]),
+                   sutherland=eq["sutherland"])
+    t3 = time.perf_counter()
+    mesh.close()
+    return {"mesh_read_s": round(t1 - t0, 2), "write_s": round(t3 - t2, 3),
+            "bytes": os.path.getsize(cells) + os.path.getsize(bc),
+            "threads": os.cpu_count()}
+
+
+def time_gpu(case: dict, inner: int, device: int = 0, only=None, vtk_from=None) -> dict:
     """ms per inner iteration for every solver choice (two untimed calls
     first: allocation, then the graph capture of the reference's solvers);
-    `only`: the one choice to run (a key of the result)."""
+    `only`: the one choice to run (a key of the result); vtk_from: the SU2
+    file, to write the first choice's final state as VTK."""
     import copy
 
     import numpy as np
@@ -110,6 +142,9 @@ def time_gpu(case: dict, inner: int, device: int = 0, only=None) -> dict:
                          "solve_iterations_last": rep["iterations"],
                          "residuals_last": [float(v) for v in rep["residual"]],
                          "finite": bool(all(np.all(np.isfinite(v)) for v in f.values()))}
+            if vtk_from and "vtk" not in out:
+                with tempfile.TemporaryDirectory() as d:
+                    out["vtk"] = write_vtk(run, vtk_from, d)
             del run
             torch.cuda.empty_cache()
     finally:
@@ -123,9 +158,13 @@ def main(argv=None) -> int:
     ap.add_argument("--inner", type=int, default=10)
     ap.add_argument("--only", default=None,
                     help="run one solver choice (e.g. fp32_refined_multicolour)")
+    ap.add_argument("--vtk", action="store_true",
+                    help="write the first choice's final state as VTK from the device, timed")
     a = ap.parse_args(argv)
-    case, info = box_case(a.size)
-    info["gpu"] = time_gpu(case, a.inner, only=a.only)
+    with tempfile.TemporaryDirectory() as d:
+        case, info = box_case(a.size, keep_dir=d if a.vtk else None)
+        info["gpu"] = time_gpu(case, a.inner, only=a.only,
+                               vtk_from=os.path.join(d, "box.su2") if a.vtk else None)
     print(json.dumps(info))
     return 0
 
