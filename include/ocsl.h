@@ -464,6 +464,24 @@ typedef struct {
 int ocsl_vtk_write(const ocsl_mesh* mesh, const ocsl_vtk_fields* fields, const char* cells_path,
                    const char* boundary_path, char* err, size_t err_len);
 
+/* CSR SpMV shape (the SpMV of every non-box pattern, e.g. tetrahedral
+ * meshes; box patterns use stencil records): lanes per row 1 (one thread per
+ * row, 32 rows per warp; the default), 4 (8 rows per warp) or 16 (2 rows per
+ * warp), where a row's lanes load its entries side by side and its first
+ * lane runs the fma chain in CSR order -- results are identical for every
+ * shape.  0 = default.  Reset by ocsl_set_pattern.  No reference
+ * counterpart (the reference's gemv is one thread per row,
+ * cmatrix_solver.cpp:338-453). */
+int ocsl_set_spmv_lanes(ocsl_ctx* ctx, int lanes);
+int ocsl_spmv_lanes(const ocsl_ctx* ctx, int* lanes);
+/* Autotuner of the CSR SpMV's lanes per row (rows per warp) for this pattern
+ * and matrix: times y = A x with its fused dot for each shape with CUDA
+ * events, in the precision a solve of `method` computes its inner SpMVs in
+ * (FP32 for OCSL_ILU_BICGSTAB_IR32, else FP64), keeps the fastest and reports
+ * it with its time in microseconds. */
+int ocsl_autotune_spmv_device(ocsl_ctx* ctx, int method, const double* d_value, int* lanes,
+                              double* spmv_us);
+
 /* Triangular-sweep kernel: 0 automatic (structured when the pattern is a
  * natural-order 7-point box stencil, level-scheduled otherwise), 1 always the
  * level-scheduled kernel, 2 the structured CTA kernel, 3 the structured

@@ -354,6 +354,25 @@ class Context:
                 "cluster": info["cluster32" if fp32 else "cluster"],
                 "wave": info["wave32" if fp32 else "wave"]}
 
+    def autotune_spmv(self, method, value):
+        """Pick the CSR SpMV's lanes per row (1, 4 or 16) for this matrix by
+        timing them (value: CUDA tensor of A); returns {"lanes", "spmv_us"}."""
+        self._follow_torch()
+        lanes, us = C.c_int(), C.c_double()
+        self._check(self._L.ocsl_autotune_spmv_device(self._h, _method(method), _dptr(value),
+                                                      C.byref(lanes), C.byref(us)),
+                    "autotune_spmv")
+        return {"lanes": lanes.value, "spmv_us": us.value}
+
+    def set_spmv_lanes(self, lanes: int):
+        """CSR SpMV lanes per row: 1 (default), 4 or 16; results are identical."""
+        self._check(self._L.ocsl_set_spmv_lanes(self._h, int(lanes)), "set_spmv_lanes")
+
+    def spmv_lanes(self) -> int:
+        v = C.c_int()
+        self._check(self._L.ocsl_spmv_lanes(self._h, C.byref(v)), "spmv_lanes")
+        return v.value
+
     def set_graphs(self, enable: bool = True):
         """Replay iteration batches from CUDA graphs (default on)."""
         self._check(self._L.ocsl_set_graphs(self._h, int(bool(enable))), "set_graphs")

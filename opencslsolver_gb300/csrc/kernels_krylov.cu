@@ -306,6 +306,7 @@ struct SpmvParams {
     Scalars* sc;
     int epi, it, maxit;
     Cols cols;
+    int lanes;  // lanes per row: 1 (spmv_kernel), 4 or 16 (spmv_lanes_kernel)
 };
 
 // y = A x (MODE 0), y = z - A x (MODE 1), y = fma(a, A x, z) (MODE 2);
@@ -395,6 +396,102 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvParams<T> p)
         }
     }
     if constexpr (ND > 0) {
+        double vals[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) vals[k] = acc[k].value();
+        finish_reduction<ND>(vals, tile, ct.ntiles, ct.col, p.R, sc, p.epi, p.it, p.maxit, s_red,
+                             &s_last);
+    }
+}
+
+// spmv_kernel with L lanes per row (32 / L rows per warp): the lanes of a
+// row group load the row's entries side by side (lane l takes entries
+// b + l, b + l + L, ...), so a warp's loads of values and column indices
+// cover contiguous stretches of the CSR arrays for rows of any length; the
+// group's first lane runs the row's fma chain in CSR order from 0.0 with the
+// entries handed over by shuffles, skipping phantoms, so y is spmv_kernel's
+// bit for bit.  The tile's results go to shared memory, and the fused dots
+// are then accumulated exactly as spmv_kernel does (thread t: rows t + 256 j
+// in j order), so the partial sums are unchanged too.  For the short rows of
+// finite-volume stencils one lane per row (spmv_kernel) is faster; longer
+// rows gain from more lanes -- the autotuner times them per matrix.
+template <typename T, int MODE, int DOTS, int L>
+__global__ void __launch_bounds__(kThreads) spmv_lanes_kernel(SpmvParams<T> p)
+{
+    const ColTile ct = col_tile(p.cols);
+    Scalars* const sc = at(p.sc, ct.col);
+    if (sc && sc->done) return;
+    constexpr int ND = DotCount<DOTS>::value;
+    constexpr int kGroups = kThreads / L;  // rows per CTA pass
+    __shared__ double s_red[kMaxDots * 8];
+    __shared__ int s_last;
+    __shared__ T s_y[kTile];
+    const int tile = ct.tile;
+    const int n = p.n;
+    const T* const xv = p.x + ct.off;
+    T* const yv = p.y + ct.off;
+    const T* const zvec = at(p.z, ct.off);
+    T* const ycp = at(p.y_copy, ct.off);
+    const T* const wv = at(p.w, ct.off);
+    const int lane = (int)threadIdx.x & 31;
+    const int g = (int)threadIdx.x / L, l = (int)threadIdx.x % L;
+    const int gbase = lane - l;  // the group's first lane within the warp
+#pragma unroll 1
+    for (int r0 = 0; r0 < kTile; r0 += kGroups) {
+        const int row = tile * kTile + r0 + g;
+        const bool in = row < n;
+        const int b = in ? __ldg(p.rp + row) : 0;
+        const int e = in ? __ldg(p.rp + row + 1) : 0;
+        // the longest row of the warp bounds the warp's uniform block loop
+        int span = e - b;
+#pragma unroll
+        for (int off = L; off < 32; off <<= 1) span = max(span, __shfl_xor_sync(0xffffffffu, span, off));
+        T dum = T(0);
+        for (int k0 = 0; k0 < span; k0 += L) {
+            const int q = b + k0 + l;
+            const bool has = q < e;
+            const int c = has ? __ldg(p.col + q) : -1;
+            const T v = has ? __ldg(p.val + q) : T(0);
+            const T xk = c >= 0 ? __ldg(xv + c) : T(0);
+#pragma unroll
+            for (int s = 0; s < L; ++s) {
+                const int cs = __shfl_sync(0xffffffffu, c, gbase + s);
+                const T vs = __shfl_sync(0xffffffffu, v, gbase + s);
+                const T xs = __shfl_sync(0xffffffffu, xk, gbase + s);
+                if (cs >= 0) dum = fma_t(vs, xs, dum);  // only the first lane's chain is used
+            }
+        }
+        if (l == 0 && in) {
+            T y;
+            if constexpr (MODE == 0) {
+                y = dum;
+            } else if constexpr (MODE == 1) {
+                y = __ldg(zvec + row) - dum;
+            } else {
+                y = fma_t(p.a, dum, __ldg(zvec + row));
+            }
+            yv[row] = y;
+            if (MODE == 1 && ycp) ycp[row] = y;
+            if constexpr (ND > 0) s_y[r0 + g] = y;
+        }
+    }
+    if constexpr (ND > 0) {
+        __syncthreads();
+        DotAcc<T> acc[ND];
+#pragma unroll 1
+        for (int j = 0; j < kRowsPerThread; ++j) {
+            const int row = tile * kTile + j * kThreads + (int)threadIdx.x;
+            if (row >= n) continue;
+            const T y = s_y[j * kThreads + (int)threadIdx.x];
+            int k = 0;
+            if constexpr ((DOTS & DOT_YY) != 0) acc[k++].add(y, y);
+            if constexpr ((DOTS & DOT_ZZ) != 0) {
+                const T zv = MODE == 0 ? T(0) : __ldg(zvec + row);
+                acc[k++].add(zv, zv);
+            }
+            if constexpr ((DOTS & DOT_WY) != 0) acc[k++].add(__ldg(wv + row), y);
+            (void)k;
+        }
         double vals[ND];
 #pragma unroll
         for (int k = 0; k < ND; ++k) vals[k] = acc[k].value();
@@ -886,7 +983,12 @@ void spmv_dispatch(cudaStream_t st, const SpmvParams<T>& p)
 {
     const int nt = ntiles_of(p.n);
     if (nt == 0) return;
-    spmv_kernel<T, MODE, DOTS><<<nt * p.cols.n, kThreads, 0, st>>>(p);
+    const unsigned grid = (unsigned)(nt * p.cols.n);
+    switch (p.lanes) {
+    case 4: spmv_lanes_kernel<T, MODE, DOTS, 4><<<grid, kThreads, 0, st>>>(p); break;
+    case 16: spmv_lanes_kernel<T, MODE, DOTS, 16><<<grid, kThreads, 0, st>>>(p); break;
+    default: spmv_kernel<T, MODE, DOTS><<<grid, kThreads, 0, st>>>(p); break;
+    }
 }
 
 template <typename T, int MODE>
@@ -949,6 +1051,7 @@ void launch_spmv(cudaStream_t st, const DevPattern& P, const T* val, const T* x,
 {
     SpmvParams<T> p;
     p.cols = cols;
+    p.lanes = P.spmv_lanes;
     p.n = P.n;
     p.rp = P.rp;
     p.col = P.col;

@@ -96,6 +96,7 @@ struct BoxGeom {
 };
 
 struct DevPattern {
+    int spmv_lanes = 1;  // CSR SpMV lanes per row (1, 4, 16; ocsl_set_spmv_lanes / autotuner)
     bool box_ok;
     BoxGeom box;    // geometry of the FP64 structured sweeps
     BoxGeom box32;  // and of the FP32 ones (tuned separately)

@@ -1443,16 +1443,16 @@ int ensure_coloured(ocsl_ctx* c)
         rbslot.assign((size_t)cp.col.size(), (signed char)-1);
         rbinfo.assign((size_t)n, 0);
         bool ok = true;
-        for (int t = 0; t < n && ok; ++t) {
-            const RbRow q = rb_row(g, t);
-            // the natural cell of row t
-            const int r = t - q.c * g.n0, rjk = r / g.hx;
+        for (int row = 0; row < n && ok; ++row) {
+            const RbRow q = rb_row(g, row);
+            // the natural cell of this row
+            const int r = row - q.c * g.n0, rjk = r / g.hx;
             const int b = (q.c + rjk % g.ny + rjk / g.ny) & 1;
-            ok = cp.perm[t] == 2 * r + b;
+            ok = cp.perm[row] == 2 * r + b;
             unsigned char f = (unsigned char)(b << 6);
             for (int s = 0; s < 6; ++s)
                 if (q.has[s]) f |= (unsigned char)(1u << s);
-            rbinfo[t] = f;
+            rbinfo[row] = f;
             // entries in the order the kernels sum them, then phantoms
             int want[7], m = 0;
             if (q.c == 0) want[m++] = 6;
@@ -1460,9 +1460,9 @@ int ensure_coloured(ocsl_ctx* c)
                 if (q.has[s]) want[m++] = s;
             if (q.c == 1) want[m++] = 6;
             int e = 0;
-            for (size_t k = cp.rp[t]; k < cp.rp[t + 1] && ok; ++k) {
+            for (size_t k = cp.rp[row]; k < cp.rp[row + 1] && ok; ++k) {
                 if (cp.col[k] == ~size_t(0)) continue;  // phantom
-                ok = e < m && (size_t)(want[e] == 6 ? t : q.nb[want[e]]) == cp.col[k];
+                ok = e < m && (size_t)(want[e] == 6 ? row : q.nb[want[e]]) == cp.col[k];
                 if (ok) rbslot[k] = (signed char)want[e++];
             }
             ok = ok && e == m;
@@ -2445,6 +2445,94 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         geo = keep;
         c->sweep_kernel = kind_keep;
         c->wave[pi] = wkeep;
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ocsl_set_spmv_lanes(ocsl_ctx* c, int lanes)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (lanes == 0) lanes = 1;
+    if (lanes != 1 && lanes != 4 && lanes != 16)
+        return fail(c, OCSL_BAD_ARGUMENT, "lanes per row must be 0, 1, 4 or 16");
+    c->drop_graph();
+    c->P.spmv_lanes = lanes;
+    return OCSL_OK;
+}
+
+int ocsl_spmv_lanes(const ocsl_ctx* c, int* lanes)
+{
+    if (!c || !lanes) return OCSL_BAD_ARGUMENT;
+    if (!c->has_pattern) return OCSL_NO_PATTERN;
+    *lanes = c->P.spmv_lanes;
+    return OCSL_OK;
+}
+
+int ocsl_autotune_spmv_device(ocsl_ctx* c, int method, const double* A, int* lanes,
+                              double* spmv_us)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (lanes) *lanes = 0;
+    if (spmv_us) *spmv_us = 0.0;
+    if (method < OCSL_CG_REF || method > OCSL_ILU_BICGSTAB_IR32)
+        return fail(c, OCSL_BAD_ARGUMENT, "unknown method");
+    if (!A || !aligned8(A)) return fail(c, OCSL_BAD_ARGUMENT, "null or misaligned value pointer");
+    if (c->P.n == 0) return OCSL_OK;
+    const bool fp32 = method == OCSL_ILU_BICGSTAB_IR32;
+    const int keep = c->P.spmv_lanes;
+    try {
+        CK(cudaSetDevice(c->device));
+        const int n = c->P.n;
+        if (fp32) {
+            c->ensure_fp32();
+            launch_convert_f64_f32(c->stream, c->P.nnz, A, c->d_A32);
+            CK(cudaMemsetAsync(c->v32[F_P], 0, sizeof(float) * (size_t)n, c->stream));
+        } else {
+            CK(cudaMemsetAsync(c->v64[P], 0, sizeof(double) * (size_t)n, c->stream));
+        }
+        // y = A x with a dot of y, the SpMV of a Krylov step (the x values do
+        // not change its time)
+        auto spmv = [&] {
+            if (fp32)
+                launch_spmv<float>(c->stream, c->P, c->d_A32, c->v32[F_P], c->v32[F_TMP], 0,
+                                   nullptr, 0.0, nullptr, nullptr, nullptr, DOT_YY, c->R,
+                                   nullptr, 0, 0, 0, Cols{});
+            else
+                launch_spmv<double>(c->stream, c->P, A, c->v64[P], c->v64[TMP], 0, nullptr, 0.0,
+                                    nullptr, nullptr, nullptr, DOT_YY, c->R, nullptr, 0, 0, 0,
+                                    Cols{});
+        };
+        static const int kLanes[] = {1, 4, 16};
+        double best = 1e300;
+        int best_l = keep;
+        for (int l : kLanes) {
+            c->P.spmv_lanes = l;
+            spmv();  // warm-up
+            double t = 1e300;
+            for (int rep = 0; rep < 5; ++rep) {
+                CK(cudaEventRecord(c->ev_start, c->stream));
+                spmv();
+                CK(cudaEventRecord(c->ev_stop, c->stream));
+                CK(cudaEventSynchronize(c->ev_stop));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, c->ev_start, c->ev_stop));
+                t = std::min(t, 1000.0 * ms);
+            }
+            if (t < best) {
+                best = t;
+                best_l = l;
+            }
+        }
+        c->drop_graph();
+        c->P.spmv_lanes = best_l;
+        if (lanes) *lanes = best_l;
+        if (spmv_us) *spmv_us = best;
+        CK(cudaGetLastError());
+    } catch (const CudaError& e) {
+        c->P.spmv_lanes = keep;
         return from_cuda(c, e);
     }
     return OCSL_OK;

@@ -6,6 +6,7 @@ Device buffers come from torch; every call goes through the C ABI."""
 import numpy as np
 import pytest
 
+import opencslsolver_gb300 as ocsl
 from opencslsolver_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -42,6 +43,29 @@ def test_gemv_bit_exact(ctx, torch_cuda, oracle, k):
         ctx.gemv_device(A, X, Y, mode=mode, a=a, z=Z if mode else None)
         want = oracle.gemv(s.row_ptr, s.column_index, s.value, x, mode, a, z)
         assert np.array_equal(host(Y), want), (s.name, mode)
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_gemv_lanes_per_row_bit_exact(ctx, torch_cuda, oracle, k):
+    """The CSR SpMV with 4 and 16 lanes per row (ocsl_set_spmv_lanes): the
+    oracle's bits for rows of 5 to 40 entries, phantoms included."""
+    s = systems()[k]
+    rng = np.random.default_rng(100 + k)
+    x, z = rng.standard_normal(s.n), rng.standard_normal(s.n)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A, X, Z = dev(torch_cuda, s.value), dev(torch_cuda, x), dev(torch_cuda, z)
+    Y = torch_cuda.empty_like(X)
+    for lanes in (4, 16):
+        ctx.set_spmv_lanes(lanes)
+        assert ctx.spmv_lanes() == lanes
+        for mode, a in ((0, 0.0), (1, 0.0), (2, -0.731)):
+            ctx.gemv_device(A, X, Y, mode=mode, a=a, z=Z if mode else None)
+            want = oracle.gemv(s.row_ptr, s.column_index, s.value, x, mode, a, z)
+            assert np.array_equal(host(Y), want), (s.name, lanes, mode)
+    with pytest.raises(ocsl.OcslError):
+        ctx.set_spmv_lanes(3)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    assert ctx.spmv_lanes() == 1  # a new pattern starts from the default
 
 
 def test_gemv_matches_reference_golden(ctx, torch_cuda, golden_small):

@@ -358,6 +358,33 @@ def test_new_pattern_drops_captured_graph(ctx, torch_cuda):
     assert torch.equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
 
 
+@pytest.mark.parametrize("method", [ocsl.BICGSTAB_REF, ocsl.PCG, ocsl.ILU_BICGSTAB,
+                                    ocsl.ILU_BICGSTAB_IR32])
+def test_spmv_lanes_give_identical_solves(ctx, torch_cuda, method):
+    """Every CSR SpMV shape (lanes per row) gives the same solve, bit for bit,
+    on the tet system, whose SpMVs carry the fused dots of every method; the
+    SpMV autotuner keeps one of them."""
+    torch = torch_cuda
+    s = W.tet_pprime(9, 8, 7, peclet=0.0 if method == ocsl.PCG else 50.0)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = torch.from_numpy(s.value).cuda()
+    B = torch.from_numpy(s.b).cuda()
+    out = {}
+    for lanes in (1, 4, 16):
+        ctx.set_spmv_lanes(lanes)
+        X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+        r = ctx.solve_device(method, A, B, X)
+        out[lanes] = (X, r["iterations"], r["status"])
+    for lanes in (4, 16):
+        assert torch.equal(out[lanes][0], out[1][0]), lanes
+        assert out[lanes][1:] == out[1][1:], lanes
+    t = ctx.autotune_spmv(method, A)
+    assert t["lanes"] in (1, 4, 16) and t["spmv_us"] > 0 and ctx.spmv_lanes() == t["lanes"]
+    X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+    ctx.solve_device(method, A, B, X)
+    assert torch.equal(X, out[1][0])
+
+
 @pytest.mark.parametrize("method", [ocsl.ILU_BICGSTAB_IR32, ocsl.ILU_BICGSTAB, ocsl.BICGSTAB_REF])
 def test_autotuned_tile_gives_identical_solves(ctx, torch_cuda, method):
     """ocsl_autotune_device picks one of its candidate tiles, keeps it for the
