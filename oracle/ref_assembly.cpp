@@ -19,6 +19,12 @@
 //                     under-relaxation, supersonic inlet, slip walls, outlet
 //          heat       100-cell heat conduction (cheat_solver.cpp), fixed
 //                     temperatures at both ends, adiabatic sides
+//          heat3d=<mesh.su2>  heat conduction on a mesh read from an SU2 file
+//                     (markers inlet, walls, outlet: 250 K, adiabatic, 450 K),
+//                     6 steps; run from <out_dir> as the working directory, the
+//                     reference's own run writes solution.vtk / solution_BC.vtk
+//                     there (croot.cpp:239-240), and final_heat.bin holds the
+//                     state they were written from
 // File format: repeated [u32 name length][name][u8 kind 'd'|'i'|'u'][u64 count][data].
 #include "croot.h"
 #include "flow_configs.h"
@@ -254,11 +260,37 @@ int main(int argc, char** argv)
         c.boundary_conditions[2].Temperature = 450.0;
         c.max_iteration = 6;
         c.max_inner_iteration = 1;
+    } else if (kase.rfind("heat3d=", 0) == 0) {
+        c.openmp_number_of_threads = 1;
+        c.eproblem_type = enums::Eproblem_type::Heat_conduction;
+        c.ematrix_solver_type = enums::Ematrix_solver_type::ILU_BICSTAB;
+        c.emesh_source = enums::Emesh_source::from_file;
+        c.mesh_filename = kase.substr(7);
+        c.set_BC_number(3);
+        c.global_delta_t = 0.5;
+        c.thermal_diffusivity = 2.0e-3;
+        ic.Temperature = 300.0;
+        c.boundary_conditions[0].ethermal_BC_type = enums::Ethermal_BC_type::constant_temperature;
+        c.boundary_conditions[0].Temperature = 250.0;
+        c.boundary_conditions[1].ethermal_BC_type = enums::Ethermal_BC_type::adiabatic;
+        c.boundary_conditions[2].ethermal_BC_type = enums::Ethermal_BC_type::constant_temperature;
+        c.boundary_conditions[2].Temperature = 450.0;
+        c.max_iteration = 6;
+        c.max_inner_iteration = 1;
     } else {
         std::fprintf(stderr, "unknown case %s\n", kase.c_str());
         return 1;
     }
     root.run_config(c);
     std::printf("solve calls: %ld\n", g_call);
+    if (kase.rfind("heat3d=", 0) == 0) {
+        using Hc = CHeat_solver::CHeat_cell;
+        using Hb = CHeat_solver::CHeat_BC_face;
+        const auto& hs = *root.Heat_solver;
+        Writer w(g_out + "/final_heat.bin");
+        w.d("cell_temperature", col(hs.cells, [](const Hc& x) { return x.Temperature; }));
+        w.d("bc_temperature", col(hs.BC_faces, [](const Hb& f) { return f.Temperature; }));
+        w.i("bc_thermal", coli(hs.BC_faces, [](const Hb& f) { return (int)f.ethermal_BC_type; }));
+    }
     return 0;
 }

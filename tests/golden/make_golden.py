@@ -43,7 +43,9 @@ then writes:
 * vtk_<cells>.npz -- the reference's own VTK output (solution.vtk and
   solution_BC.vtk, as bytes) after a short run of the 3D viscous channel on a
   jittered box of hexahedra, tetrahedra or wedges read from an SU2 file, with
-  the final state and fluid constants it was written from;
+  the final state and fluid constants it was written from; vtk_heat.npz the
+  same for a heat-conduction run on a hex box (fixed temperatures at the
+  inlet and outlet markers, adiabatic walls);
 * assembly_<case>.npz -- the inputs (cell / face state) and outputs (matrix
   values, b, x0, ap_vec, total_mdot) of the reference's face-loop assembly,
   recorded by oracle/ref_assembly.cpp right before the 5 solve calls of one
@@ -338,6 +340,26 @@ def make_vtk(out_dir):
         arrays["mesh_jitter"] = np.array(float(mesh_args["jitter"]))
         arrays["mesh_cells"] = np.array(spec["cells"])
         np.savez_compressed(os.path.join(out_dir, f"vtk_{name}.npz"), **arrays)
+    # heat conduction on a hex box (oracle/ref_assembly.cpp, case heat3d): the
+    # reference's own run_config writes the VTK files into its working directory
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_assembly")
+    mesh = {"nx": 6, "ny": 5, "nz": 4, "lengths": (1.0, 0.2, 0.1), "jitter": 0.1}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "m.su2")
+        m = dict(mesh)
+        W.write_su2_box(path, m.pop("nx"), m.pop("ny"), m.pop("nz"), cells="hex", **m)
+        subprocess.run([exe, d, f"heat3d={path}", "0", "0"], cwd=d, check=True,
+                       stdout=subprocess.DEVNULL)
+        arrays = {f"final__{k}": v
+                  for k, v in read_named_arrays(os.path.join(d, "final_heat.bin")).items()}
+        for key, f in (("cells_vtk", "solution.vtk"), ("bc_vtk", "solution_BC.vtk")):
+            with open(os.path.join(d, f), "rb") as fh:
+                arrays[key] = np.frombuffer(fh.read(), np.uint8)
+    arrays["mesh_dims"] = np.array([mesh[k] for k in ("nx", "ny", "nz")])
+    arrays["mesh_lengths"] = np.array(mesh["lengths"], float)
+    arrays["mesh_jitter"] = np.array(float(mesh["jitter"]))
+    arrays["mesh_cells"] = np.array("hex")
+    np.savez_compressed(os.path.join(out_dir, "vtk_heat.npz"), **arrays)
 
 
 def main():

@@ -6,7 +6,8 @@ wedges read from SU2 files (tests/golden/vtk_<cells>.npz, made by
 tests/golden/make_golden.py).
 
 * CPU: from the recorded final state in host memory, both files are
-  byte-identical to the reference's, for every cell kind; 17 digits give the
+  byte-identical to the reference's, for every cell kind and for a heat-
+  conduction run (oracle/ref_assembly.cpp, case heat3d); 17 digits give the
   state back bit for bit; the heat-conduction branch writes the reference's
   sections; missing fields, bad digit counts and unwritable paths are refused.
 * GPU: the same state as CUDA tensors (streamed from the device) gives the
@@ -74,6 +75,22 @@ def test_vtk_bytes_equal_reference(lib_built, tmp_path, name):
     assert (tmp_path / "b.vtk").read_bytes() == bytes(z["bc_vtk"])
 
 
+def heat_fields(z, to=lambda a: a):
+    return dict(heat=True, temperature=to(z["final__cell_temperature"]),
+                bc_temperature=to(z["final__bc_temperature"]))
+
+
+def test_vtk_heat_bytes_equal_reference(lib_built, tmp_path):
+    """A heat-conduction run of the reference on a hex box (inlet 250 K, outlet
+    450 K, adiabatic walls): its solution.vtk / solution_BC.vtk."""
+    z = fixture("heat")
+    write_mesh(z, tmp_path / "m.su2")
+    with ocsl.Mesh(str(tmp_path / "m.su2")) as m:
+        m.write_vtk(tmp_path / "c.vtk", tmp_path / "b.vtk", **heat_fields(z))
+    assert (tmp_path / "c.vtk").read_bytes() == bytes(z["cells_vtk"])
+    assert (tmp_path / "b.vtk").read_bytes() == bytes(z["bc_vtk"])
+
+
 def test_vtk_full_precision_round_trips(lib_built, tmp_path):
     z = fixture("hex")
     write_mesh(z, tmp_path / "m.su2")
@@ -134,7 +151,7 @@ def test_vtk_refuses_bad_input(lib_built, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", CASES + ("heat",))
 def test_vtk_from_device_equals_reference(lib_built, torch_cuda, tmp_path, name):
     torch = torch_cuda
     z = fixture(name)
@@ -143,8 +160,9 @@ def test_vtk_from_device_equals_reference(lib_built, torch_cuda, tmp_path, name)
     def dev(a):
         return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
+    fields = heat_fields(z, dev) if name == "heat" else flow_fields(z, dev)
     with ocsl.Mesh(str(tmp_path / "m.su2")) as m:
-        m.write_vtk(tmp_path / "c.vtk", tmp_path / "b.vtk", **flow_fields(z, dev))
+        m.write_vtk(tmp_path / "c.vtk", tmp_path / "b.vtk", **fields)
     assert (tmp_path / "c.vtk").read_bytes() == bytes(z["cells_vtk"])
     assert (tmp_path / "b.vtk").read_bytes() == bytes(z["bc_vtk"])
 
