@@ -364,6 +364,11 @@ class Context:
                     "autotune_spmv")
         return {"lanes": lanes.value, "spmv_us": us.value}
 
+    def set_device_loop(self, enable: bool = True):
+        """Run FP32-refined solves with their loops on the device (one graph
+        launch per solve, conditional WHILE nodes); results are identical."""
+        self._check(self._L.ocsl_set_device_loop(self._h, int(bool(enable))), "set_device_loop")
+
     def set_spmv_lanes(self, lanes: int):
         """CSR SpMV lanes per row: 1 (default), 4 or 16; results are identical."""
         self._check(self._L.ocsl_set_spmv_lanes(self._h, int(lanes)), "set_spmv_lanes")

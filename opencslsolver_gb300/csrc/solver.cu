@@ -189,6 +189,10 @@ struct ocsl_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     bool graphs_on = true;
     int graph_kind = 0;
+    // FP32-refined solves run their refinement and inner loops on the device
+    // (conditional graph nodes, ocsl_set_device_loop); its control block
+    bool device_loop = false;
+    void* d_irctl = nullptr;
     // several right-hand sides of the FP32-inner solver in lockstep (else one by one)
     int col_batching = 1;  // 0 one after another, 1 lockstep, 2 lockstep with the SpMM box SpMV
     const void* graph_ptr[6] = {};
@@ -364,6 +368,8 @@ void ocsl_ctx::free_all()
     if (d_fout) cudaFree(d_fout);
     if (h_fout) cudaFreeHost(h_fout);
     if (d_sc_ref) cudaFree(d_sc_ref);
+    if (d_irctl) cudaFree(d_irctl);
+    d_irctl = nullptr;
     d_fout = nullptr;
     h_fout = nullptr;
     d_sc_ref = nullptr;
@@ -1290,6 +1296,250 @@ TolResult run_bicgstab_ir32(Solve& s, const double* A, const double* b, double* 
     return res;
 }
 
+// ---- The refinement loop on the device ------------------------------------
+//
+// run_bicgstab_ir32 with its control flow on the device: the outer
+// refinement loop and the inner FP32 BiCGSTAB loop become conditional WHILE
+// graph nodes, and the decisions the host takes between them (the checks on
+// the FP64 residual, the next inner tolerance max(inner_tol, 0.5 tol /
+// relres), the inner budget, the scalar resets, the status checks after an
+// inner solve) are single-thread control kernels.  The kernels of the
+// arithmetic are the same launches in the same order, so the solve is
+// bit-identical to the host-driven one (no-op launches aside: an inner
+// iteration after convergence returns at once in both).  One graph launch
+// runs the whole solve with no host round trip.
+//
+// Every loop ends: each body's control kernel first sets its loop's
+// condition to 0 and sets it to 1 only to continue, which needs a device
+// iteration counter below its bound (inner: the budget <= inner_maxit;
+// outer: 1000 steps or maxit iterations).
+struct IrCtl {
+    int outer, total, inner_it, budget, status, stop, zero_x, pad;
+    double relres;
+};
+
+__device__ void ir_reset_block(Scalars* s, double tol2)  // the values reset_scalars stages
+{
+    *s = Scalars{};
+    s->tol2 = tol2;
+    s->alpha = 1.0;
+    s->omega = 1.0;
+    s->rhon = 1.0;
+    s->rho = 1.0;
+}
+
+__global__ void ir_begin_kernel(Scalars* s0, double tol2, IrCtl* ctl)
+{
+    ir_reset_block(s0, tol2);
+    *ctl = IrCtl{};
+}
+
+// After a refinement step's FP64 residual (EP_TB_INIT in block 0): the checks
+// at the top of run_bicgstab_ir32's loop, then the inner solve's set-up.  A
+// stop leaves blocks 0 and 1 done, so the rest of the pass is no-ops.
+__global__ void ir_step_kernel(Scalars* s0, Scalars* s1, IrCtl* ctl,
+                               cudaGraphConditionalHandle h_outer,
+                               cudaGraphConditionalHandle h_inner, double tol, double inner_tol,
+                               int maxit, int inner_maxit)
+{
+    cudaGraphSetConditional(h_outer, 0u);
+    cudaGraphSetConditional(h_inner, 0u);
+    bool stop = true;
+    ctl->relres = s0->res;
+    if (s0->status) {
+        ctl->status = s0->status;
+    } else if (s0->bb == 0.0) {
+        ctl->zero_x = 1;
+        ctl->relres = 0.0;
+    } else if (s0->done) {
+    } else if (ctl->total >= maxit || ctl->outer >= 1000) {
+        ctl->status = OCSL_NOT_CONVERGED;
+    } else {
+        stop = false;
+    }
+    if (stop) {
+        ctl->stop = 1;
+        s0->done = 1;
+        s1->done = 1;
+        s1->half = 0;
+        return;
+    }
+    const double q = 0.5 * tol / s0->res;
+    const double itol = inner_tol < q ? q : inner_tol;  // std::max(inner_tol, q)
+    ir_reset_block(s1, itol * itol);
+    ctl->inner_it = 0;
+    ctl->budget = min(inner_maxit, maxit - ctl->total);
+    if (ctl->budget > 0) cudaGraphSetConditional(h_inner, 1u);
+}
+
+__global__ void ir_zero_x_kernel(double* x, int n, const IrCtl* ctl)
+{
+    if (!ctl->zero_x) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] = 0.0;
+}
+
+// End of one inner iteration: continue while not converged and within budget.
+__global__ void ir_inner_kernel(const Scalars* s1, IrCtl* ctl, cudaGraphConditionalHandle h_inner)
+{
+    cudaGraphSetConditional(h_inner, 0u);
+    const int it = ctl->inner_it + 1;
+    ctl->inner_it = it;
+    if (!s1->done && it < ctl->budget) cudaGraphSetConditional(h_inner, 1u);
+}
+
+// After the inner solve and the update of x: the status checks at the end of
+// run_bicgstab_ir32's loop, block 0 reset for the next residual.
+__global__ void ir_post_kernel(Scalars* s0, const Scalars* s1, IrCtl* ctl,
+                               cudaGraphConditionalHandle h_outer, double tol2)
+{
+    cudaGraphSetConditional(h_outer, 0u);
+    if (ctl->stop) return;
+    ctl->total += s1->iters;
+    if (s1->status == OCSL_NONFINITE) {
+        ctl->status = OCSL_NONFINITE;
+        ctl->stop = 1;
+        return;
+    }
+    if (s1->iters == 0 && !s1->done) {
+        ctl->status = OCSL_BREAKDOWN;
+        ctl->stop = 1;
+        return;
+    }
+    ir_reset_block(s0, tol2);
+    ctl->outer += 1;
+    cudaGraphSetConditional(h_outer, 1u);
+}
+
+// A WHILE node after the work captured so far on `st`; returns its body graph.
+cudaGraph_t add_while_node(cudaStream_t st, cudaGraphConditionalHandle h)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &nd));
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, edges, nd, &p));
+    CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                           cudaStreamSetCaptureDependencies));
+    return p.conditional.phGraph_out[0];
+}
+
+// Whether run_bicgstab_ir32 can run with its loops on the device: one column,
+// a stream that can be captured, no profiling or pending fault injection.
+bool device_loop_ok(const Solve& s)
+{
+    const ocsl_ctx* c = s.c;
+    return c->device_loop && s.cols.n == 1 && !c->prof_on && !c->fault_skip_pending &&
+           s.st != nullptr && s.st != cudaStreamLegacy && s.st != cudaStreamPerThread;
+}
+
+// The graph of one FP32-refined solve of A x = b from the current x (the
+// factor, the FP32 copies and the stencil records already prepared).
+cudaGraph_t build_ir32_graph(Solve& s, const double* A, const double* b, double* x,
+                             const ocsl_opts& o)
+{
+    ocsl_ctx* c = s.c;
+    double** v = c->v64;
+    float** f = c->v32;
+    IrCtl* ctl = static_cast<IrCtl*>(c->d_irctl);
+    const double tol2 = o.tol * o.tol;
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraph_t root = nullptr, outer = nullptr, inner = nullptr;
+    CK(cudaGraphCreate(&root, 0));
+    try {
+        cudaGraphConditionalHandle h_outer, h_inner;
+        CK(cudaGraphConditionalHandleCreate(&h_outer, root, 1u, cudaGraphCondAssignDefault));
+        CK(cudaStreamBeginCaptureToGraph(s.st, root, nullptr, nullptr, 0, mode));
+        ir_begin_kernel<<<1, 1, 0, s.st>>>(c->d_sc, tol2, ctl);
+        outer = add_while_node(s.st, h_outer);
+        CK(cudaStreamEndCapture(s.st, &root));
+
+        CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0u, 0u));
+        CK(cudaStreamBeginCaptureToGraph(s.st, outer, nullptr, nullptr, 0, mode));
+        s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 0, EP_TB_INIT);
+        ir_step_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 1, ctl, h_outer, h_inner, o.tol,
+                                          o.inner_tol, o.maxit, o.inner_maxit);
+        ir_zero_x_kernel<<<std::max(1, std::min((s.n + 255) / 256, 1024)), 256, 0, s.st>>>(
+            x, s.n, ctl);
+        s.vec<float>(V_IR_SCALE, {v[R], f[F_RI], f[F_RH], f[F_P], f[F_D]}, 1, EP_IR_INNER_INIT);
+        inner = add_while_node(s.st, h_inner);
+        s.vec<float>(V_TB_HALF, {f[F_D], f[F_PH]}, 1, EP_STORE);
+        s.vec<float>(V_IR_UPDATE, {x, f[F_D]}, -1, EP_STORE);
+        ir_post_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 1, ctl, h_outer, tol2);
+        CK(cudaStreamEndCapture(s.st, &outer));
+
+        CK(cudaStreamBeginCaptureToGraph(s.st, inner, nullptr, nullptr, 0, mode));
+        // every pass fills its sweep outputs itself (the host loop skips the
+        // fills after the first iteration: same bits either way)
+        s.tb_prefilled = false;
+        bicgstab_iteration<float>(s, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI], f[F_RH],
+                                  f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH], f[F_T], f[F_TMP], 1);
+        s.tb_prefilled = false;
+        ir_inner_kernel<<<1, 1, 0, s.st>>>(c->d_sc + 1, ctl, h_inner);
+        CK(cudaStreamEndCapture(s.st, &inner));
+    } catch (...) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s.st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s.st, &g);
+        }
+        cudaGetLastError();
+        cudaGraphDestroy(root);
+        throw;
+    }
+    return root;
+}
+
+// The result of a device-driven solve, from its control block (synchronises).
+TolResult read_ir_ctl(Solve& s)
+{
+    IrCtl h;
+    CK(cudaMemcpyAsync(&h, s.c->d_irctl, sizeof h, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    TolResult r;
+    r.iters = h.total;
+    r.outer = h.outer;
+    r.relres = h.relres;
+    r.status = h.status;
+    return r;
+}
+
+TolResult run_bicgstab_ir32_device(Solve& s, const double* A, const double* b, double* x,
+                                   const ocsl_opts& o)
+{
+    ocsl_ctx* c = s.c;
+    c->ensure_fp32();
+    const double* M = s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+    (void)M;
+    if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
+    s.prepare_spmv(A, true, true);
+    if (!c->d_irctl) CK(cudaMalloc(&c->d_irctl, sizeof(IrCtl)));
+    cudaGraph_t g = build_ir32_graph(s, A, b, x, o);
+    cudaGraphExec_t e = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    struct ExecGuard {  // destroyed after the solve has finished (or on an error)
+        cudaGraphExec_t e;
+        cudaStream_t st;
+        ~ExecGuard()
+        {
+            cudaStreamSynchronize(st);
+            cudaGraphExecDestroy(e);
+        }
+    } guard{e, s.st};
+    CK(cudaGraphLaunch(e, s.st));
+    return read_ir_ctl(s);
+}
+
 // Column-batched form of run_bicgstab_ir32: nc (<= kMaxCols) right-hand
 // sides b, x ([nc][n]) of one matrix in lockstep.  Every launch serves all
 // columns -- the SpMV and vector kernels run nc column slices in one grid,
@@ -1585,6 +1835,8 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
                 t = run_pcg_tol(s, A, b, x, o);
             else if (method == OCSL_ILU_BICGSTAB)
                 t = run_bicgstab_tol(s, A, b, x, o);
+            else if (device_loop_ok(s))
+                t = run_bicgstab_ir32_device(s, A, b, x, o);
             else
                 t = run_bicgstab_ir32(s, A, b, x, o);
             CK(cudaEventRecord(c->ev_stop, c->stream));
@@ -2447,6 +2699,13 @@ int ocsl_autotune_device(ocsl_ctx* c, int method, const double* A, int* tile_a, 
         c->wave[pi] = wkeep;
         return from_cuda(c, e);
     }
+    return OCSL_OK;
+}
+
+int ocsl_set_device_loop(ocsl_ctx* c, int enable)
+{
+    if (!c) return OCSL_BAD_ARGUMENT;
+    c->device_loop = enable != 0;
     return OCSL_OK;
 }
 
