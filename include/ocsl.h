@@ -168,6 +168,17 @@ int ocsl_batch_solve_device(ocsl_batch* batch, int method, const double* const* 
                             const double* const* d_b, double* const* d_x, const ocsl_opts* opts,
                             ocsl_result* result);
 const char* ocsl_batch_last_error(const ocsl_batch* batch);
+/* One-graph mode of ocsl_batch_solve_device for OCSL_ILU_BICGSTAB_IR32: the
+ * host factors every system (as above), then ONE graph launch runs every
+ * solve of every system -- each system's right-hand sides one after another,
+ * the systems side by side, every refinement and inner loop on the device
+ * (conditional WHILE nodes with bounded control kernels, as
+ * ocsl_set_device_loop) -- with no host round trip until all are done.  The
+ * graph is instantiated on the first call and replayed while the method, the
+ * options and the value, b and x pointers stay the same.  Results are
+ * bit-identical to the host-driven batch.  Other methods keep the host-driven
+ * batch.  enable = 0 (default) turns it off.  No reference counterpart. */
+int ocsl_batch_set_graph(ocsl_batch* batch, int enable);
 
 /* Kernel-level entry points on DEVICE pointers, one per reference routine. */
 /* y = A x (mode 0); y = z - A x (mode 1); y = fma(a, A x, z) (mode 2).

@@ -542,6 +542,13 @@ class Batch:
         except Exception:
             pass
 
+    def set_graph(self, enable: bool = True):
+        """One graph launch for every FP32-refined solve of the batch, all loops
+        on the device (ocsl_batch_set_graph); results are identical."""
+        st = self._L.ocsl_batch_set_graph(self._h, int(bool(enable)))
+        if st:
+            raise OcslError(st, "batch_set_graph")
+
     def solve_device(self, method, values, Bs, Xs, **opts):
         """values[i], Bs[i] ([nrhs_i, n_i]) and Xs[i] are CUDA tensors; returns
         (status, list of per-right-hand-side result dicts).  The batch's workers

@@ -218,6 +218,7 @@ _PROTOS = {
     "ocsl_mesh_marker_name": (C.c_char_p, [_P, C.c_int]),
     "ocsl_mesh_destroy": (C.c_int, [_P]),
     "ocsl_set_device_loop": (C.c_int, [_P, C.c_int]),
+    "ocsl_batch_set_graph": (C.c_int, [_P, C.c_int]),
     "ocsl_set_spmv_lanes": (C.c_int, [_P, C.c_int]),
     "ocsl_spmv_lanes": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "ocsl_autotune_spmv_device": (C.c_int, [_P, C.c_int, _P, C.POINTER(C.c_int),

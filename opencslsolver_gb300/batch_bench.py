@@ -6,7 +6,9 @@ side) and one momentum system (3 right-hand sides sharing the matrix) --
     python -m opencslsolver_gb300.batch_bench [--count 64] [--workers 16]
 
 Prints one JSON line: wall time of the whole batch solved concurrently
-(ocsl_batch_solve_device, FP32-refined and plain FP64) and of the same 256
+(ocsl_batch_solve_device, FP32-refined and plain FP64; FP32-refined also in
+the one-graph mode, ocsl_batch_set_graph: one graph launch for all 256 solves
+with every loop on the device, replayed after its first call) and of the same 256
 plain-FP64 solves one after the other on one stream (the same batch object
 with one worker), with every solve's true relative residual checked on the
 device.  Inputs are resident on the device before the clock starts.
@@ -78,6 +80,18 @@ def main(argv=None):
     rr_ir32 = max_relres()
     t_fp64, res_fp64 = run(conc, ocsl.ILU_BICGSTAB)
     rr_fp64 = max_relres()
+    conc.set_graph(True)
+    t0 = time.perf_counter()
+    for X in Xs:  # the first call captures and instantiates the graph
+        X.zero_()
+    st_g, _ = conc.solve_device(ocsl.ILU_BICGSTAB_IR32, vals, Bs, Xs, tol=1e-10)
+    torch.cuda.synchronize()
+    t_capture = time.perf_counter() - t0
+    if st_g != 0:
+        raise RuntimeError(f"graph batch status {st_g}")
+    t_graph, res_graph = run(conc, ocsl.ILU_BICGSTAB_IR32)
+    rr_graph = max_relres()
+    same = all(r1["iterations"] == r2["iterations"] for r1, r2 in zip(res_ir32, res_graph))
     conc.close()
     seq = ocsl.Batch(spec, workers=1)
     run(seq, ocsl.ILU_BICGSTAB)  # warm-up
@@ -95,7 +109,11 @@ def main(argv=None):
         "speedup_batched_ir32_vs_sequential_fp64": round(t_seq / t_ir32, 2),
         "speedup_batched_fp64_vs_sequential_fp64": round(t_seq / t_fp64, 2),
         "solves_per_s_batched_ir32": round(solves / t_ir32, 1),
-        "max_true_relres": {"ir32": rr_ir32, "fp64": rr_fp64},
+        "graph_ir32_s": round(t_graph, 4),
+        "graph_first_call_s": round(t_capture, 4),
+        "solves_per_s_graph_ir32": round(solves / t_graph, 1),
+        "graph_iterations_equal_host_batch": same,
+        "max_true_relres": {"ir32": rr_ir32, "fp64": rr_fp64, "ir32_graph": rr_graph},
         "iterations_total": {"ir32": int(sum(r["iterations"] for r in res_ir32)),
                              "fp64": int(sum(r["iterations"] for r in res_fp64))},
         "setup_s": {"generate": round(gen_s, 1), "batch_create": round(setup_s, 1)},

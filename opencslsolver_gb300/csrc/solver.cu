@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "ocsl_internal.cuh"
+#include "ir32_graph.h"
 #include "pattern.h"
 
 using namespace ocsl;
@@ -193,6 +194,7 @@ struct ocsl_ctx {
     // (conditional graph nodes, ocsl_set_device_loop); its control block
     bool device_loop = false;
     void* d_irctl = nullptr;
+    int n_irctl = 0;
     // several right-hand sides of the FP32-inner solver in lockstep (else one by one)
     int col_batching = 1;  // 0 one after another, 1 lockstep, 2 lockstep with the SpMM box SpMV
     const void* graph_ptr[6] = {};
@@ -370,6 +372,7 @@ void ocsl_ctx::free_all()
     if (d_sc_ref) cudaFree(d_sc_ref);
     if (d_irctl) cudaFree(d_irctl);
     d_irctl = nullptr;
+    n_irctl = 0;
     d_fout = nullptr;
     h_fout = nullptr;
     d_sc_ref = nullptr;
@@ -1411,8 +1414,10 @@ __global__ void ir_post_kernel(Scalars* s0, const Scalars* s1, IrCtl* ctl,
     cudaGraphSetConditional(h_outer, 1u);
 }
 
-// A WHILE node after the work captured so far on `st`; returns its body graph.
-cudaGraph_t add_while_node(cudaStream_t st, cudaGraphConditionalHandle h)
+// A WHILE node after the work captured so far on `st`; returns its body graph
+// (and the node in *node_out).
+cudaGraph_t add_while_node(cudaStream_t st, cudaGraphConditionalHandle h,
+                           cudaGraphNode_t* node_out = nullptr)
 {
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
@@ -1429,6 +1434,7 @@ cudaGraph_t add_while_node(cudaStream_t st, cudaGraphConditionalHandle h)
     CK(cudaGraphAddNode(&node, g, deps, edges, nd, &p));
     CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
                                            cudaStreamSetCaptureDependencies));
+    if (node_out) *node_out = node;
     return p.conditional.phGraph_out[0];
 }
 
@@ -1441,26 +1447,31 @@ bool device_loop_ok(const Solve& s)
            s.st != nullptr && s.st != cudaStreamLegacy && s.st != cudaStreamPerThread;
 }
 
-// The graph of one FP32-refined solve of A x = b from the current x (the
-// factor, the FP32 copies and the stencil records already prepared).
-cudaGraph_t build_ir32_graph(Solve& s, const double* A, const double* b, double* x,
-                             const ocsl_opts& o)
+// Captures one FP32-refined solve of A x = b from the current x into `root`
+// (the factor, the FP32 copies and the stencil records already prepared),
+// after node *last (none: at the root); *last becomes the solve's last node.
+// Its result goes to control block `ctl`.
+void capture_ir32(Solve& s, cudaGraph_t root, cudaGraphNode_t* last, const double* A,
+                  const double* b, double* x, const ocsl_opts& o, IrCtl* ctl)
 {
     ocsl_ctx* c = s.c;
     double** v = c->v64;
     float** f = c->v32;
-    IrCtl* ctl = static_cast<IrCtl*>(c->d_irctl);
     const double tol2 = o.tol * o.tol;
     const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
-    cudaGraph_t root = nullptr, outer = nullptr, inner = nullptr;
-    CK(cudaGraphCreate(&root, 0));
+    cudaGraph_t outer = nullptr, inner = nullptr;
     try {
         cudaGraphConditionalHandle h_outer, h_inner;
         CK(cudaGraphConditionalHandleCreate(&h_outer, root, 1u, cudaGraphCondAssignDefault));
-        CK(cudaStreamBeginCaptureToGraph(s.st, root, nullptr, nullptr, 0, mode));
+        const bool after = last && *last;
+        CK(cudaStreamBeginCaptureToGraph(s.st, root, after ? last : nullptr, nullptr,
+                                         after ? 1 : 0, mode));
         ir_begin_kernel<<<1, 1, 0, s.st>>>(c->d_sc, tol2, ctl);
-        outer = add_while_node(s.st, h_outer);
-        CK(cudaStreamEndCapture(s.st, &root));
+        cudaGraphNode_t loop = nullptr;
+        outer = add_while_node(s.st, h_outer, &loop);
+        cudaGraph_t got = nullptr;
+        CK(cudaStreamEndCapture(s.st, &got));
+        if (last) *last = loop;
 
         CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0u, 0u));
         CK(cudaStreamBeginCaptureToGraph(s.st, outer, nullptr, nullptr, 0, mode));
@@ -1492,17 +1503,27 @@ cudaGraph_t build_ir32_graph(Solve& s, const double* A, const double* b, double*
             cudaStreamEndCapture(s.st, &g);
         }
         cudaGetLastError();
-        cudaGraphDestroy(root);
         throw;
     }
-    return root;
 }
 
-// The result of a device-driven solve, from its control block (synchronises).
-TolResult read_ir_ctl(Solve& s)
+// At least `count` control blocks on the context.
+void ensure_irctl(ocsl_ctx* c, int count)
+{
+    if (c->n_irctl >= count) return;
+    if (c->d_irctl) CK(cudaFree(c->d_irctl));
+    c->d_irctl = nullptr;
+    c->n_irctl = 0;
+    CK(cudaMalloc(&c->d_irctl, sizeof(IrCtl) * (size_t)count));
+    c->n_irctl = count;
+}
+
+// The result of a device-driven solve, from control block `slot` (synchronises).
+TolResult read_ir_ctl(Solve& s, int slot = 0)
 {
     IrCtl h;
-    CK(cudaMemcpyAsync(&h, s.c->d_irctl, sizeof h, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaMemcpyAsync(&h, static_cast<IrCtl*>(s.c->d_irctl) + slot, sizeof h,
+                       cudaMemcpyDeviceToHost, s.st));
     CK(cudaStreamSynchronize(s.st));
     TolResult r;
     r.iters = h.total;
@@ -1521,8 +1542,15 @@ TolResult run_bicgstab_ir32_device(Solve& s, const double* A, const double* b, d
     (void)M;
     if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
     s.prepare_spmv(A, true, true);
-    if (!c->d_irctl) CK(cudaMalloc(&c->d_irctl, sizeof(IrCtl)));
-    cudaGraph_t g = build_ir32_graph(s, A, b, x, o);
+    ensure_irctl(c, 1);
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    try {
+        capture_ir32(s, g, nullptr, A, b, x, o, static_cast<IrCtl*>(c->d_irctl));
+    } catch (...) {
+        cudaGraphDestroy(g);
+        throw;
+    }
     cudaGraphExec_t e = nullptr;
     const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
     cudaGraphDestroy(g);
@@ -1964,6 +1992,90 @@ const char* missing_state_field(const ocsl_assembly& q, const ocsl_flow_state& s
 }
 
 }  // namespace
+
+namespace ocsl {
+
+int ir32_graph_prepare(ocsl_ctx* c, const double* A, const ocsl_opts* opts, int slots)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!A || !aligned8(A)) return fail(c, OCSL_BAD_ARGUMENT, "null or misaligned value pointer");
+    if (c->ordering == OCSL_ORDER_MULTICOLOUR)
+        return fail(c, OCSL_BAD_ARGUMENT, "the one-graph batch runs the natural ordering");
+    const ocsl_opts o = resolve(opts);
+    try {
+        CK(cudaSetDevice(c->device));
+        Solve s{c, c->stream, c->P, c->P.n};
+        c->fac_M = nullptr;
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+        ensure_irctl(c, std::max(1, slots));
+        if (c->P.n == 0) return OCSL_OK;
+        c->ensure_fp32();
+        s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+        const int pv = s.pivot_status();
+        if (pv != OCSL_OK) return pv;
+        s.prepare_spmv(A, true, true);
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ir32_graph_capture(ocsl_ctx* c, cudaGraph_t root, cudaGraphNode_t* last, const double* A,
+                       const double* b, double* x, const ocsl_opts* opts, int slot)
+{
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!b || !x || !aligned8(b) || !aligned8(x))
+        return fail(c, OCSL_BAD_ARGUMENT, "null or misaligned b or x pointer");
+    if (slot < 0 || slot >= c->n_irctl) return fail(c, OCSL_BAD_ARGUMENT, "no such control block");
+    if (c->P.n == 0) return OCSL_OK;
+    if (!c->fac_M) return fail(c, OCSL_BAD_ARGUMENT, "ir32_graph_prepare first");
+    if (c->prof_on || c->fault_skip_pending || c->stream == nullptr ||
+        c->stream == cudaStreamLegacy || c->stream == cudaStreamPerThread)
+        return fail(c, OCSL_BAD_ARGUMENT, "this context cannot capture its solve");
+    const ocsl_opts o = resolve(opts);
+    try {
+        CK(cudaSetDevice(c->device));
+        Solve s{c, c->stream, c->P, c->P.n};
+        s.reuse = true;  // the prepared factor and records: no launches here
+        s.factored(A, o.ilu_sweeps, true, true, -1, false, true, true);
+        s.prepare_spmv(A, true, true);
+        capture_ir32(s, root, last, A, b, x, o, static_cast<IrCtl*>(c->d_irctl) + slot);
+    } catch (const CudaError& e) {
+        return from_cuda(c, e);
+    }
+    return OCSL_OK;
+}
+
+int ir32_graph_result(ocsl_ctx* c, int slot, ocsl_result* r)
+{
+    if (!c || !r) return OCSL_BAD_ARGUMENT;
+    std::memset(r, 0, sizeof *r);
+    if (c->P.n == 0) return OCSL_OK;
+    if (slot < 0 || slot >= c->n_irctl) return fail(c, OCSL_BAD_ARGUMENT, "no such control block");
+    int status = OCSL_OK;
+    try {
+        Solve s{c, c->stream, c->P, c->P.n};
+        const TolResult t = read_ir_ctl(s, slot);
+        r->residual = t.relres;
+        r->iterations = t.iters;
+        r->outer_iterations = t.outer;
+        status = t.status;
+        const int derr = s.device_error();
+        if (derr) status = derr;
+    } catch (const CudaError& e) {
+        status = from_cuda(c, e);
+    }
+    r->status = status;
+    if (status == OCSL_TIMEOUT) c->last_error = "a triangular-sweep wait hit its bound";
+    return status;
+}
+
+cudaStream_t ir32_graph_stream(const ocsl_ctx* c) { return c ? c->stream : nullptr; }
+
+}  // namespace ocsl
 
 // =================================================================== C ABI
 

@@ -188,3 +188,42 @@ def test_batch_workload_shape():
     assert len(dims) == 64
     assert cells.min() >= 0.6 * 10_000 and cells.max() <= 1.4 * 500_000
     assert max(max(d) / min(d) for d in dims) > 2.0
+
+
+def test_batch_graph_equals_host_batch(torch_cuda):
+    """ocsl_batch_set_graph: one graph launch runs every FP32-refined solve of
+    the batch with its loops on the device; x, iteration and step counts,
+    residuals and statuses equal the host-driven batch's, on the first call
+    (capture) and on a replay; a right-hand side with a NaN reports its own
+    status only."""
+    torch = torch_cuda
+    systems = small_batch()
+    batch = ocsl.Batch([(b.system.row_ptr, b.system.column_index, b.rhs.shape[0])
+                        for b in systems], workers=4)
+    vals = [torch.from_numpy(b.system.value).cuda() for b in systems]
+    Bs = [torch.from_numpy(np.ascontiguousarray(b.rhs)).cuda() for b in systems]
+    X1 = [torch.zeros_like(B) for B in Bs]
+    st1, res1 = batch.solve_device(ocsl.ILU_BICGSTAB_IR32, vals, Bs, X1, tol=1e-10)
+    assert st1 == 0
+    batch.set_graph(True)
+    X2 = [torch.zeros_like(B) for B in Bs]
+    keys = ("iterations", "outer_iterations", "status", "residual")
+    for rep in range(2):
+        for X in X2:
+            X.zero_()
+        st2, res2 = batch.solve_device(ocsl.ILU_BICGSTAB_IR32, vals, Bs, X2, tol=1e-10)
+        assert st2 == 0, res2
+        for i, (a, b) in enumerate(zip(X1, X2)):
+            assert torch.equal(a, b), (rep, i)
+        for r1, r2 in zip(res1, res2):
+            assert all(r1[k] == r2[k] for k in keys), (rep, r1, r2)
+    Bs[1][0, 9] = float("nan")
+    for X in X2:
+        X.zero_()
+    st3, res3 = batch.solve_device(ocsl.ILU_BICGSTAB_IR32, vals, Bs, X2, tol=1e-10)
+    assert st3 == _abi.NONFINITE
+    n0 = systems[0].rhs.shape[0]
+    assert res3[n0]["status"] == _abi.NONFINITE
+    assert all(r["status"] == 0 for k, r in enumerate(res3) if k != n0)
+    assert torch.equal(X2[0], X1[0])
+    batch.close()
