@@ -195,6 +195,7 @@ struct ocsl_ctx {
     bool device_loop = false;
     void* d_irctl = nullptr;
     int n_irctl = 0;
+    cudaStream_t capture_stream = nullptr;  // loop bodies captured inside another capture
     // several right-hand sides of the FP32-inner solver in lockstep (else one by one)
     int col_batching = 1;  // 0 one after another, 1 lockstep, 2 lockstep with the SpMM box SpMV
     const void* graph_ptr[6] = {};
@@ -373,6 +374,8 @@ void ocsl_ctx::free_all()
     if (d_irctl) cudaFree(d_irctl);
     d_irctl = nullptr;
     n_irctl = 0;
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+    capture_stream = nullptr;
     d_fout = nullptr;
     h_fout = nullptr;
     d_sc_ref = nullptr;
@@ -1331,10 +1334,29 @@ __device__ void ir_reset_block(Scalars* s, double tol2)  // the values reset_sca
     s->rho = 1.0;
 }
 
-__global__ void ir_begin_kernel(Scalars* s0, double tol2, IrCtl* ctl)
+// Start of a solve; a zero or infinite pivot of the factor (flagged in *err
+// by the factor kernels) runs no iteration and leaves x unchanged.
+__global__ void ir_begin_kernel(Scalars* s0, double tol2, IrCtl* ctl, const int* err,
+                                cudaGraphConditionalHandle h_outer)
 {
     ir_reset_block(s0, tol2);
     *ctl = IrCtl{};
+    if (*err == OCSL_ZERO_PIVOT) {
+        ctl->status = OCSL_ZERO_PIVOT;
+        ctl->relres = __longlong_as_double(0x7FF8000000000000LL);
+        ctl->stop = 1;
+        cudaGraphSetConditional(h_outer, 0u);
+    }
+}
+
+// The iteration count and status of a solve inside the SIMPLE iteration's
+// graph, into the iteration's output block; *err (a sweep wait that gave up,
+// a zero pivot) takes precedence, as in a direct solve, and is cleared.
+__global__ void ir_flow_out_kernel(const IrCtl* ctl, int* err, int* iters_out, int* err_out)
+{
+    *iters_out = ctl->total;
+    *err_out = *err ? *err : ctl->status;
+    *err = 0;
 }
 
 // After a refinement step's FP64 residual (EP_TB_INIT in block 0): the checks
@@ -1447,6 +1469,55 @@ bool device_loop_ok(const Solve& s)
            s.st != nullptr && s.st != cudaStreamLegacy && s.st != cudaStreamPerThread;
 }
 
+// The two loop bodies of a captured FP32-refined solve: the refinement step
+// into `outer` (the body of the WHILE node of h_outer) with a nested WHILE
+// node for the inner loop, captured on sb.st.
+void capture_ir32_bodies(Solve& sb, cudaGraph_t outer, cudaGraphConditionalHandle h_outer,
+                         const double* A, const double* b, double* x, const ocsl_opts& o,
+                         IrCtl* ctl)
+{
+    ocsl_ctx* c = sb.c;
+    double** v = c->v64;
+    float** f = c->v32;
+    const double tol2 = o.tol * o.tol;
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraph_t inner = nullptr;
+    cudaGraphConditionalHandle h_inner;
+    CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0u, 0u));
+    CK(cudaStreamBeginCaptureToGraph(sb.st, outer, nullptr, nullptr, 0, mode));
+    sb.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 0, EP_TB_INIT);
+    ir_step_kernel<<<1, 1, 0, sb.st>>>(c->d_sc, c->d_sc + 1, ctl, h_outer, h_inner, o.tol,
+                                       o.inner_tol, o.maxit, o.inner_maxit);
+    ir_zero_x_kernel<<<std::max(1, std::min((sb.n + 255) / 256, 1024)), 256, 0, sb.st>>>(
+        x, sb.n, ctl);
+    sb.vec<float>(V_IR_SCALE, {v[R], f[F_RI], f[F_RH], f[F_P], f[F_D]}, 1, EP_IR_INNER_INIT);
+    inner = add_while_node(sb.st, h_inner);
+    sb.vec<float>(V_TB_HALF, {f[F_D], f[F_PH]}, 1, EP_STORE);
+    sb.vec<float>(V_IR_UPDATE, {x, f[F_D]}, -1, EP_STORE);
+    ir_post_kernel<<<1, 1, 0, sb.st>>>(c->d_sc, c->d_sc + 1, ctl, h_outer, tol2);
+    CK(cudaStreamEndCapture(sb.st, &outer));
+
+    CK(cudaStreamBeginCaptureToGraph(sb.st, inner, nullptr, nullptr, 0, mode));
+    // every pass fills its sweep outputs itself (the host loop skips the
+    // fills after the first iteration: same bits either way)
+    sb.tb_prefilled = false;
+    bicgstab_iteration<float>(sb, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI], f[F_RH],
+                              f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH], f[F_T], f[F_TMP], 1);
+    sb.tb_prefilled = false;
+    ir_inner_kernel<<<1, 1, 0, sb.st>>>(c->d_sc + 1, ctl, h_inner);
+    CK(cudaStreamEndCapture(sb.st, &inner));
+}
+
+void end_any_capture(cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+    }
+    cudaGetLastError();
+}
+
 // Captures one FP32-refined solve of A x = b from the current x into `root`
 // (the factor, the FP32 copies and the stencil records already prepared),
 // after node *last (none: at the root); *last becomes the solve's last node.
@@ -1455,54 +1526,45 @@ void capture_ir32(Solve& s, cudaGraph_t root, cudaGraphNode_t* last, const doubl
                   const double* b, double* x, const ocsl_opts& o, IrCtl* ctl)
 {
     ocsl_ctx* c = s.c;
-    double** v = c->v64;
-    float** f = c->v32;
     const double tol2 = o.tol * o.tol;
-    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
-    cudaGraph_t outer = nullptr, inner = nullptr;
     try {
-        cudaGraphConditionalHandle h_outer, h_inner;
+        cudaGraphConditionalHandle h_outer;
         CK(cudaGraphConditionalHandleCreate(&h_outer, root, 1u, cudaGraphCondAssignDefault));
         const bool after = last && *last;
         CK(cudaStreamBeginCaptureToGraph(s.st, root, after ? last : nullptr, nullptr,
-                                         after ? 1 : 0, mode));
-        ir_begin_kernel<<<1, 1, 0, s.st>>>(c->d_sc, tol2, ctl);
+                                         after ? 1 : 0, cudaStreamCaptureModeThreadLocal));
+        ir_begin_kernel<<<1, 1, 0, s.st>>>(c->d_sc, tol2, ctl, c->d_err, h_outer);
         cudaGraphNode_t loop = nullptr;
-        outer = add_while_node(s.st, h_outer, &loop);
+        cudaGraph_t outer = add_while_node(s.st, h_outer, &loop);
         cudaGraph_t got = nullptr;
         CK(cudaStreamEndCapture(s.st, &got));
         if (last) *last = loop;
-
-        CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0u, 0u));
-        CK(cudaStreamBeginCaptureToGraph(s.st, outer, nullptr, nullptr, 0, mode));
-        s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 0, EP_TB_INIT);
-        ir_step_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 1, ctl, h_outer, h_inner, o.tol,
-                                          o.inner_tol, o.maxit, o.inner_maxit);
-        ir_zero_x_kernel<<<std::max(1, std::min((s.n + 255) / 256, 1024)), 256, 0, s.st>>>(
-            x, s.n, ctl);
-        s.vec<float>(V_IR_SCALE, {v[R], f[F_RI], f[F_RH], f[F_P], f[F_D]}, 1, EP_IR_INNER_INIT);
-        inner = add_while_node(s.st, h_inner);
-        s.vec<float>(V_TB_HALF, {f[F_D], f[F_PH]}, 1, EP_STORE);
-        s.vec<float>(V_IR_UPDATE, {x, f[F_D]}, -1, EP_STORE);
-        ir_post_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 1, ctl, h_outer, tol2);
-        CK(cudaStreamEndCapture(s.st, &outer));
-
-        CK(cudaStreamBeginCaptureToGraph(s.st, inner, nullptr, nullptr, 0, mode));
-        // every pass fills its sweep outputs itself (the host loop skips the
-        // fills after the first iteration: same bits either way)
-        s.tb_prefilled = false;
-        bicgstab_iteration<float>(s, c->d_A32, c->d_M32, c->d_dinv32, f[F_D], f[F_RI], f[F_RH],
-                                  f[F_P], f[F_PH], f[F_V], f[F_S], f[F_SH], f[F_T], f[F_TMP], 1);
-        s.tb_prefilled = false;
-        ir_inner_kernel<<<1, 1, 0, s.st>>>(c->d_sc + 1, ctl, h_inner);
-        CK(cudaStreamEndCapture(s.st, &inner));
+        capture_ir32_bodies(s, outer, h_outer, A, b, x, o, ctl);
     } catch (...) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        if (cudaStreamIsCapturing(s.st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
-            cudaGraph_t g = nullptr;
-            cudaStreamEndCapture(s.st, &g);
-        }
-        cudaGetLastError();
+        end_any_capture(s.st);
+        throw;
+    }
+}
+
+// The same solve inserted into the capture in progress on s.st (the factor
+// and records captured before it); its loop bodies are captured on `scratch`.
+void capture_ir32_inline(Solve& s, cudaStream_t scratch, const double* A, const double* b,
+                         double* x, const ocsl_opts& o, IrCtl* ctl)
+{
+    ocsl_ctx* c = s.c;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamGetCaptureInfo(s.st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    cudaGraphConditionalHandle h_outer;
+    CK(cudaGraphConditionalHandleCreate(&h_outer, g, 1u, cudaGraphCondAssignDefault));
+    ir_begin_kernel<<<1, 1, 0, s.st>>>(c->d_sc, o.tol * o.tol, ctl, c->d_err, h_outer);
+    cudaGraph_t outer = add_while_node(s.st, h_outer);
+    Solve sb = s;
+    sb.st = scratch;
+    try {
+        capture_ir32_bodies(sb, outer, h_outer, A, b, x, o, ctl);
+    } catch (...) {
+        end_any_capture(scratch);
         throw;
     }
 }
@@ -1511,6 +1573,7 @@ void capture_ir32(Solve& s, cudaGraph_t root, cudaGraphNode_t* last, const doubl
 void ensure_irctl(ocsl_ctx* c, int count)
 {
     if (c->n_irctl >= count) return;
+    c->drop_flow_graph();  // a captured iteration may point at the old blocks
     if (c->d_irctl) CK(cudaFree(c->d_irctl));
     c->d_irctl = nullptr;
     c->n_irctl = 0;
@@ -3309,6 +3372,10 @@ static int flow_iterate_graphed(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_
     add(it, sizeof *it);
     add(methods, 3 * sizeof(int));
     add(&o.ilu_sweeps, sizeof o.ilu_sweeps);
+    add(&o.tol, sizeof o.tol);  // the FP32-refined solves' tolerances and budgets too
+    add(&o.maxit, sizeof o.maxit);
+    add(&o.inner_tol, sizeof o.inner_tol);
+    add(&o.inner_maxit, sizeof o.inner_maxit);
     add(&c->stream, sizeof c->stream);
     if (key != c->flow_key) {
         c->drop_flow_graph();
@@ -3323,6 +3390,14 @@ static int flow_iterate_graphed(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_
         CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     }
+    bool ir32 = false;
+    for (int e = 0; e < 3; ++e) ir32 = ir32 || methods[e] == OCSL_ILU_BICGSTAB_IR32;
+    if (ir32) {  // everything a captured FP32-refined solve needs, allocated outside the capture
+        c->ensure_fp32();
+        ensure_irctl(c, 5);
+        if (!c->capture_stream)
+            CK(cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking));
+    }
     const cudaStream_t caller = c->stream;
     const cudaStream_t work = capturable(caller) ? caller : c->own_stream;
     if (work != caller) {
@@ -3334,6 +3409,33 @@ static int flow_iterate_graphed(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_
         enqueue_flow(c, work, q, s, it, methods, f, [&](int slot, int method) {
             Solve sv{c, work, c->P, c->P.n};
             c->fac_M = nullptr;
+            if (method == OCSL_ILU_BICGSTAB_IR32) {
+                cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+                CK(cudaStreamIsCapturing(work, &cs));
+                if (cs == cudaStreamCaptureStatusActive) {
+                    // the factor, the records and the device-driven loops
+                    sv.factored(c->d_fval, o.ilu_sweeps, true, true, -1, false, true, true);
+                    sv.prepare_spmv(c->d_fval, true, true);
+                    IrCtl* ctl = static_cast<IrCtl*>(c->d_irctl) + slot;
+                    capture_ir32_inline(sv, c->capture_stream, c->d_fval, c->d_fb, c->d_fx, o,
+                                        ctl);
+                    ir_flow_out_kernel<<<1, 1, 0, work>>>(ctl, c->d_err,
+                                                          c->d_fout->iterations + slot,
+                                                          c->d_fout->err + slot);
+                } else {
+                    // the first call of a key runs directly (it allocates)
+                    const TolResult t =
+                        run_bicgstab_ir32(sv, c->d_fval, c->d_fb, c->d_fx, o);
+                    const int derr = sv.device_error();
+                    const int out[2] = {t.iters, derr ? derr : t.status};
+                    CK(cudaMemcpy(c->d_fout->iterations + slot, &out[0], sizeof(int),
+                                  cudaMemcpyHostToDevice));
+                    CK(cudaMemcpy(c->d_fout->err + slot, &out[1], sizeof(int),
+                                  cudaMemcpyHostToDevice));
+                    CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), work));
+                }
+                return;
+            }
             if (method == OCSL_CG_REF)
                 run_cg_ref(sv, c->d_fval, c->d_fb, c->d_fx, true);
             else
@@ -3392,8 +3494,9 @@ static int flow_iterate_graphed(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_
         // host-side choices baked into the graph may no longer hold
         if (status == OCSL_TIMEOUT) c->wave_faces_dirty = true;
         c->drop_flow_graph();
-        c->last_error = status == OCSL_TIMEOUT ? "a triangular-sweep wait hit its bound"
-                                               : "the factor has a zero or infinite pivot";
+        c->last_error = status == OCSL_TIMEOUT      ? "a triangular-sweep wait hit its bound"
+                        : status == OCSL_ZERO_PIVOT ? "the factor has a zero or infinite pivot"
+                                                    : ocsl_status_string(status);
     }
     return status;
 }
@@ -3406,11 +3509,16 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
 {
     if (report) std::memset(report, 0, sizeof *report);
     if (!methods) return c ? fail(c, OCSL_BAD_ARGUMENT, "null methods") : OCSL_BAD_ARGUMENT;
-    bool ref_only = true;
+    // one CUDA graph per iteration: the reference's solvers, and the
+    // FP32-refined one with its loops on the device (ocsl_set_device_loop)
+    bool graphable = true;
     for (int e = 0; e < 3; ++e) {
         if (methods[e] < OCSL_CG_REF || methods[e] > OCSL_ILU_BICGSTAB_IR32)
             return c ? fail(c, OCSL_BAD_ARGUMENT, "unknown method") : OCSL_BAD_ARGUMENT;
-        ref_only = ref_only && (methods[e] == OCSL_CG_REF || methods[e] == OCSL_BICGSTAB_REF);
+        graphable = graphable &&
+                    (methods[e] == OCSL_CG_REF || methods[e] == OCSL_BICGSTAB_REF ||
+                     (methods[e] == OCSL_ILU_BICGSTAB_IR32 && c && c->device_loop &&
+                      c->ordering != OCSL_ORDER_MULTICOLOUR));
     }
     FlowDev f{};
     int status = OCSL_OK;
@@ -3443,7 +3551,7 @@ int ocsl_flow_iterate_device(ocsl_ctx* c, const ocsl_assembly* q, const ocsl_flo
             CK(cudaMallocHost(&c->h_fout, sizeof *c->h_fout));
         }
         const ocsl_opts o = resolve(opts);
-        if (ref_only && c->graphs_on && !c->prof_on && !c->fault_skip_pending) {
+        if (graphable && c->graphs_on && !c->prof_on && !c->fault_skip_pending) {
             status = flow_iterate_graphed(c, q, s, it, methods, o, f, rep);
         } else {
             // solves through the ordinary entry (tolerance-mode iterations

@@ -266,3 +266,42 @@ def test_flow_run_from_su2_bit_exact_vs_oracle(ctx, torch_cuda, tmp_path, cells)
                 assert rep["iterations"] == list(want["iterations"]), (cells, mode, rep)
             run.end_step()
             FC.end_step(c, orc.flow_end_step)
+
+
+@pytest.mark.parametrize("case", ["shocktube", "box3d"])
+def test_ir32_iteration_graph_equals_direct(ctx, torch_cuda, case):
+    """With ocsl_set_device_loop the SIMPLE iteration with FP32-refined solves
+    is one CUDA graph too (from the second call; the solves' loops as
+    conditional graph nodes): every field, residual, iteration count and
+    status equals the directly launched iteration's, step by step; the time
+    per inner iteration of both is printed."""
+    torch = torch_cuda
+    g = golden(case)
+    steps = 3
+    runs = {}
+    for dev_loop in (False, True):
+        dev = FC.DeviceCase(torch, g.case())
+        dev.bind(ctx)
+        ctx.set_device_loop(dev_loop)
+        stream = torch.cuda.Stream()
+        reps, fields = [], []
+        with torch.cuda.stream(stream):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                for _ in range(g.inner):
+                    reps.append(dev.iterate(ctx, METHODS["ir32"]))
+                    fields.append(dev.written())
+                dev.end_step(ctx)
+            stream.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3 / (steps * g.inner)
+        runs[dev_loop] = (reps, fields, ms)
+    ctx.set_device_loop(False)
+    (r0, f0, ms0), (r1, f1, ms1) = runs[False], runs[True]
+    for k, (a, b) in enumerate(zip(r0, r1)):
+        assert a["status"] == b["status"] == [0] * 5, (k, a, b)
+        assert a["iterations"] == b["iterations"] and a["residual"] == b["residual"], (k, a, b)
+    for k, (a, b) in enumerate(zip(f0, f1)):
+        _same(b, a, (case, k))
+    print(f"{case}: FP32-refined SIMPLE iteration {ms0:.2f} ms direct, {ms1:.2f} ms as one graph "
+          f"(host wall clock, first calls included)")
