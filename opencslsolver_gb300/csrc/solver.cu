@@ -196,6 +196,9 @@ struct ocsl_ctx {
     void* d_irctl = nullptr;
     int n_irctl = 0;
     cudaStream_t capture_stream = nullptr;  // loop bodies captured inside another capture
+    // the instantiated graph of the last device-driven solve and its key
+    cudaGraphExec_t ir_exec = nullptr;
+    std::vector<unsigned char> ir_key;
     // several right-hand sides of the FP32-inner solver in lockstep (else one by one)
     int col_batching = 1;  // 0 one after another, 1 lockstep, 2 lockstep with the SpMM box SpMV
     const void* graph_ptr[6] = {};
@@ -288,6 +291,9 @@ struct ocsl_ctx {
         graph_exec = nullptr;
         graph_kind = 0;
         drop_flow_graph();
+        if (ir_exec) cudaGraphExecDestroy(ir_exec);
+        ir_exec = nullptr;
+        ir_key.clear();
     }
     void ensure_reduce(int ntiles);
     void ensure_fp32();
@@ -376,6 +382,9 @@ void ocsl_ctx::free_all()
     n_irctl = 0;
     if (capture_stream) cudaStreamDestroy(capture_stream);
     capture_stream = nullptr;
+    if (ir_exec) cudaGraphExecDestroy(ir_exec);
+    ir_exec = nullptr;
+    ir_key.clear();
     d_fout = nullptr;
     h_fout = nullptr;
     d_sc_ref = nullptr;
@@ -1573,7 +1582,7 @@ void capture_ir32_inline(Solve& s, cudaStream_t scratch, const double* A, const 
 void ensure_irctl(ocsl_ctx* c, int count)
 {
     if (c->n_irctl >= count) return;
-    c->drop_flow_graph();  // a captured iteration may point at the old blocks
+    c->drop_graph();  // captured solves and iterations may point at the old blocks
     if (c->d_irctl) CK(cudaFree(c->d_irctl));
     c->d_irctl = nullptr;
     c->n_irctl = 0;
@@ -1606,28 +1615,38 @@ TolResult run_bicgstab_ir32_device(Solve& s, const double* A, const double* b, d
     if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
     s.prepare_spmv(A, true, true);
     ensure_irctl(c, 1);
-    cudaGraph_t g = nullptr;
-    CK(cudaGraphCreate(&g, 0));
-    try {
-        capture_ir32(s, g, nullptr, A, b, x, o, static_cast<IrCtl*>(c->d_irctl));
-    } catch (...) {
-        cudaGraphDestroy(g);
-        throw;
-    }
-    cudaGraphExec_t e = nullptr;
-    const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
-    cudaGraphDestroy(g);
-    CK(ie);
-    struct ExecGuard {  // destroyed after the solve has finished (or on an error)
-        cudaGraphExec_t e;
-        cudaStream_t st;
-        ~ExecGuard()
-        {
-            cudaStreamSynchronize(st);
-            cudaGraphExecDestroy(e);
+    // the graph reads these pointers and settings; it is replayed while they hold
+    std::vector<unsigned char> key;
+    auto add = [&](const void* p, size_t bytes) {
+        const unsigned char* q = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), q, q + bytes);
+    };
+    const void* ptrs[7] = {A, b, x, s.st, s.soa32, s.recA32, c->d_irctl};
+    add(ptrs, sizeof ptrs);
+    add(&o.tol, sizeof o.tol);
+    add(&o.maxit, sizeof o.maxit);
+    add(&o.inner_tol, sizeof o.inner_tol);
+    add(&o.inner_maxit, sizeof o.inner_maxit);
+    if (!c->ir_exec || key != c->ir_key) {
+        if (c->ir_exec) cudaGraphExecDestroy(c->ir_exec);
+        c->ir_exec = nullptr;
+        c->ir_key.clear();
+        cudaGraph_t g = nullptr;
+        CK(cudaGraphCreate(&g, 0));
+        try {
+            capture_ir32(s, g, nullptr, A, b, x, o, static_cast<IrCtl*>(c->d_irctl));
+        } catch (...) {
+            cudaGraphDestroy(g);
+            throw;
         }
-    } guard{e, s.st};
-    CK(cudaGraphLaunch(e, s.st));
+        cudaGraphExec_t e = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
+        cudaGraphDestroy(g);
+        CK(ie);
+        c->ir_exec = e;
+        c->ir_key = key;
+    }
+    CK(cudaGraphLaunch(c->ir_exec, s.st));
     return read_ir_ctl(s);
 }
 

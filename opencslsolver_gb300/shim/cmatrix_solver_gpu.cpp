@@ -60,6 +60,10 @@ GpuSolver& gpu_for(CMatrix_solver* s)
         const char* dev = std::getenv("OCSL_DEVICE");
         const int rc = ocsl_create(&g.ctx, dev ? std::atoi(dev) : 0);
         if (rc != OCSL_OK) die("ocsl_create", rc, nullptr);
+        // an OCSL_SOLVER=ilu_bicgstab_ir32 solve runs as one graph launch with
+        // its loops on the device (same results, no host round trip per batch
+        // of iterations; the other methods are unaffected)
+        ocsl_set_device_loop(g.ctx, 1);
     }
     // The pattern is fixed once per run (cfvm.cpp:84-97); upload it again only
     // if the vectors were replaced or resized.

@@ -58,6 +58,13 @@ int ocsl_destroy(ocsl_ctx* c)
     return OCSL_OK;
 }
 
+/* The CPU restatement has no device loop to switch: accepted, nothing changes. */
+int ocsl_set_device_loop(ocsl_ctx* c, int enable)
+{
+    (void)enable;
+    return c ? OCSL_OK : OCSL_BAD_ARGUMENT;
+}
+
 int ocsl_set_pattern(ocsl_ctx* c, size_t n, const size_t* rp, const size_t* col)
 {
     const size_t nnz = rp[n];

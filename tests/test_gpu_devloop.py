@@ -120,3 +120,36 @@ def test_device_loop_full_size(ctx, torch_cuda, hex128):
     ctx.set_device_loop(False)
     print(f"128^3 FP32-refined solve: host loop {ms[False]:.2f} ms, device loop {ms[True]:.2f} ms "
           f"({out[1][1]['iterations']} inner iterations, {out[1][1]['outer_iterations']} steps)")
+
+
+def test_device_loop_small_system_replays_its_graph(ctx, torch_cuda):
+    """Repeated solves of a small system (the latency-bound case, where the
+    host loop's round trips cost the most): the device loop's graph is
+    instantiated once and replayed; same bits; both times are printed."""
+    torch = torch_cuda
+    s = W.hex_pprime(16, 14, 12, peclet=10.0)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    A = torch.from_numpy(s.value).cuda()
+    B = torch.from_numpy(s.b).cuda()
+    stream = torch.cuda.Stream()
+    out, ms = {}, {}
+    with torch.cuda.stream(stream):
+        for dev in (False, True):
+            ctx.set_device_loop(dev)
+            X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
+            ctx.solve_device(IR32, A, B, X)  # warm-up (and capture)
+            import time
+
+            stream.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(20):
+                X.zero_()
+                r = ctx.solve_device(IR32, A, B, X)
+            stream.synchronize()
+            ms[dev] = (time.perf_counter() - t0) * 1e3 / 20
+            out[dev] = (X.clone(), r)
+    ctx.set_device_loop(False)
+    assert torch.equal(out[False][0], out[True][0])
+    assert out[False][1]["iterations"] == out[True][1]["iterations"]
+    print(f"{s.n}-row FP32-refined solve: host loop {ms[False]:.3f} ms, device loop "
+          f"{ms[True]:.3f} ms per solve ({out[True][1]['iterations']} inner iterations)")
