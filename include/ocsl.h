@@ -475,17 +475,19 @@ typedef struct {
 int ocsl_vtk_write(const ocsl_mesh* mesh, const ocsl_vtk_fields* fields, const char* cells_path,
                    const char* boundary_path, char* err, size_t err_len);
 
-/* OCSL_ILU_BICGSTAB_IR32 solves with their control flow on the device: the
- * refinement loop and the inner FP32 loop run as conditional WHILE graph
+/* Tolerance-mode solves with their control flow on the device: the loops of
+ * OCSL_ILU_BICGSTAB_IR32 (refinement and inner FP32 loop), OCSL_ILU_BICGSTAB
+ * and OCSL_PCG (restarts and Krylov loop) run as conditional WHILE graph
  * nodes with single-thread control kernels taking the decisions the host
- * takes otherwise (residual checks, next inner tolerance, budgets, statuses),
- * so one graph launch runs the whole solve with no host round trip; every
- * loop continues only below a device iteration bound (the inner budget, 1000
- * refinement steps, maxit).  Results are bit-identical to the host-driven
- * loop.  Applies to single-right-hand-side solves on a stream that can be
- * captured (not the legacy default stream), without profiling; otherwise the
- * host drives the loop.  enable = 0 (default) keeps the host loop.  No
- * reference counterpart. */
+ * takes otherwise (residual checks, the next inner tolerance, budgets,
+ * restarts, statuses), so one graph launch runs the whole solve with no host
+ * round trip; every loop continues only below a device iteration bound (the
+ * inner budget, 1000 refinement steps or 64 restarts, maxit).  The graph is
+ * kept and replayed while its pointers and options hold.  Results are
+ * bit-identical to the host-driven loop.  Applies to single-right-hand-side
+ * solves on a stream that can be captured (not the legacy default stream),
+ * without profiling; otherwise the host drives the loop.  enable = 0
+ * (default) keeps the host loop.  No reference counterpart. */
 int ocsl_set_device_loop(ocsl_ctx* ctx, int enable);
 
 /* CSR SpMV shape (the SpMV of every non-box pattern, e.g. tetrahedral

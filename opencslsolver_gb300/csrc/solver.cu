@@ -1621,6 +1621,8 @@ TolResult run_bicgstab_ir32_device(Solve& s, const double* A, const double* b, d
         const unsigned char* q = static_cast<const unsigned char*>(p);
         key.insert(key.end(), q, q + bytes);
     };
+    const int kind = 3;  // the FP32-refined solve (the restarted drivers use 1, 2)
+    add(&kind, sizeof kind);
     const void* ptrs[7] = {A, b, x, s.st, s.soa32, s.recA32, c->d_irctl};
     add(ptrs, sizeof ptrs);
     add(&o.tol, sizeof o.tol);
@@ -1648,6 +1650,231 @@ TolResult run_bicgstab_ir32_device(Solve& s, const double* A, const double* b, d
     }
     CK(cudaGraphLaunch(c->ir_exec, s.st));
     return read_ir_ctl(s);
+}
+
+// ---- The restarted FP64 drivers' loop on the device -------------------------
+//
+// run_restarted (plain FP64 ILU-BiCGSTAB and Jacobi PCG) with its control
+// flow on the device, as run_bicgstab_ir32_device does for the refinement
+// loop: the restart loop (at most 64 passes) and the Krylov loop (at most the
+// remaining maxit iterations) as conditional WHILE nodes, the host's checks
+// as single-thread control kernels over a control block (the IrCtl fields:
+// outer = restarts, total, inner_it / budget of the Krylov loop, status,
+// relres; pad = breakdown seen).  Same launches in the same order.
+struct RsCtl {
+    IrCtl k;
+    int converged, pass_stop;
+};
+
+__global__ void rs_begin_kernel(RsCtl* ctl) { *ctl = RsCtl{}; }
+
+// Top of a restart: block 0 as reset_scalars leaves it.
+__global__ void rs_reset_kernel(Scalars* s0, double tol2, RsCtl* ctl)
+{
+    ir_reset_block(s0, tol2);
+    ctl->pass_stop = 0;
+}
+
+// After the first residual (EP_TB_INIT) and the method's init: the checks at
+// the top of a restart, then the Krylov loop's budget.  A stop leaves block 0
+// without a pending half step and block 2 done, so the rest is no-ops.
+__global__ void rs_step_kernel(Scalars* s0, Scalars* s2, RsCtl* ctl,
+                               cudaGraphConditionalHandle h_inner, int maxit)
+{
+    cudaGraphSetConditional(h_inner, 0u);
+    IrCtl& k = ctl->k;
+    bool stop = true;
+    k.relres = s0->res;
+    if (s0->status) {
+        k.status = s0->status;
+    } else if (s0->bb == 0.0) {
+        k.zero_x = 1;
+        k.relres = 0.0;
+        ctl->converged = 1;
+    } else if (s0->done) {
+        ctl->converged = 1;
+    } else if (k.total >= maxit) {
+    } else {
+        stop = false;
+    }
+    if (stop) {
+        ctl->pass_stop = 1;
+        k.stop = 1;
+        s0->done = 1;
+        s0->half = 0;
+        s2->done = 1;
+        return;
+    }
+    k.inner_it = 0;
+    k.budget = maxit - k.total;
+    if (k.budget > 0) cudaGraphSetConditional(h_inner, 1u);
+}
+
+__global__ void rs_zero_x_kernel(double* x, int n, const RsCtl* ctl)
+{
+    if (!ctl->k.zero_x) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] = 0.0;
+}
+
+// After the Krylov loop: its count, breakdown and status; block 2 reset for
+// the true residual.
+__global__ void rs_mid_kernel(Scalars* s0, Scalars* s2, RsCtl* ctl, double tol2)
+{
+    if (ctl->pass_stop) return;
+    IrCtl& k = ctl->k;
+    k.total += s0->iters;
+    k.pad = s0->breakdown != 0;  // broke
+    if (s0->status) {
+        k.status = s0->status;
+        ctl->pass_stop = 1;
+        k.stop = 1;
+        s0->half = 0;
+        s2->done = 1;
+        return;
+    }
+    ir_reset_block(s2, tol2);
+}
+
+// After the true residual (EP_TRUE_RES in block 2): converged, or restart.
+__global__ void rs_post_kernel(const Scalars* s0, const Scalars* s2, RsCtl* ctl,
+                               cudaGraphConditionalHandle h_outer, double tol2)
+{
+    cudaGraphSetConditional(h_outer, 0u);
+    IrCtl& k = ctl->k;
+    if (!ctl->pass_stop) {
+        k.relres = s2->res;
+        if (!isfinite(s2->res)) {
+            k.status = OCSL_NONFINITE;
+            k.stop = 1;
+        } else {
+            ctl->converged = s2->rr <= tol2 * s2->bb;
+            k.outer += 1;
+            if (ctl->converged || (k.pad && s0->iters == 0) || k.outer >= 64)
+                k.stop = 1;
+            else
+                cudaGraphSetConditional(h_outer, 1u);
+        }
+    }
+    if (k.stop && !ctl->converged && k.status == OCSL_OK)
+        k.status = k.pad ? OCSL_BREAKDOWN : OCSL_NOT_CONVERGED;
+}
+
+template <typename Init, typename Iter, typename Half>
+TolResult run_restarted_device(Solve& s, const double* A, const double* b, double* x,
+                               const ocsl_opts& o, Init&& init, Iter&& iteration, Half&& half,
+                               int kind, std::initializer_list<const void*> ptrs)
+{
+    ocsl_ctx* c = s.c;
+    double** v = c->v64;
+    const double tol2 = o.tol * o.tol;
+    if (c->n_irctl < 2) ensure_irctl(c, 2);  // an RsCtl takes two IrCtl slots
+    RsCtl* ctl = static_cast<RsCtl*>(c->d_irctl);
+    static_assert(sizeof(RsCtl) <= 2 * sizeof(IrCtl), "control block size");
+    std::vector<unsigned char> key;
+    auto add = [&](const void* p, size_t bytes) {
+        const unsigned char* q = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), q, q + bytes);
+    };
+    add(&kind, sizeof kind);
+    for (const void* p : ptrs) add(&p, sizeof p);
+    const void* more[5] = {A, b, x, s.st, c->d_irctl};
+    add(more, sizeof more);
+    add(&o.tol, sizeof o.tol);
+    add(&o.maxit, sizeof o.maxit);
+    if (!c->ir_exec || key != c->ir_key) {
+        if (c->ir_exec) cudaGraphExecDestroy(c->ir_exec);
+        c->ir_exec = nullptr;
+        c->ir_key.clear();
+        const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+        cudaGraph_t root = nullptr;
+        CK(cudaGraphCreate(&root, 0));
+        try {
+            cudaGraphConditionalHandle h_outer, h_inner;
+            CK(cudaGraphConditionalHandleCreate(&h_outer, root, 1u, cudaGraphCondAssignDefault));
+            CK(cudaStreamBeginCaptureToGraph(s.st, root, nullptr, nullptr, 0, mode));
+            rs_begin_kernel<<<1, 1, 0, s.st>>>(ctl);
+            cudaGraph_t outer = add_while_node(s.st, h_outer);
+            cudaGraph_t got = nullptr;
+            CK(cudaStreamEndCapture(s.st, &got));
+
+            CK(cudaGraphConditionalHandleCreate(&h_inner, outer, 0u, 0u));
+            CK(cudaStreamBeginCaptureToGraph(s.st, outer, nullptr, nullptr, 0, mode));
+            rs_reset_kernel<<<1, 1, 0, s.st>>>(c->d_sc, tol2, ctl);
+            s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 0, EP_TB_INIT);
+            init();
+            rs_step_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 2, ctl, h_inner, o.maxit);
+            rs_zero_x_kernel<<<std::max(1, std::min((s.n + 255) / 256, 1024)), 256, 0, s.st>>>(
+                x, s.n, ctl);
+            cudaGraph_t inner = add_while_node(s.st, h_inner);
+            rs_mid_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 2, ctl, tol2);
+            half();
+            s.spmv<double>(A, x, v[R], 1, b, nullptr, nullptr, DOT_YY | DOT_ZZ, 2, EP_TRUE_RES);
+            rs_post_kernel<<<1, 1, 0, s.st>>>(c->d_sc, c->d_sc + 2, ctl, h_outer, tol2);
+            CK(cudaStreamEndCapture(s.st, &outer));
+
+            CK(cudaStreamBeginCaptureToGraph(s.st, inner, nullptr, nullptr, 0, mode));
+            s.tb_prefilled = false;  // every pass fills its sweep outputs (same bits)
+            iteration(0);
+            s.tb_prefilled = false;
+            ir_inner_kernel<<<1, 1, 0, s.st>>>(c->d_sc, &ctl->k, h_inner);
+            CK(cudaStreamEndCapture(s.st, &inner));
+        } catch (...) {
+            end_any_capture(s.st);
+            cudaGraphDestroy(root);
+            throw;
+        }
+        cudaGraphExec_t e = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&e, root, 0);
+        cudaGraphDestroy(root);
+        CK(ie);
+        c->ir_exec = e;
+        c->ir_key = key;
+    }
+    CK(cudaGraphLaunch(c->ir_exec, s.st));
+    RsCtl h;
+    CK(cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    TolResult r;
+    r.iters = h.k.total;
+    r.relres = h.k.relres;
+    r.status = h.k.status;
+    return r;
+}
+
+TolResult run_bicgstab_tol_device(Solve& s, const double* A, const double* b, double* x,
+                                  const ocsl_opts& o)
+{
+    double** v = s.c->v64;
+    const double* M = s.factored(A, o.ilu_sweeps, true, false, -1, true, true, false);
+    if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
+    s.prepare_spmv(A, true, false);
+    return run_restarted_device(
+        s, A, b, x, o, [&] { s.vec<double>(V_COPY2, {v[RH], v[P], v[R]}, 0, EP_STORE); },
+        [&](int) {
+            bicgstab_iteration<double>(s, A, M, s.c->d_dinv, x, v[R], v[RH], v[P], v[PH], v[V],
+                                       v[S], v[SH], v[T], v[TMP], 0);
+        },
+        [&] { s.vec<double>(V_TB_HALF, {x, v[PH]}, 0, EP_STORE); }, 1,
+        {M, s.soa64, s.recA64, s.c->d_dinv});
+}
+
+TolResult run_pcg_tol_device(Solve& s, const double* A, const double* b, double* x,
+                             const ocsl_opts& o)
+{
+    double** v = s.c->v64;
+    s.factored(A, 0, true, false, -1, false, false, false);  // Jacobi: dinv = 1 / A_ii
+    if (s.pivot_status() != OCSL_OK) return zero_pivot_result();
+    s.prepare_spmv(A, true, false);
+    return run_restarted_device(
+        s, A, b, x, o,
+        [&] { s.vec<double>(V_PC_INIT, {v[Z], v[P], v[R], s.c->d_dinv}, 0, EP_PC_INIT); },
+        [&](int) {
+            s.spmv<double>(A, v[P], v[Q], 0, nullptr, nullptr, v[P], DOT_WY, 0, EP_PC_ALPHA);
+            s.vec<double>(V_PC_XRZ, {x, v[P], v[R], v[Q], v[Z], s.c->d_dinv}, 0, EP_PC_RUPD);
+            s.vec<double>(V_PC_P, {v[P], v[Z]}, 0, EP_STORE);
+        },
+        [] {}, 2, {s.recA64, s.c->d_dinv});
 }
 
 // Column-batched form of run_bicgstab_ir32: nc (<= kMaxCols) right-hand
@@ -1942,9 +2169,11 @@ int solve_device_impl(ocsl_ctx* c, int method, const double* A, const double* b,
         } else {
             TolResult t;
             if (method == OCSL_PCG)
-                t = run_pcg_tol(s, A, b, x, o);
+                t = device_loop_ok(s) ? run_pcg_tol_device(s, A, b, x, o)
+                                      : run_pcg_tol(s, A, b, x, o);
             else if (method == OCSL_ILU_BICGSTAB)
-                t = run_bicgstab_tol(s, A, b, x, o);
+                t = device_loop_ok(s) ? run_bicgstab_tol_device(s, A, b, x, o)
+                                      : run_bicgstab_tol(s, A, b, x, o);
             else if (device_loop_ok(s))
                 t = run_bicgstab_ir32_device(s, A, b, x, o);
             else

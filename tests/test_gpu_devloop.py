@@ -21,8 +21,9 @@ pytestmark = pytest.mark.gpu
 IR32 = ocsl.ILU_BICGSTAB_IR32
 
 
-def _both(ctx, torch, s, b, **opts):
+def _both(ctx, torch, s, b, method=None, **opts):
     """The solve host-driven, then device-driven, on a created stream."""
+    method = IR32 if method is None else method
     A = torch.from_numpy(s.value).cuda()
     B = b if isinstance(b, torch.Tensor) else torch.from_numpy(b).cuda()
     out = []
@@ -31,7 +32,7 @@ def _both(ctx, torch, s, b, **opts):
         for dev in (False, True):
             ctx.set_device_loop(dev)
             X = torch.zeros(s.n, dtype=torch.float64, device="cuda")
-            r = ctx.solve_device(IR32, A, B, X, **opts)
+            r = ctx.solve_device(method, A, B, X, **opts)
             stream.synchronize()
             out.append((X.clone(), r))
     ctx.set_device_loop(False)
@@ -153,3 +154,28 @@ def test_device_loop_small_system_replays_its_graph(ctx, torch_cuda):
     assert out[False][1]["iterations"] == out[True][1]["iterations"]
     print(f"{s.n}-row FP32-refined solve: host loop {ms[False]:.3f} ms, device loop "
           f"{ms[True]:.3f} ms per solve ({out[True][1]['iterations']} inner iterations)")
+
+
+@pytest.mark.parametrize("method", [ocsl.ILU_BICGSTAB, ocsl.PCG])
+@pytest.mark.parametrize("kind", ["hex", "tet"])
+def test_restarted_device_loop_equals_host_loop(ctx, torch_cuda, kind, method):
+    """The plain FP64 ILU-BiCGSTAB and Jacobi PCG with their restart and
+    Krylov loops on the device: the host loop's bits, iteration counts,
+    residuals and statuses, including b = 0, a NaN and an exhausted maxit."""
+    torch = torch_cuda
+    pe = 0.0 if method == ocsl.PCG else 10.0
+    s = W.hex_pprime(21, 17, 13, peclet=pe) if kind == "hex" else W.tet_pprime(9, 8, 7,
+                                                                                 peclet=pe)
+    ctx.set_pattern(s.row_ptr, s.column_index)
+    for opts in ({"tol": 1e-10}, {"tol": 1e-13}, {"tol": 1e-12, "maxit": 9}):
+        out = _both(ctx, torch, s, s.b, method=method, **opts)
+        _same(out, (kind, method, opts))
+    assert out[1][1]["status"] == _abi.NOT_CONVERGED
+    out = _both(ctx, torch, s, np.zeros(s.n), method=method)
+    _same(out, (kind, method, "b=0"))
+    assert torch.count_nonzero(out[1][0]) == 0 and out[1][1]["status"] == 0
+    b = s.b.copy()
+    b[5] = np.nan
+    out = _both(ctx, torch, s, b, method=method)
+    _same(out, (kind, method, "nan"))
+    assert out[1][1]["status"] == _abi.NONFINITE
