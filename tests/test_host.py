@@ -223,3 +223,20 @@ def test_dot_noalloc_refuses_bad_pointers_before_any_cuda_call(lib_built):
         assert b"aligned" in L.ocsl_noalloc_last_error()
     # with n = 0 the inputs are not read, only the result pointer is checked
     assert L.ocsl_dot_noalloc(0, odd, odd, odd, None) == _abi.BAD_ARGUMENT
+
+
+def test_new_entry_points_refuse_null_handles(lib_built):
+    """Host-side argument checks of the device-loop, batch-graph, SpMV-shape and
+    VTK entry points: null handles are OCSL_BAD_ARGUMENT, before any CUDA call."""
+    L = lib_built
+    assert L.ocsl_set_device_loop(None, 1) == _abi.BAD_ARGUMENT
+    assert L.ocsl_batch_set_graph(None, 1) == _abi.BAD_ARGUMENT
+    assert L.ocsl_set_spmv_lanes(None, 4) == _abi.BAD_ARGUMENT
+    lanes = C.c_int(-1)
+    assert L.ocsl_spmv_lanes(None, C.byref(lanes)) == _abi.BAD_ARGUMENT
+    us = C.c_double()
+    assert L.ocsl_autotune_spmv_device(None, 0, None, C.byref(lanes), C.byref(us)) == \
+        _abi.BAD_ARGUMENT
+    err = C.create_string_buffer(64)
+    assert L.ocsl_vtk_write(None, None, None, None, err, 64) == _abi.BAD_ARGUMENT
+    assert b"null" in err.value
