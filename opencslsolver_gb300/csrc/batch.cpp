@@ -150,6 +150,7 @@ int solve_graph(ocsl_batch* b, const double* const* d_value, const double* const
                 double* const* d_x, const ocsl_opts* opts, ocsl_result* result)
 {
     const int count = (int)b->ctx.size();
+    if (count == 0) return OCSL_OK;
     ocsl_opts o;
     ocsl_default_opts(&o);
     if (opts) o = *opts;
